@@ -1,0 +1,407 @@
+/* Device library for generated bitstream programs (compiled by NVRTC for sm_103a).
+ *
+ * Stream layout (the reference's, bitgen/bitstream.py:228-258 and
+ * bitgen/template/cuda/kernel.cu:60-100): a stream is a sequence of 32-bit words, character
+ * 32*w + j at bit 31 - j of word w.  Advance moves marks to higher character positions, i.e.
+ * toward the low bits of a word and then into the next word.
+ *
+ * Execution model: a warp owns a tile.  Lane l holds words [l*WPT, l*WPT + WPT) of the tile in
+ * registers (type S).  Lanes [0, HL) are a halo: they re-compute the last HL*WPT words of the
+ * previous tile so that every Advance of the program finds its source words inside the warp.
+ * Lanes [HL, 32) are written out.  The generated kernel defines BG_WPT and BG_HL before
+ * including this file.
+ *
+ * Additions (MatchStar, ScanThru) need the exact carry entering the tile.  For addition k the
+ * carry is injected at lane DL_k, the first lane where both addends are exact.  If the addition
+ * does not propagate through that lane the carry cannot change anything downstream and it is
+ * resolved locally; otherwise the predecessor tile (which computed the same lane and knows it
+ * is needed) publishes its carry-out, first as a (generate, propagate) aggregate and then as
+ * an inclusive carry, and this tile reads it with a decoupled look-back.  Every wait is bounded
+ * by a clock64 budget; on timeout the kernel records BG_DEV_ERR_TIMEOUT and continues.
+ */
+#pragma once
+#include "bg_params.h"
+#include "bg_transpose.cuh"
+
+#ifndef BG_WPT
+#error "BG_WPT must be defined"
+#endif
+#ifndef BG_HL
+#error "BG_HL must be defined"
+#endif
+
+namespace bg {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int WPT = BG_WPT;
+constexpr int HL = BG_HL;
+constexpr int SL = 32 - HL;                 /* output lanes per tile   */
+constexpr long long SW = (long long)SL * WPT; /* output words per tile */
+static_assert(HL >= 0 && HL < 32, "halo must leave output lanes");
+
+struct S {
+  uint32_t w[WPT];
+};
+
+__device__ __forceinline__ S zero() {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = 0u;
+  return r;
+}
+__device__ __forceinline__ S ones() {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = FULL;
+  return r;
+}
+__device__ __forceinline__ S operator&(const S &a, const S &b) {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = a.w[j] & b.w[j];
+  return r;
+}
+__device__ __forceinline__ S operator|(const S &a, const S &b) {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = a.w[j] | b.w[j];
+  return r;
+}
+__device__ __forceinline__ S operator^(const S &a, const S &b) {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = a.w[j] ^ b.w[j];
+  return r;
+}
+__device__ __forceinline__ S operator~(const S &a) {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = ~a.w[j];
+  return r;
+}
+__device__ __forceinline__ S &operator|=(S &a, const S &b) {
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) a.w[j] |= b.w[j];
+  return a;
+}
+/* SEL(c, a, b) = (c & a) | (~c & b)   (bitgen/inst/inst_sel.py:42-57) */
+__device__ __forceinline__ S sel(const S &c, const S &a, const S &b) {
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) r.w[j] = (c.w[j] & a.w[j]) | (~c.w[j] & b.w[j]);
+  return r;
+}
+/* warp-wide "any bit set" (zero-block skipping test) */
+__device__ __forceinline__ bool any(const S &x) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) o |= x.w[j];
+  return __any_sync(FULL, o != 0u);
+}
+
+/* word (lane*WPT + J) of the tile as seen from this lane, J may be negative (earlier lanes). */
+__device__ __forceinline__ uint32_t word_back(const S &x, int J) {
+  if (J >= 0) return x.w[J];
+  const int L = (-J + WPT - 1) / WPT;
+  const int I = J + L * WPT;
+  return __shfl_up_sync(FULL, x.w[I], L);
+}
+
+struct Tile {
+  long long gtile;   /* global tile id                                   */
+  long long first;   /* global id of the first tile of this input        */
+  long long base;    /* input word index of lane 0 word 0 (may be < 0)   */
+  long long n;       /* characters in the input                          */
+  long long W;       /* words in the input                               */
+  unsigned long long epoch;
+  int input;
+  int lane;
+  S vm;              /* per word: all ones if the word index is >= 0     */
+};
+
+/* Advance(x, N): marks move N positions forward; words before the input start read as 0. */
+template <int N>
+__device__ __forceinline__ S adv(const S &xin, const Tile &t) {
+  constexpr int Q = N / 32, R = N % 32;
+  const S x = xin & t.vm;
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const uint32_t cur = word_back(x, j - Q);
+    if (R == 0) {
+      r.w[j] = cur;
+    } else {
+      const uint32_t prev = word_back(x, j - Q - 1);
+      r.w[j] = __funnelshift_r(cur, prev, R);
+    }
+  }
+  return r;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+/* record = epoch << 4 | flag << 2 | P << 1 | G ; flag 1 = aggregate, 2 = inclusive carry */
+__device__ __forceinline__ void publish(const BgParams &p, const Tile &t, int k, uint32_t flag,
+                                        uint32_t P, uint32_t G) {
+  if (t.lane == 0) {
+    unsigned long long r = (t.epoch << 4) | ((unsigned long long)flag << 2) |
+                           ((unsigned long long)P << 1) | (unsigned long long)G;
+    st_relaxed(p.records + (long long)k * p.n_tiles + t.gtile, r);
+  }
+}
+
+/* Bounded wait for a look-back record; returns an inclusive zero carry on timeout.
+ * Lane 0 polls and broadcasts, so every lane takes the same path.  The wait ends when the
+ * record carries this launch's epoch, after spin_limit clock64 cycles or 2^22 polls, or at once
+ * when an earlier wait of this launch already timed out (so one lost record cannot make every
+ * later tile wait its full budget). */
+__device__ __forceinline__ unsigned long long wait_record(const unsigned long long *addr,
+                                                          unsigned long long epoch,
+                                                          long long spin_limit, uint32_t *state,
+                                                          int lane) {
+  unsigned long long r = 0;
+  if (lane == 0) {
+    const long long t0 = clock64();
+    unsigned ns = 32;
+    for (unsigned it = 0;; ++it) {
+      r = ld_relaxed(addr);
+      if ((r >> 4) == epoch) break;
+      const bool aborted = (*(volatile uint32_t *)(state + 1) & BG_DEV_ERR_TIMEOUT) != 0u;
+      if (aborted || it >= (1u << 22) || clock64() - t0 > spin_limit) {
+        atomicOr(state + 1, BG_DEV_ERR_TIMEOUT);
+        r = (epoch << 4) | (2ull << 2);
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 1024) ns <<= 1;
+    }
+  }
+  return __shfl_sync(FULL, r, 0);
+}
+
+/* Carry entering tile `gtile`'s look-back lane for the addition whose records start at `rec`
+ * (decoupled look-back over the predecessors' aggregates and inclusive carries). */
+__device__ __noinline__ uint32_t lookback(const unsigned long long *rec, long long gtile,
+                                          long long first, unsigned long long epoch,
+                                          long long spin_limit, uint32_t *state, int lane) {
+  uint32_t accG = 0, accP = 1;
+  for (long long j = gtile - 1;; --j) {
+    if (j < first) {
+      if (lane == 0) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
+      return accG;
+    }
+    const unsigned long long r = wait_record(rec + j, epoch, spin_limit, state, lane);
+    const uint32_t flag = (uint32_t)(r >> 2) & 3u;
+    const uint32_t G = (uint32_t)r & 1u, P = (uint32_t)(r >> 1) & 1u;
+    if (flag == 2u) return accG | (accP & G);
+    accG |= accP & G;
+    accP &= P;
+    if (!accP) return accG;
+  }
+}
+
+/* Carry vector for addition k: bit l = carry entering lane l.  Gm/Pm are the lanes that
+ * generate / propagate a carry; lanes below DL are ignored and the carry enters at DL. */
+template <int DL>
+__device__ __forceinline__ uint32_t carries(const BgParams &p, const Tile &t, int k, uint32_t Gm,
+                                            uint32_t Pm) {
+  static_assert(DL >= 0 && DL < HL || (HL == 0 && DL == 0), "carry lane must be in the halo");
+  constexpr int OUTL = SL + DL; /* the successor tile's carry lane, in our coordinates */
+  const uint32_t keep = ~((1u << DL) - 1u);
+  Gm &= keep;
+  Pm &= keep;
+  const uint32_t A = Gm | Pm, B = Gm;
+  uint32_t cin = 0;
+  const bool own = (HL > 0) && ((Pm >> DL) & 1u);
+  const bool succ = (HL > 0) && ((Pm >> (OUTL & 31)) & 1u);
+  if (own) {
+    if (succ) {
+      const uint32_t c0 = (uint32_t)((unsigned long long)A + B) ^ A ^ B;
+      const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
+      const uint32_t Pagg = (((Pm >> DL) & span) == span) ? 1u : 0u;
+      publish(p, t, k, 1u, Pagg, (c0 >> OUTL) & 1u);
+    }
+    cin = lookback(p.records + (long long)k * p.n_tiles, t.gtile, t.first, t.epoch, p.spin_limit,
+                   p.state, t.lane);
+  }
+  const uint32_t cvec =
+      (uint32_t)((unsigned long long)A + B + ((unsigned long long)cin << DL)) ^ A ^ B;
+  if (succ) publish(p, t, k, 2u, 0u, (cvec >> OUTL) & 1u);
+  return cvec;
+}
+
+/* Exact X + Y over the tile (positions ascend with bit significance after __brev). */
+template <int DL>
+__device__ __forceinline__ S add_carry(const BgParams &p, const Tile &t, int k, const S &X,
+                                       const S &Y) {
+  uint32_t xb[WPT], yb[WPT];
+  uint32_t G = 0u, P = 1u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    xb[j] = __brev(X.w[j] & t.vm.w[j]);
+    yb[j] = __brev(Y.w[j] & t.vm.w[j]);
+    const uint32_t s = xb[j] + yb[j];
+    const uint32_t g = s < xb[j] ? 1u : 0u;
+    const uint32_t pp = s == FULL ? 1u : 0u;
+    G = g | (pp & G);
+    P &= pp;
+  }
+  const uint32_t Gm = __ballot_sync(FULL, G), Pm = __ballot_sync(FULL, P);
+  const uint32_t cvec = carries<DL>(p, t, k, Gm, Pm);
+  uint32_t c = (cvec >> t.lane) & 1u;
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const unsigned long long s = (unsigned long long)xb[j] + yb[j] + c;
+    r.w[j] = __brev((uint32_t)s);
+    c = (uint32_t)(s >> 32);
+  }
+  return r;
+}
+
+/* Sum C + carry-in, for a marker that is zero in the whole warp (only the carry entering the
+ * tile can make the result non-zero). */
+template <int DL>
+__device__ __forceinline__ S add_zero_marker(const BgParams &p, const Tile &t, int k, const S &C) {
+  uint32_t allones = 1u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) allones &= ((C.w[j] & t.vm.w[j]) == FULL) ? 1u : 0u;
+  const uint32_t Pm = __ballot_sync(FULL, allones);
+  const uint32_t cvec = carries<DL>(p, t, k, 0u, Pm);
+  if (!__any_sync(FULL, cvec != 0u)) return C & t.vm;
+  /* a carry enters: sum = C + carry (brev domain) */
+  uint32_t c = (cvec >> t.lane) & 1u;
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const uint32_t cb = __brev(C.w[j] & t.vm.w[j]);
+    const unsigned long long s = (unsigned long long)cb + c;
+    r.w[j] = __brev((uint32_t)s);
+    c = (uint32_t)(s >> 32);
+  }
+  return r;
+}
+
+/* MatchStar(M, C) = (((M & C) + C) ^ C) | M   (bitgen/template/template_torch.py:392-407) */
+template <int DL>
+__device__ __noinline__ S matchstar(const BgParams &p, const Tile &t, int k, const S &M,
+                                       const S &C) {
+  if (!any(M)) return add_zero_marker<DL>(p, t, k, C) ^ (C & t.vm);
+  const S sum = add_carry<DL>(p, t, k, M & C, C);
+  return (sum ^ (C & t.vm)) | M;
+}
+
+/* ScanThru(M, C) = (M + C) & ~C   (bitgen/template/template_torch.py:377-389) */
+template <int DL>
+__device__ __noinline__ S scanthru(const BgParams &p, const Tile &t, int k, const S &M,
+                                      const S &C) {
+  if (!any(M)) return add_zero_marker<DL>(p, t, k, C) & ~C;
+  const S sum = add_carry<DL>(p, t, k, M, C);
+  return sum & ~C;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Tile scheduling, loads and stores
+ * --------------------------------------------------------------------------------------- */
+__device__ __forceinline__ void init(const BgParams &p, Tile &t) {
+  t.lane = threadIdx.x & 31;
+  t.epoch = *(volatile const unsigned long long *)(p.state + 2);
+}
+
+/* Claim the next tile (tiles are handed out in increasing order, which is what makes the
+ * look-back deadlock free: a tile only waits for tiles claimed before it). */
+__device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
+  unsigned int g = 0;
+  if (t.lane == 0) g = atomicAdd(p.state, 1u);
+  g = __shfl_sync(FULL, g, 0);
+  if ((long long)g >= p.n_tiles) return false;
+  int lo = 0, hi = p.n_inputs; /* find i: prefix[i] <= g < prefix[i+1] */
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (p.tile_prefix[mid] <= (long long)g) lo = mid; else hi = mid;
+  }
+  t.input = lo;
+  t.gtile = g;
+  t.first = p.tile_prefix[lo];
+  t.n = p.in_len[lo];
+  t.W = (t.n + 31) >> 5;
+  t.base = ((long long)g - t.first) * SW - (long long)HL * WPT;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j)
+    t.vm.w[j] = (t.base + t.lane * WPT + j >= 0) ? FULL : 0u;
+  if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
+    (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
+                      p.spin_limit, p.state, t.lane);
+  return true;
+}
+
+__device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b[8]) {
+  if (p.input_kind == BG_INPUT_BASIS) {
+    const uint32_t *src = p.in_basis + p.in_off[t.input];
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      const long long w = t.base + t.lane * WPT + j;
+      const bool ok = w >= 0 && w < t.W;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) b[i].w[j] = ok ? __ldg(src + i * p.basis_stride + w) : 0u;
+    }
+    return;
+  }
+  const uint8_t *src = p.in_bytes + p.in_off[t.input];
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    uint32_t u[8];
+    if (w >= 0 && 32 * w + 32 <= t.n) {
+      const uint4 *q = reinterpret_cast<const uint4 *>(src + 32 * w);
+      const uint4 a = __ldg(q), c = __ldg(q + 1);
+      u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
+      u[4] = c.x; u[5] = c.y; u[6] = c.z; u[7] = c.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) u[q] = 0u;
+      if (w >= 0 && w < t.W) {
+        const long long rem = t.n - 32 * w;
+        for (long long k = 0; k < rem; ++k)
+          u[k >> 2] |= (uint32_t)__ldg(src + 32 * w + k) << (8 * (k & 3));
+      }
+    }
+    uint32_t o[8];
+    transpose32(u, o);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
+  }
+}
+
+/* Write output stream o for this tile (lanes >= HL, words inside the input; characters at or
+ * beyond n are cleared) and add its popcount to counts[o][input]. */
+__device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, const S &v) {
+  uint32_t cnt = 0;
+  uint32_t *dst = p.out ? p.out + (long long)o * p.out_stride + p.out_off[t.input] : nullptr;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    if (t.lane >= HL && w >= 0 && w < t.W) {
+      uint32_t val = v.w[j];
+      const long long rem = t.n - 32 * w;
+      if (rem < 32) val &= FULL << (32 - rem);
+      if (dst) dst[w] = val;
+      cnt += __popc(val);
+    }
+  }
+  if (p.counts) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(FULL, cnt, d);
+    if (t.lane == 0 && cnt)
+      atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, (unsigned long long)cnt);
+  }
+}
+
+}  // namespace bg

@@ -1,0 +1,445 @@
+/* bitgen_gb300 runtime: the C ABI declared in include/bitgen_gb300.h.
+ *
+ * Host side of the engine: NVRTC compilation of generated scan kernels for sm_103a (with an
+ * on-disk cubin cache), per-layout launch plans holding the device-side tables and look-back
+ * records, the stand-alone byte -> basis transpose kernel, and a whole-stream executor for
+ * Pablo programs that keep while/if blocks.  It replaces the reference's cuda-python driver
+ * (bitgen/backend/cuda/cuda_kernel.py) and its torch extension (bitgen/template/cuda/).
+ */
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bitgen_gb300.h"
+#include "bg_params.h"
+#include "bg_transpose.cuh"
+
+extern "C" const char *bg_embedded_device_cuh;
+extern "C" const char *bg_embedded_params_h;
+extern "C" const char *bg_embedded_transpose_cuh;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define BG_CUDA(call)                                                                 \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(BG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+/* ------------------------------------------------------------------------------------ */
+/* Stand-alone transpose: one thread per 32-byte word, grid-stride, coalesced stores.     */
+/* ------------------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(256) bg_transpose_kernel(const uint8_t *__restrict__ bytes,
+                                                           uint32_t *__restrict__ basis,
+                                                           int64_t W, int64_t total) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t input = g / W, w = g - input * W;
+    const uint4 *q = reinterpret_cast<const uint4 *>(bytes + 32 * g);
+    const uint4 a = __ldg(q), c = __ldg(q + 1);
+    const uint32_t u[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+    uint32_t o[8];
+    bg::transpose32(u, o);
+    uint32_t *dst = basis + input * 8 * W + w;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) dst[i * W] = o[i];
+  }
+}
+
+__global__ void bg_prologue_kernel(uint32_t *state) {
+  state[0] = 0u;
+  unsigned long long *ep = reinterpret_cast<unsigned long long *>(state + 2);
+  *ep = *ep + 1ull;
+}
+
+int sm_count() {
+  static int n = -1;
+  if (n < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 1;
+  }
+  return n;
+}
+
+/* FNV-1a 64 */
+uint64_t fnv(const std::string &s, uint64_t h = 1469598103934665603ull) {
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+}  // namespace
+
+/* ======================================================================================== */
+/* Program                                                                                  */
+/* ======================================================================================== */
+struct bg_program {
+  bg_kernel_desc desc{};
+  std::string name;
+  std::string log;
+  std::vector<char> cubin;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kernel = nullptr;
+  int regs = 0, local_bytes = 0, blocks_per_sm = 1;
+};
+
+struct bg_plan {
+  bg_program *prog = nullptr;
+  bg_layout layout{};
+  int64_t n_tiles = 0;
+  int64_t *d_tables = nullptr; /* in_off | in_len | tile_prefix | out_off */
+  unsigned long long *d_records = nullptr;
+  uint32_t *d_state = nullptr;
+  int grid = 1;
+  int64_t debug_wait_tile = -1;
+  int64_t spin_limit = 0;
+};
+
+extern "C" {
+
+const char *bg_status_string(int s) {
+  switch (s) {
+    case BG_OK: return "ok";
+    case BG_ERR_INVALID: return "invalid argument";
+    case BG_ERR_CUDA: return "CUDA error";
+    case BG_ERR_COMPILE: return "NVRTC compilation failed";
+    case BG_ERR_TIMEOUT: return "bounded device wait timed out";
+    case BG_ERR_ALIGN: return "input not 16-byte aligned";
+    case BG_ERR_NOMEM: return "out of memory";
+    case BG_ERR_DEVICE: return "device reported an internal inconsistency";
+    default: return "unknown status";
+  }
+}
+
+const char *bg_last_error(void) { return g_last_error.c_str(); }
+
+int bg_interp_fail(int code, const char *msg) { return fail(code, msg ? msg : ""); }
+
+int bg_device_available(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n > 0 ? 1 : 0;
+}
+
+int bg_transpose(const uint8_t *bytes, uint32_t *basis, int64_t n_bytes_padded, int64_t n_inputs,
+                 void *stream) {
+  if (!bytes || !basis || n_bytes_padded < 0 || n_inputs < 0 || n_bytes_padded % 32)
+    return fail(BG_ERR_INVALID, "bg_transpose: bad arguments");
+  if (!aligned16(bytes)) return fail(BG_ERR_ALIGN, "bg_transpose: bytes not 16-byte aligned");
+  const int64_t W = n_bytes_padded / 32, total = W * n_inputs;
+  if (total == 0) return BG_OK;
+  const int64_t want = (total + 255) / 256;
+  const int grid = (int)std::min<int64_t>(want, (int64_t)sm_count() * 16);
+  bg_transpose_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(bytes, basis, W, total);
+  BG_CUDA(cudaGetLastError());
+  return BG_OK;
+}
+
+static int compile_cubin(const std::string &src, const std::string &name, std::string &log,
+                         std::vector<char> &cubin) {
+  const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
+                        "--device-as-default-execution-space", "--split-compile=0"};
+  const int n_opts = sizeof(opts) / sizeof(opts[0]);
+  int major = 0, minor = 0;
+  nvrtcVersion(&major, &minor);
+  std::string key = src + "|" + name + "|" + std::to_string(major) + "." + std::to_string(minor);
+  for (int i = 0; i < n_opts; ++i) key += std::string("|") + opts[i];
+  key += bg_embedded_device_cuh;
+  key += bg_embedded_params_h;
+  key += bg_embedded_transpose_cuh;
+  char hex[40];
+  snprintf(hex, sizeof hex, "%016llx%016llx", (unsigned long long)fnv(key),
+           (unsigned long long)fnv(key, 0x84222325cbf29ce4ull));
+  const char *dir = getenv("BG_CACHE_DIR");
+  std::string path = dir && *dir ? std::string(dir) + "/" + hex + ".cubin" : std::string();
+  if (!path.empty()) {
+    if (FILE *f = fopen(path.c_str(), "rb")) {
+      fseek(f, 0, SEEK_END);
+      long sz = ftell(f);
+      fseek(f, 0, SEEK_SET);
+      cubin.resize(sz > 0 ? (size_t)sz : 0);
+      size_t got = sz > 0 ? fread(cubin.data(), 1, (size_t)sz, f) : 0;
+      fclose(f);
+      if (sz > 0 && got == (size_t)sz) {
+        log = "cubin cache hit " + path;
+        return BG_OK;
+      }
+      cubin.clear();
+    }
+  }
+  nvrtcProgram prog;
+  const char *headers[] = {bg_embedded_device_cuh, bg_embedded_params_h, bg_embedded_transpose_cuh};
+  const char *names[] = {"bg_device.cuh", "bg_params.h", "bg_transpose.cuh"};
+  if (nvrtcCreateProgram(&prog, src.c_str(), (name + ".cu").c_str(), 3, headers, names) !=
+      NVRTC_SUCCESS)
+    return fail(BG_ERR_COMPILE, "nvrtcCreateProgram failed");
+  nvrtcResult r = nvrtcCompileProgram(prog, n_opts, opts);
+  size_t logsz = 0;
+  nvrtcGetProgramLogSize(prog, &logsz);
+  log.assign(logsz, '\0');
+  if (logsz) nvrtcGetProgramLog(prog, &log[0]);
+  if (r != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return fail(BG_ERR_COMPILE, std::string("NVRTC: ") + nvrtcGetErrorString(r) + "\n" + log);
+  }
+  size_t sz = 0;
+  nvrtcGetCUBINSize(prog, &sz);
+  cubin.resize(sz);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  if (!path.empty()) {
+    std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
+    if (FILE *f = fopen(tmp.c_str(), "wb")) {
+      fwrite(cubin.data(), 1, cubin.size(), f);
+      fclose(f);
+      rename(tmp.c_str(), path.c_str());
+    }
+  }
+  return BG_OK;
+}
+
+int bg_nvrtc_check(const char *source, size_t source_len, const char *name, char *log_buf,
+                   size_t log_len) {
+  if (!source || !name) return fail(BG_ERR_INVALID, "bg_nvrtc_check: bad arguments");
+  std::string src(source, source_len ? source_len : strlen(source)), log;
+  std::vector<char> cubin;
+  const int rc = compile_cubin(src, name, log, cubin);
+  if (log_buf && log_len) {
+    const std::string &m = rc == BG_OK ? log : g_last_error;
+    size_t n = std::min(log_len - 1, m.size());
+    memcpy(log_buf, m.data(), n);
+    log_buf[n] = '\0';
+  }
+  return rc;
+}
+
+int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
+  if (!desc || !out || !desc->source || !desc->name || desc->wpt < 1 || desc->wpt > 8 ||
+      desc->halo_lanes < 0 || desc->halo_lanes > 31 || desc->n_outputs < 0 || desc->n_adds < 0 ||
+      desc->block < 32 || desc->block % 32)
+    return fail(BG_ERR_INVALID, "bg_program_create: bad descriptor");
+  *out = nullptr;
+  bg_program *p = new (std::nothrow) bg_program();
+  if (!p) return fail(BG_ERR_NOMEM, "bg_program_create: out of host memory");
+  p->desc = *desc;
+  p->name = desc->name;
+  p->desc.name = p->name.c_str();
+  p->desc.source = nullptr;
+  std::string src(desc->source, desc->source_len ? desc->source_len : strlen(desc->source));
+  int rc = compile_cubin(src, p->name, p->log, p->cubin);
+  if (rc != BG_OK) {
+    std::string keep = g_last_error;
+    delete p;
+    g_last_error = keep;
+    return rc;
+  }
+  cudaError_t e = cudaLibraryLoadData(&p->lib, p->cubin.data(), nullptr, nullptr, 0, nullptr,
+                                      nullptr, 0);
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&p->kernel, p->lib, p->name.c_str());
+  if (e != cudaSuccess) {
+    std::string msg = std::string("loading the compiled program: ") + cudaGetErrorString(e);
+    if (p->lib) cudaLibraryUnload(p->lib);
+    delete p;
+    return fail(BG_ERR_CUDA, msg);
+  }
+  cudaFuncAttributes attr{};
+  if (cudaFuncGetAttributes(&attr, (const void *)p->kernel) == cudaSuccess) {
+    p->regs = attr.numRegs;
+    p->local_bytes = (int)attr.localSizeBytes;
+  } else {
+    cudaGetLastError();
+  }
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)p->kernel, desc->block,
+                                                    0) == cudaSuccess && nb > 0) {
+    p->blocks_per_sm = nb;
+  } else {
+    cudaGetLastError();
+    int regs = p->regs > 0 ? p->regs : 128;
+    p->blocks_per_sm = std::max(1, 65536 / (regs * desc->block));
+  }
+  *out = p;
+  return BG_OK;
+}
+
+int bg_program_log(const bg_program *prog, char *buf, size_t len) {
+  if (!prog || !buf || !len) return fail(BG_ERR_INVALID, "bg_program_log: bad arguments");
+  size_t n = std::min(len - 1, prog->log.size());
+  memcpy(buf, prog->log.data(), n);
+  buf[n] = '\0';
+  return BG_OK;
+}
+
+int bg_program_info(const bg_program *prog, int32_t *regs, int32_t *local_bytes,
+                    int32_t *max_blocks_per_sm) {
+  if (!prog) return fail(BG_ERR_INVALID, "bg_program_info: null program");
+  if (regs) *regs = prog->regs;
+  if (local_bytes) *local_bytes = prog->local_bytes;
+  if (max_blocks_per_sm) *max_blocks_per_sm = prog->blocks_per_sm;
+  return BG_OK;
+}
+
+int bg_program_destroy(bg_program *prog) {
+  if (!prog) return BG_OK;
+  if (prog->lib) cudaLibraryUnload(prog->lib);
+  delete prog;
+  return BG_OK;
+}
+
+/* ======================================================================================== */
+/* Plans                                                                                    */
+/* ======================================================================================== */
+int bg_plan_create(bg_program *prog, const bg_layout *L, bg_plan **out) {
+  if (!prog || !L || !out || L->n_inputs < 1 || !L->in_off || !L->in_len || !L->out_off ||
+      (L->input_kind != BG_INPUT_BYTES && L->input_kind != BG_INPUT_BASIS))
+    return fail(BG_ERR_INVALID, "bg_plan_create: bad layout");
+  *out = nullptr;
+  const int64_t n = L->n_inputs;
+  const int64_t tile_words = (int64_t)(32 - prog->desc.halo_lanes) * prog->desc.wpt;
+  std::vector<int64_t> tables(4 * n + 1);
+  int64_t *in_off = tables.data(), *in_len = in_off + n, *prefix = in_len + n,
+          *out_off = prefix + n + 1;
+  prefix[0] = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (L->in_len[i] < 0 || L->in_off[i] < 0)
+      return fail(BG_ERR_INVALID, "bg_plan_create: negative offset or length");
+    if (L->input_kind == BG_INPUT_BYTES && (L->in_off[i] & 15))
+      return fail(BG_ERR_ALIGN, "bg_plan_create: byte offsets must be multiples of 16");
+    in_off[i] = L->in_off[i];
+    in_len[i] = L->in_len[i];
+    out_off[i] = L->out_off[i];
+    const int64_t W = (L->in_len[i] + 31) / 32;
+    prefix[i + 1] = prefix[i] + std::max<int64_t>(1, (W + tile_words - 1) / tile_words);
+  }
+  bg_plan *p = new (std::nothrow) bg_plan();
+  if (!p) return fail(BG_ERR_NOMEM, "bg_plan_create: out of host memory");
+  p->prog = prog;
+  p->layout = *L;
+  p->n_tiles = prefix[n];
+  if (p->n_tiles >= (int64_t)0xffffffffll) {
+    delete p;
+    return fail(BG_ERR_INVALID, "bg_plan_create: too many tiles for one launch");
+  }
+  auto cleanup = [&](int code, const std::string &m) {
+    if (p->d_tables) cudaFree(p->d_tables);
+    if (p->d_records) cudaFree(p->d_records);
+    if (p->d_state) cudaFree(p->d_state);
+    delete p;
+    return fail(code, m);
+  };
+  if (cudaMalloc(&p->d_tables, tables.size() * sizeof(int64_t)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_create: tables");
+  if (cudaMemcpy(p->d_tables, tables.data(), tables.size() * sizeof(int64_t),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return cleanup(BG_ERR_CUDA, "bg_plan_create: table upload");
+  const size_t nrec = (size_t)std::max(1, prog->desc.n_adds) * (size_t)p->n_tiles;
+  if (cudaMalloc(&p->d_records, nrec * sizeof(unsigned long long)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_create: look-back records");
+  if (cudaMemset(p->d_records, 0, nrec * sizeof(unsigned long long)) != cudaSuccess)
+    return cleanup(BG_ERR_CUDA, "bg_plan_create: clearing records");
+  if (cudaMalloc(&p->d_state, 8 * sizeof(uint32_t)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_create: state");
+  if (cudaMemset(p->d_state, 0, 8 * sizeof(uint32_t)) != cudaSuccess)
+    return cleanup(BG_ERR_CUDA, "bg_plan_create: clearing state");
+  const int warps_per_block = prog->desc.block / 32;
+  const int64_t need = (p->n_tiles + warps_per_block - 1) / warps_per_block;
+  p->grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * prog->blocks_per_sm));
+  *out = p;
+  return BG_OK;
+}
+
+int64_t bg_plan_tiles(const bg_plan *plan) { return plan ? plan->n_tiles : -1; }
+
+int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t debug_wait_tile) {
+  if (!plan) return fail(BG_ERR_INVALID, "bg_plan_set_wait_limit: null plan");
+  plan->spin_limit = spin_limit_cycles;
+  plan->debug_wait_tile = debug_wait_tile;
+  return BG_OK;
+}
+
+int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
+                   unsigned long long *counts, void *stream) {
+  if (!plan || !input) return fail(BG_ERR_INVALID, "bg_plan_launch: null plan or input");
+  const bg_layout &L = plan->layout;
+  if (L.input_kind == BG_INPUT_BYTES && !aligned16(input))
+    return fail(BG_ERR_ALIGN, "bg_plan_launch: input not 16-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = L.n_inputs;
+  BgParams prm{};
+  prm.in_bytes = L.input_kind == BG_INPUT_BYTES ? (const uint8_t *)input : nullptr;
+  prm.in_basis = L.input_kind == BG_INPUT_BASIS ? (const uint32_t *)input : nullptr;
+  prm.in_off = plan->d_tables;
+  prm.in_len = plan->d_tables + n;
+  prm.tile_prefix = plan->d_tables + 2 * n;
+  prm.out_off = plan->d_tables + 3 * n + 1;
+  prm.out = out_streams;
+  prm.counts = counts;
+  prm.records = plan->d_records;
+  prm.state = plan->d_state;
+  prm.basis_stride = L.basis_stride;
+  prm.out_stride = L.out_stride;
+  prm.n_tiles = plan->n_tiles;
+  prm.spin_limit = 2000000000ll; /* ~1 s at 2 GHz */
+  prm.debug_wait_tile = plan->debug_wait_tile;
+  if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
+  prm.n_inputs = (int32_t)n;
+  prm.input_kind = L.input_kind;
+  if (counts)
+    BG_CUDA(cudaMemsetAsync(counts, 0,
+                            sizeof(unsigned long long) * (size_t)plan->prog->desc.n_outputs * n, s));
+  bg_prologue_kernel<<<1, 1, 0, s>>>(plan->d_state);
+  BG_CUDA(cudaGetLastError());
+  void *args[] = {&prm};
+  BG_CUDA(cudaLaunchKernel((const void *)plan->prog->kernel, dim3(plan->grid),
+                           dim3(plan->prog->desc.block), args, 0, s));
+  return BG_OK;
+}
+
+int bg_plan_sync(bg_plan *plan, void *stream) {
+  if (!plan) return fail(BG_ERR_INVALID, "bg_plan_sync: null plan");
+  BG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  uint32_t st = 0;
+  BG_CUDA(cudaMemcpy(&st, plan->d_state + 1, sizeof st, cudaMemcpyDeviceToHost));
+  if (st) {
+    BG_CUDA(cudaMemset(plan->d_state + 1, 0, sizeof st));
+    if (st & BG_DEV_ERR_TIMEOUT) return fail(BG_ERR_TIMEOUT, "carry look-back wait timed out");
+    return fail(BG_ERR_DEVICE, "carry look-back walked past the start of its input");
+  }
+  return BG_OK;
+}
+
+int bg_plan_destroy(bg_plan *plan) {
+  if (!plan) return BG_OK;
+  cudaFree(plan->d_tables);
+  cudaFree(plan->d_records);
+  cudaFree(plan->d_state);
+  delete plan;
+  return BG_OK;
+}
+
+}  // extern "C"

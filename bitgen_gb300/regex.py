@@ -1,0 +1,508 @@
+"""Regex -> Pablo compiler (stands in for the icgrep ``-print-pablo`` step).
+
+BitGen turns each regex group into Pablo text by running icgrep
+(``bitgen/tool/pcre2pablo.py:33-48``: ``-print-pablo``, ``-disable-matchstar``,
+``-if-insertion-gap=2147483647``, ``-disable-Unicode-linebreak``).  icgrep is an external fork
+that is not part of the reference tree, so this module is the project's own emitter.  It emits
+the same dialect (see :mod:`bitgen_gb300.pablo`) and can emit unbounded repetition either as
+``pablo.MatchStar`` or as the ``while`` loop form icgrep produces under ``-disable-matchstar``.
+
+Match convention (stated here because icgrep's is not pinned by the reference's tests): the
+result stream of a regex has bit ``p`` set iff some non-empty match of the regex ends with the
+byte at position ``p`` (its last byte), with matches allowed to start anywhere.  Line semantics
+follow grep with LF-only line breaks (``-disable-Unicode-linebreak``): ``.`` and negated classes
+do not match LF, ``^`` matches at position 0 and after every LF.  ``*?`` / ``+?`` / ``??`` (lazy)
+have the same set of match ends as their greedy forms and are compiled alike.
+
+Supported syntax: literals and escapes (``\\xHH``, ``\\n \\r \\t \\f \\v \\e \\a``, escaped
+punctuation), classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S``, ``.``,
+groups ``(...)`` / ``(?:...)``, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``.
+``$`` is rejected with :class:`UnsupportedRegex`.
+
+Compilation keeps two markers per regex state: ``L`` (positions of the last byte consumed) and
+``P`` (positions where the next byte is to be matched, i.e. ``Advance(L, 1)`` plus any
+zero-width starts).  A character class ``C`` maps ``(L, P)`` to ``(P & C, Advance(P & C, 1))``;
+``C*`` maps it to ``(L | (MatchStar(P, C) & C), MatchStar(P, C))``.  Character classes are
+compiled to a shared, reduced decision diagram over ``basis0`` (bit 7) .. ``basis7`` (bit 0).
+"""
+
+from __future__ import annotations
+
+import re
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Tuple
+
+from .pablo import Group, Op, While
+
+LF = 0x0A
+
+
+class UnsupportedRegex(ValueError):
+    pass
+
+
+# ----------------------------------------------------------------------------------------
+# AST
+# ----------------------------------------------------------------------------------------
+
+@dataclass(frozen=True)
+class CC:
+    bytes_: frozenset
+
+
+@dataclass(frozen=True)
+class Seq:
+    items: tuple
+
+
+@dataclass(frozen=True)
+class Alt:
+    items: tuple
+
+
+@dataclass(frozen=True)
+class Rep:
+    item: object
+    lo: int
+    hi: Optional[int]  # None = unbounded
+
+
+@dataclass(frozen=True)
+class Start:
+    pass
+
+
+ALL_BYTES = frozenset(range(256))
+DIGIT = frozenset(range(0x30, 0x3A))
+WORD = frozenset(list(range(0x30, 0x3A)) + list(range(0x41, 0x5B)) + list(range(0x61, 0x7B)) + [0x5F])
+SPACE = frozenset([0x20, 0x09, 0x0A, 0x0B, 0x0C, 0x0D])
+DOT = ALL_BYTES - {LF}
+
+_SIMPLE_ESC = {"n": 0x0A, "r": 0x0D, "t": 0x09, "f": 0x0C, "v": 0x0B, "e": 0x1B, "a": 0x07, "0": 0x00}
+_CLASS_ESC = {"d": DIGIT, "D": ALL_BYTES - DIGIT, "w": WORD, "W": ALL_BYTES - WORD,
+              "s": SPACE, "S": ALL_BYTES - SPACE}
+
+
+class _Parser:
+    def __init__(self, s: str):
+        self.s = s
+        self.i = 0
+
+    def peek(self):
+        return self.s[self.i] if self.i < len(self.s) else None
+
+    def take(self):
+        c = self.s[self.i]
+        self.i += 1
+        return c
+
+    def parse(self):
+        node = self.alt()
+        if self.i != len(self.s):
+            raise UnsupportedRegex(f"unexpected {self.s[self.i]!r} at {self.i} in {self.s!r}")
+        return node
+
+    def alt(self):
+        items = [self.seq()]
+        while self.peek() == "|":
+            self.take()
+            items.append(self.seq())
+        return items[0] if len(items) == 1 else Alt(tuple(items))
+
+    def seq(self):
+        items = []
+        while self.peek() is not None and self.peek() not in "|)":
+            a = self.atom()
+            a = self.quant(a)
+            items.append(a)
+        return Seq(tuple(items))
+
+    def quant(self, a):
+        while True:
+            c = self.peek()
+            if c == "*":
+                self.take(); a = Rep(a, 0, None)
+            elif c == "+":
+                self.take(); a = Rep(a, 1, None)
+            elif c == "?":
+                self.take(); a = Rep(a, 0, 1)
+            elif c == "{" and self._is_counted():
+                self.take()
+                j = self.s.index("}", self.i)
+                body = self.s[self.i:j]
+                self.i = j + 1
+                if "," in body:
+                    lo_s, hi_s = body.split(",", 1)
+                    lo = int(lo_s) if lo_s.strip() else 0
+                    hi = int(hi_s) if hi_s.strip() else None
+                else:
+                    lo = hi = int(body)
+                if hi is not None and hi < lo:
+                    raise UnsupportedRegex(f"bad repeat {{{body}}}")
+                a = Rep(a, lo, hi)
+            else:
+                return a
+            # lazy suffix: same match-end set as greedy
+            if self.peek() == "?":
+                self.take()
+            elif self.peek() == "+":
+                raise UnsupportedRegex("possessive quantifiers are not supported")
+
+    def _is_counted(self):
+        j = self.s.find("}", self.i)
+        if j < 0:
+            return False
+        return re.fullmatch(r"\d+(,\d*)?|,\d+", self.s[self.i + 1:j]) is not None
+
+    def atom(self):
+        c = self.take()
+        if c == "(":
+            if self.s.startswith("?:", self.i):
+                self.i += 2
+            elif self.peek() == "?":
+                raise UnsupportedRegex("group modifiers other than (?: are not supported")
+            node = self.alt()
+            if self.peek() != ")":
+                raise UnsupportedRegex("missing )")
+            self.take()
+            return node
+        if c == "[":
+            return CC(self.cls())
+        if c == ".":
+            return CC(DOT)
+        if c == "^":
+            return Start()
+        if c == "$":
+            raise UnsupportedRegex("$ anchors are not supported by this emitter")
+        if c == "\\":
+            e = self.escape()
+            return CC(e) if isinstance(e, frozenset) else CC(frozenset([e]))
+        if c in "*+?":
+            raise UnsupportedRegex(f"nothing to repeat at {self.i - 1}")
+        b = c.encode("latin1")
+        return CC(frozenset([b[0]]))
+
+    def escape(self):
+        c = self.take()
+        if c == "x":
+            h = self.s[self.i:self.i + 2]
+            if len(h) != 2:
+                raise UnsupportedRegex("bad \\x escape")
+            self.i += 2
+            return int(h, 16)
+        if c in _SIMPLE_ESC:
+            return _SIMPLE_ESC[c]
+        if c in _CLASS_ESC:
+            return _CLASS_ESC[c]
+        if c.isalnum():
+            raise UnsupportedRegex(f"unsupported escape \\{c}")
+        return c.encode("latin1")[0]
+
+    def cls(self):
+        neg = False
+        if self.peek() == "^":
+            self.take()
+            neg = True
+        items = set()
+        first = True
+        while True:
+            c = self.peek()
+            if c is None:
+                raise UnsupportedRegex("unterminated class")
+            if c == "]" and not first:
+                self.take()
+                break
+            first = False
+            self.take()
+            if c == "\\":
+                lo = self.escape()
+            else:
+                lo = c.encode("latin1")[0]
+            if isinstance(lo, frozenset):
+                items |= lo
+                continue
+            if self.peek() == "-" and self.i + 1 < len(self.s) and self.s[self.i + 1] != "]":
+                self.take()
+                h = self.take()
+                hi = self.escape() if h == "\\" else h.encode("latin1")[0]
+                if isinstance(hi, frozenset) or hi < lo:
+                    raise UnsupportedRegex("bad class range")
+                items |= set(range(lo, hi + 1))
+            else:
+                items.add(lo)
+        s = frozenset(items)
+        if neg:
+            s = ALL_BYTES - s - {LF}
+        return s
+
+
+def parse_regex(s: str):
+    return _Parser(s).parse()
+
+
+# ----------------------------------------------------------------------------------------
+# Pablo builder with hash-consing (CSE) and constant folding
+# ----------------------------------------------------------------------------------------
+
+class _Builder:
+    def __init__(self):
+        self.scopes: List[Tuple[List, Dict]] = [([], {})]  # (stmts, cse-table)
+        self.n = 0
+        self.cc_memo: Dict = {}
+        self.top = False
+
+    @property
+    def stmts(self):
+        return self.scopes[0][0]
+
+    def fresh(self, stem="t"):
+        self.n += 1
+        return f"{stem}_{self.n}"
+
+    def _lookup(self, key):
+        for _, table in reversed(self.scopes):
+            if key in table:
+                return table[key]
+        return None
+
+    def emit(self, op, args, shift=0, stem="t", cse=True):
+        key = (op, tuple(args), shift)
+        if cse:
+            hit = self._lookup(key)
+            if hit is not None:
+                return hit
+        d = self.fresh(stem)
+        # loop-invariant values (character classes, line starts) are hoisted to the top
+        # level so that they stay defined after a loop whose body never ran
+        scope = self.scopes[0] if self.top else self.scopes[-1]
+        scope[0].append(Op(d, op, tuple(args), shift=shift))
+        if cse:
+            scope[1][key] = d
+        return d
+
+    def assign(self, dst, src):
+        self.scopes[-1][0].append(Op(dst, "assign", (src,)))
+
+    # folded constructors ---------------------------------------------------------------
+    def AND(self, a, b):
+        if a == "0" or b == "0":
+            return "0"
+        if a == "1":
+            return b
+        if b == "1" or a == b:
+            return a
+        a, b = sorted((a, b))
+        return self.emit("and", (a, b))
+
+    def OR(self, a, b):
+        if a == "1" or b == "1":
+            return "1"
+        if a == "0":
+            return b
+        if b == "0" or a == b:
+            return a
+        a, b = sorted((a, b))
+        return self.emit("or", (a, b))
+
+    def NOT(self, a):
+        if a == "0":
+            return "1"
+        if a == "1":
+            return "0"
+        return self.emit("not", (a,))
+
+    def SEL(self, c, a, b):
+        if a == b:
+            return a
+        if b == "0":
+            return self.AND(c, a)
+        if a == "0":
+            return self.AND(self.NOT(c), b)
+        if a == "1":
+            return self.OR(c, b)
+        if b == "1":
+            return self.OR(self.NOT(c), a)
+        return self.emit("sel", (c, a, b))
+
+    def ADV(self, a, n=1):
+        if a == "0" or n == 0:
+            return a
+        return self.emit("advance", (a,), shift=n)
+
+    def MATCHSTAR(self, m, c):
+        if m == "0":
+            return "0"
+        if c == "0":
+            return m
+        return self.emit("matchstar", (m, c))
+
+    # character classes ---------------------------------------------------------------
+    def cc(self, s: frozenset) -> str:
+        saved, self.top = self.top, True
+        try:
+            return self._cc(s, 0)
+        finally:
+            self.top = saved
+
+    def _cc(self, s: frozenset, level: int) -> str:
+        if not s:
+            return "0"
+        span = 1 << (8 - level)
+        if len(s) == span:
+            return "1"
+        key = (level, s)
+        hit = self.cc_memo.get(key)
+        if hit is not None:
+            return hit
+        bit = 1 << (7 - level)
+        s1 = frozenset(x for x in s if x & bit)
+        s0 = frozenset(x for x in s if not x & bit)
+        f1 = self._cc(s1, level + 1)
+        f0 = self._cc(s0, level + 1)
+        r = self.SEL(f"basis{level}", f1, f0)
+        self.cc_memo[key] = r
+        return r
+
+
+# ----------------------------------------------------------------------------------------
+# Regex -> Pablo
+# ----------------------------------------------------------------------------------------
+
+class _Compiler:
+    """Compiles one regex AST into the shared builder.  State = (L, P-or-None)."""
+
+    def __init__(self, b: _Builder, matchstar: bool):
+        self.b = b
+        self.use_matchstar = matchstar
+        self._sol = None
+
+    def P(self, st):
+        L, P = st
+        return P if P is not None else self.b.ADV(L, 1)
+
+    def sol(self):
+        if self._sol is None:
+            lf = self.b.cc(frozenset([LF]))
+            saved, self.b.top = self.b.top, True
+            self._sol = self.b.NOT(self.b.ADV(self.b.NOT(lf), 1))
+            self.b.top = saved
+        return self._sol
+
+    def run(self, node, st):
+        b = self.b
+        if isinstance(node, CC):
+            c = b.cc(node.bytes_)
+            L = b.AND(self.P(st), c)
+            return (L, None)
+        if isinstance(node, Seq):
+            for it in node.items:
+                st = self.run(it, st)
+            return st
+        if isinstance(node, Alt):
+            outs = [self.run(it, st) for it in node.items]
+            L = "0"
+            P = "0"
+            for o in outs:
+                L = b.OR(L, o[0])
+                P = b.OR(P, self.P(o))
+            return (L, P)
+        if isinstance(node, Start):
+            return ("0", b.AND(self.P(st), self.sol()))
+        if isinstance(node, Rep):
+            return self.rep(node, st)
+        raise UnsupportedRegex(str(node))
+
+    def opt(self, node, st):
+        o = self.run(node, st)
+        return (self.b.OR(st[0], o[0]), self.b.OR(self.P(st), self.P(o)))
+
+    def rep(self, node, st):
+        b = self.b
+        for _ in range(node.lo):
+            st = self.run(node.item, st)
+        if node.hi is not None:
+            for _ in range(node.hi - node.lo):
+                st = self.opt(node.item, st)
+            return st
+        return self.star(node.item, st)
+
+    def star(self, item, st):
+        b = self.b
+        P = self.P(st)
+        if isinstance(item, CC):
+            c = b.cc(item.bytes_)
+            if self.use_matchstar:
+                ms = b.MATCHSTAR(P, c)
+            else:
+                ms = self._star_loop_cc(P, c)
+            return (b.OR(st[0], b.AND(ms, c)), ms)
+        # general star: while loop over the frontier of post-positions
+        test = b.fresh("test")
+        accum = b.fresh("accum")
+        accL = b.fresh("accL")
+        b.assign(test, P)
+        b.assign(accum, P)
+        b.assign(accL, "0")
+        body: List = []
+        b.scopes.append((body, {}))
+        o = self.run(item, ("0", test))
+        px = self.P(o)
+        nacc = b.NOT(accum)
+        new = b.AND(px, nacc)
+        b.assign(accum, b.OR(accum, px) if px != "0" else accum)
+        b.assign(accL, b.OR(accL, o[0]) if o[0] != "0" else accL)
+        b.assign(test, new)
+        b.scopes.pop()
+        b.scopes[-1][0].append(While(test, body))
+        return (b.OR(st[0], accL), accum)
+
+    def _star_loop_cc(self, P, c):
+        """icgrep's -disable-matchstar form of MatchStar(P, c)."""
+        b = self.b
+        test = b.fresh("test")
+        accum = b.fresh("accum")
+        b.assign(test, P)
+        b.assign(accum, P)
+        body: List = []
+        b.scopes.append((body, {}))
+        m1 = b.emit("and", (test, c), cse=False)
+        adv = b.emit("advance", (m1,), shift=1, cse=False)
+        nacc = b.emit("not", (accum,), cse=False)
+        new = b.emit("and", (adv, nacc), cse=False)
+        b.assign(accum, b.emit("or", (adv, accum), cse=False))
+        b.assign(test, new)
+        b.scopes.pop()
+        b.scopes[-1][0].append(While(test, body))
+        return accum
+
+
+def compile_group(regexes: List[str], matchstar: bool = True) -> Group:
+    """Compile a regex group to one Pablo program.
+
+    The group result is the OR of the member regexes' match-end streams, the shape
+    BitGen's CUDA backend produces per group (``bitgen/bitparser/bitstream_parser.py:270-276``).
+    ``regex_results`` holds each member's own stream.
+    """
+    b = _Builder()
+    results = []
+    for r in regexes:
+        ast = parse_regex(r)
+        comp = _Compiler(b, matchstar)
+        L, _ = comp.run(ast, ("0", "1"))
+        results.append(L)
+    acc = "0"
+    for L in results:
+        acc = b.OR(acc, L)
+    res = acc
+    # give the group result and every per-regex result a stable, distinct name
+    names = []
+    for i, L in enumerate(results):
+        nm = f"re_{i}"
+        b.scopes[0][0].append(Op(nm, "assign", (L,)))
+        names.append(nm)
+    b.scopes[0][0].append(Op("result", "assign", (res,)))
+    return Group(b.stmts, "result", regex_results=names, regexes=list(regexes))
+
+
+def compile_regex(regex: str, matchstar: bool = True) -> Group:
+    return compile_group([regex], matchstar=matchstar)

@@ -1,0 +1,142 @@
+/* bitgen_gb300: C ABI of the GB300 (sm_103a) bitstream execution engine.
+ *
+ * The entry points replace, one for one, what BitGen's CUDA backend binds for its hot path:
+ *
+ *   bg_transpose         <- byte_stream_transpose(bytestream, bitstream)
+ *                           bitgen/template/cuda/pybind.cpp:9, bitgen/template/cuda/kernel.cu:102-124
+ *   bg_program_create    <- CUDA_Kernel.init / init_single (NVRTC compile + module load)
+ *                           bitgen/backend/cuda/cuda_kernel.py:64-171
+ *   bg_program_destroy   <- CUDA_Kernel.free   bitgen/backend/cuda/cuda_kernel.py:400-406
+ *   bg_plan_create       <- init_args (result / scratch allocation, kernel argument packing)
+ *                           bitgen/backend/cuda/template/template.py:9-112
+ *   bg_plan_launch       <- run_kernel / CUDA_Kernel.run (cuLaunchKernel)
+ *                           template.py:116-121, cuda_kernel.py:411-427
+ *   bg_plan_sync         <- the cuStreamSynchronize + checkCudaErrors after each run
+ *                           cuda_kernel.py:35-47,411-427
+ *   bg_interp_*          <- the reference's whole-stream semantics of Pablo while/if
+ *                           (bitgen/inst/inst_block_while.py:137-153, inst_block_if.py:314-342)
+ *
+ * All pointers to device memory are plain CUDA device pointers; `stream` is a cudaStream_t
+ * (NULL = legacy default stream).  Every function returns a bg_status; none exits the process
+ * (the reference's transpose calls exit() on a CUDA error, kernel.cu:7-15).
+ * A bg_program / bg_plan must be used from one host thread at a time.
+ */
+#ifndef BITGEN_GB300_H
+#define BITGEN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bg_status {
+  BG_OK = 0,
+  BG_ERR_INVALID = 1,  /* bad argument, shape or layout                           */
+  BG_ERR_CUDA = 2,     /* a CUDA runtime call failed                              */
+  BG_ERR_COMPILE = 3,  /* NVRTC rejected the program (see bg_program_log)         */
+  BG_ERR_TIMEOUT = 4,  /* a bounded device wait (carry look-back) gave up         */
+  BG_ERR_ALIGN = 5,    /* an input pointer or offset is not 16-byte aligned        */
+  BG_ERR_NOMEM = 6,    /* device or host allocation failed                        */
+  BG_ERR_DEVICE = 7    /* kernel reported an internal inconsistency               */
+} bg_status;
+
+#define BG_INPUT_BYTES 0 /* raw bytes, transposed inside the scan kernel             */
+#define BG_INPUT_BASIS 1 /* reference basis planes uint32 [8][W] per input            */
+
+const char *bg_status_string(int status);
+/* Human-readable detail of the last failing call on this host thread. */
+const char *bg_last_error(void);
+/* 1 if a CUDA device is usable by this process, 0 otherwise. */
+int bg_device_available(void);
+
+/* Byte -> basis transpose.  bytes: uint8 [n_inputs][n_bytes_padded] (n_bytes_padded % 32 == 0,
+ * 16-byte aligned); basis: uint32 [n_inputs][8][n_bytes_padded / 32].  Plane i holds bit 7-i
+ * of every byte; character 32w+j is bit 31-j of word w.  Asynchronous on `stream`. */
+int bg_transpose(const uint8_t *bytes, uint32_t *basis, int64_t n_bytes_padded, int64_t n_inputs,
+                 void *stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Fused scan programs (CUDA C++ generated by bitgen_gb300.compiler, compiled with NVRTC for
+ * sm_103a).  `source` may #include "bg_device.cuh" and "bg_params.h": the library supplies them.
+ * ------------------------------------------------------------------------------------- */
+typedef struct bg_program bg_program;
+typedef struct bg_kernel_desc {
+  const char *source;
+  size_t source_len;
+  const char *name;   /* __global__ entry point                                       */
+  int32_t n_outputs;  /* output streams written by one launch                          */
+  int32_t n_adds;     /* MatchStar / ScanThru additions (look-back record sets)         */
+  int32_t halo_lanes; /* tile geometry: 32 lanes, the first halo_lanes re-computed      */
+  int32_t wpt;        /* 32-bit words per lane                                          */
+  int32_t block;      /* threads per CTA                                                */
+} bg_kernel_desc;
+
+int bg_program_create(const bg_kernel_desc *desc, bg_program **out);
+/* Compile only (no device needed): returns BG_OK or BG_ERR_COMPILE, log copied into log_buf. */
+int bg_nvrtc_check(const char *source, size_t source_len, const char *name, char *log_buf,
+                   size_t log_len);
+/* Copies the NVRTC log (NUL-terminated, truncated to len) into buf. */
+int bg_program_log(const bg_program *prog, char *buf, size_t len);
+/* Registers, local memory and shared memory per thread/CTA of the compiled kernel. */
+int bg_program_info(const bg_program *prog, int32_t *regs, int32_t *local_bytes,
+                    int32_t *max_blocks_per_sm);
+int bg_program_destroy(bg_program *prog);
+
+/* Where the inputs and outputs of one launch live.  All arrays are host arrays, copied. */
+typedef struct bg_layout {
+  int32_t input_kind;     /* BG_INPUT_BYTES or BG_INPUT_BASIS                              */
+  int32_t n_inputs;
+  const int64_t *in_off;  /* [n_inputs] byte offset (bytes; multiple of 16) or word offset of
+                             plane 0 (basis)                                               */
+  const int64_t *in_len;  /* [n_inputs] characters in each input                          */
+  int64_t basis_stride;   /* words between the 8 planes of one input (basis kind)          */
+  const int64_t *out_off; /* [n_inputs] word offset of each input inside an output stream  */
+  int64_t out_stride;     /* words between consecutive output streams                      */
+} bg_layout;
+
+typedef struct bg_plan bg_plan;
+int bg_plan_create(bg_program *prog, const bg_layout *layout, bg_plan **out);
+/* Number of tiles one launch processes. */
+int64_t bg_plan_tiles(const bg_plan *plan);
+/* Bound (clock64 cycles, 0 = default of about 1 s) for every look-back wait of later launches.
+ * debug_wait_tile >= 0 makes that tile first wait on a record no kernel writes, so that the
+ * bound and the BG_ERR_TIMEOUT report can be exercised without faulting or hanging the GPU. */
+int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t debug_wait_tile);
+/* Enqueue one scan on `stream`: input is the device base of the bytes / basis planes;
+ * out_streams (may be NULL) receives n_outputs streams in the reference bit layout, positions at
+ * or beyond an input's length cleared; counts (may be NULL) receives uint64 popcounts
+ * [n_outputs][n_inputs] (zeroed by the call).  Only asynchronous work is enqueued, so the call
+ * can be captured into a CUDA graph. */
+int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
+                   unsigned long long *counts, void *stream);
+/* Wait for `stream`, then report (and clear) device-side errors of earlier launches. */
+int bg_plan_sync(bg_plan *plan, void *stream);
+int bg_plan_destroy(bg_plan *plan);
+
+/* ---------------------------------------------------------------------------------------
+ * Whole-stream executor for programs that keep while / if blocks (global any-bit semantics).
+ * The program is a flat instruction list:
+ *   op = 0 AND, 1 OR, 2 XOR, 3 NOT, 4 SEL, 5 ADVANCE, 6 MATCHSTAR, 7 SCANTHRU, 8 COPY,
+ *        9 WHILE (a = condition slot, shift = body length), 10 IF (a = condition slot,
+ *        shift = then length, b = else length; else body follows the then body)
+ *   dst/a/b/c are variable slots; slot 0..7 = basis0..7, slot 8 = all zeros, 9 = all ones.
+ * ------------------------------------------------------------------------------------- */
+typedef struct bg_instr {
+  int32_t op, dst, a, b, c, shift;
+} bg_instr;
+typedef struct bg_interp bg_interp;
+int bg_interp_create(const bg_instr *code, int32_t n_code, int32_t n_slots,
+                     const int32_t *out_slots, int32_t n_outputs, bg_interp **out);
+/* Runs the program over each input of the layout (basis kind or bytes kind), synchronously.
+ * max_iterations bounds every while loop (0 = no bound); exceeding it returns BG_ERR_TIMEOUT. */
+int bg_interp_run(bg_interp *prog, const bg_layout *layout, const void *input,
+                  uint32_t *out_streams, unsigned long long *counts, int64_t max_iterations,
+                  void *stream);
+int bg_interp_destroy(bg_interp *prog);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,130 @@
+"""Independent regex oracle: byte-level Thompson NFA simulation (test infrastructure only).
+
+It shares nothing with the bitstream compiler except the regex parser: the parsed regex is
+turned into an epsilon-NFA and simulated position by position, injecting the start state at
+every position (matches may start anywhere).  Bit ``p`` of the result is set iff some non-empty
+match ends with the byte at ``p``.  ``^`` holds at position 0 and after an LF.  This is the
+match-end convention stated in ``bitgen_gb300.regex`` for BitGen's count check against icgrep
+(``bitgen/from_icgrep.py:59-121``): the count of a group is the popcount of the OR of its
+regexes' streams (``bitgen/bitstream.py:60-61``).
+"""
+
+from __future__ import annotations
+
+from bitgen_gb300.regex import CC, Alt, Rep, Seq, Start, parse_regex
+
+LF = 0x0A
+
+
+class _NFA:
+    def __init__(self):
+        self.kind = []   # 'eps' | 'cc' | 'sol' | 'acc'
+        self.arg = []    # byte set for 'cc'
+        self.out = []    # list of successor ids
+
+    def new(self, kind, arg=None):
+        self.kind.append(kind)
+        self.arg.append(arg)
+        self.out.append([])
+        return len(self.kind) - 1
+
+    def frag(self, node):
+        """Return (entry, exit) state ids; exit is an 'eps' state with no successors yet."""
+        if isinstance(node, CC):
+            a = self.new("cc", node.bytes_)
+            e = self.new("eps")
+            self.out[a].append(e)
+            return a, e
+        if isinstance(node, Start):
+            a = self.new("sol")
+            e = self.new("eps")
+            self.out[a].append(e)
+            return a, e
+        if isinstance(node, Seq):
+            a = self.new("eps")
+            cur = a
+            for it in node.items:
+                s, e = self.frag(it)
+                self.out[cur].append(s)
+                cur = e
+            return a, cur
+        if isinstance(node, Alt):
+            a = self.new("eps")
+            e = self.new("eps")
+            for it in node.items:
+                s, x = self.frag(it)
+                self.out[a].append(s)
+                self.out[x].append(e)
+            return a, e
+        if isinstance(node, Rep):
+            a = self.new("eps")
+            cur = a
+            for _ in range(node.lo):
+                s, x = self.frag(node.item)
+                self.out[cur].append(s)
+                cur = x
+            if node.hi is None:
+                s, x = self.frag(node.item)
+                loop = self.new("eps")
+                self.out[cur].append(loop)
+                self.out[loop].append(s)
+                self.out[x].append(loop)
+                e = self.new("eps")
+                self.out[loop].append(e)
+                return a, e
+            e = self.new("eps")
+            for _ in range(node.hi - node.lo):
+                s, x = self.frag(node.item)
+                self.out[cur].append(s)
+                self.out[cur].append(e)
+                cur = x
+            self.out[cur].append(e)
+            return a, e
+        raise TypeError(node)
+
+
+def match_ends(regex: str, data: bytes) -> int:
+    """Match-end stream of ``regex`` over ``data`` as a big int (bit p = position p)."""
+    nfa = _NFA()
+    start, end = nfa.frag(parse_regex(regex))
+    acc = nfa.new("acc")
+    nfa.out[end].append(acc)
+
+    def closure(states, sol):
+        seen = set()
+        stack = list(states)
+        while stack:
+            s = stack.pop()
+            if s in seen:
+                continue
+            seen.add(s)
+            k = nfa.kind[s]
+            if k == "eps":
+                stack.extend(nfa.out[s])
+            elif k == "sol" and sol:
+                stack.extend(nfa.out[s])
+        return seen
+
+    result = 0
+    cur = set()
+    n = len(data)
+    for p in range(n):
+        sol = p == 0 or data[p - 1] == LF
+        active = closure(cur | {start}, sol)
+        byte = data[p]
+        nxt = set()
+        for s in active:
+            if nfa.kind[s] == "cc" and byte in nfa.arg[s]:
+                nxt.update(nfa.out[s])
+        sol_next = byte == LF
+        cur = closure(nxt, sol_next)
+        if acc in cur:
+            result |= 1 << p
+    return result
+
+
+def group_match_ends(regexes, data: bytes) -> int:
+    r = 0
+    for x in regexes:
+        r |= match_ends(x, data)
+    return r

@@ -1,0 +1,137 @@
+"""Generate the golden vectors under tests/golden/ by running the reference's own Python code.
+
+Run in a checkout where the reference BitGen tree is available (path in BITGEN_REF, default
+/root/reference); it is imported read-only with stub modules for its optional dependencies
+(pandas, colorlog, colorama, matplotlib, the compiled ``bitgen.cuda`` extension).  The GPU-less
+parts of the reference are what pin the oracle:
+
+* ``transpose.npz``  - ``transpose_bytestream_to_bitstream_py`` (bitgen/bitstream.py:228-258) on
+  seeded random inputs, including all 256 byte values and ragged lengths;
+* ``ops.npz``        - numpy stream templates ``bs_advance`` / ``bs_add`` / ``bs_match_star``
+  (bitgen/template/template.py:63-103) on seeded random bool streams;
+* ``parser.json``    - the reference parser's instruction list (type, operands, result) for the
+  hand-written fixture bitgen/bitparser/xml_lexical_parsing.pablo and for Pablo emitted by this
+  project (while-loop form), to pin the dialect this project's parser accepts.
+
+Usage:  python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("BITGEN_REF", "/root/reference")
+
+
+def import_reference():
+    os.environ.setdefault("PYTHONDONTWRITEBYTECODE", "1")
+    sys.dont_write_bytecode = True
+    for name in ("pandas", "colorlog", "colorama", "matplotlib", "matplotlib.pyplot"):
+        m = types.ModuleType(name)
+        m.Fore = types.SimpleNamespace(RED="", GREEN="", YELLOW="", BLUE="", RESET="", CYAN="")
+        m.Style = types.SimpleNamespace(RESET_ALL="", BRIGHT="")
+        m.ColoredFormatter = object
+        sys.modules.setdefault(name, m)
+    cuda = types.ModuleType("bitgen.cuda")
+    cuda.byte_stream_transpose = lambda *a, **k: None
+    cuda.cub_exclusive_scan = lambda *a, **k: None
+    sys.modules["bitgen.cuda"] = cuda
+    sys.path.insert(0, REF)
+    import bitgen.config as cfg  # noqa: E402
+    cfg.set_config("backend", "cuda")
+    return cfg
+
+
+def main():
+    cfg = import_reference()
+    import torch
+    from bitgen import bitstream as ref_bs
+    from bitgen.template import template as ref_tpl
+    from bitgen.bitparser import BitstreamParser
+
+    # ---- transpose: the CPU path ends in .cuda(); keep the tensor on the host -------------
+    torch.Tensor.cuda = lambda self, *a, **k: self
+    rng = np.random.default_rng(20261203)
+    cases = {}
+    lens = [32, 64, 96, 320, 1024]
+    for i, n in enumerate(lens):
+        cases[f"in{i}"] = rng.integers(0, 256, size=n, dtype=np.uint8)
+    cases["in_all256"] = np.arange(256, dtype=np.uint8).repeat(1)
+    cases["in_multi"] = rng.integers(0, 256, size=(3, 128), dtype=np.uint8)
+    out = {}
+    for k, v in cases.items():
+        arr = v if v.ndim == 2 else v[None, :]
+        t = torch.from_numpy(arr.copy())[None]           # [S=1, M, n]
+        planes = ref_bs.transpose_bytestream_to_bitstream_py(t).numpy()
+        out[k] = v
+        out[k.replace("in", "out", 1)] = planes.astype(np.uint32)
+    np.savez_compressed(os.path.join(HERE, "transpose.npz"), **out)
+
+    # ---- numpy op templates ------------------------------------------------------------
+    ops = {}
+    for i in range(12):
+        n = int(rng.integers(1, 300))
+        dens = [0.05, 0.5, 0.95][i % 3]
+        m = rng.random(n) < dens * 0.2
+        c = rng.random(n) < dens
+        k = int(rng.integers(1, 70))
+        ops[f"m{i}"] = m
+        ops[f"c{i}"] = c
+        ops[f"k{i}"] = np.int64(k)
+        ops[f"adv{i}"] = ref_tpl.bs_advance(m.copy(), k) if k < n else np.zeros(n, bool)
+        ops[f"add{i}"] = ref_tpl.bs_add(m.copy(), c.copy())
+        ops[f"ms{i}"] = ref_tpl.bs_match_star(m.copy(), c.copy())
+    np.savez_compressed(os.path.join(HERE, "ops.npz"), **ops)
+
+    # ---- parser ------------------------------------------------------------------------
+    sys.path.insert(0, REPO)
+    from bitgen_gb300.regex import compile_group
+
+    def dump(path):
+        p = BitstreamParser()
+        insts = p.parse_file(path)
+        names = p.var_name_map
+
+        def enc(inst):
+            d = {"type": inst.type.name, "ret": names.get(inst.ret, str(inst.ret))
+                 if not isinstance(inst.ret, list) else [names.get(r, r) for r in inst.ret]}
+            if inst.type.name == "WHILE":
+                d["cond"] = names[inst.condition]
+                d["body"] = [enc(x) for x in inst.body.body]
+            else:
+                ops_ = []
+                for o in inst.operands:
+                    ops_.append(names.get(o, o) if isinstance(o, int) else str(o))
+                d["operands"] = ops_
+            return d
+
+        return [enc(x) for x in insts]
+
+    parser_cases = {"xml_lexical_parsing": os.path.join(REF, "bitgen/bitparser/xml_lexical_parsing.pablo")}
+    emitted = {}
+    import tempfile
+    tmpdir = tempfile.mkdtemp(prefix="bg_golden_")
+    for name, rx in {"literal": ["abc"], "class_star": ["a[bc]*d"], "group_star": ["q(rs)*t"],
+                     "alt": ["(ab|cd)e", "x{2,3}y"]}.items():
+        g = compile_group(rx, matchstar=False)
+        txt = g.to_pablo()
+        path = os.path.join(tmpdir, f"golden_{name}.pablo")
+        with open(path, "w") as f:
+            f.write(txt)
+        parser_cases[name] = path
+        emitted[name] = txt
+    res = {k: dump(v) for k, v in parser_cases.items()}
+    with open(os.path.join(HERE, "parser.json"), "w") as f:
+        json.dump({"reference_ir": res, "emitted_pablo": emitted}, f, indent=1, sort_keys=True)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,207 @@
+"""GPU parity: the fused sm_103a scan kernels and the whole-stream executor against the oracle.
+
+Every comparison is bit-exact (integer work): output streams in the reference layout and their
+popcounts.  Inputs are seeded; sizes keep the big-integer oracle within seconds.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from bitgen_gb300.compiler import Tuning
+from bitgen_gb300.engine import Program, basis_input, pack_bytes, transpose
+from bitgen_gb300.pablo import parse_pablo
+from bitgen_gb300.refir import group_from_ir
+from bitgen_gb300.regex import compile_group
+from bitgen_gb300 import workloads
+from oracle.pablo_ref import transpose_ref
+from tests.helpers import first_diff, oracle_streams, rand_text
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def check(prog: Program, groups, items, per_regex=False):
+    inp = pack_bytes(items)
+    res = prog.scan(inp)
+    torch.cuda.synchronize()
+    streams = res.streams.cpu().numpy()
+    counts = res.counts.cpu().numpy()
+    for i, data in enumerate(items):
+        data = np.asarray(data, dtype=np.uint8)
+        want = oracle_streams(groups, data, per_regex)
+        assert len(want) == prog.n_outputs
+        o = res.word_offsets[i]
+        W = res.words[i]
+        for k, w in enumerate(want):
+            got = streams[k, o:o + W]
+            d = first_diff(got, w)
+            assert d is None, f"input {i} (n={data.size}) output {k}: {d}"
+            assert counts[k, i] == int(np.unpackbits(w.view(np.uint8)).sum())
+
+
+SMALL = None
+
+
+def small():
+    global SMALL
+    if SMALL is None:
+        ps, text = workloads.small_workload()
+        groups = [compile_group(g) for g in ps.groups(4)]
+        SMALL = (ps, text, groups)
+    return SMALL
+
+
+@pytest.mark.parametrize("wpt,skip,block", [(1, 1, 256), (2, 1, 256), (4, 1, 128), (2, 0, 64), (2, 3, 256)])
+def test_small_workload_tunings(cuda, wpt, skip, block):
+    ps, text, groups = small()
+    prog = Program(groups, tuning=Tuning(wpt=wpt, skip_interval=skip, block=block))
+    check(prog, groups, [text])
+    prog.close()
+
+
+def test_small_workload_per_regex(cuda):
+    ps, text, groups = small()
+    prog = Program(groups, per_regex=True)
+    check(prog, groups, [text], per_regex=True)
+
+
+def test_ragged_lengths_and_tile_edges(cuda):
+    groups = [compile_group(["ab[0-9]*c", "x.{2,4}y"]), compile_group(["q+", "[^a-m]z"])]
+    prog = Program(groups, tuning=Tuning(wpt=1))
+    tile_chars = prog.spec.tile_words * 32
+    lens = list(range(0, 70)) + [tile_chars + d for d in (-33, -32, -1, 0, 1, 31, 32, 33)] + \
+        [3 * tile_chars + 7, 17 * tile_chars - 5]
+    items = [rand_text(n, 100 + n, b"abcqxyz0123\n") for n in lens]
+    check(prog, groups, items)
+
+
+def test_long_carries_across_many_tiles(cuda):
+    # '.*' on text without LF: one early prefix match turns every later position on
+    groups = [compile_group(["k9.*zz"]), compile_group(["a[ab]*b", "c[^d]*e"])]
+    n = 300_000
+    t = rand_text(n, 7, b"abcefgh")
+    t[5:7] = np.frombuffer(b"k9", np.uint8)
+    t[-3:] = np.frombuffer(b"zz ", np.uint8)
+    t2 = np.full(n, ord("a"), np.uint8)  # one 'a' run spanning every tile, 'b' at the end
+    t2[-1] = ord("b")
+    for wpt in (1, 4):
+        prog = Program(groups, tuning=Tuning(wpt=wpt))
+        check(prog, groups, [t, t2, t2[:1000], t[:5]])
+
+
+def test_scanthru_and_while_forms(cuda):
+    src = """
+lf = (basis4 & basis6)
+a = (~basis0)
+m = (a & basis1)
+s = pablo.ScanThru(m, a)
+st = pablo.MatchStar(m, lf)
+r = (s | st)
+output.matches = r
+"""
+    g = parse_pablo(src)
+    items = [rand_text(n, n, bytes(range(0, 256))) for n in (1, 100, 5000, 70000)]
+    check(Program([g]), [g], items)
+    # icgrep's -disable-matchstar loop form compiles to MatchStar on the fused path and runs
+    # literally on the whole-stream executor; both agree with the oracle
+    gw = compile_group(["ab*c", "x(yz)*w", "[0-9]+k"], matchstar=False)
+    items = [rand_text(n, n, b"abcxyzwk0123") for n in (10, 999, 40000)]
+    fused = Program([gw])
+    assert fused.fused
+    check(fused, [gw], items)
+    check(Program([gw], executor="interp"), [gw], items)
+
+
+def test_reference_fixture_program_on_executor(cuda):
+    with open(os.path.join(GOLDEN, "parser.json")) as f:
+        ir = json.load(f)["reference_ir"]["xml_lexical_parsing"]
+    g = group_from_ir(ir)
+    prog = Program([g])
+    assert not prog.fused  # its while loop is not a MatchStar loop: whole-stream semantics
+    items = [np.frombuffer(b"<a<bcd<EFGH>x<yz>" * k, np.uint8) for k in (1, 7, 300)]
+    items.append(rand_text(5000, 3, b"<>abAB xyz"))
+    check(prog, [g], items)
+
+
+def test_if_else_whole_stream(cuda):
+    src = """
+a = (basis1 & basis2)
+b = (~basis3)
+if a:
+  x = pablo.Advance(a, 3)
+else:
+  x = b
+y = (x | a)
+output.matches = y
+"""
+    g = parse_pablo(src)
+    items = [rand_text(100, 1, b"0123"), rand_text(100, 2, b"abcd"), rand_text(4000, 3)]
+    check(Program([g]), [g], items)
+
+
+def test_fused_equals_executor_on_throughput_patterns(cuda):
+    ps = workloads.throughput_patterns(seed=3, n=48)
+    groups = [compile_group(g) for g in ps.groups(4)]
+    base = workloads.plant(workloads.printable_text(1 << 16, 4), ps.witnesses, 1024, 5)
+    a = Program(groups)
+    b = Program(groups, executor="interp")
+    inp = pack_bytes([base])
+    ra, rb = a.scan(inp), b.scan(inp)
+    assert torch.equal(ra.streams, rb.streams)
+    assert torch.equal(ra.counts, rb.counts)
+    assert int(ra.counts.sum()) > 0
+
+
+def test_basis_input_matches_bytes(cuda):
+    ps, text, groups = small()
+    prog = Program(groups)
+    M = 3
+    npad = -(-text.size // 32) * 32
+    bytestream = torch.zeros((1, M, npad), dtype=torch.uint8, device=cuda)
+    for m in range(M):
+        bytestream[0, m, :text.size] = torch.from_numpy(np.roll(text, 97 * m).copy())
+    basis = torch.zeros((1, M, 8, npad // 32), dtype=torch.uint32, device=cuda)
+    transpose(bytestream, basis)
+    res = prog.scan(basis_input(basis, [text.size] * M))
+    for m in range(M):
+        want = oracle_streams(groups, np.roll(text, 97 * m))
+        for k, w in enumerate(want):
+            assert first_diff(res.stream(k, m).cpu().numpy(), w) is None
+
+
+def test_transpose_against_reference_vectors(cuda):
+    gold = np.load(os.path.join(GOLDEN, "transpose.npz"))
+    for k in gold.files:
+        if not k.startswith("in"):
+            continue
+        src = gold[k]
+        want = gold[k.replace("in", "out", 1)]
+        arr = src if src.ndim == 2 else src[None]
+        t = torch.from_numpy(arr.copy()).to(cuda)[None].contiguous()
+        out = torch.zeros((1, arr.shape[0], 8, arr.shape[1] // 32), dtype=torch.uint32, device=cuda)
+        transpose(t, out)
+        assert np.array_equal(out.cpu().numpy().reshape(want.shape), want), k
+
+
+@pytest.mark.parametrize("n,m", [(32, 1), (1 << 20, 1), (4096, 5), (96, 130)])
+def test_transpose_random(cuda, n, m):
+    rng = np.random.default_rng(n + m)
+    a = rng.integers(0, 256, size=(m, n), dtype=np.uint8)
+    t = torch.from_numpy(a).to(cuda)[None].contiguous()
+    out = torch.zeros((1, m, 8, n // 32), dtype=torch.uint32, device=cuda)
+    transpose(t, out)
+    got = out.cpu().numpy()[0]
+    for i in range(m):
+        assert np.array_equal(got[i], transpose_ref(a[i])), i
+
+
+def test_many_inputs_one_launch(cuda):
+    ps = workloads.throughput_patterns(seed=11, n=24)
+    groups = [compile_group(g) for g in ps.groups(3)]
+    lens = workloads.batched_lengths(300, seed=12, median=900, lo=1, hi=5000)
+    items = workloads.batched_inputs(lens, 13, ps.witnesses)
+    check(Program(groups), groups, items)
