@@ -1,0 +1,305 @@
+"""Benchmark: input GB/s of the fused bitstream scan on the 256-regex throughput workload.
+
+Workload (one step = one scan of the whole input): 256 seeded synthetic regexes (8-40 chars,
+30% with an unbounded repetition), 16 groups of 16, over 1 MiB of printable ASCII with ~1
+planted match per 4 KiB, tiled to 256 MiB.  Each step writes the 16 per-group match streams
+(the reference's result shape) and the per-group match counts.  The input (256 MiB) is larger
+than L2 (129 MB), so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the CPU evaluator (``oracle/bg_cpu.c``, all host threads) on a bounded
+sample of the same workload: the reference's own GPU path cannot execute these programs (its
+parser rejects MatchStar, ``bitgen/bitparser/bitstream_parser.py:202-211``) and its CPU
+comparison point, icgrep, is not part of the reference tree.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "input GB/s @256 regexes (bit-exact)"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--bytes", type=int, default=256 << 20, help="input bytes per GPU")
+    ap.add_argument("--regexes", type=int, default=256)
+    ap.add_argument("--groups", type=int, default=16)
+    ap.add_argument("--wpt", type=int, default=0, help="words per lane (0 = autotuned default)")
+    ap.add_argument("--cpu-sample", type=int, default=4 << 20, help="bytes of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    import numpy as np
+    from bitgen_gb300 import workloads
+    ps, base, reps = workloads.throughput_workload(total_bytes=args.bytes, n_regex=args.regexes)
+    groups = ps.groups(args.groups)
+    return ps, groups, base, reps
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def recorded_traffic():
+    """DRAM bytes per launch of the scan kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "bg_scan_throughput_256re.md")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_full_launch:"):
+                return int(float(line.split(":", 1)[1].split()[0]))
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-i", str(index), "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.3)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(groups, base, sample_bytes):
+    """C evaluator on the host: all 16 groups on their own threads over a bounded sample."""
+    import numpy as np
+    from oracle import cpu
+    from bitgen_gb300.regex import compile_group
+
+    gs = [compile_group(g) for g in groups]
+    reps = -(-sample_bytes // base.size)
+    data = np.tile(base, reps)[:sample_bytes]
+    threads = min(os.cpu_count() or 1, len(gs))
+    cpu.run_groups(gs, data[:1 << 16], threads=threads)  # warm
+    t0 = time.perf_counter()
+    _, counts = cpu.run_groups(gs, data, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(sample_bytes / dt / 1e9, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sample_bytes} bytes of the same input, all {len(gs)} groups, one group per thread "
+                      f"(C word-parallel evaluator, oracle/bg_cpu.c), {dt:.2f} s"}, counts
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    ps, groups, base, reps = workload(args)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb, _ = cpu_baseline(groups, base, args.cpu_sample)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded)",
+            "config": {"workload": f"throughput: {args.regexes} synthetic regexes, {args.groups} groups, "
+                                   f"CPU sample of {args.cpu_sample} bytes"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from bitgen_gb300.compiler import Tuning
+    from bitgen_gb300.engine import Program, bytes_input, out_layout
+    from bitgen_gb300.regex import compile_group
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    ps, groups, base, reps = workload(args)
+    gs = [compile_group(g) for g in groups]
+    tuning = Tuning(wpt=args.wpt or 2)
+    t0 = time.perf_counter()
+    prog = Program(gs, tuning=tuning)
+    compile_s = time.perf_counter() - t0
+    n = args.bytes
+    host = torch.from_numpy(np.tile(base, reps)[:n].copy()).pin_memory()
+    data = host.to(dev)
+    inp = bytes_input(data)
+    offs, words, total = out_layout([n])
+    out = torch.empty((prog.n_outputs, total), dtype=torch.uint32, device=dev)
+    counts = torch.empty((prog.n_outputs, 1), dtype=torch.int64, device=dev)
+    plan = prog.plan(inp, offs, total)
+    stream = torch.cuda.current_stream(dev)
+    sp = int(stream.cuda_stream)
+
+    def step():
+        plan.launch(data.data_ptr(), out.data_ptr(), counts.data_ptr(), sp)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    plan.sync(sp)
+    # bit-exact self-check of this very configuration against the CPU evaluator (rank 0, sample)
+    check = None
+    if rank == 0 and not args.no_cpu:
+        cb, cpu_counts = cpu_baseline(groups, base, args.cpu_sample)
+        sub = bytes_input(data[:args.cpu_sample].contiguous())
+        r = prog.scan(sub, streams=False, counts=True)
+        gpu_counts = [int(x) for x in r.counts[:, 0].tolist()]
+        check = gpu_counts == list(cpu_counts)
+    else:
+        cb = None
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = Clocks(local)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    plan.sync(sp)
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    # per-launch kernel time (scan kernel only) for the roofline
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    kt = []
+    for _ in range(5):
+        k0.record(stream)
+        step()
+        k1.record(stream)
+        torch.cuda.synchronize(dev)
+        kt.append(k0.elapsed_time(k1))
+    kernel_ms = statistics.median(kt)
+
+    # end to end through the public API: pinned host bytes in, counts out, every step
+    e2e_steps = max(3, min(args.steps, 10))
+    h_counts = torch.empty((prog.n_outputs, 1), dtype=torch.int64).pin_memory()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        data.copy_(host, non_blocking=True)
+        step()
+        h_counts.copy_(counts, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+
+    t = torch.tensor([ms, kernel_ms, e2e_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms, kernel_ms, e2e_ms = [float(x) for x in t.tolist()]
+    total_bytes = n * world
+    value = total_bytes / (ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    b_alg = n + prog.n_outputs * ((n + 31) // 32) * 4   # input once + each output stream once
+    achieved = b_alg / (kernel_ms / 1e3) / 1e9
+    info = prog.info()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded regexes and printable-ASCII text)",
+        "config": {"workload": f"throughput: {args.regexes} synthetic regexes in {len(gs)} groups over "
+                               f"{n >> 20} MiB printable ASCII (1 MiB tiled), per-group match streams + counts",
+                   "regexes": args.regexes, "groups": len(gs), "input_bytes": n,
+                   "parallelism": f"replicas x{world}", "l2": "input larger than L2 (no flush)",
+                   "tuning": {"wpt": info.get("wpt"), "halo_lanes": info.get("halo_lanes"),
+                              "block": tuning.block, "skip_interval": tuning.skip_interval},
+                   "registers": info.get("registers"), "adds": info.get("adds"),
+                   "compile_s": round(compile_s, 2), "bit_exact_vs_cpu_sample": check},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 5), "traffic": recorded_traffic(),
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg,
+                     "kernel_ms": round(kernel_ms, 4)},
+        "e2e": {"value": round(total_bytes / (e2e_ms / 1e3) / 1e9, 3), "unit": UNIT,
+                "h2d_bytes_per_step": n, "d2h_bytes_per_step": prog.n_outputs * 8},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    if cb is not None:
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

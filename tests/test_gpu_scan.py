@@ -108,12 +108,17 @@ output.matches = r
     check(Program([g]), [g], items)
     # icgrep's -disable-matchstar loop form compiles to MatchStar on the fused path and runs
     # literally on the whole-stream executor; both agree with the oracle
-    gw = compile_group(["ab*c", "x(yz)*w", "[0-9]+k"], matchstar=False)
+    gw = compile_group(["ab*c", "x[yz]*w", "[0-9]+k"], matchstar=False)
     items = [rand_text(n, n, b"abcxyzwk0123") for n in (10, 999, 40000)]
     fused = Program([gw])
     assert fused.fused
     check(fused, [gw], items)
     check(Program([gw], executor="interp"), [gw], items)
+    # a loop over a multi-character group stays a loop: whole-stream executor
+    gg = compile_group(["x(yz)*w", "a(bc)+d"], matchstar=False)
+    prog = Program([gg])
+    assert not prog.fused
+    check(prog, [gg], [rand_text(n, n, b"abcdxyzw") for n in (1, 500, 20000)])
 
 
 def test_reference_fixture_program_on_executor(cuda):

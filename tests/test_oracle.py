@@ -1,0 +1,184 @@
+"""CPU tests: the oracle pinned to the reference's golden vectors, and the host-side compiler.
+
+* transpose restatement == reference CPU transpose (bitgen/bitstream.py:228-258) on its vectors;
+* Advance / add / MatchStar == the reference numpy templates (bitgen/template/template.py);
+* this project's Pablo parser == the reference parser's IR (semantically, on random inputs);
+* regex emitter == independent NFA == Python ``re`` on random inputs;
+* C word-parallel oracle == big-integer oracle (block and whole-stream modes);
+* while -> MatchStar conversion preserves results.
+"""
+
+import json
+import os
+import random
+import re
+
+import numpy as np
+import pytest
+
+from bitgen_gb300.compiler import convert_star_loops, fusable, generate_kernel, Tuning, NotFusable
+from bitgen_gb300.engine import lower_interp
+from bitgen_gb300.grouping import balance_regex_groups, group_regex_in_list, regex_custom_length
+from bitgen_gb300.pablo import Op, While, parse_pablo, PabloSyntaxError
+from bitgen_gb300.refir import group_from_ir
+from bitgen_gb300.regex import UnsupportedRegex, compile_group, compile_regex
+from oracle import cpu
+from oracle.nfa_ref import match_ends
+from oracle.pablo_ref import (advance, int_to_words, matchstar, run_group, transpose_ref,
+                              words_to_int)
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def bools_to_int(b):
+    return int("".join("1" if x else "0" for x in reversed(list(b))) or "0", 2)
+
+
+def test_transpose_matches_reference_vectors():
+    g = np.load(os.path.join(GOLDEN, "transpose.npz"))
+    n = 0
+    for k in g.files:
+        if not k.startswith("in"):
+            continue
+        src, want = g[k], g[k.replace("in", "out", 1)]
+        rows = src if src.ndim == 2 else src[None]
+        for m, row in enumerate(rows):
+            assert np.array_equal(transpose_ref(row), want.reshape(-1, 8, want.shape[-1])[m]), k
+            n += 1
+    assert n >= 9
+
+
+def test_word_layout_roundtrip():
+    rng = np.random.default_rng(0)
+    for W in (1, 2, 7, 33):
+        w = rng.integers(0, 1 << 32, size=W, dtype=np.uint64).astype(np.uint32)
+        assert np.array_equal(int_to_words(words_to_int(w), W), w)
+    # position 0 is the MSB of word 0 in the reference layout
+    assert int_to_words(1, 1)[0] == 0x80000000
+
+
+def test_ops_match_reference_templates():
+    g = np.load(os.path.join(GOLDEN, "ops.npz"))
+    for i in range(12):
+        m, c, k = g[f"m{i}"], g[f"c{i}"], int(g[f"k{i}"])
+        n = m.size
+        mask = (1 << n) - 1
+        M, Cc = bools_to_int(m), bools_to_int(c)
+        assert advance(M, k, mask) == bools_to_int(g[f"adv{i}"])
+        assert (M + Cc) & mask == bools_to_int(g[f"add{i}"])
+        assert matchstar(M, Cc, mask) == bools_to_int(g[f"ms{i}"])
+
+
+def test_parser_agrees_with_reference_parser():
+    gold = json.load(open(os.path.join(GOLDEN, "parser.json")))
+    rng = np.random.default_rng(1)
+    for name, ir in gold["reference_ir"].items():
+        ref_group = group_from_ir(ir)
+        if name in gold["emitted_pablo"]:
+            mine = parse_pablo(gold["emitted_pablo"][name])
+        else:
+            mine = None
+        for n in (1, 31, 64, 257):
+            data = rng.integers(0, 256, size=n, dtype=np.uint8)
+            if name == "xml_lexical_parsing":
+                data = np.frombuffer(bytes(rng.choice(list(b"<>abAB "), size=n)), np.uint8)
+            r = run_group(ref_group, data)
+            if mine is not None:
+                assert run_group(mine, data) == r, (name, n)
+
+
+def test_parser_rejects_bad_programs():
+    for bad in ("x = (a & b)\n", "x = pablo.Foo(basis0, 1)\n", "basis0 = basis1\n", "x = (basis0 & basis1\n  y = x\n"):
+        with pytest.raises(PabloSyntaxError):
+            parse_pablo(bad)
+
+
+REGEXES = [r"abc", r"a[bc]+d", r"x.*y", r"(ab|cd)e", r"a{2,5}", r"[a-c]{3}", r"^ab", r"(^|xy)z",
+           r"a(bc)*d", r"a\d+b", r"[^a]b", r"k.{2,4}m", r"(a|b)*c", r"\x61\x62", r"a+?b", r"q(rs)+t",
+           r"[0-9]{0,2}z"]
+
+
+@pytest.mark.parametrize("matchstar_form", [True, False])
+def test_emitter_matches_nfa_and_python_re(matchstar_form):
+    rnd = random.Random(7)
+    for r in REGEXES:
+        g = parse_pablo(compile_regex(r, matchstar=matchstar_form).to_pablo())
+        pr = re.compile(r.replace("[^", "[^\\n").encode(), re.M)
+        for _ in range(6):
+            n = rnd.randint(0, 90)
+            data = bytes(rnd.choice(b"abcdxyzkmqrst\n0123") for _ in range(n))
+            want_re = 0
+            for e in range(n):
+                if any(pr.fullmatch(data, s, e + 1) for s in range(e + 1)):
+                    want_re |= 1 << e
+            assert run_group(g, data) == match_ends(r, data) == want_re, (r, data)
+
+
+def test_emitter_rejects_unsupported():
+    for r in ("a$", "(?=x)", r"\bword", "a++"):
+        with pytest.raises(UnsupportedRegex):
+            compile_regex(r)
+
+
+def test_star_loops_become_matchstar():
+    g = compile_group(["ab*c", "x[0-9]*y"], matchstar=False)
+    assert any(isinstance(s, While) for s in g.stmts)
+    conv = convert_star_loops(g.stmts)
+    assert not any(isinstance(s, While) for s in conv)
+    assert sum(isinstance(s, Op) and s.op == "matchstar" for s in conv) == 2
+    assert fusable(g)
+    rng = np.random.default_rng(3)
+    for n in (0, 5, 300):
+        data = np.frombuffer(bytes(rng.choice(list(b"abcxy0129"), size=n)), np.uint8) if n else np.zeros(0, np.uint8)
+        g2 = type(g)(conv, g.result)
+        assert run_group(g, data) == run_group(g2, data)
+    # a loop over a group (not a single class) keeps its while form
+    assert not fusable(compile_group(["q(rs)*t"], matchstar=False))
+
+
+@pytest.mark.parametrize("block_words", [1, 3, 256])
+def test_c_oracle_matches_bigint_oracle(block_words):
+    rnd = random.Random(11)
+    for ms in (True, False):
+        for trial in range(12):
+            n = rnd.randint(0, 900)
+            data = np.frombuffer(bytes(rnd.choice(b"abcdxyzkmqrst\n01") for _ in range(n)), np.uint8)
+            g = compile_group(rnd.sample(REGEXES, rnd.randint(1, 4)), matchstar=ms)
+            code, ns, outs = lower_interp([g])
+            s, c = cpu.run_code(code, ns, outs, data, block_words=block_words)
+            ref = run_group(g, data)
+            assert words_to_int(s[0]) == ref
+            assert int(c[0]) == bin(ref).count("1")
+
+
+def test_interp_lowering_reuses_slots():
+    g = compile_group([f"ab{c}d[0-9]+e" for c in "ghijklmnopqrstuv"])
+    code, n_slots, outs = lower_interp([g])
+    n_vars = len({s.dst for s in g.stmts})
+    assert n_slots < n_vars  # live ranges let slots be reused
+    for ins in code:
+        if ins[0] == 5:  # Advance never in place
+            assert ins[1] != ins[2]
+
+
+def test_halo_grows_with_advance_depth():
+    src = "a = (basis0 & basis1)\nb = pablo.Advance(a, 100)\noutput.matches = b\n"
+    g = parse_pablo(src)
+    assert generate_kernel([g], Tuning(wpt=1)).halo_lanes == 4   # ceil(100 / 32)
+    assert generate_kernel([g], Tuning(wpt=4)).halo_lanes == 1
+    src2 = src.replace("output.matches = b", "c = pablo.MatchStar(b, a)\noutput.matches = c")
+    assert generate_kernel([parse_pablo(src2)], Tuning(wpt=1)).halo_lanes == 5
+    deep = "a = (basis0 & basis1)\nb = pablo.Advance(a, 2000)\noutput.matches = b\n"
+    with pytest.raises(NotFusable):
+        generate_kernel([parse_pablo(deep)], Tuning(wpt=1))
+
+
+def test_grouping_follows_reference_rule():
+    rx = ["abc", r"\x41\x42", "[a-z]+q", "hello.*world", "x", "yy", "zzz[0-9]"]
+    assert regex_custom_length(r"\x41[abc]d") == 3
+    groups = balance_regex_groups(list(rx), 3)
+    assert sorted(sum(groups, [])) == sorted(rx)
+    loads = [sum(regex_custom_length(r) for r in g) for g in groups]
+    assert max(loads) - min(loads) <= max(regex_custom_length(r) for r in rx)
+    assert group_regex_in_list(rx[:2], 5) == [[r"\x41\x42"], ["abc"]] or len(group_regex_in_list(rx[:2], 5)) == 2
+    assert group_regex_in_list(rx, 0) == [[r] for r in rx]
