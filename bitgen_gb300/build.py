@@ -91,7 +91,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if force or jobs or _stale(LIB, objs):
         libdir = os.path.join(home, "lib64")
         tmp = LIB + ".tmp"
-        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, f"-L{libdir}", "-lnvrtc",
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, f"-L{libdir}", "-lnvrtc", "-lnvJitLink",
                "-Xlinker", f"-rpath={libdir}"]
         run(cmd)
         os.replace(tmp, LIB)

@@ -314,9 +314,12 @@ class Tuning:
     wpt: int = 2            # 32-bit words per lane
     block: int = 256        # threads per CTA
     skip_interval: int = 1  # check for an all-zero marker every k AND steps (0 = never)
+    part_cap: int = 32      # most OR-ed terms one part function computes
+    window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
+    min_blocks: int = 2     # __launch_bounds__ minimum resident blocks per SM (caps registers)
 
     def key(self):
-        return (self.wpt, self.block, self.skip_interval)
+        return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window, self.min_blocks)
 
 
 @dataclass
@@ -525,7 +528,10 @@ class _Gen:
                 return a if self.dbits[a] >= self.dbits[b] else b
         return None
 
-    def mat_chain(self, v: int) -> str:
+    def mat_chain(self, v: int, acc: Optional[List[str]] = None) -> Optional[str]:
+        """Emit the chain of zero-preserving steps ending in `v` under zero-skip guards.  With
+        `acc`, OR the value into those accumulators inside the innermost guard instead of
+        returning it."""
         d = self.d
         chain = [v]
         u = self.chain_operand(v)
@@ -545,7 +551,8 @@ class _Gen:
                 if not d.is_cc(other):
                     self.mat(other)
         name = f"v{v}"
-        self.declare_zero(name)
+        if acc is None:
+            self.declare_zero(name)
         depth = 0
         prev = rname
         ands = 0
@@ -553,36 +560,242 @@ class _Gen:
         for c in reversed(chain):
             n = d.nodes[c]
             if n.op == "and":
-                if k > 0 and ands % k == 0:
+                # the step before the first AND is dense (a class, one Advance); guards start
+                # after the first AND and then repeat every k ANDs
+                if k > 0 and ands >= 1 and (ands - 1) % k == 0:
                     self.open(self.any_expr(prev))
                     depth += 1
                 ands += 1
                 a = [prev, self.mat(side[c])]
             else:
                 a = [prev]
-            if c == v:
+            if c == v and acc is None:
                 self.emit_op(name, n, a, declare=False)
             else:
                 tmp = f"v{c}"
                 self.emit_op(tmp, n, a)
                 prev = tmp
+        if acc is not None:
+            for a_ in acc:
+                for j in range(self.t.wpt):
+                    self.emit(f"{a_}_{j} |= {name}_{j};")
         for _ in range(depth):
             self.close()
+        if acc is not None:
+            return None
         self.scopes[-1][v] = name
         return name
 
-    # kernel pieces ---------------------------------------------------------------------------
-    def body(self, outputs: Sequence[int], out_names: Sequence[str], out_base: int) -> str:
-        """Code computing and storing `outputs` (analyse() must have run)."""
+    def first_and(self, v: int) -> Optional[int]:
+        """The first AND (closest to the root) of the single-use chain ending in `v`."""
+        d = self.d
+        u, found = v, None
+        while (u is not None and d.nodes[u].op in CHAIN_OPS and not d.is_cc(u)
+               and (u == v or self.uses.get(u, 0) <= 1) and self.lookup(u) is None):
+            if d.nodes[u].op == "and":
+                found = u
+            u = self.chain_operand(u)
+        return found
+
+    def accumulate(self, v: int, accs: List[str]):
+        """OR node `v` into accumulators; a single-use chain accumulates inside its guards."""
+        n = self.d.nodes[v]
+        if (self.lookup(v) is None and n.op in CHAIN_OPS and not self.d.is_cc(v)
+                and self.uses.get(v, 0) <= 1):
+            self.mat_chain(v, acc=accs)
+            return
+        r = self.mat(v)
+        if r == "0u":
+            return
+        for a_ in accs:
+            for j in range(self.t.wpt):
+                self.emit(f"{a_}_{j} |= {self.w(r, j)};")
+
+    def or_leaves(self, v: int) -> List[int]:
+        """Split an output into the OR-ed terms it is made of (single-use OR nodes only)."""
+        n = self.d.nodes[v]
+        if n.op == "or" and not self.d.is_cc(v) and self.uses.get(v, 0) <= 1:
+            return self.or_leaves(n.args[0]) + self.or_leaves(n.args[1])
+        return [v]
+
+    def heavy_ancestors(self, v: int) -> set:
+        out, stack = set(), [v]
+        while stack:
+            x = stack.pop()
+            if x in out or self.d.is_cc(x):
+                continue
+            out.add(x)
+            stack.extend(self.d.nodes[x].args)
+        return out
+
+    def part(self, terms: Sequence[Tuple[int, int]]) -> str:
+        """Body of one part function: every (node, output) term OR-ed into the warp's
+        shared-memory accumulator of its output.
+
+        Zero-block skipping by guard regions.  A checkpoint is an AND on a marker path (1st AND,
+        then every `skip_interval` ANDs, counting restarts after an addition).  cz(v) is the set
+        of checkpoints whose being zero in the whole tile makes v zero in its exact lanes:
+        AND/Advance inherit the union of their marker operands' sets, OR/XOR/SEL the
+        intersection, everything else nothing.  v is computed inside the guard of the latest
+        checkpoint in cz(v) other than itself (its home); a value used outside its home is
+        declared zero in the enclosing region both share.  Within a region the unguarded work
+        is emitted first and child guard blocks are opened as late as dependencies allow, so
+        the dense part of all terms forms one basic block."""
+        d = self.d
+        k = max(1, self.t.skip_interval) if self.t.skip_interval > 0 else 0
         self.lines = []
         self.indent = 2
         self.scopes = [{}]
-        for i, (o, nm) in enumerate(zip(outputs, out_names)):
-            self.emit(f"/* output {out_base + i}: {nm} */")
-            r = self.mat(o)
-            self.emit(f"store(p, t, {out_base + i}, {self.pack(r)});")
-        return "\n".join(self.lines)
+        term_outs: Dict[int, List[int]] = {}
+        for v, o in terms:
+            term_outs.setdefault(v, []).append(o)
+        # heavy nodes of this part, in topological (id) order
+        heavy = sorted(set().union(*[self.heavy_ancestors(v) for v in term_outs]))
+        hs = set(heavy)
+        andd: Dict[int, int] = {}
+        cz: Dict[int, frozenset] = {}
+        ckpt = set()
+        for v in heavy:
+            n = d.nodes[v]
+            ha = [a for a in n.args if a in hs]
+            if n.op in ADD_OPS:
+                andd[v] = 0
+                cz[v] = frozenset()
+                continue
+            andd[v] = max([andd[a] for a in ha] + [0]) + (1 if n.op == "and" else 0)
+            if n.op == "and":
+                c = frozenset().union(*[cz[a] for a in ha]) if ha else frozenset()
+                if k and andd[v] >= 1 and (andd[v] - 1) % k == 0:
+                    ckpt.add(v)
+                    c = c | {v}
+            elif n.op == "advance":
+                c = cz[ha[0]] if ha else frozenset()
+            elif n.op in ("or", "xor"):
+                c = cz[ha[0]] & cz[ha[1]] if len(ha) == 2 else frozenset()
+            elif n.op == "sel":
+                a1, a2 = n.args[1], n.args[2]
+                c = (cz[a1] if a1 in hs else frozenset()) & (cz[a2] if a2 in hs else frozenset()) \
+                    if (a1 in hs and a2 in hs) else frozenset()
+            else:
+                c = frozenset()
+            cz[v] = c
+        TOP = -1
+        home: Dict[int, int] = {}
+        for v in heavy:
+            c = cz[v] - {v}
+            home[v] = max(c) if c else TOP
+        parent = {z: home[z] for z in ckpt}
 
+        def chain(r):  # regions from r up to TOP
+            out = [r]
+            while r != TOP:
+                r = parent[r]
+                out.append(r)
+            return out
+
+        def lca(a, b):
+            ca = chain(a)
+            sb = set(chain(b))
+            for r in ca:
+                if r in sb:
+                    return r
+            return TOP
+
+        users: Dict[int, List[int]] = {v: [] for v in heavy}
+        for v in heavy:
+            for a in d.nodes[v].args:
+                if a in hs:
+                    users[a].append(v)
+        decl: Dict[int, int] = {}
+        for v in heavy:
+            r = home[v]
+            for u in users[v]:
+                r = lca(r, home[u])
+            decl[v] = r
+        by_home: Dict[int, List[int]] = {}
+        for v in heavy:
+            by_home.setdefault(home[v], []).append(v)
+        lifted_at: Dict[int, List[int]] = {}
+        for v in heavy:
+            if decl[v] != home[v]:
+                lifted_at.setdefault(decl[v], []).append(v)
+        children: Dict[int, List[int]] = {}
+        for z in sorted(ckpt):
+            children.setdefault(parent[z], []).append(z)
+
+        def child_of(R, r):
+            """The child region of R on the path to region r, or None."""
+            prev = None
+            while r != R:
+                if r == TOP:
+                    return None
+                prev = r
+                r = parent[r]
+            return prev
+
+        def compute(v):
+            n = d.nodes[v]
+            name = f"v{v}"
+            declare = decl[v] == home[v]
+            if n.op in ADD_OPS:
+                m = self.mat(n.args[0])
+                c = self.mat(n.args[1])
+                fn = "matchstar" if n.op == "matchstar" else "scanthru"
+                self.emit(f"const S {name}_s = {fn}<{self.dl[v]}>(p, t, {self.adds[v]}, {self.pack(m)}, {self.pack(c)});")
+                for j in range(self.t.wpt):
+                    pre = "const uint32_t " if declare else ""
+                    self.emit(f"{pre}{name}_{j} = {name}_s.w[{j}];")
+            else:
+                a = [self.mat(x) for x in n.args]
+                self.emit_op(name, n, a, declare=declare)
+            self.scopes[-1][v] = name
+            if declare is False:
+                self.scopes[0][v] = name  # visible everywhere below its declaration
+            for o in term_outs.get(v, []):
+                self.emit(f"acc_or(acc, {o}, {self.pack(name)});")
+
+        def emit_region(R):
+            for v in lifted_at.get(R, []):
+                self.emit("uint32_t " + ", ".join(f"v{v}_{j} = 0u" for j in range(self.t.wpt)) + ";")
+                self.scopes[-1][v] = f"v{v}"
+            kids = set(children.get(R, []))
+            ready: List[int] = []          # computed checkpoints whose block is not emitted yet
+            done_children = set()
+            for v in by_home.get(R, []):
+                for a in d.nodes[v].args:
+                    if a in hs and home[a] != R:
+                        c = child_of(R, home[a])
+                        if c is not None and c not in done_children:
+                            emit_child(c)
+                            done_children.add(c)
+                            if c in ready:
+                                ready.remove(c)
+                compute(v)
+                if v in kids:
+                    ready.append(v)
+                    while len(ready) > self.t.window:
+                        c = ready.pop(0)
+                        emit_child(c)
+                        done_children.add(c)
+            for c in sorted(kids):
+                if c not in done_children:
+                    emit_child(c)
+                    done_children.add(c)
+
+        def emit_child(z):
+            self.open(self.any_expr(f"v{z}"))
+            emit_region(z)
+            self.close()
+
+        emit_region(TOP)
+        # terms that are pure character classes (no heavy node)
+        for v, os_ in term_outs.items():
+            if v not in hs:
+                r = self.mat(v)
+                if r != "0u":
+                    for o in os_:
+                        self.emit(f"acc_or(acc, {o}, {self.pack(r)});")
+        return "\n".join(self.lines)
 
 def _basis_params(wpt: int) -> str:
     return ", ".join(f"uint32_t b{i}_{j}" for i in range(8) for j in range(wpt))
@@ -608,56 +821,112 @@ def build_dag(groups: Sequence[Group], per_regex: bool = False) -> Tuple[Dag, Li
     return dag, outs, names
 
 
+SMEM_BUDGET = 48 * 1024
+
+
+def _cluster_terms(gen: "_Gen", terms: List[Tuple[int, int]], cap: int) -> List[List[Tuple[int, int]]]:
+    """Union terms that share a non-character-class node (a common prefix chain, an addition),
+    so that shared work is done once per tile; clusters hold at most `cap` terms."""
+    parent = list(range(len(terms)))
+    size = [1] * len(terms)
+
+    def find(i):
+        while parent[i] != i:
+            parent[i] = parent[parent[i]]
+            i = parent[i]
+        return i
+
+    owner: Dict[int, int] = {}
+    for i, (v, _) in enumerate(terms):
+        for h in sorted(gen.heavy_ancestors(v)):
+            if h in owner:
+                a, b = find(i), find(owner[h])
+                if a != b and size[a] + size[b] <= cap:
+                    if size[a] < size[b]:
+                        a, b = b, a
+                    parent[b] = a
+                    size[a] += size[b]
+            else:
+                owner[h] = i
+    groups: Dict[int, List[Tuple[int, int]]] = {}
+    for i, t in enumerate(terms):
+        groups.setdefault(find(i), []).append(t)
+    # pack small clusters together so there are few, mid-sized functions
+    out: List[List[Tuple[int, int]]] = []
+    cur: List[Tuple[int, int]] = []
+    for g in sorted(groups.values(), key=len, reverse=True):
+        if cur and len(cur) + len(g) > cap:
+            out.append(cur)
+            cur = []
+        cur = cur + g
+    if cur:
+        out.append(cur)
+    return out
+
+
 def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
                     per_regex: bool = False, name: str = "bg_scan") -> KernelSpec:
-    """Lower the pattern set into one kernel: one non-inlined device function per group (so
-    compile time grows linearly and NVRTC can split the work across threads), called in turn on
-    every tile after the tile's bytes are loaded and transposed once."""
+    """Lower the pattern set into one kernel.
+
+    All groups share one hash-consed DAG.  Its outputs are split into OR-ed terms, and terms that
+    share work (a common literal prefix, the same addition) are clustered into non-inlined part
+    functions (compile time grows linearly with the pattern set; NVRTC can split the work).
+    Each part ORs its terms into per-warp shared-memory accumulators, one per output; after all
+    parts ran on a tile, the accumulators are written out.  Output grouping is therefore
+    independent of how the computation is partitioned."""
     tuning = tuning or Tuning()
-    parts = []
-    hl = 0
-    max_dbits = 0
-    n_nodes = 0
-    names_all: List[str] = []
-    for gi, g in enumerate(groups):
-        dag, outs, names = build_dag([g], per_regex)
-        names = [nm.replace("group 0", f"group {gi}", 1) for nm in names]
-        gen = _Gen(dag, tuning)
-        gen.analyse(outs)
-        hl = max(hl, gen.hl)
-        max_dbits = max(max_dbits, gen.max_dbits)
-        n_nodes += len(dag.nodes)
-        parts.append((gen, outs, names))
-    add_base = 0
-    out_base = 0
-    funcs = []
     wpt = tuning.wpt
-    for gi, (gen, outs, names) in enumerate(parts):
-        gen.adds = {v: add_base + k for v, k in gen.adds.items()}
-        add_base += len(gen.adds)
-        code = gen.body(outs, [nm.replace("*/", "* /") for nm in names], out_base)
-        out_base += len(outs)
-        names_all.extend(names)
+    dag, outs, names = build_dag(groups, per_regex)
+    gen = _Gen(dag, tuning)
+    gen.analyse(outs)
+    n_out = len(outs)
+    warps = tuning.block // 32
+    smem_words = warps * n_out * wpt * 32
+    if smem_words * 4 > SMEM_BUDGET:
+        raise NotFusable(f"{n_out} outputs need {smem_words * 4} bytes of accumulators per block; "
+                         f"use fewer outputs per program or a smaller block")
+    terms: List[Tuple[int, int]] = []
+    for o, v in enumerate(outs):
+        for leaf in gen.or_leaves(v):
+            terms.append((leaf, o))
+    clusters = _cluster_terms(gen, terms, tuning.part_cap)
+    funcs = []
+    for ci, cl in enumerate(clusters):
+        code = gen.part(cl)
         funcs.append(
-            f"__device__ __noinline__ void bg_group_{gi}(const BgParams &p, const Tile &t, {_basis_params(wpt)}) {{\n"
-            f"{code}\n}}\n")
-    calls = "\n".join(f"    bg_group_{gi}(p, t, {_basis_args(wpt)});" for gi in range(len(parts)))
+            f"//@@BG_PART\n"
+            f'extern "C" __device__ __noinline__ void bg_part_{ci}(const BgParams &p, const Tile t, uint32_t *acc, '
+            f"{_basis_params(wpt)}) {{\n{code}\n}}\n")
+    decls = "\n".join(
+        f'extern "C" __device__ void bg_part_{ci}(const BgParams &p, const Tile t, uint32_t *acc, {_basis_params(wpt)});'
+        for ci in range(len(clusters)))
+    calls = "\n".join(f"    bg_part_{ci}(p, t, acc, {_basis_args(wpt)});" for ci in range(len(clusters)))
+    comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
+    maxreg = max(32, min(255, (65536 // (tuning.block * max(1, tuning.min_blocks))) // 8 * 8))
     src = (
+        f"//@@BG_MAXREG {maxreg}\n"
         f"#define BG_WPT {wpt}\n"
-        f"#define BG_HL {hl}\n"
+        f"#define BG_HL {gen.hl}\n"
+        f"#define BG_NOUT {n_out}\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"
+        f"{comments}\n"
         + "\n".join(funcs) +
-        f'extern "C" __global__ void __launch_bounds__({tuning.block}) {name}(const __grid_constant__ BgParams p) {{\n'
+        f"//@@BG_KERNEL\n{decls}\n"
+        f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
+        f"  __shared__ uint32_t bg_acc[{warps} * BG_NOUT * BG_WPT * 32];\n"
+        f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
         f"  while (next_tile(p, t)) {{\n"
+        f"    acc_clear(acc, t);\n"
         f"    S b[8];\n"
         f"    load_basis(p, t, b);\n"
         f"{calls}\n"
+        f"    acc_store(p, t, acc);\n"
         f"  }}\n"
         f"}}\n"
     )
-    return KernelSpec(source=src, name=name, n_outputs=out_base, n_adds=add_base,
-                      halo_lanes=hl, wpt=wpt, block=tuning.block, max_depth_bits=max_dbits,
-                      n_nodes=n_nodes, output_names=names_all)
+    return KernelSpec(source=src, name=name, n_outputs=n_out, n_adds=len(gen.adds),
+                      halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
+                      n_nodes=len(dag.nodes), output_names=names)

@@ -186,34 +186,76 @@ __device__ __forceinline__ unsigned long long wait_record(const unsigned long lo
   return __shfl_sync(FULL, r, 0);
 }
 
-/* Carry entering tile `gtile`'s look-back lane for the addition whose records start at `rec`
- * (decoupled look-back over the predecessors' aggregates and inclusive carries). */
-__device__ __noinline__ uint32_t lookback(const unsigned long long *rec, long long gtile,
+/* Carry entering tile `gtile`'s look-back lane for the addition whose records start at `rec`:
+ * decoupled look-back, 32 predecessor records per step (lane i reads tile gtile-1-i).  Walking
+ * back, every aggregate that propagates (P = 1) contributes its generate bit; the walk stops at
+ * the nearest record that fixes the carry by itself: an inclusive carry, or an aggregate that
+ * does not propagate.  Control flow is warp-uniform (decisions come from ballots / lane 0).
+ * Waits are bounded like wait_record. */
+static __device__ __noinline__ uint32_t lookback(const unsigned long long *rec, long long gtile,
                                           long long first, unsigned long long epoch,
                                           long long spin_limit, uint32_t *state, int lane) {
-  uint32_t accG = 0, accP = 1;
-  for (long long j = gtile - 1;; --j) {
-    if (j < first) {
-      if (lane == 0) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
-      return accG;
+  uint32_t acc = 0;
+  long long base = gtile - 1;
+  long long t0 = clock64();
+  unsigned ns = 32, polls = 0;
+  for (;;) {
+    const long long j = base - lane;
+    bool valid = true;
+    unsigned long long r = (epoch << 4) | (2ull << 2); /* before the input: carry 0 */
+    if (j >= first) {
+      r = ld_relaxed(rec + j);
+      valid = (r >> 4) == epoch;
     }
-    const unsigned long long r = wait_record(rec + j, epoch, spin_limit, state, lane);
     const uint32_t flag = (uint32_t)(r >> 2) & 3u;
     const uint32_t G = (uint32_t)r & 1u, P = (uint32_t)(r >> 1) & 1u;
-    if (flag == 2u) return accG | (accP & G);
-    accG |= accP & G;
-    accP &= P;
-    if (!accP) return accG;
+    /* a record fixes the carry by itself if it is inclusive, or an aggregate that generates a
+     * carry or does not propagate one */
+    const bool term = valid && (flag == 2u || (flag == 1u && (P == 0u || G == 1u)));
+    const uint32_t vmask = __ballot_sync(FULL, valid);
+    const uint32_t tmask = __ballot_sync(FULL, term);
+    const int tl = tmask ? __ffs(tmask) - 1 : 32;
+    const uint32_t need = tl >= 31 ? FULL : ((2u << tl) - 1u);
+    if ((vmask & need) == need) {
+      /* records before the terminator propagate and do not generate: they pass the carry on */
+      if (tl < 32) {
+        if (base - tl < first && lane == 0) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
+        return acc | __shfl_sync(FULL, G, tl);
+      }
+      base -= 32;
+      t0 = clock64();
+      polls = 0;
+      ns = 32;
+      continue;
+    }
+    /* some record before the first terminator is not published yet: wait, bounded */
+    long long el = clock64() - t0;
+    el = __shfl_sync(FULL, el, 0);
+    const uint32_t ab = __shfl_sync(FULL, *(volatile uint32_t *)(state + 1), 0);
+    if ((ab & BG_DEV_ERR_TIMEOUT) || ++polls >= (1u << 22) || el > spin_limit) {
+      if (lane == 0) atomicOr(state + 1, BG_DEV_ERR_TIMEOUT);
+      return acc;
+    }
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
   }
 }
+
+/* What an addition needs to know about its tile (passed by value to the out-of-line path). */
+struct Lk {
+  long long gtile, first;
+  unsigned long long epoch;
+  S vm;
+};
 
 /* Carry vector for addition k: bit l = carry entering lane l.  Gm/Pm are the lanes that
  * generate / propagate a carry; lanes below DL are ignored and the carry enters at DL. */
 template <int DL>
-__device__ __forceinline__ uint32_t carries(const BgParams &p, const Tile &t, int k, uint32_t Gm,
+__device__ __forceinline__ uint32_t carries(const BgParams &p, const Lk &L, int k, uint32_t Gm,
                                             uint32_t Pm) {
   static_assert(DL >= 0 && DL < HL || (HL == 0 && DL == 0), "carry lane must be in the halo");
   constexpr int OUTL = SL + DL; /* the successor tile's carry lane, in our coordinates */
+  const int lane = threadIdx.x & 31;
   const uint32_t keep = ~((1u << DL) - 1u);
   Gm &= keep;
   Pm &= keep;
@@ -221,32 +263,33 @@ __device__ __forceinline__ uint32_t carries(const BgParams &p, const Tile &t, in
   uint32_t cin = 0;
   const bool own = (HL > 0) && ((Pm >> DL) & 1u);
   const bool succ = (HL > 0) && ((Pm >> (OUTL & 31)) & 1u);
+  unsigned long long *rec = p.records + (long long)k * p.n_tiles;
   if (own) {
     if (succ) {
       const uint32_t c0 = (uint32_t)((unsigned long long)A + B) ^ A ^ B;
       const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
       const uint32_t Pagg = (((Pm >> DL) & span) == span) ? 1u : 0u;
-      publish(p, t, k, 1u, Pagg, (c0 >> OUTL) & 1u);
+      if (lane == 0) st_relaxed(rec + L.gtile, (L.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1) | ((c0 >> OUTL) & 1u));
     }
-    cin = lookback(p.records + (long long)k * p.n_tiles, t.gtile, t.first, t.epoch, p.spin_limit,
-                   p.state, t.lane);
+    cin = lookback(rec, L.gtile, L.first, L.epoch, p.spin_limit, p.state, lane);
   }
   const uint32_t cvec =
       (uint32_t)((unsigned long long)A + B + ((unsigned long long)cin << DL)) ^ A ^ B;
-  if (succ) publish(p, t, k, 2u, 0u, (cvec >> OUTL) & 1u);
+  if (succ && lane == 0) st_relaxed(rec + L.gtile, (L.epoch << 4) | (2ull << 2) | ((cvec >> OUTL) & 1u));
   return cvec;
 }
 
 /* Exact X + Y over the tile (positions ascend with bit significance after __brev). */
 template <int DL>
-__device__ __forceinline__ S add_carry(const BgParams &p, const Tile &t, int k, const S &X,
+__device__ __forceinline__ S add_carry(const BgParams &p, const Lk &L, int k, const S &X,
                                        const S &Y) {
+  const int lane = threadIdx.x & 31;
   uint32_t xb[WPT], yb[WPT];
   uint32_t G = 0u, P = 1u;
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
-    xb[j] = __brev(X.w[j] & t.vm.w[j]);
-    yb[j] = __brev(Y.w[j] & t.vm.w[j]);
+    xb[j] = __brev(X.w[j] & L.vm.w[j]);
+    yb[j] = __brev(Y.w[j] & L.vm.w[j]);
     const uint32_t s = xb[j] + yb[j];
     const uint32_t g = s < xb[j] ? 1u : 0u;
     const uint32_t pp = s == FULL ? 1u : 0u;
@@ -254,8 +297,8 @@ __device__ __forceinline__ S add_carry(const BgParams &p, const Tile &t, int k, 
     P &= pp;
   }
   const uint32_t Gm = __ballot_sync(FULL, G), Pm = __ballot_sync(FULL, P);
-  const uint32_t cvec = carries<DL>(p, t, k, Gm, Pm);
-  uint32_t c = (cvec >> t.lane) & 1u;
+  const uint32_t cvec = carries<DL>(p, L, k, Gm, Pm);
+  uint32_t c = (cvec >> lane) & 1u;
   S r;
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
@@ -266,45 +309,52 @@ __device__ __forceinline__ S add_carry(const BgParams &p, const Tile &t, int k, 
   return r;
 }
 
-/* Sum C + carry-in, for a marker that is zero in the whole warp (only the carry entering the
- * tile can make the result non-zero). */
+/* Out-of-line part of MatchStar (mode 0) / ScanThru (mode 1): the general addition. */
 template <int DL>
-__device__ __forceinline__ S add_zero_marker(const BgParams &p, const Tile &t, int k, const S &C) {
-  uint32_t allones = 1u;
-#pragma unroll
-  for (int j = 0; j < WPT; ++j) allones &= ((C.w[j] & t.vm.w[j]) == FULL) ? 1u : 0u;
-  const uint32_t Pm = __ballot_sync(FULL, allones);
-  const uint32_t cvec = carries<DL>(p, t, k, 0u, Pm);
-  if (!__any_sync(FULL, cvec != 0u)) return C & t.vm;
-  /* a carry enters: sum = C + carry (brev domain) */
-  uint32_t c = (cvec >> t.lane) & 1u;
-  S r;
+__device__ __noinline__ S add_slow(const BgParams &p, const Lk L, int k, int mode, const S M,
+                                   const S C) {
+  const S Cm = C & L.vm;
+  const S X = mode == 0 ? (M & C) : M;
+  const S sum = add_carry<DL>(p, L, k, X, C);
+  return mode == 0 ? ((sum ^ Cm) | M) : (sum & ~C);
+}
+
+/* Inline fast path shared by MatchStar and ScanThru: when the marker is zero in the whole warp
+ * and the carry lane does not propagate, no carry can enter and the result is zero; the
+ * successor's carry (zero) is published if it will be needed. */
+template <int DL>
+__device__ __forceinline__ bool add_is_zero(const BgParams &p, const Tile &t, int k, const S &M,
+                                            const S &C) {
+  uint32_t mo = 0u, ao = 1u;
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
-    const uint32_t cb = __brev(C.w[j] & t.vm.w[j]);
-    const unsigned long long s = (unsigned long long)cb + c;
-    r.w[j] = __brev((uint32_t)s);
-    c = (uint32_t)(s >> 32);
+    mo |= M.w[j];
+    ao &= ((C.w[j] & t.vm.w[j]) == FULL) ? 1u : 0u;
   }
-  return r;
+  if (__any_sync(FULL, mo != 0u)) return false;
+  const uint32_t Pm = __ballot_sync(FULL, ao);
+  if ((Pm >> DL) & 1u) return false;
+  if ((Pm >> ((SL + DL) & 31)) & 1u) {
+    if (t.lane == 0)
+      st_relaxed(p.records + (long long)k * p.n_tiles + t.gtile, (t.epoch << 4) | (2ull << 2));
+  }
+  return true;
 }
 
 /* MatchStar(M, C) = (((M & C) + C) ^ C) | M   (bitgen/template/template_torch.py:392-407) */
 template <int DL>
-__device__ __noinline__ S matchstar(const BgParams &p, const Tile &t, int k, const S &M,
+__device__ __forceinline__ S matchstar(const BgParams &p, const Tile &t, int k, const S &M,
                                        const S &C) {
-  if (!any(M)) return add_zero_marker<DL>(p, t, k, C) ^ (C & t.vm);
-  const S sum = add_carry<DL>(p, t, k, M & C, C);
-  return (sum ^ (C & t.vm)) | M;
+  if (add_is_zero<DL>(p, t, k, M, C)) return zero();
+  return add_slow<DL>(p, Lk{t.gtile, t.first, t.epoch, t.vm}, k, 0, M, C);
 }
 
 /* ScanThru(M, C) = (M + C) & ~C   (bitgen/template/template_torch.py:377-389) */
 template <int DL>
-__device__ __noinline__ S scanthru(const BgParams &p, const Tile &t, int k, const S &M,
+__device__ __forceinline__ S scanthru(const BgParams &p, const Tile &t, int k, const S &M,
                                       const S &C) {
-  if (!any(M)) return add_zero_marker<DL>(p, t, k, C) & ~C;
-  const S sum = add_carry<DL>(p, t, k, M, C);
-  return sum & ~C;
+  if (add_is_zero<DL>(p, t, k, M, C)) return zero();
+  return add_slow<DL>(p, Lk{t.gtile, t.first, t.epoch, t.vm}, k, 1, M, C);
 }
 
 /* ---------------------------------------------------------------------------------------
@@ -382,7 +432,7 @@ __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b
 
 /* Write output stream o for this tile (lanes >= HL, words inside the input; characters at or
  * beyond n are cleared) and add its popcount to counts[o][input]. */
-__device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, const S &v) {
+static __device__ __noinline__ void store(const BgParams &p, const Tile t, int o, const S v) {
   uint32_t cnt = 0;
   uint32_t *dst = p.out ? p.out + (long long)o * p.out_stride + p.out_off[t.input] : nullptr;
 #pragma unroll
@@ -403,5 +453,34 @@ __device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, cons
       atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, (unsigned long long)cnt);
   }
 }
+
+#ifdef BG_NOUT
+/* Per-warp output accumulators in shared memory, laid out [output][word][lane] so that a warp's
+ * accesses are conflict free.  Only the owning warp touches its region. */
+__device__ __forceinline__ void acc_clear(uint32_t *acc, const Tile &t) {
+#pragma unroll 4
+  for (int i = 0; i < BG_NOUT * WPT; ++i) acc[i * 32 + t.lane] = 0u;
+}
+
+__device__ __forceinline__ void acc_or(uint32_t *acc, int o, const S v) {
+  const int lane = threadIdx.x & 31;
+  uint32_t x = 0;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) x |= v.w[j];
+  if (__any_sync(FULL, x != 0u)) {
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) acc[(o * WPT + j) * 32 + lane] |= v.w[j];
+  }
+}
+
+__device__ __forceinline__ void acc_store(const BgParams &p, const Tile &t, const uint32_t *acc) {
+  for (int o = 0; o < BG_NOUT; ++o) {
+    S v;
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) v.w[j] = acc[(o * WPT + j) * 32 + t.lane];
+    store(p, t, o, v);
+  }
+}
+#endif
 
 }  // namespace bg

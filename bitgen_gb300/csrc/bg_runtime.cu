@@ -7,15 +7,18 @@
  * (bitgen/backend/cuda/cuda_kernel.py) and its torch extension (bitgen/template/cuda/).
  */
 #include <cuda_runtime.h>
+#include <nvJitLink.h>
 #include <nvrtc.h>
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bitgen_gb300.h"
@@ -160,15 +163,113 @@ int bg_transpose(const uint8_t *bytes, uint32_t *basis, int64_t n_bytes_padded, 
   return BG_OK;
 }
 
+/* One NVRTC compilation of `src` to a cubin (relocatable when `rdc`). */
+static int nvrtc_one(const std::string &src, const std::string &name, bool rdc, std::string &log,
+                     std::vector<char> &cubin) {
+  /* "//@@BG_MAXREG n" in the source caps registers in every translation unit (the linker
+   * requires callees of a __launch_bounds__ kernel to fit its register budget) */
+  std::string maxreg;
+  const size_t mp = src.find("//@@BG_MAXREG ");
+  if (mp != std::string::npos) maxreg = "--maxrregcount=" + std::to_string(atoi(src.c_str() + mp + 14));
+  std::vector<const char *> base = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
+                                    "--device-as-default-execution-space"};
+  if (rdc) base.push_back("--relocatable-device-code=true");
+  if (!maxreg.empty()) base.push_back(maxreg.c_str());
+  const int n_opts = (int)base.size();
+  nvrtcProgram prog;
+  const char *headers[] = {bg_embedded_device_cuh, bg_embedded_params_h, bg_embedded_transpose_cuh};
+  const char *names[] = {"bg_device.cuh", "bg_params.h", "bg_transpose.cuh"};
+  if (nvrtcCreateProgram(&prog, src.c_str(), (name + ".cu").c_str(), 3, headers, names) !=
+      NVRTC_SUCCESS)
+    return fail(BG_ERR_COMPILE, "nvrtcCreateProgram failed");
+  nvrtcResult r = nvrtcCompileProgram(prog, n_opts, base.data());
+  size_t logsz = 0;
+  nvrtcGetProgramLogSize(prog, &logsz);
+  log.assign(logsz, '\0');
+  if (logsz) nvrtcGetProgramLog(prog, &log[0]);
+  if (r != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return fail(BG_ERR_COMPILE, std::string("NVRTC: ") + nvrtcGetErrorString(r) + "\n" + log);
+  }
+  size_t sz = 0;
+  nvrtcGetCUBINSize(prog, &sz);
+  cubin.resize(sz);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  return BG_OK;
+}
+
+/* Sources generated with "//@@BG_PART" / "//@@BG_KERNEL" section markers are compiled as one
+ * relocatable translation unit per section (prelude + section) on parallel host threads and
+ * linked with nvJitLink; other sources are compiled whole. */
+static int compile_sections(const std::string &src, const std::string &name, std::string &log,
+                            std::vector<char> &cubin) {
+  const std::string PART = "//@@BG_PART\n", KERN = "//@@BG_KERNEL\n";
+  std::vector<size_t> cuts;
+  for (size_t pos = src.find("//@@BG_"); pos != std::string::npos; pos = src.find("//@@BG_", pos + 1))
+    if (src.compare(pos, PART.size(), PART) == 0 || src.compare(pos, KERN.size(), KERN) == 0)
+      cuts.push_back(pos);
+  if (cuts.size() < 3) return nvrtc_one(src, name, false, log, cubin);
+  const std::string prelude = src.substr(0, cuts[0]);
+  std::vector<std::string> units;
+  for (size_t i = 0; i < cuts.size(); ++i) {
+    const size_t e = i + 1 < cuts.size() ? cuts[i + 1] : src.size();
+    units.push_back(prelude + src.substr(cuts[i], e - cuts[i]));
+  }
+  const size_t n = units.size();
+  std::vector<std::vector<char>> objs(n);
+  std::vector<std::string> logs(n), errs(n);
+  std::vector<int> rcs(n, BG_OK);
+  unsigned hw = std::thread::hardware_concurrency();
+  const size_t workers = std::max<size_t>(1, std::min<size_t>(n, hw ? hw : 4));
+  std::vector<std::thread> pool;
+  std::atomic<size_t> next{0};
+  for (size_t w = 0; w < workers; ++w)
+    pool.emplace_back([&]() {
+      for (size_t i = next++; i < n; i = next++) {
+        rcs[i] = nvrtc_one(units[i], name + "_" + std::to_string(i), true, logs[i], objs[i]);
+        if (rcs[i] != BG_OK) errs[i] = g_last_error;
+      }
+    });
+  for (auto &t : pool) t.join();
+  for (size_t i = 0; i < n; ++i) {
+    if (!logs[i].empty()) log += logs[i];
+    if (rcs[i] != BG_OK) return fail(rcs[i], errs[i]);
+  }
+  nvJitLinkHandle h;
+  const char *lopts[] = {"-arch=sm_103a"};
+  if (nvJitLinkCreate(&h, 1, lopts) != NVJITLINK_SUCCESS)
+    return fail(BG_ERR_COMPILE, "nvJitLinkCreate failed");
+  int rc = BG_OK;
+  for (size_t i = 0; i < n && rc == BG_OK; ++i) {
+    const std::string nm = name + "_" + std::to_string(i) + ".cubin";
+    if (nvJitLinkAddData(h, NVJITLINK_INPUT_CUBIN, objs[i].data(), objs[i].size(), nm.c_str()) !=
+        NVJITLINK_SUCCESS)
+      rc = BG_ERR_COMPILE;
+  }
+  if (rc == BG_OK && nvJitLinkComplete(h) != NVJITLINK_SUCCESS) rc = BG_ERR_COMPILE;
+  if (rc != BG_OK) {
+    size_t ls = 0;
+    nvJitLinkGetErrorLogSize(h, &ls);
+    std::string el(ls, '\0');
+    if (ls) nvJitLinkGetErrorLog(h, &el[0]);
+    nvJitLinkDestroy(&h);
+    return fail(BG_ERR_COMPILE, "nvJitLink: " + el);
+  }
+  size_t sz = 0;
+  nvJitLinkGetLinkedCubinSize(h, &sz);
+  cubin.resize(sz);
+  nvJitLinkGetLinkedCubin(h, cubin.data());
+  nvJitLinkDestroy(&h);
+  return BG_OK;
+}
+
 static int compile_cubin(const std::string &src, const std::string &name, std::string &log,
                          std::vector<char> &cubin) {
-  const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
-                        "--device-as-default-execution-space", "--split-compile=0"};
-  const int n_opts = sizeof(opts) / sizeof(opts[0]);
   int major = 0, minor = 0;
   nvrtcVersion(&major, &minor);
   std::string key = src + "|" + name + "|" + std::to_string(major) + "." + std::to_string(minor);
-  for (int i = 0; i < n_opts; ++i) key += std::string("|") + opts[i];
+  key += "|sm_103a|rdc-sections-v1";
   key += bg_embedded_device_cuh;
   key += bg_embedded_params_h;
   key += bg_embedded_transpose_cuh;
@@ -192,26 +293,8 @@ static int compile_cubin(const std::string &src, const std::string &name, std::s
       cubin.clear();
     }
   }
-  nvrtcProgram prog;
-  const char *headers[] = {bg_embedded_device_cuh, bg_embedded_params_h, bg_embedded_transpose_cuh};
-  const char *names[] = {"bg_device.cuh", "bg_params.h", "bg_transpose.cuh"};
-  if (nvrtcCreateProgram(&prog, src.c_str(), (name + ".cu").c_str(), 3, headers, names) !=
-      NVRTC_SUCCESS)
-    return fail(BG_ERR_COMPILE, "nvrtcCreateProgram failed");
-  nvrtcResult r = nvrtcCompileProgram(prog, n_opts, opts);
-  size_t logsz = 0;
-  nvrtcGetProgramLogSize(prog, &logsz);
-  log.assign(logsz, '\0');
-  if (logsz) nvrtcGetProgramLog(prog, &log[0]);
-  if (r != NVRTC_SUCCESS) {
-    nvrtcDestroyProgram(&prog);
-    return fail(BG_ERR_COMPILE, std::string("NVRTC: ") + nvrtcGetErrorString(r) + "\n" + log);
-  }
-  size_t sz = 0;
-  nvrtcGetCUBINSize(prog, &sz);
-  cubin.resize(sz);
-  nvrtcGetCUBIN(prog, cubin.data());
-  nvrtcDestroyProgram(&prog);
+  const int rc = compile_sections(src, name, log, cubin);
+  if (rc != BG_OK) return rc;
   if (!path.empty()) {
     std::string tmp = path + ".tmp" + std::to_string((long long)getpid());
     if (FILE *f = fopen(tmp.c_str(), "wb")) {

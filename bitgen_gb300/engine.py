@@ -285,8 +285,15 @@ class Program:
         self._interp = None
         self._plans: Dict[tuple, Plan] = {}
         if fuse:
+            try:
+                self.spec = generate_kernel(self.groups, self.tuning, per_regex, name)
+            except NotFusable:
+                if executor == "fused":
+                    raise
+                fuse = False
+        self.fused = fuse
+        if fuse:
             _ensure_cache_dir()
-            self.spec = generate_kernel(self.groups, self.tuning, per_regex, name)
             self.n_outputs = self.spec.n_outputs
             src = self.spec.source.encode()
             self._desc = N.KernelDesc(src, len(src), name.encode(), self.spec.n_outputs,

@@ -345,6 +345,9 @@ class _Builder:
             self.top = saved
 
     def _cc(self, s: frozenset, level: int) -> str:
+        """Decision diagram deciding bit `level` (basis7 = bit 0 first) of the byte; `s` holds
+        the byte's remaining high bits (byte >> level).  Deciding the low bits first makes the
+        shared sub-functions the high-bit prefixes (e.g. "011" of every lowercase letter)."""
         if not s:
             return "0"
         span = 1 << (8 - level)
@@ -354,12 +357,11 @@ class _Builder:
         hit = self.cc_memo.get(key)
         if hit is not None:
             return hit
-        bit = 1 << (7 - level)
-        s1 = frozenset(x for x in s if x & bit)
-        s0 = frozenset(x for x in s if not x & bit)
+        s1 = frozenset(x >> 1 for x in s if x & 1)
+        s0 = frozenset(x >> 1 for x in s if not x & 1)
         f1 = self._cc(s1, level + 1)
         f0 = self._cc(s0, level + 1)
-        r = self.SEL(f"basis{level}", f1, f0)
+        r = self.SEL(f"basis{7 - level}", f1, f0)
         self.cc_memo[key] = r
         return r
 
