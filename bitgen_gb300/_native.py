@@ -32,7 +32,7 @@ class BitgenError(RuntimeError):
 class KernelDesc(C.Structure):
     _fields_ = [("source", C.c_char_p), ("source_len", C.c_size_t), ("name", C.c_char_p),
                 ("n_outputs", C.c_int32), ("n_adds", C.c_int32), ("halo_lanes", C.c_int32),
-                ("wpt", C.c_int32), ("block", C.c_int32)]
+                ("wpt", C.c_int32), ("block", C.c_int32), ("tail_lanes", C.c_int32)]
 
 
 class Layout(C.Structure):
@@ -60,6 +60,8 @@ SIGNATURES = {
                                   C.POINTER(C.c_int32)]),
     "bg_program_destroy": (C.c_int, [C.c_void_p]),
     "bg_plan_create": (C.c_int, [C.c_void_p, C.POINTER(Layout), C.POINTER(C.c_void_p)]),
+    "bg_plan_reserve": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
+    "bg_plan_set_layout": (C.c_int, [C.c_void_p, C.POINTER(Layout), C.c_void_p]),
     "bg_plan_tiles": (C.c_int64, [C.c_void_p]),
     "bg_plan_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "bg_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

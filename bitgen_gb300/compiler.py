@@ -316,7 +316,7 @@ class Tuning:
     skip_interval: int = 1  # check for an all-zero marker every k AND steps (0 = never)
     part_cap: int = 32      # most OR-ed terms one part function computes
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
-    min_blocks: int = 2     # __launch_bounds__ minimum resident blocks per SM (caps registers)
+    min_blocks: int = 3     # __launch_bounds__ minimum resident blocks per SM (caps registers)
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window, self.min_blocks)
@@ -334,10 +334,11 @@ class KernelSpec:
     max_depth_bits: int
     n_nodes: int
     output_names: List[str] = field(default_factory=list)
+    tail_lanes: int = 0
 
     @property
     def tile_words(self):
-        return (32 - self.halo_lanes) * self.wpt
+        return (32 - self.halo_lanes - self.tail_lanes) * self.wpt
 
     def digest(self) -> str:
         return hashlib.sha256(self.source.encode()).hexdigest()[:16]
@@ -355,15 +356,56 @@ class _Gen:
         self.tmp = 0
 
     # analysis ---------------------------------------------------------------------------
+    def byteset(self, v: int) -> int:
+        """256-bit set of the byte values a character-class node is true for."""
+        memo = self._bs
+        if v in memo:
+            return memo[v]
+        n = self.d.nodes[v]
+        full = (1 << 256) - 1
+        if n.op == "basis":
+            r = sum(1 << b for b in range(256) if (b >> (7 - n.basis)) & 1)
+        elif n.op == "zero":
+            r = 0
+        elif n.op == "ones":
+            r = full
+        else:
+            a = [self.byteset(x) for x in n.args]
+            r = {"and": lambda: a[0] & a[1], "or": lambda: a[0] | a[1], "xor": lambda: a[0] ^ a[1],
+                 "not": lambda: ~a[0] & full,
+                 "sel": lambda: (a[0] & a[1]) | (~a[0] & a[2] & full)}[n.op]()
+        memo[v] = r
+        return r
+
+    def wide_class(self, v: int) -> bool:
+        """True if the class almost surely covers whole words of text (e.g. '.', '[^x]'), so
+        an addition over it will usually need its predecessor's carry."""
+        if not self.d.is_cc(v):
+            return True
+        bs = self.byteset(v)
+        printable = sum(1 for b in range(0x20, 0x7F) if (bs >> b) & 1)
+        return printable >= 90 or bin(bs).count("1") >= 200
+
     def analyse(self, outputs: Sequence[int]):
         d = self.d
         d.analyse()
+        self._bs: Dict[int, int] = {}
         lane_bits = 32 * self.t.wpt
         self.dbits: Dict[int, int] = {}
+        self.fbits: Dict[int, int] = {}
         self.dl: Dict[int, int] = {}
         for n in d.nodes:
             if n.op in ("basis", "zero", "ones"):
+                self.fbits[n.id] = 0
+            elif n.op == "lookahead":
+                self.fbits[n.id] = self.fbits[n.args[0]] + n.shift
+            else:
+                self.fbits[n.id] = max(self.fbits[a] for a in n.args)
+        for n in d.nodes:
+            if n.op in ("basis", "zero", "ones"):
                 self.dbits[n.id] = 0
+            elif n.op == "lookahead":
+                self.dbits[n.id] = self.dbits[n.args[0]]
             elif n.op == "advance":
                 self.dbits[n.id] = self.dbits[n.args[0]] + n.shift
             elif n.op in ADD_OPS:
@@ -388,9 +430,13 @@ class _Gen:
         for v in live:
             if v in self.dl:
                 hl = max(hl, self.dl[v] + 1)
-        if hl >= 32:
-            raise NotFusable(f"program depth needs {hl} halo lanes at {self.t.wpt} words/lane")
+        tl = 0
+        for v in live:
+            tl = max(tl, -(-self.fbits[v] // lane_bits))
+        if hl + tl >= 32:
+            raise NotFusable(f"program depth needs {hl} + {tl} halo lanes at {self.t.wpt} words/lane")
         self.hl = hl
+        self.tl = tl
         self.max_dbits = max([self.dbits[o] for o in outputs] + [0])
         for v in live:
             for a in d.nodes[v].args:
@@ -441,6 +487,17 @@ class _Gen:
         I = J + L * wpt
         return f"__shfl_up_sync(FULL, {self.w(ref, I)} & t.vm.w[{I}], {L})"
 
+    def word_fwd(self, ref: str, J: int) -> str:
+        """Word (lane*WPT + J) of `ref` for J >= 0 (later lanes via shuffle down); positions at
+        or beyond the end of the input read as zero."""
+        wpt = self.t.wpt
+        if ref in ("0u",):
+            return "0u"
+        if J < wpt:
+            return f"({self.w(ref, J)} & t.em.w[{J}])"
+        L, I = divmod(J, wpt)
+        return f"__shfl_down_sync(FULL, {self.w(ref, I)} & t.em.w[{I}], {L})"
+
     def emit_op(self, name: str, n: Node, a: List[str], declare: bool = True):
         wpt = self.t.wpt
         op = n.op
@@ -457,6 +514,14 @@ class _Gen:
                 e = f"~{x[0]}"
             elif op == "sel":
                 e = f"({x[0]} & {x[1]}) | (~{x[0]} & {x[2]})"
+            elif op == "lookahead":
+                q, r = divmod(n.shift, 32)
+                cur = self.word_fwd(a[0], j + q)
+                if r == 0:
+                    e = cur
+                else:
+                    nxt = self.word_fwd(a[0], j + q + 1)
+                    e = f"__funnelshift_l({nxt}, {cur}, {r})"
             elif op == "advance":
                 q, r = divmod(n.shift, 32)
                 cur = self.word_back(a[0], j - q)
@@ -655,6 +720,16 @@ class _Gen:
         andd: Dict[int, int] = {}
         cz: Dict[int, frozenset] = {}
         ckpt = set()
+        # late = needs the result of an addition; additions are split so that their carry
+        # look-back is issued after all early work of the part
+        late: Dict[int, bool] = {}
+        late_in: Dict[int, bool] = {}
+        for v in heavy:
+            n = d.nodes[v]
+            ha = [a for a in n.args if a in hs]
+            late_in[v] = any(late[a] for a in ha)
+            deferred = n.op in ADD_OPS and self.wide_class(n.args[1])
+            late[v] = deferred or late_in[v]
         for v in heavy:
             n = d.nodes[v]
             ha = [a for a in n.args if a in hs]
@@ -668,7 +743,7 @@ class _Gen:
                 if k and andd[v] >= 1 and (andd[v] - 1) % k == 0:
                     ckpt.add(v)
                     c = c | {v}
-            elif n.op == "advance":
+            elif n.op in ("advance", "lookahead"):
                 c = cz[ha[0]] if ha else frozenset()
             elif n.op in ("or", "xor"):
                 c = cz[ha[0]] & cz[ha[1]] if len(ha) == 2 else frozenset()
@@ -678,6 +753,8 @@ class _Gen:
                     if (a1 in hs and a2 in hs) else frozenset()
             else:
                 c = frozenset()
+            if late[v]:  # late work only runs inside late guards, so regions never mix
+                c = frozenset(z for z in c if late[z])
             cz[v] = c
         TOP = -1
         home: Dict[int, int] = {}
@@ -733,15 +810,27 @@ class _Gen:
                 r = parent[r]
             return prev
 
+        begun = set()
+
+        def add_begin(v):
+            n = d.nodes[v]
+            m, c = self.mat(n.args[0]), self.mat(n.args[1])
+            mode = 0 if n.op == "matchstar" else 1
+            self.emit(f"const AddState st{v} = add_begin<{self.dl[v]}>(p, t, {self.adds[v]}, {mode}, "
+                      f"{self.pack(m)}, {self.pack(c)});")
+            begun.add(v)
+
         def compute(v):
             n = d.nodes[v]
             name = f"v{v}"
             declare = decl[v] == home[v]
             if n.op in ADD_OPS:
-                m = self.mat(n.args[0])
-                c = self.mat(n.args[1])
-                fn = "matchstar" if n.op == "matchstar" else "scanthru"
-                self.emit(f"const S {name}_s = {fn}<{self.dl[v]}>(p, t, {self.adds[v]}, {self.pack(m)}, {self.pack(c)});")
+                if v not in begun:
+                    add_begin(v)
+                m, c = self.mat(n.args[0]), self.mat(n.args[1])
+                mode = 0 if n.op == "matchstar" else 1
+                self.emit(f"const S {name}_s = add_end<{self.dl[v]}>(p, t, {self.adds[v]}, {mode}, st{v}, "
+                          f"{self.pack(m)}, {self.pack(c)});")
                 for j in range(self.t.wpt):
                     pre = "const uint32_t " if declare else ""
                     self.emit(f"{pre}{name}_{j} = {name}_s.w[{j}];")
@@ -753,6 +842,47 @@ class _Gen:
                 self.scopes[0][v] = name  # visible everywhere below its declaration
             for o in term_outs.get(v, []):
                 self.emit(f"acc_or(acc, {o}, {self.pack(name)});")
+
+        def emit_top():
+            for v in lifted_at.get(TOP, []):
+                self.emit("uint32_t " + ", ".join(f"v{v}_{j} = 0u" for j in range(self.t.wpt)) + ";")
+                self.scopes[-1][v] = f"v{v}"
+            kids = children.get(TOP, [])
+            done_children = set()
+            for phase in (1, 2):
+                ready: List[int] = []
+                for v in by_home.get(TOP, []):
+                    is_add = d.nodes[v].op in ADD_OPS
+                    if phase == 1:
+                        if late_in[v]:
+                            continue
+                        if not is_add and late[v]:
+                            continue
+                    else:
+                        if not late[v]:
+                            continue
+                    for a in d.nodes[v].args:
+                        if a in hs and home[a] != TOP:
+                            c = child_of(TOP, home[a])
+                            if c is not None and c not in done_children:
+                                emit_child(c)
+                                done_children.add(c)
+                                if c in ready:
+                                    ready.remove(c)
+                    if phase == 1 and is_add and late[v]:
+                        add_begin(v)      # deferred: the look-back is issued in phase 2
+                        continue
+                    compute(v)
+                    if v in kids:
+                        ready.append(v)
+                        while len(ready) > self.t.window:
+                            c = ready.pop(0)
+                            emit_child(c)
+                            done_children.add(c)
+                for c in sorted(kids):
+                    if c not in done_children and (phase == 2 or not late[c]):
+                        emit_child(c)
+                        done_children.add(c)
 
         def emit_region(R):
             for v in lifted_at.get(R, []):
@@ -787,7 +917,7 @@ class _Gen:
             emit_region(z)
             self.close()
 
-        emit_region(TOP)
+        emit_top()
         # terms that are pure character classes (no heavy node)
         for v, os_ in term_outs.items():
             if v not in hs:
@@ -907,6 +1037,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"//@@BG_MAXREG {maxreg}\n"
         f"#define BG_WPT {wpt}\n"
         f"#define BG_HL {gen.hl}\n"
+        f"#define BG_TL {gen.tl}\n"
         f"#define BG_NOUT {n_out}\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"
@@ -929,4 +1060,4 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     )
     return KernelSpec(source=src, name=name, n_outputs=n_out, n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
-                      n_nodes=len(dag.nodes), output_names=names)
+                      n_nodes=len(dag.nodes), output_names=names, tail_lanes=gen.tl)

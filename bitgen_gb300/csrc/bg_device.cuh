@@ -8,7 +8,8 @@
  * Execution model: a warp owns a tile.  Lane l holds words [l*WPT, l*WPT + WPT) of the tile in
  * registers (type S).  Lanes [0, HL) are a halo: they re-compute the last HL*WPT words of the
  * previous tile so that every Advance of the program finds its source words inside the warp.
- * Lanes [HL, 32) are written out.  The generated kernel defines BG_WPT and BG_HL before
+ * Lanes [32-TL, 32) are a tail halo for Lookahead, which reads later positions.  Lanes
+ * [HL, 32-TL) are written out.  The generated kernel defines BG_WPT, BG_HL and BG_TL before
  * including this file.
  *
  * Additions (MatchStar, ScanThru) need the exact carry entering the tile.  For addition k the
@@ -29,15 +30,19 @@
 #ifndef BG_HL
 #error "BG_HL must be defined"
 #endif
+#ifndef BG_TL
+#define BG_TL 0
+#endif
 
 namespace bg {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int WPT = BG_WPT;
 constexpr int HL = BG_HL;
-constexpr int SL = 32 - HL;                 /* output lanes per tile   */
-constexpr long long SW = (long long)SL * WPT; /* output words per tile */
-static_assert(HL >= 0 && HL < 32, "halo must leave output lanes");
+constexpr int TL = BG_TL;                   /* tail halo lanes (for Lookahead)     */
+constexpr int SL = 32 - HL - TL;            /* output lanes per tile               */
+constexpr long long SW = (long long)SL * WPT; /* output words per tile             */
+static_assert(HL >= 0 && TL >= 0 && HL + TL < 32, "halos must leave output lanes");
 
 struct S {
   uint32_t w[WPT];
@@ -117,6 +122,7 @@ struct Tile {
   int input;
   int lane;
   S vm;              /* per word: all ones if the word index is >= 0     */
+  S em;              /* per word: the bits of positions before the input end */
 };
 
 /* Advance(x, N): marks move N positions forward; words before the input start read as 0. */
@@ -357,6 +363,91 @@ __device__ __forceinline__ S scanthru(const BgParams &p, const Tile &t, int k, c
   return add_slow<DL>(p, Lk{t.gtile, t.first, t.epoch, t.vm}, k, 1, M, C);
 }
 
+/* Split form of an addition, so that the wait for a predecessor's carry overlaps other work:
+ * add_begin computes the lanes' generate/propagate masks and publishes this tile's aggregate
+ * right away (or, when the carry lane does not propagate, resolves everything locally);
+ * add_end, issued later, runs the look-back if one is needed and forms the result. */
+struct AddState {
+  uint32_t xb[WPT], yb[WPT];
+  uint32_t Gm, Pm, cvec;
+  uint32_t state; /* 0 = look-back pending, 1 = result is zero, 2 = carries resolved */
+};
+
+template <int DL>
+__device__ __forceinline__ AddState add_begin(const BgParams &p, const Tile &t, int k, int mode,
+                                              const S &M, const S &C) {
+  AddState a;
+  a.Gm = a.Pm = a.cvec = 0u;
+  if (add_is_zero<DL>(p, t, k, M, C)) {
+    a.state = 1u;
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) a.xb[j] = a.yb[j] = 0u;
+    return a;
+  }
+  uint32_t G = 0u, P = 1u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const uint32_t x = mode == 0 ? (M.w[j] & C.w[j]) : M.w[j];
+    a.xb[j] = __brev(x & t.vm.w[j]);
+    a.yb[j] = __brev(C.w[j] & t.vm.w[j]);
+    const uint32_t s = a.xb[j] + a.yb[j];
+    const uint32_t g = s < a.xb[j] ? 1u : 0u;
+    const uint32_t pp = s == FULL ? 1u : 0u;
+    G = g | (pp & G);
+    P &= pp;
+  }
+  constexpr int OUTL = SL + DL;
+  const uint32_t keep = ~((1u << DL) - 1u);
+  a.Gm = __ballot_sync(FULL, G) & keep;
+  a.Pm = __ballot_sync(FULL, P) & keep;
+  const uint32_t A = a.Gm | a.Pm, B = a.Gm;
+  const bool own = (a.Pm >> DL) & 1u;
+  const bool succ = (a.Pm >> (OUTL & 31)) & 1u;
+  unsigned long long *rec = p.records + (long long)k * p.n_tiles;
+  if (own) {
+    if (succ && t.lane == 0) {
+      const uint32_t c0 = (uint32_t)((unsigned long long)A + B) ^ A ^ B;
+      const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
+      const uint32_t Pagg = (((a.Pm >> DL) & span) == span) ? 1u : 0u;
+      st_relaxed(rec + t.gtile, (t.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1) |
+                                    ((c0 >> OUTL) & 1u));
+    }
+    a.state = 0u;
+  } else {
+    a.cvec = (uint32_t)((unsigned long long)A + B) ^ A ^ B;
+    if (succ && t.lane == 0)
+      st_relaxed(rec + t.gtile, (t.epoch << 4) | (2ull << 2) | ((a.cvec >> OUTL) & 1u));
+    a.state = 2u;
+  }
+  return a;
+}
+
+template <int DL>
+__device__ __forceinline__ S add_end(const BgParams &p, const Tile &t, int k, int mode,
+                                     const AddState &a, const S &M, const S &C) {
+  if (a.state == 1u) return zero();
+  uint32_t cvec = a.cvec;
+  if (a.state == 0u) {
+    constexpr int OUTL = SL + DL;
+    unsigned long long *rec = p.records + (long long)k * p.n_tiles;
+    const uint32_t cin = lookback(rec, t.gtile, t.first, t.epoch, p.spin_limit, p.state, t.lane);
+    const uint32_t A = a.Gm | a.Pm, B = a.Gm;
+    cvec = (uint32_t)((unsigned long long)A + B + ((unsigned long long)cin << DL)) ^ A ^ B;
+    if (((a.Pm >> (OUTL & 31)) & 1u) && t.lane == 0)
+      st_relaxed(rec + t.gtile, (t.epoch << 4) | (2ull << 2) | ((cvec >> OUTL) & 1u));
+  }
+  uint32_t c = (cvec >> t.lane) & 1u;
+  S r;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const unsigned long long s = (unsigned long long)a.xb[j] + a.yb[j] + c;
+    const uint32_t sum = __brev((uint32_t)s);
+    c = (uint32_t)(s >> 32);
+    r.w[j] = mode == 0 ? ((sum ^ (C.w[j] & t.vm.w[j])) | M.w[j]) : (sum & ~C.w[j]);
+  }
+  return r;
+}
+
 /* ---------------------------------------------------------------------------------------
  * Tile scheduling, loads and stores
  * --------------------------------------------------------------------------------------- */
@@ -384,8 +475,12 @@ __device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
   t.W = (t.n + 31) >> 5;
   t.base = ((long long)g - t.first) * SW - (long long)HL * WPT;
 #pragma unroll
-  for (int j = 0; j < WPT; ++j)
-    t.vm.w[j] = (t.base + t.lane * WPT + j >= 0) ? FULL : 0u;
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    t.vm.w[j] = (w >= 0) ? FULL : 0u;
+    const long long rem = t.n - 32 * w;
+    t.em.w[j] = rem >= 32 ? FULL : (rem <= 0 ? 0u : (FULL << (32 - rem)));
+  }
   if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
     (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
                       p.spin_limit, p.state, t.lane);
@@ -438,7 +533,7 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile t, int o
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
     const long long w = t.base + t.lane * WPT + j;
-    if (t.lane >= HL && w >= 0 && w < t.W) {
+    if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) {
       uint32_t val = v.w[j];
       const long long rem = t.n - 32 * w;
       if (rem < 32) val &= FULL << (32 - rem);

@@ -28,7 +28,7 @@ constexpr int T = 256; /* threads (= words) per block */
 constexpr unsigned FULL = 0xffffffffu;
 
 enum { OP_AND = 0, OP_OR, OP_XOR, OP_NOT, OP_SEL, OP_ADV, OP_MATCHSTAR, OP_SCANTHRU, OP_COPY,
-       OP_WHILE, OP_IF };
+       OP_WHILE, OP_IF, OP_LOOK };
 
 __global__ void k_bitwise(int op, uint32_t *__restrict__ d, const uint32_t *__restrict__ a,
                           const uint32_t *__restrict__ b, const uint32_t *__restrict__ c,
@@ -64,6 +64,26 @@ __global__ void k_advance(uint32_t *__restrict__ d, const uint32_t *__restrict__
     const uint32_t cur = (w - q >= 0) ? a[w - q] : 0u;
     const uint32_t prev = (w - q - 1 >= 0) ? a[w - q - 1] : 0u;
     d[w] = r == 0 ? cur : __funnelshift_r(cur, prev, r);
+  }
+}
+
+/* Lookahead(a, shift): character p takes a[p + shift]; positions >= n read as 0. */
+__global__ void k_lookahead(uint32_t *__restrict__ d, const uint32_t *__restrict__ a, int64_t shift,
+                            int64_t W, int64_t n) {
+  const int64_t q = shift / 32;
+  const int r = (int)(shift % 32);
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < W;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t v[2];
+    for (int k = 0; k < 2; ++k) {
+      const int64_t i = w + q + k;
+      uint32_t x = i < W ? a[i] : 0u;
+      const int64_t rem = n - 32 * i;
+      if (rem <= 0) x = 0u;
+      else if (rem < 32) x &= FULL << (32 - rem);
+      v[k] = x;
+    }
+    d[w] = r == 0 ? v[0] : __funnelshift_l(v[1], v[0], r);
   }
 }
 
@@ -263,6 +283,15 @@ struct Exec {
           k_advance<<<grid_for(W), T, 0, s>>>(slot[I.dst], slot[I.a], I.shift, W);
           ++pc;
           break;
+        case OP_LOOK:
+          if (I.dst == I.a) {
+            status = BG_ERR_INVALID;
+            err = "Lookahead must not write its own operand";
+            return;
+          }
+          k_lookahead<<<grid_for(W), T, 0, s>>>(slot[I.dst], slot[I.a], I.shift, W, n);
+          ++pc;
+          break;
         case OP_MATCHSTAR: case OP_SCANTHRU: {
           const int64_t nb = (W + T - 1) / T;
           k_add_agg<<<(unsigned)nb, T, 0, s>>>(I.op, slot[I.a], slot[I.b], W, agg);
@@ -312,8 +341,8 @@ int bg_interp_create(const bg_instr *code, int32_t n_code, int32_t n_slots,
   for (int32_t i = 0; i < n_code; ++i) {
     const bg_instr &I = code[i];
     auto bad = [&](int v) { return v < -1 || v >= n_slots; };
-    if (I.op < 0 || I.op > OP_IF || bad(I.dst) || bad(I.a) || bad(I.b) || bad(I.c) ||
-        (I.op <= OP_COPY && (I.dst < 10 || I.a < 0)) || I.shift < 0 ||
+    if (I.op < 0 || I.op > OP_LOOK || bad(I.dst) || bad(I.a) || bad(I.b) || bad(I.c) ||
+        ((I.op <= OP_COPY || I.op == OP_LOOK) && (I.dst < 10 || I.a < 0)) || I.shift < 0 ||
         ((I.op == OP_AND || I.op == OP_OR || I.op == OP_XOR || I.op == OP_MATCHSTAR ||
           I.op == OP_SCANTHRU) && I.b < 0) || (I.op == OP_SEL && (I.b < 0 || I.c < 0)) ||
         (I.op == OP_WHILE && i + 1 + (int64_t)I.shift > n_code) ||

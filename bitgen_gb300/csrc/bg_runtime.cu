@@ -118,6 +118,10 @@ struct bg_plan {
   int grid = 1;
   int64_t debug_wait_tile = -1;
   int64_t spin_limit = 0;
+  int64_t cap_inputs = 0, cap_tiles = 0;
+  int64_t *h_stage = nullptr; /* pinned staging of the tables */
+  cudaEvent_t staged = nullptr;
+  bool staged_pending = false;
 };
 
 extern "C" {
@@ -323,7 +327,8 @@ int bg_nvrtc_check(const char *source, size_t source_len, const char *name, char
 
 int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   if (!desc || !out || !desc->source || !desc->name || desc->wpt < 1 || desc->wpt > 8 ||
-      desc->halo_lanes < 0 || desc->halo_lanes > 31 || desc->n_outputs < 0 || desc->n_adds < 0 ||
+      desc->halo_lanes < 0 || desc->tail_lanes < 0 || desc->halo_lanes + desc->tail_lanes > 31 ||
+      desc->n_outputs < 0 || desc->n_adds < 0 ||
       desc->block < 32 || desc->block % 32)
     return fail(BG_ERR_INVALID, "bg_program_create: bad descriptor");
   *out = nullptr;
@@ -397,61 +402,115 @@ int bg_program_destroy(bg_program *prog) {
 /* ======================================================================================== */
 /* Plans                                                                                    */
 /* ======================================================================================== */
-int bg_plan_create(bg_program *prog, const bg_layout *L, bg_plan **out) {
-  if (!prog || !L || !out || L->n_inputs < 1 || !L->in_off || !L->in_len || !L->out_off ||
-      (L->input_kind != BG_INPUT_BYTES && L->input_kind != BG_INPUT_BASIS))
-    return fail(BG_ERR_INVALID, "bg_plan_create: bad layout");
-  *out = nullptr;
+/* tables for a layout: in_off | in_len | tile_prefix | out_off; returns the tile count or < 0 */
+static int64_t build_tables(const bg_program *prog, const bg_layout *L, int64_t *t) {
   const int64_t n = L->n_inputs;
-  const int64_t tile_words = (int64_t)(32 - prog->desc.halo_lanes) * prog->desc.wpt;
-  std::vector<int64_t> tables(4 * n + 1);
-  int64_t *in_off = tables.data(), *in_len = in_off + n, *prefix = in_len + n,
-          *out_off = prefix + n + 1;
+  const int64_t tile_words =
+      (int64_t)(32 - prog->desc.halo_lanes - prog->desc.tail_lanes) * prog->desc.wpt;
+  int64_t *in_off = t, *in_len = t + n, *prefix = t + 2 * n, *out_off = t + 3 * n + 1;
   prefix[0] = 0;
   for (int64_t i = 0; i < n; ++i) {
-    if (L->in_len[i] < 0 || L->in_off[i] < 0)
-      return fail(BG_ERR_INVALID, "bg_plan_create: negative offset or length");
+    if (L->in_len[i] < 0 || L->in_off[i] < 0) return -fail(BG_ERR_INVALID, "layout: negative offset or length");
     if (L->input_kind == BG_INPUT_BYTES && (L->in_off[i] & 15))
-      return fail(BG_ERR_ALIGN, "bg_plan_create: byte offsets must be multiples of 16");
+      return -fail(BG_ERR_ALIGN, "layout: byte offsets must be multiples of 16");
     in_off[i] = L->in_off[i];
     in_len[i] = L->in_len[i];
     out_off[i] = L->out_off[i];
     const int64_t W = (L->in_len[i] + 31) / 32;
     prefix[i + 1] = prefix[i] + std::max<int64_t>(1, (W + tile_words - 1) / tile_words);
   }
+  return prefix[n];
+}
+
+static bool layout_ok(const bg_layout *L) {
+  return L && L->n_inputs >= 1 && L->in_off && L->in_len && L->out_off &&
+         (L->input_kind == BG_INPUT_BYTES || L->input_kind == BG_INPUT_BASIS);
+}
+
+int bg_plan_reserve(bg_program *prog, int32_t input_kind, int32_t max_inputs, int64_t max_tiles,
+                    bg_plan **out) {
+  if (!prog || !out || max_inputs < 1 || max_tiles < 1 || max_tiles >= (int64_t)0xffffffffll ||
+      (input_kind != BG_INPUT_BYTES && input_kind != BG_INPUT_BASIS))
+    return fail(BG_ERR_INVALID, "bg_plan_reserve: bad arguments");
+  *out = nullptr;
   bg_plan *p = new (std::nothrow) bg_plan();
-  if (!p) return fail(BG_ERR_NOMEM, "bg_plan_create: out of host memory");
+  if (!p) return fail(BG_ERR_NOMEM, "bg_plan_reserve: out of host memory");
   p->prog = prog;
-  p->layout = *L;
-  p->n_tiles = prefix[n];
-  if (p->n_tiles >= (int64_t)0xffffffffll) {
-    delete p;
-    return fail(BG_ERR_INVALID, "bg_plan_create: too many tiles for one launch");
-  }
+  p->layout.input_kind = input_kind;
+  p->cap_inputs = max_inputs;
+  p->cap_tiles = max_tiles;
   auto cleanup = [&](int code, const std::string &m) {
-    if (p->d_tables) cudaFree(p->d_tables);
-    if (p->d_records) cudaFree(p->d_records);
-    if (p->d_state) cudaFree(p->d_state);
-    delete p;
+    bg_plan_destroy(p);
     return fail(code, m);
   };
-  if (cudaMalloc(&p->d_tables, tables.size() * sizeof(int64_t)) != cudaSuccess)
-    return cleanup(BG_ERR_NOMEM, "bg_plan_create: tables");
-  if (cudaMemcpy(p->d_tables, tables.data(), tables.size() * sizeof(int64_t),
-                 cudaMemcpyHostToDevice) != cudaSuccess)
-    return cleanup(BG_ERR_CUDA, "bg_plan_create: table upload");
-  const size_t nrec = (size_t)std::max(1, prog->desc.n_adds) * (size_t)p->n_tiles;
+  const size_t ntab = 4 * (size_t)max_inputs + 1;
+  if (cudaMalloc(&p->d_tables, ntab * sizeof(int64_t)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: tables");
+  if (cudaMallocHost(&p->h_stage, ntab * sizeof(int64_t)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: staging");
+  if (cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming) != cudaSuccess)
+    return cleanup(BG_ERR_CUDA, "bg_plan_reserve: event");
+  const size_t nrec = (size_t)std::max(1, prog->desc.n_adds) * (size_t)max_tiles;
   if (cudaMalloc(&p->d_records, nrec * sizeof(unsigned long long)) != cudaSuccess)
-    return cleanup(BG_ERR_NOMEM, "bg_plan_create: look-back records");
+    return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: look-back records");
   if (cudaMemset(p->d_records, 0, nrec * sizeof(unsigned long long)) != cudaSuccess)
-    return cleanup(BG_ERR_CUDA, "bg_plan_create: clearing records");
+    return cleanup(BG_ERR_CUDA, "bg_plan_reserve: clearing records");
   if (cudaMalloc(&p->d_state, 8 * sizeof(uint32_t)) != cudaSuccess)
-    return cleanup(BG_ERR_NOMEM, "bg_plan_create: state");
+    return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: state");
   if (cudaMemset(p->d_state, 0, 8 * sizeof(uint32_t)) != cudaSuccess)
-    return cleanup(BG_ERR_CUDA, "bg_plan_create: clearing state");
-  const int warps_per_block = prog->desc.block / 32;
-  const int64_t need = (p->n_tiles + warps_per_block - 1) / warps_per_block;
-  p->grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sm_count() * prog->blocks_per_sm));
+    return cleanup(BG_ERR_CUDA, "bg_plan_reserve: clearing state");
+  *out = p;
+  return BG_OK;
+}
+
+int bg_plan_set_layout(bg_plan *p, const bg_layout *L, void *stream) {
+  if (!p || !layout_ok(L) || L->input_kind != p->layout.input_kind)
+    return fail(BG_ERR_INVALID, "bg_plan_set_layout: bad layout");
+  if (L->n_inputs > p->cap_inputs)
+    return fail(BG_ERR_INVALID, "bg_plan_set_layout: more inputs than reserved");
+  /* the staging buffer may still feed the previous upload */
+  if (p->staged_pending) {
+    if (cudaEventSynchronize(p->staged) != cudaSuccess)
+      return fail(BG_ERR_CUDA, "bg_plan_set_layout: waiting for the previous upload");
+    p->staged_pending = false;
+  }
+  const int64_t tiles = build_tables(p->prog, L, p->h_stage);
+  if (tiles < 0) return (int)-tiles;
+  if (tiles > p->cap_tiles)
+    return fail(BG_ERR_INVALID, "bg_plan_set_layout: more tiles than reserved");
+  const size_t ntab = 4 * (size_t)L->n_inputs + 1;
+  cudaStream_t s = (cudaStream_t)stream;
+  BG_CUDA(cudaMemcpyAsync(p->d_tables, p->h_stage, ntab * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  BG_CUDA(cudaEventRecord(p->staged, s));
+  p->staged_pending = true;
+  p->layout = *L;
+  p->layout.in_off = p->layout.in_len = p->layout.out_off = nullptr; /* not retained */
+  p->n_tiles = tiles;
+  const int warps_per_block = p->prog->desc.block / 32;
+  const int64_t need = (tiles + warps_per_block - 1) / warps_per_block;
+  p->grid = (int)std::max<int64_t>(
+      1, std::min<int64_t>(need, (int64_t)sm_count() * p->prog->blocks_per_sm));
+  return BG_OK;
+}
+
+int bg_plan_create(bg_program *prog, const bg_layout *L, bg_plan **out) {
+  if (!prog || !out || !layout_ok(L)) return fail(BG_ERR_INVALID, "bg_plan_create: bad layout");
+  *out = nullptr;
+  std::vector<int64_t> tables(4 * (size_t)L->n_inputs + 1);
+  const int64_t tiles = build_tables(prog, L, tables.data());
+  if (tiles < 0) return (int)-tiles;
+  if (tiles >= (int64_t)0xffffffffll) return fail(BG_ERR_INVALID, "bg_plan_create: too many tiles");
+  bg_plan *p = nullptr;
+  int rc = bg_plan_reserve(prog, L->input_kind, L->n_inputs, tiles, &p);
+  if (rc != BG_OK) return rc;
+  rc = bg_plan_set_layout(p, L, nullptr);
+  if (rc == BG_OK && cudaStreamSynchronize(nullptr) != cudaSuccess) rc = fail(BG_ERR_CUDA, "bg_plan_create: upload");
+  if (rc != BG_OK) {
+    std::string keep = g_last_error;
+    bg_plan_destroy(p);
+    g_last_error = keep;
+    return rc;
+  }
   *out = p;
   return BG_OK;
 }
@@ -518,9 +577,14 @@ int bg_plan_sync(bg_plan *plan, void *stream) {
 
 int bg_plan_destroy(bg_plan *plan) {
   if (!plan) return BG_OK;
-  cudaFree(plan->d_tables);
-  cudaFree(plan->d_records);
-  cudaFree(plan->d_state);
+  if (plan->staged) {
+    cudaEventSynchronize(plan->staged);
+    cudaEventDestroy(plan->staged);
+  }
+  if (plan->d_tables) cudaFree(plan->d_tables);
+  if (plan->d_records) cudaFree(plan->d_records);
+  if (plan->d_state) cudaFree(plan->d_state);
+  if (plan->h_stage) cudaFreeHost(plan->h_stage);
   delete plan;
   return BG_OK;
 }

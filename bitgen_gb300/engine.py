@@ -52,7 +52,7 @@ def _stream_ptr(stream: Optional[torch.cuda.Stream]) -> int:
 # whole-stream executor lowering
 # ----------------------------------------------------------------------------------------
 _IOP = {"and": 0, "or": 1, "xor": 2, "not": 3, "sel": 4, "advance": 5, "matchstar": 6,
-        "scanthru": 7, "assign": 8}
+        "scanthru": 7, "assign": 8, "lookahead": 11}
 OP_WHILE, OP_IF = 9, 10
 
 
@@ -231,16 +231,37 @@ def out_layout(lengths: Sequence[int], align_words: int = 4) -> Tuple[List[int],
 
 
 class Plan:
-    """A launch plan: device tables + look-back records for one input layout."""
+    """A launch plan: device tables + look-back records for an input layout.
 
-    def __init__(self, program: "Program", inp: Inputs, out_offsets: Sequence[int], out_stride: int):
+    ``Plan(program, inp, ...)`` binds one fixed layout; ``Plan.reserve(...)`` makes a plan with
+    room for changing layouts set by :meth:`set_layout` (batched / served scans)."""
+
+    def __init__(self, program: "Program", inp: Optional[Inputs], out_offsets: Sequence[int] = (),
+                 out_stride: int = 0, _handle=None):
         self.program = program
+        if _handle is not None:
+            self._h = _handle
+            self.n_inputs = 0
+            return
         self.n_inputs = inp.n
         lay = N.Layout(inp.kind, inp.n, _i64(inp.offsets), _i64(inp.lengths), inp.basis_stride,
                        _i64(out_offsets), out_stride)
         h = C.c_void_p()
         N.check(N.lib().bg_plan_create(program._handle, C.byref(lay), C.byref(h)), "bg_plan_create")
         self._h = h
+
+    @classmethod
+    def reserve(cls, program: "Program", kind: int, max_inputs: int, max_tiles: int) -> "Plan":
+        h = C.c_void_p()
+        N.check(N.lib().bg_plan_reserve(program._handle, kind, max_inputs, max_tiles, C.byref(h)),
+                "bg_plan_reserve")
+        return cls(program, None, _handle=h)
+
+    def set_layout(self, inp: Inputs, out_offsets: Sequence[int], out_stride: int, stream: int):
+        lay = N.Layout(inp.kind, inp.n, _i64(inp.offsets), _i64(inp.lengths), inp.basis_stride,
+                       _i64(out_offsets), out_stride)
+        N.check(N.lib().bg_plan_set_layout(self._h, C.byref(lay), stream), "bg_plan_set_layout")
+        self.n_inputs = inp.n
 
     @property
     def tiles(self) -> int:
@@ -298,7 +319,7 @@ class Program:
             src = self.spec.source.encode()
             self._desc = N.KernelDesc(src, len(src), name.encode(), self.spec.n_outputs,
                                       self.spec.n_adds, self.spec.halo_lanes, self.spec.wpt,
-                                      self.spec.block)
+                                      self.spec.block, self.spec.tail_lanes)
             h = C.c_void_p()
             N.check(lib.bg_program_create(C.byref(self._desc), C.byref(h)), "bg_program_create")
             self._handle = h
@@ -326,6 +347,11 @@ class Program:
         return {"executor": "fused", "registers": r.value, "local_bytes": l.value,
                 "blocks_per_sm": b.value, "halo_lanes": self.spec.halo_lanes, "wpt": self.spec.wpt,
                 "adds": self.spec.n_adds, "outputs": self.spec.n_outputs}
+
+    def tiles_for(self, lengths: Sequence[int]) -> int:
+        """Tiles one launch over inputs of these lengths needs."""
+        tw = self.spec.tile_words
+        return sum(max(1, -(-(-(-int(n) // 32)) // tw)) for n in lengths)
 
     def plan(self, inp: Inputs, out_offsets: Sequence[int], out_stride: int) -> Plan:
         key = (inp.kind, tuple(inp.offsets), tuple(inp.lengths), inp.basis_stride,

@@ -4,7 +4,9 @@ The dialect is the one BitGen's front end reads (icgrep's ``-print-pablo`` outpu
 
 * ``x = (a & b)``, ``(a | b)``, ``(a ^ b)``, ``~a`` / ``(~a)``, ``(c ? a : b)``
   (``bitgen/bitparser/bitstream_parser.py:47-100``);
-* ``x = pablo.Advance(a, n)``, ``pablo.MatchStar(m, c)``, ``pablo.ScanThru(m, c)``
+* ``x = pablo.Advance(a, n)``, ``pablo.MatchStar(m, c)``, ``pablo.ScanThru(m, c)``,
+  ``pablo.Lookahead(a, n)`` (icgrep's later Pablo has it; the reference parser does not; used
+  here for the ``$`` anchor)
   (``operation_name_map``, ``bitstream_parser.py:9-17``).  The reference parser raises
   ``NotImplementedError`` for the last two (``bitstream_parser.py:202-211``); this engine
   executes them;
@@ -44,6 +46,7 @@ OP_ARITY = {
     "xor": 2,
     "sel": 3,        # sel(c, a, b) = (c & a) | (~c & b)
     "advance": 1,    # advance(a; n)
+    "lookahead": 1,  # lookahead(a; n): position p takes a[p + n]; zeros enter past the end
     "matchstar": 2,  # matchstar(m, c) = (((m & c) + c) ^ c) | m
     "scanthru": 2,   # scanthru(m, c) = (m + c) & ~c
 }
@@ -61,8 +64,8 @@ class Op:
             raise ValueError(f"unknown op {self.op}")
         if len(self.args) != OP_ARITY[self.op]:
             raise ValueError(f"{self.op} takes {OP_ARITY[self.op]} operands, got {self.args}")
-        if self.op == "advance" and self.shift < 0:
-            raise ValueError("Advance distance must be >= 0")
+        if self.op in ("advance", "lookahead") and self.shift < 0:
+            raise ValueError("Advance / Lookahead distance must be >= 0")
 
     def text(self) -> str:
         a = self.args
@@ -77,6 +80,8 @@ class Op:
             rhs = f"({a[0]} ? {a[1]} : {a[2]})"
         elif self.op == "advance":
             rhs = f"pablo.Advance({a[0]}, {self.shift})"
+        elif self.op == "lookahead":
+            rhs = f"pablo.Lookahead({a[0]}, {self.shift})"
         elif self.op == "matchstar":
             rhs = f"pablo.MatchStar({a[0]}, {a[1]})"
         else:
@@ -189,10 +194,11 @@ def _parse_rhs(dst: str, expr: str, defined: set, lineno: int) -> Op:
         args = [a.strip() for a in argtxt.split(",")]
         if fn == "Next":
             return Op(dst, "assign", (_operand(args[0], defined, lineno),))
-        if fn == "pablo.Advance":
+        if fn in ("pablo.Advance", "pablo.Lookahead"):
             if len(args) != 2:
-                raise PabloSyntaxError(f"line {lineno}: Advance takes 2 arguments")
-            return Op(dst, "advance", (_operand(args[0], defined, lineno),), shift=int(args[1]))
+                raise PabloSyntaxError(f"line {lineno}: {fn} takes 2 arguments")
+            op = "advance" if fn == "pablo.Advance" else "lookahead"
+            return Op(dst, op, (_operand(args[0], defined, lineno),), shift=int(args[1]))
         if fn in ("pablo.MatchStar", "pablo.ScanThru"):
             if len(args) != 2:
                 raise PabloSyntaxError(f"line {lineno}: {fn} takes 2 arguments")

@@ -16,8 +16,10 @@ have the same set of match ends as their greedy forms and are compiled alike.
 
 Supported syntax: literals and escapes (``\\xHH``, ``\\n \\r \\t \\f \\v \\e \\a``, escaped
 punctuation), classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S``, ``.``,
-groups ``(...)`` / ``(?:...)``, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``.
-``$`` is rejected with :class:`UnsupportedRegex`.
+groups ``(...)`` / ``(?:...)``, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
+and ``$`` where nothing can follow it (end of the regex or of a final alternative): a match ending
+at p counts only if byte p+1 is LF or p is the last position, i.e.
+``L & ~Lookahead(~LF, 1)``.
 
 Compilation keeps two markers per regex state: ``L`` (positions of the last byte consumed) and
 ``P`` (positions where the next byte is to be matched, i.e. ``Advance(L, 1)`` plus any
@@ -69,6 +71,11 @@ class Rep:
 
 @dataclass(frozen=True)
 class Start:
+    pass
+
+
+@dataclass(frozen=True)
+class End:
     pass
 
 
@@ -173,7 +180,7 @@ class _Parser:
         if c == "^":
             return Start()
         if c == "$":
-            raise UnsupportedRegex("$ anchors are not supported by this emitter")
+            return End()
         if c == "\\":
             e = self.escape()
             return CC(e) if isinstance(e, frozenset) else CC(frozenset([e]))
@@ -382,6 +389,17 @@ class _Compiler:
         L, P = st
         return P if P is not None else self.b.ADV(L, 1)
 
+    def eol(self):
+        """Positions followed by LF or by the end of the input: ~Lookahead(~LF, 1)."""
+        if getattr(self, "_eol", None) is None:
+            lf = self.b.cc(frozenset([LF]))
+            saved, self.b.top = self.b.top, True
+            nlf = self.b.NOT(lf)
+            la = self.b.emit("lookahead", (nlf,), shift=1)
+            self._eol = self.b.NOT(la)
+            self.b.top = saved
+        return self._eol
+
     def sol(self):
         if self._sol is None:
             lf = self.b.cc(frozenset([LF]))
@@ -390,18 +408,22 @@ class _Compiler:
             self.b.top = saved
         return self._sol
 
-    def run(self, node, st):
+    def run(self, node, st, at_end=False):
         b = self.b
+        if isinstance(node, End):
+            if not at_end:
+                raise UnsupportedRegex("$ is only supported where nothing can follow it")
+            return (b.AND(st[0], self.eol()), "0")
         if isinstance(node, CC):
             c = b.cc(node.bytes_)
             L = b.AND(self.P(st), c)
             return (L, None)
         if isinstance(node, Seq):
-            for it in node.items:
-                st = self.run(it, st)
+            for i, it in enumerate(node.items):
+                st = self.run(it, st, at_end and i == len(node.items) - 1)
             return st
         if isinstance(node, Alt):
-            outs = [self.run(it, st) for it in node.items]
+            outs = [self.run(it, st, at_end) for it in node.items]
             L = "0"
             P = "0"
             for o in outs:
@@ -490,7 +512,7 @@ def compile_group(regexes: List[str], matchstar: bool = True) -> Group:
     for r in regexes:
         ast = parse_regex(r)
         comp = _Compiler(b, matchstar)
-        L, _ = comp.run(ast, ("0", "1"))
+        L, _ = comp.run(ast, ("0", "1"), at_end=True)
         results.append(L)
     acc = "0"
     for L in results:

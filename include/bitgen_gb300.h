@@ -68,9 +68,11 @@ typedef struct bg_kernel_desc {
   const char *name;   /* __global__ entry point                                       */
   int32_t n_outputs;  /* output streams written by one launch                          */
   int32_t n_adds;     /* MatchStar / ScanThru additions (look-back record sets)         */
-  int32_t halo_lanes; /* tile geometry: 32 lanes, the first halo_lanes re-computed      */
+  int32_t halo_lanes; /* tile geometry: 32 lanes, the first halo_lanes and the last
+                         tail_lanes re-computed; (32-halo-tail)*wpt words written       */
   int32_t wpt;        /* 32-bit words per lane                                          */
   int32_t block;      /* threads per CTA                                                */
+  int32_t tail_lanes;
 } bg_kernel_desc;
 
 int bg_program_create(const bg_kernel_desc *desc, bg_program **out);
@@ -97,7 +99,15 @@ typedef struct bg_layout {
 } bg_layout;
 
 typedef struct bg_plan bg_plan;
+/* Plan for one fixed layout (tables uploaded synchronously). */
 int bg_plan_create(bg_program *prog, const bg_layout *layout, bg_plan **out);
+/* Plan with room for up to max_inputs inputs / max_tiles tiles, for layouts that change between
+ * launches (batched and served scans); no layout is set yet. */
+int bg_plan_reserve(bg_program *prog, int32_t input_kind, int32_t max_inputs, int64_t max_tiles,
+                    bg_plan **out);
+/* Set the layout of later launches: tables are staged in pinned memory and uploaded on `stream`
+ * (stream-ordered before the next bg_plan_launch on the same stream). */
+int bg_plan_set_layout(bg_plan *plan, const bg_layout *layout, void *stream);
 /* Number of tiles one launch processes. */
 int64_t bg_plan_tiles(const bg_plan *plan);
 /* Bound (clock64 cycles, 0 = default of about 1 s) for every look-back wait of later launches.
@@ -120,7 +130,8 @@ int bg_plan_destroy(bg_plan *plan);
  * The program is a flat instruction list:
  *   op = 0 AND, 1 OR, 2 XOR, 3 NOT, 4 SEL, 5 ADVANCE, 6 MATCHSTAR, 7 SCANTHRU, 8 COPY,
  *        9 WHILE (a = condition slot, shift = body length), 10 IF (a = condition slot,
- *        shift = then length, b = else length; else body follows the then body)
+ *        shift = then length, b = else length; else body follows the then body),
+ *        11 LOOKAHEAD (position p takes a[p + shift]; zeros past the end of the input)
  *   dst/a/b/c are variable slots; slot 0..7 = basis0..7, slot 8 = all zeros, 9 = all ones.
  * ------------------------------------------------------------------------------------- */
 typedef struct bg_instr {

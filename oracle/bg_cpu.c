@@ -3,7 +3,8 @@
  * Executes the flat instruction list of include/bitgen_gb300.h (bg_instr) over one input on the
  * host, with the semantics of the reference's stream operators:
  *   bitwise ops            bitgen/template/template.py:27-61
- *   Advance                template.py:63-70 (zeros enter at position 0)
+ *   Advance                template.py:63-70 (zeros enter at position 0); Lookahead is its
+ *                          mirror image (zeros enter past the end of the input)
  *   MatchStar              (((M & C) + C) ^ C) | M        template_torch.py:392-407
  *   ScanThru               (M + C) & ~C                   template_torch.py:377-389
  *   SEL                    (c & a) | (~c & b)             bitgen/inst/inst_sel.py:42-57
@@ -26,7 +27,7 @@ typedef struct bgc_instr {
 } bgc_instr;
 
 enum { OP_AND = 0, OP_OR, OP_XOR, OP_NOT, OP_SEL, OP_ADV, OP_MATCHSTAR, OP_SCANTHRU, OP_COPY,
-       OP_WHILE, OP_IF };
+       OP_WHILE, OP_IF, OP_LOOK };
 
 #define BGC_OK 0
 #define BGC_ERR_INVALID 1
@@ -159,6 +160,23 @@ static void exec_range(Ctx *C, int pc, int end) {
         if (C->carry) C->carry[pc] = (uint8_t)cy;
         break;
       }
+      case OP_LOOK: { /* position p takes a[p + shift]; positions at or beyond n read as 0 */
+        const int64_t q = I->shift / 64;
+        const int r = (int)(I->shift % 64);
+        const int64_t full = C->n / 64, rem = C->n % 64;
+        for (int64_t w = 0; w < nw; ++w) {
+          uint64_t v[2];
+          for (int k = 0; k < 2; ++k) {
+            const int64_t i = w + q + k;
+            uint64_t x = i < nw ? a[i] : 0;
+            if (i > full || (i == full && rem == 0)) x = 0;
+            else if (i == full) x &= (1ull << rem) - 1;
+            v[k] = x;
+          }
+          d[w] = r ? ((v[0] >> r) | (v[1] << (64 - r))) : v[0];
+        }
+        break;
+      }
       case OP_WHILE: {
         int64_t it = 0;
         while (C->status == BGC_OK && any_bits(C, C->slot[I->a])) {
@@ -214,7 +232,7 @@ int bgc_run(const bgc_instr *code, int n_code, int n_slots, const int *outs, int
   int control = 0;
   int64_t max_q = 0;
   for (int i = 0; i < n_code; ++i) {
-    if (code[i].op == OP_WHILE || code[i].op == OP_IF) control = 1;
+    if (code[i].op == OP_WHILE || code[i].op == OP_IF || code[i].op == OP_LOOK) control = 1;
     if (code[i].op == OP_ADV && code[i].shift / 64 + 1 > max_q) max_q = code[i].shift / 64 + 1;
   }
   const int64_t NW = (n + 63) / 64;

@@ -3,7 +3,8 @@
 It shares nothing with the bitstream compiler except the regex parser: the parsed regex is
 turned into an epsilon-NFA and simulated position by position, injecting the start state at
 every position (matches may start anywhere).  Bit ``p`` of the result is set iff some non-empty
-match ends with the byte at ``p``.  ``^`` holds at position 0 and after an LF.  This is the
+match ends with the byte at ``p``.  ``^`` holds at position 0 and after an LF; ``$`` holds before
+an LF and at the end of the input.  This is the
 match-end convention stated in ``bitgen_gb300.regex`` for BitGen's count check against icgrep
 (``bitgen/from_icgrep.py:59-121``): the count of a group is the popcount of the OR of its
 regexes' streams (``bitgen/bitstream.py:60-61``).
@@ -11,7 +12,7 @@ regexes' streams (``bitgen/bitstream.py:60-61``).
 
 from __future__ import annotations
 
-from bitgen_gb300.regex import CC, Alt, Rep, Seq, Start, parse_regex
+from bitgen_gb300.regex import CC, Alt, End, Rep, Seq, Start, parse_regex
 
 LF = 0x0A
 
@@ -32,6 +33,11 @@ class _NFA:
         """Return (entry, exit) state ids; exit is an 'eps' state with no successors yet."""
         if isinstance(node, CC):
             a = self.new("cc", node.bytes_)
+            e = self.new("eps")
+            self.out[a].append(e)
+            return a, e
+        if isinstance(node, End):
+            a = self.new("eol")
             e = self.new("eps")
             self.out[a].append(e)
             return a, e
@@ -90,7 +96,7 @@ def match_ends(regex: str, data: bytes) -> int:
     acc = nfa.new("acc")
     nfa.out[end].append(acc)
 
-    def closure(states, sol):
+    def closure(states, sol, eol=False):
         seen = set()
         stack = list(states)
         while stack:
@@ -102,6 +108,8 @@ def match_ends(regex: str, data: bytes) -> int:
             if k == "eps":
                 stack.extend(nfa.out[s])
             elif k == "sol" and sol:
+                stack.extend(nfa.out[s])
+            elif k == "eol" and eol:
                 stack.extend(nfa.out[s])
         return seen
 
@@ -117,7 +125,8 @@ def match_ends(regex: str, data: bytes) -> int:
             if nfa.kind[s] == "cc" and byte in nfa.arg[s]:
                 nxt.update(nfa.out[s])
         sol_next = byte == LF
-        cur = closure(nxt, sol_next)
+        eol_next = p + 1 == n or data[p + 1] == LF
+        cur = closure(nxt, sol_next, eol_next)
         if acc in cur:
             result |= 1 << p
     return result

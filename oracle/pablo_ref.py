@@ -16,7 +16,8 @@ It restates, in plain Python/numpy, what the reference computes on its hot path:
 
   - bitwise ops: ``bitgen/template/template.py:27-61``;
   - ``Advance(a, n)`` moves marks to higher positions and shifts zeros in at position 0
-    (``template.py:63-70``; ``bitgen/bitstream.py:152-159``);
+    (``template.py:63-70``; ``bitgen/bitstream.py:152-159``); ``Lookahead(a, n)`` is its mirror
+    image (position p takes a[p + n], zeros enter past the end of the input);
   - ``MatchStar(M, C) = (((M & C) + C) ^ C) | M`` (``template.py:96-103``,
     ``bitgen/template/template_torch.py:392-407``);
   - ``ScanThru(M, C) = (M + C) & ~C`` (``template_torch.py:377-389``; the numpy template at
@@ -126,6 +127,8 @@ def run_group(group: Group, data, n: int | None = None, max_iters: int = 1 << 24
                     r = (x[0] & x[1]) | (~x[0] & x[2] & mask)
                 elif s.op == "advance":
                     r = advance(x[0], s.shift, mask)
+                elif s.op == "lookahead":
+                    r = (x[0] & mask) >> s.shift
                 elif s.op == "matchstar":
                     r = matchstar(x[0], x[1], mask)
                 elif s.op == "scanthru":

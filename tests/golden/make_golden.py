@@ -9,6 +9,9 @@ parts of the reference are what pin the oracle:
   seeded random inputs, including all 256 byte values and ragged lengths;
 * ``ops.npz``        - numpy stream templates ``bs_advance`` / ``bs_add`` / ``bs_match_star``
   (bitgen/template/template.py:63-103) on seeded random bool streams;
+* ``readme_kat.npz`` - the reference's quick-start known answer (``README.md:124-142``): the 8
+  regexes of ``datasets_small/snort_small.regex``, the first 10 000 bytes of
+  ``datasets_small/snort_10KB.input``, 4 groups, published count 16;
 * ``parser.json``    - the reference parser's instruction list (type, operands, result) for the
   hand-written fixture bitgen/bitparser/xml_lexical_parsing.pablo and for Pablo emitted by this
   project (while-loop form), to pin the dialect this project's parser accepts.
@@ -89,6 +92,15 @@ def main():
         ops[f"add{i}"] = ref_tpl.bs_add(m.copy(), c.copy())
         ops[f"ms{i}"] = ref_tpl.bs_match_star(m.copy(), c.copy())
     np.savez_compressed(os.path.join(HERE, "ops.npz"), **ops)
+
+    # ---- README quick-start known answer ----------------------------------------------
+    from bitgen.tool.pcre import read_regex_from_pcre_file
+    rx = read_regex_from_pcre_file(os.path.join(REF, "datasets_small/snort_small.regex"))
+    with open(os.path.join(REF, "datasets_small/snort_10KB.input"), "rb") as f:
+        kat_input = np.frombuffer(f.read()[:10000], dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "readme_kat.npz"), input=kat_input,
+                        regexes=np.array(rx), n_groups=np.int64(4),
+                        expected_count=np.int64(16))  # README.md:138-142 "count 16"
 
     # ---- parser ------------------------------------------------------------------------
     sys.path.insert(0, REPO)
