@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--wpt", type=int, default=0, help="words per lane (0 = autotuned default)")
     ap.add_argument("--cpu-sample", type=int, default=4 << 20, help="bytes of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-modes", action="store_true", help="skip the batched / served legs")
+    ap.add_argument("--served-requests", type=int, default=600)
     return ap.parse_args()
 
 
@@ -139,6 +141,83 @@ def cpu_baseline(groups, base, sample_bytes):
     return {"value": round(sample_bytes / dt / 1e9, 6), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{sample_bytes} bytes of the same input, all {len(gs)} groups, one group per thread "
                       f"(C word-parallel evaluator, oracle/bg_cpu.c), {dt:.2f} s"}, counts
+
+
+def batched_leg(prog, ps, dev):
+    """4096 inputs, log-normal lengths (median 8 KiB, sigma 1, 200 B - 64 KiB): one persistent
+    CUDA-graph launch vs one launch per input, same GPU, outputs compared bit for bit."""
+    import numpy as np
+    import torch
+    from bitgen_gb300 import workloads
+    from bitgen_gb300.batched import BatchScanner, PerInputScanner
+
+    lens = workloads.batched_lengths(4096, seed=7)
+    items = workloads.batched_inputs(lens, 7, ps.witnesses)
+    total = int(sum(lens))
+    b = BatchScanner(prog, items, device=dev, graph=True)
+    p = PerInputScanner(prog, items, device=dev)
+    for _ in range(2):
+        b.run(); b.sync(); p.run(); p.sync()
+
+    def timed(sc, reps):
+        s = sc.stream
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            sc.run()
+        e1.record(s)
+        sc.sync()
+        return e0.elapsed_time(e1) / reps
+
+    tb = timed(b, 10)
+    tp = timed(p, 3)
+    exact = bool(torch.equal(b.counts, p.counts) and torch.equal(b.out, p.out))
+    return {"inputs": len(items), "bytes": total, "graph": True,
+            "batched_GBps": round(total / tb / 1e6, 3), "plain_GBps": round(total / tp / 1e6, 3),
+            "batched_ms": round(tb, 4), "plain_ms": round(tp, 4), "speedup": round(tp / tb, 2),
+            "bit_exact": exact, "median_len": int(np.median(lens))}
+
+
+def served_leg(dev, n_req, load_GBps):
+    """Poisson arrivals (seed 8) of requests with log-uniform lengths 64 B - 4 MiB over three
+    resident pattern sets (32, 256, 1024 regexes); continuous batching vs one launch per request."""
+    import numpy as np
+    from bitgen_gb300 import workloads
+    from bitgen_gb300.engine import Program
+    from bitgen_gb300.regex import compile_group
+    from bitgen_gb300.served import Request, Server, latency_stats, serve_plain
+
+    sets = {}
+    for name, n, seed in (("p32", 32, 81), ("p256", 256, 3), ("p1024", 1024, 83)):
+        ps = workloads.throughput_patterns(seed=seed, n=n)
+        sets[name] = (ps, Program([compile_group(g) for g in ps.groups(max(1, n // 16))]))
+    mean_len = ((4 << 20) - 64) / np.log((4 << 20) / 64)
+    rate = max(1.0, 0.8 * load_GBps * 1e9 / mean_len)
+    arr, lens, which = workloads.served_requests(n_req, seed=8, rate_per_s=rate)
+    names = list(sets)
+    reqs = []
+    for i in range(n_req):
+        nm = names[int(which[i])]
+        data = workloads.printable_text(int(lens[i]), 10_000 + i)
+        reqs.append(Request(i, float(arr[i]), nm, data))
+    progs = {k: v[1] for k, v in sets.items()}
+    srv = Server(progs, hbm_budget=120 << 30, slots=4, max_batch_bytes=64 << 20, max_batch_inputs=256)
+    import time
+    t0 = time.perf_counter()
+    got = srv.serve(reqs, realtime=True)
+    span = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    plain = serve_plain(progs, reqs, realtime=True)
+    pspan = time.perf_counter() - t1
+    total = int(sum(lens))
+    exact = all(np.array_equal(got[r.rid].counts, plain[r.rid].counts) for r in reqs)
+    return {"requests": n_req, "bytes": total, "offered_rate_per_s": round(rate, 1),
+            "pattern_sets": {k: len(v[0].regexes) for k, v in sets.items()},
+            "served": {**{k: round(v, 3) for k, v in latency_stats(got).items() if k != "n"},
+                       "GBps": round(total / span / 1e9, 3)},
+            "plain": {**{k: round(v, 3) for k, v in latency_stats(plain).items() if k != "n"},
+                      "GBps": round(total / pspan / 1e9, 3)},
+            "counts_equal_plain": exact, "hbm_budget_GB": 120}
 
 
 def run_reference(args):
@@ -295,6 +374,9 @@ def main():
     }
     if cb is not None:
         line["cpu_baseline"] = cb
+    if rank == 0 and not args.no_modes:
+        line["batched"] = batched_leg(prog, ps, dev)
+        line["served"] = served_leg(dev, args.served_requests, line["batched"]["batched_GBps"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -482,10 +482,10 @@ class _Gen:
         if ref in ("0u",):
             return "0u"
         if J >= 0:
-            return f"({self.w(ref, J)} & t.vm.w[{J}])"
+            return f"({self.w(ref, J)} & VM({J}))"
         L = (-J + wpt - 1) // wpt
         I = J + L * wpt
-        return f"__shfl_up_sync(FULL, {self.w(ref, I)} & t.vm.w[{I}], {L})"
+        return f"__shfl_up_sync(FULL, {self.w(ref, I)} & VM({I}), {L})"
 
     def word_fwd(self, ref: str, J: int) -> str:
         """Word (lane*WPT + J) of `ref` for J >= 0 (later lanes via shuffle down); positions at
@@ -494,9 +494,9 @@ class _Gen:
         if ref in ("0u",):
             return "0u"
         if J < wpt:
-            return f"({self.w(ref, J)} & t.em.w[{J}])"
+            return f"({self.w(ref, J)} & EM({J}))"
         L, I = divmod(J, wpt)
-        return f"__shfl_down_sync(FULL, {self.w(ref, I)} & t.em.w[{I}], {L})"
+        return f"__shfl_down_sync(FULL, {self.w(ref, I)} & EM({I}), {L})"
 
     def emit_op(self, name: str, n: Node, a: List[str], declare: bool = True):
         wpt = self.t.wpt
@@ -816,7 +816,7 @@ class _Gen:
             n = d.nodes[v]
             m, c = self.mat(n.args[0]), self.mat(n.args[1])
             mode = 0 if n.op == "matchstar" else 1
-            self.emit(f"const AddState st{v} = add_begin<{self.dl[v]}>(p, t, {self.adds[v]}, {mode}, "
+            self.emit(f"const AddState st{v} = add_begin<{self.dl[v]}, E>(p, t, {self.adds[v]}, {mode}, "
                       f"{self.pack(m)}, {self.pack(c)});")
             begun.add(v)
 
@@ -829,7 +829,7 @@ class _Gen:
                     add_begin(v)
                 m, c = self.mat(n.args[0]), self.mat(n.args[1])
                 mode = 0 if n.op == "matchstar" else 1
-                self.emit(f"const S {name}_s = add_end<{self.dl[v]}>(p, t, {self.adds[v]}, {mode}, st{v}, "
+                self.emit(f"const S {name}_s = add_end<{self.dl[v]}, E>(p, t, {self.adds[v]}, {mode}, st{v}, "
                           f"{self.pack(m)}, {self.pack(c)});")
                 for j in range(self.t.wpt):
                     pre = "const uint32_t " if declare else ""
@@ -1021,16 +1021,25 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
             terms.append((leaf, o))
     clusters = _cluster_terms(gen, terms, tuning.part_cap)
     funcs = []
+    sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
+    args = f"p, t, acc, {', '.join(f'b{i}_{j}' for i in range(8) for j in range(wpt))}"
     for ci, cl in enumerate(clusters):
         code = gen.part(cl)
+        # E = the tile touches an input boundary: only then are the start/end masks applied
         funcs.append(
             f"//@@BG_PART\n"
-            f'extern "C" __device__ __noinline__ void bg_part_{ci}(const BgParams &p, const Tile t, uint32_t *acc, '
-            f"{_basis_params(wpt)}) {{\n{code}\n}}\n")
+            f"template <bool E> __device__ __forceinline__ void bg_part_{ci}_body({sig}) {{\n{code}\n}}\n"
+            f'extern "C" __device__ __noinline__ void bg_part_{ci}_0({sig}) {{ bg_part_{ci}_body<false>({args}); }}\n'
+            f'extern "C" __device__ __noinline__ void bg_part_{ci}_1({sig}) {{ bg_part_{ci}_body<true>({args}); }}\n')
     decls = "\n".join(
-        f'extern "C" __device__ void bg_part_{ci}(const BgParams &p, const Tile t, uint32_t *acc, {_basis_params(wpt)});'
-        for ci in range(len(clusters)))
-    calls = "\n".join(f"    bg_part_{ci}(p, t, acc, {_basis_args(wpt)});" for ci in range(len(clusters)))
+        f'extern "C" __device__ void bg_part_{ci}_{e}({sig});'
+        for ci in range(len(clusters)) for e in (0, 1))
+    ba = _basis_args(wpt)
+    calls = ("    if (t.edge) {\n"
+             + "\n".join(f"      bg_part_{ci}_1(p, t, acc, {ba});" for ci in range(len(clusters)))
+             + "\n    } else {\n"
+             + "\n".join(f"      bg_part_{ci}_0(p, t, acc, {ba});" for ci in range(len(clusters)))
+             + "\n    }")
     comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
     maxreg = max(32, min(255, (65536 // (tuning.block * max(1, tuning.min_blocks))) // 8 * 8))
     src = (
@@ -1041,6 +1050,8 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"#define BG_NOUT {n_out}\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"
+        f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"
+        f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
         f"{comments}\n"
         + "\n".join(funcs) +
         f"//@@BG_KERNEL\n{decls}\n"

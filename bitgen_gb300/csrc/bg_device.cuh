@@ -123,6 +123,7 @@ struct Tile {
   int lane;
   S vm;              /* per word: all ones if the word index is >= 0     */
   S em;              /* per word: the bits of positions before the input end */
+  bool edge;         /* the tile has words before the input start or reaches its last word */
 };
 
 /* Advance(x, N): marks move N positions forward; words before the input start read as 0. */
@@ -198,7 +199,7 @@ __device__ __forceinline__ unsigned long long wait_record(const unsigned long lo
  * the nearest record that fixes the carry by itself: an inclusive carry, or an aggregate that
  * does not propagate.  Control flow is warp-uniform (decisions come from ballots / lane 0).
  * Waits are bounded like wait_record. */
-static __device__ __noinline__ uint32_t lookback(const unsigned long long *rec, long long gtile,
+static __device__ __forceinline__ uint32_t lookback(const unsigned long long *rec, long long gtile,
                                           long long first, unsigned long long epoch,
                                           long long spin_limit, uint32_t *state, int lane) {
   uint32_t acc = 0;
@@ -328,14 +329,14 @@ __device__ __noinline__ S add_slow(const BgParams &p, const Lk L, int k, int mod
 /* Inline fast path shared by MatchStar and ScanThru: when the marker is zero in the whole warp
  * and the carry lane does not propagate, no carry can enter and the result is zero; the
  * successor's carry (zero) is published if it will be needed. */
-template <int DL>
+template <int DL, bool E = true>
 __device__ __forceinline__ bool add_is_zero(const BgParams &p, const Tile &t, int k, const S &M,
                                             const S &C) {
   uint32_t mo = 0u, ao = 1u;
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
     mo |= M.w[j];
-    ao &= ((C.w[j] & t.vm.w[j]) == FULL) ? 1u : 0u;
+    ao &= ((C.w[j] & (E ? t.vm.w[j] : FULL)) == FULL) ? 1u : 0u;
   }
   if (__any_sync(FULL, mo != 0u)) return false;
   const uint32_t Pm = __ballot_sync(FULL, ao);
@@ -373,12 +374,12 @@ struct AddState {
   uint32_t state; /* 0 = look-back pending, 1 = result is zero, 2 = carries resolved */
 };
 
-template <int DL>
+template <int DL, bool E = true>
 __device__ __forceinline__ AddState add_begin(const BgParams &p, const Tile &t, int k, int mode,
                                               const S &M, const S &C) {
   AddState a;
   a.Gm = a.Pm = a.cvec = 0u;
-  if (add_is_zero<DL>(p, t, k, M, C)) {
+  if (add_is_zero<DL, E>(p, t, k, M, C)) {
     a.state = 1u;
 #pragma unroll
     for (int j = 0; j < WPT; ++j) a.xb[j] = a.yb[j] = 0u;
@@ -388,8 +389,8 @@ __device__ __forceinline__ AddState add_begin(const BgParams &p, const Tile &t, 
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
     const uint32_t x = mode == 0 ? (M.w[j] & C.w[j]) : M.w[j];
-    a.xb[j] = __brev(x & t.vm.w[j]);
-    a.yb[j] = __brev(C.w[j] & t.vm.w[j]);
+    a.xb[j] = __brev(E ? (x & t.vm.w[j]) : x);
+    a.yb[j] = __brev(E ? (C.w[j] & t.vm.w[j]) : C.w[j]);
     const uint32_t s = a.xb[j] + a.yb[j];
     const uint32_t g = s < a.xb[j] ? 1u : 0u;
     const uint32_t pp = s == FULL ? 1u : 0u;
@@ -422,7 +423,7 @@ __device__ __forceinline__ AddState add_begin(const BgParams &p, const Tile &t, 
   return a;
 }
 
-template <int DL>
+template <int DL, bool E = true>
 __device__ __forceinline__ S add_end(const BgParams &p, const Tile &t, int k, int mode,
                                      const AddState &a, const S &M, const S &C) {
   if (a.state == 1u) return zero();
@@ -443,7 +444,7 @@ __device__ __forceinline__ S add_end(const BgParams &p, const Tile &t, int k, in
     const unsigned long long s = (unsigned long long)a.xb[j] + a.yb[j] + c;
     const uint32_t sum = __brev((uint32_t)s);
     c = (uint32_t)(s >> 32);
-    r.w[j] = mode == 0 ? ((sum ^ (C.w[j] & t.vm.w[j])) | M.w[j]) : (sum & ~C.w[j]);
+    r.w[j] = mode == 0 ? ((sum ^ (E ? (C.w[j] & t.vm.w[j]) : C.w[j])) | M.w[j]) : (sum & ~C.w[j]);
   }
   return r;
 }
@@ -481,6 +482,7 @@ __device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
     const long long rem = t.n - 32 * w;
     t.em.w[j] = rem >= 32 ? FULL : (rem <= 0 ? 0u : (FULL << (32 - rem)));
   }
+  t.edge = t.base < 0 || t.base + 32 * WPT >= t.W;
   if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
     (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
                       p.spin_limit, p.state, t.lane);
@@ -527,7 +529,7 @@ __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b
 
 /* Write output stream o for this tile (lanes >= HL, words inside the input; characters at or
  * beyond n are cleared) and add its popcount to counts[o][input]. */
-static __device__ __noinline__ void store(const BgParams &p, const Tile t, int o, const S v) {
+static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, const S v) {
   uint32_t cnt = 0;
   uint32_t *dst = p.out ? p.out + (long long)o * p.out_stride + p.out_off[t.input] : nullptr;
 #pragma unroll

@@ -79,4 +79,7 @@ def test_dollar_and_lookahead_programs(cuda):
                 assert first_diff(res.stream(o, i).cpu().numpy(), w) is None, (wpt, i, o)
     interp = Program(groups, executor="interp")
     r2 = interp.scan(pack_bytes(items))
-    assert torch.equal(r2.streams, res.streams)
+    for i in range(len(items)):      # padding words between inputs are not part of any output
+        for o in range(prog.n_outputs):
+            assert torch.equal(r2.stream(o, i), res.stream(o, i)), (i, o)
+    assert torch.equal(r2.counts, res.counts)
