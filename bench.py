@@ -190,7 +190,7 @@ def served_leg(dev, n_req, load_GBps):
     sets = {}
     for name, n, seed in (("p32", 32, 81), ("p256", 256, 3), ("p1024", 1024, 83)):
         ps = workloads.throughput_patterns(seed=seed, n=n)
-        sets[name] = (ps, Program([compile_group(g) for g in ps.groups(max(1, n // 16))]))
+        sets[name] = (ps, Program([compile_group(g) for g in ps.groups(min(16, max(1, n // 16)))]))
     mean_len = ((4 << 20) - 64) / np.log((4 << 20) / 64)
     rate = max(1.0, 0.8 * load_GBps * 1e9 / mean_len)
     arr, lens, which = workloads.served_requests(n_req, seed=8, rate_per_s=rate)
@@ -255,13 +255,11 @@ def main():
     from bitgen_gb300.engine import Program, bytes_input, out_layout
     from bitgen_gb300.regex import compile_group
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from bitgen_gb300 import replicas
+    _, world, local = replicas.world()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=dev)
+    rank, world = replicas.init("nccl", dev)
 
     ps, groups, base, reps = workload(args)
     gs = [compile_group(g) for g in groups]
@@ -297,8 +295,7 @@ def main():
     else:
         cb = None
 
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     torch.cuda.synchronize(dev)
     clocks = Clocks(local)
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -309,8 +306,7 @@ def main():
     ev1.record(stream)
     torch.cuda.synchronize(dev)
     plan.sync(sp)
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
     # per-launch kernel time (scan kernel only) for the roofline
@@ -340,10 +336,7 @@ def main():
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
 
-    t = torch.tensor([ms, kernel_ms, e2e_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, kernel_ms, e2e_ms = [float(x) for x in t.tolist()]
+    ms, kernel_ms, e2e_ms = replicas.max_over_ranks([ms, kernel_ms, e2e_ms], device=dev)
     total_bytes = n * world
     value = total_bytes / (ms / 1e3) / 1e9
     peak, peak_kind = peaks()
@@ -375,11 +368,18 @@ def main():
     if cb is not None:
         line["cpu_baseline"] = cb
     if rank == 0 and not args.no_modes:
-        line["batched"] = batched_leg(prog, ps, dev)
-        line["served"] = served_leg(dev, args.served_requests, line["batched"]["batched_GBps"])
+        try:
+            line["batched"] = batched_leg(prog, ps, dev)
+        except Exception as e:  # a failed leg is reported, it does not void the main line
+            line["batched"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        try:
+            load = line["batched"].get("batched_GBps", value)
+            line["served"] = served_leg(dev, args.served_requests, load)
+        except Exception as e:
+            line["served"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
+    if dist.is_initialized():
         dist.destroy_process_group()
 
 

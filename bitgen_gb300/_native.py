@@ -13,7 +13,7 @@ import threading
 
 from .build import LIB
 
-BG_OK, BG_ERR_INVALID, BG_ERR_CUDA, BG_ERR_COMPILE, BG_ERR_TIMEOUT, BG_ERR_ALIGN, BG_ERR_NOMEM, BG_ERR_DEVICE = range(8)
+BG_OK, BG_ERR_INVALID, BG_ERR_CUDA, BG_ERR_COMPILE, BG_ERR_TIMEOUT, BG_ERR_ALIGN, BG_ERR_NOMEM, BG_ERR_DEVICE, BG_ERR_CAPACITY = range(9)
 BG_INPUT_BYTES, BG_INPUT_BASIS = 0, 1
 
 _lock = threading.Lock()
@@ -64,6 +64,8 @@ SIGNATURES = {
     "bg_plan_set_layout": (C.c_int, [C.c_void_p, C.POINTER(Layout), C.c_void_p]),
     "bg_plan_tiles": (C.c_int64, [C.c_void_p]),
     "bg_plan_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
+    "bg_plan_set_positions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "bg_plan_positions_written": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
     "bg_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "bg_plan_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
     "bg_plan_destroy": (C.c_int, [C.c_void_p]),

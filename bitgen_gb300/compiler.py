@@ -317,9 +317,16 @@ class Tuning:
     part_cap: int = 32      # most OR-ed terms one part function computes
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
     min_blocks: int = 3     # __launch_bounds__ minimum resident blocks per SM (caps registers)
+    edge_variants: bool = False  # separate unmasked part code for tiles away from input ends
+    inline_lookback: bool = False
+    lockstep: bool = False  # warps of a block run each part together (barrier between parts)
+    lookback_width: int = 1  # predecessor records each lane examines per look-back step
+    lookback_spin: int = 0   # look-back polls before sleeping
 
     def key(self):
-        return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window, self.min_blocks)
+        return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
+                self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
+                self.lookback_width, self.lookback_spin)
 
 
 @dataclass
@@ -1026,36 +1033,27 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     for ci, cl in enumerate(clusters):
         code = gen.part(cl)
         # E = the tile touches an input boundary: only then are the start/end masks applied
+        fast = (f'extern "C" __device__ __noinline__ void bg_part_{ci}_0({sig}) {{ bg_part_{ci}_body<false>({args}); }}\n'
+                if tuning.edge_variants else "")
         funcs.append(
             f"//@@BG_PART\n"
             f"template <bool E> __device__ __forceinline__ void bg_part_{ci}_body({sig}) {{\n{code}\n}}\n"
-            f'extern "C" __device__ __noinline__ void bg_part_{ci}_0({sig}) {{ bg_part_{ci}_body<false>({args}); }}\n'
+            + fast +
             f'extern "C" __device__ __noinline__ void bg_part_{ci}_1({sig}) {{ bg_part_{ci}_body<true>({args}); }}\n')
     decls = "\n".join(
         f'extern "C" __device__ void bg_part_{ci}_{e}({sig});'
-        for ci in range(len(clusters)) for e in (0, 1))
+        for ci in range(len(clusters)) for e in ((0, 1) if tuning.edge_variants else (1,)))
     ba = _basis_args(wpt)
-    calls = ("    if (t.edge) {\n"
-             + "\n".join(f"      bg_part_{ci}_1(p, t, acc, {ba});" for ci in range(len(clusters)))
-             + "\n    } else {\n"
-             + "\n".join(f"      bg_part_{ci}_0(p, t, acc, {ba});" for ci in range(len(clusters)))
-             + "\n    }")
+    if tuning.edge_variants:
+        calls = ("    if (t.edge) {\n"
+                 + "\n".join(f"      bg_part_{ci}_1(p, t, acc, {ba});" for ci in range(len(clusters)))
+                 + "\n    } else {\n"
+                 + "\n".join(f"      bg_part_{ci}_0(p, t, acc, {ba});" for ci in range(len(clusters)))
+                 + "\n    }")
+    else:
+        calls = "\n".join(f"    bg_part_{ci}_1(p, t, acc, {ba});" for ci in range(len(clusters)))
     comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
-    maxreg = max(32, min(255, (65536 // (tuning.block * max(1, tuning.min_blocks))) // 8 * 8))
-    src = (
-        f"//@@BG_MAXREG {maxreg}\n"
-        f"#define BG_WPT {wpt}\n"
-        f"#define BG_HL {gen.hl}\n"
-        f"#define BG_TL {gen.tl}\n"
-        f"#define BG_NOUT {n_out}\n"
-        f'#include "bg_device.cuh"\n'
-        f"using namespace bg;\n"
-        f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"
-        f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
-        f"{comments}\n"
-        + "\n".join(funcs) +
-        f"//@@BG_KERNEL\n{decls}\n"
-        f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
+    kernel_free = (
         f"  __shared__ uint32_t bg_acc[{warps} * BG_NOUT * BG_WPT * 32];\n"
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
         f"  Tile t;\n"
@@ -1067,7 +1065,45 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"{calls}\n"
         f"    acc_store(p, t, acc);\n"
         f"  }}\n"
-        f"}}\n"
+        f"}}\n")
+    lock_calls = "\n".join(f"    if (has) bg_part_{ci}_1(p, t, acc, {ba});\n    __syncthreads();"
+                            for ci in range(len(clusters)))
+    kernel_lockstep = (
+        f"  __shared__ uint32_t bg_acc[{warps} * BG_NOUT * BG_WPT * 32];\n"
+        f"  __shared__ unsigned int bg_claim;\n"
+        f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
+        f"  Tile t;\n"
+        f"  init(p, t);\n"
+        f"  for (;;) {{\n"
+        f"    const unsigned int g0 = claim_block(p, &bg_claim);\n"
+        f"    if ((long long)g0 >= p.n_tiles) break;\n"
+        f"    const unsigned int g = g0 + (threadIdx.x >> 5);\n"
+        f"    const bool has = (long long)g < p.n_tiles;\n"
+        f"    S b[8];\n"
+        f"    if (has) {{ setup_tile(p, t, g); acc_clear(acc, t); load_basis(p, t, b); }}\n"
+        f"{lock_calls}\n"
+        f"    if (has) acc_store(p, t, acc);\n"
+        f"  }}\n"
+        f"}}\n")
+    maxreg = max(32, min(255, (65536 // (tuning.block * max(1, tuning.min_blocks))) // 8 * 8))
+    src = (
+        f"//@@BG_MAXREG {maxreg}\n"
+        f"#define BG_WPT {wpt}\n"
+        f"#define BG_HL {gen.hl}\n"
+        f"#define BG_TL {gen.tl}\n"
+        f"#define BG_NOUT {n_out}\n"
+        f"#define BG_LOOKBACK_INLINE {int(tuning.inline_lookback)}\n"
+        f"#define BG_LBK {tuning.lookback_width}\n"
+        f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
+        f'#include "bg_device.cuh"\n'
+        f"using namespace bg;\n"
+        f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"
+        f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
+        f"{comments}\n"
+        + "\n".join(funcs) +
+        f"//@@BG_KERNEL\n{decls}\n"
+        f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
+        + (kernel_lockstep if tuning.lockstep else kernel_free)
     )
     return KernelSpec(source=src, name=name, n_outputs=n_out, n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,

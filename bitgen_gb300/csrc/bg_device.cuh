@@ -33,6 +33,15 @@
 #ifndef BG_TL
 #define BG_TL 0
 #endif
+#ifndef BG_LOOKBACK_INLINE
+#define BG_LOOKBACK_INLINE 0
+#endif
+#ifndef BG_LBK
+#define BG_LBK 1 /* look-back records per lane per step */
+#endif
+#ifndef BG_LB_SPIN
+#define BG_LB_SPIN 0 /* look-back polls before the first sleep */
+#endif
 
 namespace bg {
 
@@ -194,57 +203,81 @@ __device__ __forceinline__ unsigned long long wait_record(const unsigned long lo
 }
 
 /* Carry entering tile `gtile`'s look-back lane for the addition whose records start at `rec`:
- * decoupled look-back, 32 predecessor records per step (lane i reads tile gtile-1-i).  Walking
- * back, every aggregate that propagates (P = 1) contributes its generate bit; the walk stops at
- * the nearest record that fixes the carry by itself: an inclusive carry, or an aggregate that
- * does not propagate.  Control flow is warp-uniform (decisions come from ballots / lane 0).
- * Waits are bounded like wait_record. */
-static __device__ __forceinline__ uint32_t lookback(const unsigned long long *rec, long long gtile,
-                                          long long first, unsigned long long epoch,
-                                          long long spin_limit, uint32_t *state, int lane) {
-  uint32_t acc = 0;
+ * decoupled look-back, LBK * 32 predecessor records per step (lane l reads tiles
+ * gtile-1-l*LBK .. gtile-(l+1)*LBK, nearest first).  A record "terminates" the walk when it fixes
+ * the carry by itself: an inclusive carry, or an aggregate that generates a carry or does not
+ * propagate one.  Every record before the nearest terminator is an aggregate that propagates and
+ * does not generate, so the carry is simply the terminator's bit.  Control flow is warp-uniform
+ * (decisions come from ballots / lane 0).  Waits are bounded like wait_record. */
+#if BG_LOOKBACK_INLINE
+static __device__ __forceinline__
+#else
+static __device__ __noinline__
+#endif
+uint32_t lookback(const unsigned long long *rec, long long gtile, long long first,
+                  unsigned long long epoch, long long spin_limit, uint32_t *state, int lane) {
+  constexpr int LBK = BG_LBK;
   long long base = gtile - 1;
   long long t0 = clock64();
-  unsigned ns = 32, polls = 0;
+  unsigned ns = 0, polls = 0;
   for (;;) {
-    const long long j = base - lane;
-    bool valid = true;
-    unsigned long long r = (epoch << 4) | (2ull << 2); /* before the input: carry 0 */
-    if (j >= first) {
-      r = ld_relaxed(rec + j);
-      valid = (r >> 4) == epoch;
-    }
-    const uint32_t flag = (uint32_t)(r >> 2) & 3u;
-    const uint32_t G = (uint32_t)r & 1u, P = (uint32_t)(r >> 1) & 1u;
-    /* a record fixes the carry by itself if it is inclusive, or an aggregate that generates a
-     * carry or does not propagate one */
-    const bool term = valid && (flag == 2u || (flag == 1u && (P == 0u || G == 1u)));
-    const uint32_t vmask = __ballot_sync(FULL, valid);
-    const uint32_t tmask = __ballot_sync(FULL, term);
-    const int tl = tmask ? __ffs(tmask) - 1 : 32;
-    const uint32_t need = tl >= 31 ? FULL : ((2u << tl) - 1u);
-    if ((vmask & need) == need) {
-      /* records before the terminator propagate and do not generate: they pass the carry on */
-      if (tl < 32) {
-        if (base - tl < first && lane == 0) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
-        return acc | __shfl_sync(FULL, G, tl);
+    int term = LBK;        /* index of my nearest terminator, LBK = none                    */
+    bool blocked = false;  /* an unpublished record comes before my nearest terminator      */
+    uint32_t tG = 0u;
+    bool before_input = false;
+#pragma unroll
+    for (int i = 0; i < LBK; ++i) {
+      const long long j = base - (long long)lane * LBK - i;
+      unsigned long long r;
+      bool valid = true;
+      if (j >= first) {
+        r = ld_relaxed(rec + j);
+        valid = (r >> 4) == epoch;
+      } else {
+        r = (epoch << 4) | (2ull << 2); /* before the input: carry 0 */
       }
-      base -= 32;
+      if (term == LBK && !blocked) {
+        if (!valid) {
+          blocked = true;
+        } else {
+          const uint32_t flag = (uint32_t)(r >> 2) & 3u;
+          const uint32_t G = (uint32_t)r & 1u, P = (uint32_t)(r >> 1) & 1u;
+          if (flag == 2u || (flag == 1u && (P == 0u || G == 1u))) {
+            term = i;
+            tG = G;
+            before_input = j < first;
+          }
+        }
+      }
+    }
+    const uint32_t tmask = __ballot_sync(FULL, term < LBK);
+    const uint32_t bmask = __ballot_sync(FULL, blocked);
+    const uint32_t stop = tmask | bmask;
+    if (stop == 0u) { /* 32 * LBK propagating aggregates: keep walking */
+      base -= 32 * LBK;
       t0 = clock64();
       polls = 0;
-      ns = 32;
+      ns = 0;
       continue;
     }
-    /* some record before the first terminator is not published yet: wait, bounded */
+    const int l0 = __ffs(stop) - 1;
+    if ((tmask >> l0) & 1u) {
+      const uint32_t bi = __shfl_sync(FULL, before_input ? 1u : 0u, l0);
+      if (bi && lane == 0) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
+      return __shfl_sync(FULL, tG, l0);
+    }
+    /* a record before the nearest terminator is not published yet: wait, bounded */
     long long el = clock64() - t0;
     el = __shfl_sync(FULL, el, 0);
     const uint32_t ab = __shfl_sync(FULL, *(volatile uint32_t *)(state + 1), 0);
     if ((ab & BG_DEV_ERR_TIMEOUT) || ++polls >= (1u << 22) || el > spin_limit) {
       if (lane == 0) atomicOr(state + 1, BG_DEV_ERR_TIMEOUT);
-      return acc;
+      return 0u;
     }
-    __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
+    if (polls > BG_LB_SPIN) {
+      __nanosleep(ns);
+      ns = ns ? (ns < 1024 ? ns * 2 : ns) : 64;
+    }
   }
 }
 
@@ -459,11 +492,8 @@ __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
 
 /* Claim the next tile (tiles are handed out in increasing order, which is what makes the
  * look-back deadlock free: a tile only waits for tiles claimed before it). */
-__device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
-  unsigned int g = 0;
-  if (t.lane == 0) g = atomicAdd(p.state, 1u);
-  g = __shfl_sync(FULL, g, 0);
-  if ((long long)g >= p.n_tiles) return false;
+/* Fill `t` for global tile g. */
+__device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g) {
   int lo = 0, hi = p.n_inputs; /* find i: prefix[i] <= g < prefix[i+1] */
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
@@ -486,7 +516,26 @@ __device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
   if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
     (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
                       p.spin_limit, p.state, t.lane);
+}
+
+/* Claim the next tile (tiles are handed out in increasing order, which is what makes the
+ * look-back deadlock free: a tile only waits for tiles claimed before it). */
+__device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
+  unsigned int g = 0;
+  if (t.lane == 0) g = atomicAdd(p.state, 1u);
+  g = __shfl_sync(FULL, g, 0);
+  if ((long long)g >= p.n_tiles) return false;
+  setup_tile(p, t, g);
   return true;
+}
+
+/* Block-wide claim of one tile per warp (lockstep form: the warps of a block run the same part
+ * functions between barriers).  Returns the block's first tile; all threads must call it. */
+__device__ __forceinline__ unsigned int claim_block(const BgParams &p, unsigned int *slot) {
+  __syncthreads();
+  if (threadIdx.x == 0) *slot = atomicAdd(p.state, blockDim.x >> 5);
+  __syncthreads();
+  return *slot;
 }
 
 __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b[8]) {
@@ -532,15 +581,48 @@ __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b
 static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, const S v) {
   uint32_t cnt = 0;
   uint32_t *dst = p.out ? p.out + (long long)o * p.out_stride + p.out_off[t.input] : nullptr;
+  uint32_t vals[WPT];
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
     const long long w = t.base + t.lane * WPT + j;
+    vals[j] = 0u;
     if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) {
       uint32_t val = v.w[j];
       const long long rem = t.n - 32 * w;
       if (rem < 32) val &= FULL << (32 - rem);
       if (dst) dst[w] = val;
       cnt += __popc(val);
+      vals[j] = val;
+    }
+  }
+  if (p.positions && __any_sync(FULL, cnt != 0u)) {
+    /* sparse output: one slot range per warp, then each lane writes its own positions */
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(FULL, incl, d);
+      if (t.lane >= d) incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    unsigned long long at = 0;
+    if (t.lane == 31)
+      at = atomicAdd(reinterpret_cast<unsigned long long *>(p.state + 6), (unsigned long long)total);
+    at = __shfl_sync(FULL, at, 31) + (incl - cnt);
+    const unsigned long long key =
+        ((unsigned long long)o << 52) | ((unsigned long long)t.input << 32);
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      uint32_t val = vals[j];
+      const long long w = t.base + t.lane * WPT + j;
+      while (val) {
+        const int b = 31 - __clz(val); /* highest set bit = lowest position */
+        val &= ~(1u << b);
+        if ((long long)at < p.pos_capacity)
+          p.positions[at] = key | (unsigned long long)(32 * w + (31 - b));
+        else
+          atomicOr(p.state + 1, BG_DEV_ERR_CAPACITY);
+        ++at;
+      }
     }
   }
   if (p.counts) {

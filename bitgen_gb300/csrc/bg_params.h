@@ -25,6 +25,7 @@ typedef unsigned long long uint64_t;
 /* status bits written by kernels into state[1] */
 #define BG_DEV_ERR_TIMEOUT 1u /* a look-back wait ran out of time                    */
 #define BG_DEV_ERR_CHAIN 2u   /* a look-back walked past the first tile of its input */
+#define BG_DEV_ERR_CAPACITY 4u /* the match-position buffer was too small             */
 
 typedef struct BgParams {
   const uint8_t *in_bytes;   /* BG_INPUT_BYTES: base of all inputs                        */
@@ -37,7 +38,10 @@ typedef struct BgParams {
   unsigned long long *counts;/* [n_outputs][n_inputs] popcounts, or NULL                  */
   unsigned long long *records;/* [n_adds][n_tiles] look-back records                      */
   uint32_t *state;           /* [0] tile counter, [1] status, [2..3] epoch (u64),
-                                [4..5] a record no kernel ever writes (wait-limit test)     */
+                                [4..5] a record no kernel ever writes (wait-limit test),
+                                [6..7] match positions written (u64)                         */
+  unsigned long long *positions; /* sparse output or NULL: (output << 52 | input << 32 | pos) */
+  int64_t pos_capacity;
   int64_t basis_stride;      /* words between the basis planes of one input               */
   int64_t out_stride;        /* words between two output streams                          */
   int64_t n_tiles;

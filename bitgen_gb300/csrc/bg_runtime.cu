@@ -69,6 +69,8 @@ __global__ void __launch_bounds__(256) bg_transpose_kernel(const uint8_t *__rest
 
 __global__ void bg_prologue_kernel(uint32_t *state) {
   state[0] = 0u;
+  state[6] = 0u; /* match positions written */
+  state[7] = 0u;
   unsigned long long *ep = reinterpret_cast<unsigned long long *>(state + 2);
   *ep = *ep + 1ull;
 }
@@ -119,6 +121,8 @@ struct bg_plan {
   int64_t debug_wait_tile = -1;
   int64_t spin_limit = 0;
   int64_t cap_inputs = 0, cap_tiles = 0;
+  unsigned long long *positions = nullptr;
+  int64_t pos_capacity = 0;
   int64_t *h_stage = nullptr; /* pinned staging of the tables */
   cudaEvent_t staged = nullptr;
   bool staged_pending = false;
@@ -136,6 +140,7 @@ const char *bg_status_string(int s) {
     case BG_ERR_ALIGN: return "input not 16-byte aligned";
     case BG_ERR_NOMEM: return "out of memory";
     case BG_ERR_DEVICE: return "device reported an internal inconsistency";
+    case BG_ERR_CAPACITY: return "output buffer too small";
     default: return "unknown status";
   }
 }
@@ -517,6 +522,25 @@ int bg_plan_create(bg_program *prog, const bg_layout *L, bg_plan **out) {
 
 int64_t bg_plan_tiles(const bg_plan *plan) { return plan ? plan->n_tiles : -1; }
 
+int bg_plan_set_positions(bg_plan *plan, unsigned long long *positions, int64_t capacity) {
+  if (!plan || capacity < 0 || (capacity > 0 && !positions))
+    return fail(BG_ERR_INVALID, "bg_plan_set_positions: bad arguments");
+  if (plan->prog->desc.n_outputs >= 4096 || plan->cap_inputs >= (1 << 20))
+    return fail(BG_ERR_INVALID, "bg_plan_set_positions: more than 4095 outputs or 2^20 inputs");
+  plan->positions = capacity ? positions : nullptr;
+  plan->pos_capacity = capacity;
+  return BG_OK;
+}
+
+int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written) {
+  if (!plan || !written) return fail(BG_ERR_INVALID, "bg_plan_positions_written: bad arguments");
+  unsigned long long v = 0;
+  BG_CUDA(cudaMemcpyAsync(&v, plan->d_state + 6, sizeof v, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  BG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  *written = (int64_t)v;
+  return BG_OK;
+}
+
 int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t debug_wait_tile) {
   if (!plan) return fail(BG_ERR_INVALID, "bg_plan_set_wait_limit: null plan");
   plan->spin_limit = spin_limit_cycles;
@@ -548,6 +572,8 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   prm.n_tiles = plan->n_tiles;
   prm.spin_limit = 2000000000ll; /* ~1 s at 2 GHz */
   prm.debug_wait_tile = plan->debug_wait_tile;
+  prm.positions = plan->positions;
+  prm.pos_capacity = plan->pos_capacity;
   if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
   prm.n_inputs = (int32_t)n;
   prm.input_kind = L.input_kind;
@@ -570,6 +596,8 @@ int bg_plan_sync(bg_plan *plan, void *stream) {
   if (st) {
     BG_CUDA(cudaMemset(plan->d_state + 1, 0, sizeof st));
     if (st & BG_DEV_ERR_TIMEOUT) return fail(BG_ERR_TIMEOUT, "carry look-back wait timed out");
+    if (st & BG_DEV_ERR_CAPACITY)
+      return fail(BG_ERR_CAPACITY, "match positions exceeded the buffer; counts are complete");
     return fail(BG_ERR_DEVICE, "carry look-back walked past the start of its input");
   }
   return BG_OK;

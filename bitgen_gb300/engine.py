@@ -213,10 +213,19 @@ class ScanResult:
     counts: Optional[torch.Tensor]    # int64 [n_outputs, n_inputs]
     word_offsets: List[int]
     words: List[int]
+    positions: Optional["np.ndarray"] = None  # sorted u64 (output << 52 | input << 32 | pos)
 
     def stream(self, output: int, input_index: int = 0) -> torch.Tensor:
         o = self.word_offsets[input_index]
         return self.streams[output, o:o + self.words[input_index]]
+
+    def match_positions(self, output: int, input_index: int = 0):
+        """Sorted match-end positions of one output over one input (sparse output)."""
+        import numpy as np
+        key = (np.uint64(output) << np.uint64(52)) | (np.uint64(input_index) << np.uint64(32))
+        lo = np.searchsorted(self.positions, key)
+        hi = np.searchsorted(self.positions, key + np.uint64(1 << 32))
+        return (self.positions[lo:hi] & np.uint64(0xFFFFFFFF)).astype(np.int64)
 
 
 def out_layout(lengths: Sequence[int], align_words: int = 4) -> Tuple[List[int], List[int], int]:
@@ -266,6 +275,16 @@ class Plan:
     @property
     def tiles(self) -> int:
         return int(N.lib().bg_plan_tiles(self._h))
+
+    def set_positions(self, buf: Optional[torch.Tensor]):
+        """Sparse output buffer (int64 view of u64 entries) for later launches, or None."""
+        ptr, cap = (buf.data_ptr(), buf.numel()) if buf is not None else (None, 0)
+        N.check(N.lib().bg_plan_set_positions(self._h, ptr, cap), "bg_plan_set_positions")
+
+    def positions_written(self, stream: int) -> int:
+        v = C.c_int64()
+        N.check(N.lib().bg_plan_positions_written(self._h, stream, C.byref(v)), "bg_plan_positions_written")
+        return int(v.value)
 
     def set_wait_limit(self, cycles: int, debug_wait_tile: int = -1):
         N.check(N.lib().bg_plan_set_wait_limit(self._h, cycles, debug_wait_tile), "bg_plan_set_wait_limit")
@@ -365,7 +384,8 @@ class Program:
     def scan(self, inp: Inputs, streams: bool = True, counts: bool = True,
              out: Optional[torch.Tensor] = None, out_offsets: Optional[Sequence[int]] = None,
              out_stride: Optional[int] = None, stream: Optional[torch.cuda.Stream] = None,
-             sync: bool = True, max_iterations: Optional[int] = None) -> ScanResult:
+             sync: bool = True, max_iterations: Optional[int] = None,
+             positions: bool = False, pos_capacity: int = 1 << 22) -> ScanResult:
         dev = inp.data.device
         if out_offsets is None:
             offs, words, total = out_layout(inp.lengths)
@@ -380,11 +400,19 @@ class Program:
         out_ptr = out.data_ptr() if streams else 0
         cnt_ptr = cnt.data_ptr() if counts else 0
         stride = out_stride if out_stride is not None else total
+        pos = None
         if self.fused:
             plan = self.plan(inp, offs, stride)
+            pbuf = torch.empty(pos_capacity, dtype=torch.int64, device=dev) if positions else None
+            plan.set_positions(pbuf)
             plan.launch(inp.data.data_ptr(), out_ptr, cnt_ptr, sp)
-            if sync:
+            if sync or positions:
                 plan.sync(sp)
+            if positions:
+                import numpy as np
+                n = plan.positions_written(sp)
+                pos = np.sort(pbuf[:min(n, pos_capacity)].cpu().numpy().view(np.uint64))
+                plan.set_positions(None)
         else:
             if max_iterations is None:  # a monotone Pablo loop settles within n iterations
                 max_iterations = 4 * max(inp.lengths + [0]) + 64
@@ -393,7 +421,7 @@ class Program:
             N.check(N.lib().bg_interp_run(self._interp, C.byref(lay), inp.data.data_ptr(),
                                           out_ptr or None, cnt_ptr or None, max_iterations, sp),
                     "bg_interp_run")
-        return ScanResult(out if streams else None, cnt, offs, words)
+        return ScanResult(out if streams else None, cnt, offs, words, pos)
 
     def close(self):
         for p in self._plans.values():

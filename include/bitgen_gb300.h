@@ -39,7 +39,8 @@ typedef enum bg_status {
   BG_ERR_TIMEOUT = 4,  /* a bounded device wait (carry look-back) gave up         */
   BG_ERR_ALIGN = 5,    /* an input pointer or offset is not 16-byte aligned        */
   BG_ERR_NOMEM = 6,    /* device or host allocation failed                        */
-  BG_ERR_DEVICE = 7    /* kernel reported an internal inconsistency               */
+  BG_ERR_DEVICE = 7,   /* kernel reported an internal inconsistency               */
+  BG_ERR_CAPACITY = 8  /* a caller-provided output buffer was too small           */
 } bg_status;
 
 #define BG_INPUT_BYTES 0 /* raw bytes, transposed inside the scan kernel             */
@@ -114,6 +115,13 @@ int64_t bg_plan_tiles(const bg_plan *plan);
  * debug_wait_tile >= 0 makes that tile first wait on a record no kernel writes, so that the
  * bound and the BG_ERR_TIMEOUT report can be exercised without faulting or hanging the GPU. */
 int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t debug_wait_tile);
+/* Sparse output for later launches: every set bit of every output stream is also appended to
+ * `positions` as (output << 52) | (input << 32) | position (unordered; limits: < 4096 outputs,
+ * < 2^20 inputs, positions < 2^32).  capacity 0 turns it off.  Entries beyond the capacity are
+ * dropped and bg_plan_sync reports BG_ERR_CAPACITY (the counts stay exact). */
+int bg_plan_set_positions(bg_plan *plan, unsigned long long *positions, int64_t capacity);
+/* Number of positions the last launch on `stream` produced (waits for the stream). */
+int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written);
 /* Enqueue one scan on `stream`: input is the device base of the bytes / basis planes;
  * out_streams (may be NULL) receives n_outputs streams in the reference bit layout, positions at
  * or beyond an input's length cleared; counts (may be NULL) receives uint64 popcounts

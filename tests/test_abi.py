@@ -30,7 +30,7 @@ def test_exports_every_declared_symbol(native):
 
 
 def test_status_strings(native):
-    for s in range(8):
+    for s in range(9):
         assert N.status_string(s)
     assert N.status_string(N.BG_ERR_TIMEOUT) == "bounded device wait timed out"
 

@@ -55,10 +55,13 @@ def small():
     return SMALL
 
 
-@pytest.mark.parametrize("wpt,skip,block", [(1, 1, 256), (2, 1, 256), (4, 1, 128), (2, 0, 64), (2, 3, 256)])
-def test_small_workload_tunings(cuda, wpt, skip, block):
+@pytest.mark.parametrize("wpt,skip,block,extra", [(1, 1, 256, {}), (2, 1, 256, {}), (4, 1, 128, {}),
+                                                  (2, 0, 64, {}), (2, 3, 256, {}),
+                                                  (2, 1, 256, {"lockstep": True}),
+                                                  (2, 1, 256, {"edge_variants": True, "part_cap": 4})])
+def test_small_workload_tunings(cuda, wpt, skip, block, extra):
     ps, text, groups = small()
-    prog = Program(groups, tuning=Tuning(wpt=wpt, skip_interval=skip, block=block))
+    prog = Program(groups, tuning=Tuning(wpt=wpt, skip_interval=skip, block=block, **extra))
     check(prog, groups, [text])
     prog.close()
 
@@ -88,8 +91,9 @@ def test_long_carries_across_many_tiles(cuda):
     t[-3:] = np.frombuffer(b"zz ", np.uint8)
     t2 = np.full(n, ord("a"), np.uint8)  # one 'a' run spanning every tile, 'b' at the end
     t2[-1] = ord("b")
-    for wpt in (1, 4):
-        prog = Program(groups, tuning=Tuning(wpt=wpt))
+    for tun in (Tuning(wpt=1), Tuning(wpt=4, block=128), Tuning(lockstep=True),
+                Tuning(edge_variants=True)):
+        prog = Program(groups, tuning=tun)
         check(prog, groups, [t, t2, t2[:1000], t[:5]])
 
 
@@ -210,3 +214,26 @@ def test_many_inputs_one_launch(cuda):
     lens = workloads.batched_lengths(300, seed=12, median=900, lo=1, hi=5000)
     items = workloads.batched_inputs(lens, 13, ps.witnesses)
     check(Program(groups), groups, items)
+
+
+def test_sparse_positions_match_streams(cuda):
+    ps = workloads.throughput_patterns(seed=51, n=24)
+    groups = [compile_group(g) for g in ps.groups(3)]
+    lens = [0, 5, 4000, 70000, 33]
+    items = [workloads.plant(workloads.printable_text(n, 52 + n), ps.witnesses, 512, 53 + n) for n in lens]
+    prog = Program(groups)
+    res = prog.scan(pack_bytes(items), positions=True)
+    total = 0
+    for i, data in enumerate(items):
+        for o in range(prog.n_outputs):
+            words = res.stream(o, i).cpu().numpy()
+            bits = np.unpackbits(words.astype(">u4").view(np.uint8))
+            want = np.nonzero(bits)[0]
+            assert np.array_equal(res.match_positions(o, i), want), (i, o)
+            total += want.size
+    assert total == int(res.counts.sum()) > 0
+    # a buffer that is too small is reported, counts stay exact
+    from bitgen_gb300 import _native as N
+    with pytest.raises(N.BitgenError) as e:
+        prog.scan(pack_bytes(items), positions=True, pos_capacity=3)
+    assert e.value.status == N.BG_ERR_CAPACITY
