@@ -69,6 +69,8 @@ SIGNATURES = {
     "bg_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "bg_plan_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
     "bg_plan_destroy": (C.c_int, [C.c_void_p]),
+    "bg_scan_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                  C.c_void_p, C.c_void_p, C.c_void_p]),
     "bg_interp_create": (C.c_int, [C.POINTER(Instr), C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                    C.c_int32, C.POINTER(C.c_void_p)]),
     "bg_interp_run": (C.c_int, [C.c_void_p, C.POINTER(Layout), C.c_void_p, C.c_void_p, C.c_void_p,

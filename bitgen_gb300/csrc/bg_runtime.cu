@@ -618,3 +618,147 @@ int bg_plan_destroy(bg_plan *plan) {
 }
 
 }  // extern "C"
+
+/* ======================================================================================== */
+/* Allocation-free scan of one byte input                                                  */
+/* ======================================================================================== */
+/* Some callers may not allocate device memory while they scan: a host whose device memory is
+ * owned by a pooling allocator with a fixed budget, or a latency-bound loop where cudaFree's
+ * device-wide synchronisation would stall other streams.  bg_scan_noalloc serves them with
+ * the same fused kernel as bg_plan_launch.  The look-back records, the one-input launch tables
+ * and the state words live in this fixed array, which the library's module carries.
+ *
+ * Layout in 64-bit words:
+ *   [0, 4)    state: the eight 32-bit slots of a plan's state (tile counter, status, epoch,
+ *             a record no kernel writes, match positions written);
+ *   [4, 9)    tables of the one input: in_off, in_len, tile_prefix[0..1], out_off;
+ *   [32, end) look-back records, [n_adds][n_tiles].
+ * The array starts zeroed when the module loads.  Every call then clears the counters and
+ * the status, and bumps the epoch.  Records left by an earlier call carry an older epoch, so
+ * the look-back reads them as not yet published and they need no clearing.  Calls share the
+ * array, so calls that overlap on the GPU race on it. */
+namespace {
+
+constexpr int64_t kNoallocWords = BG_NOALLOC_SCRATCH_BYTES / 8;
+constexpr int64_t kNoallocRecordsAt = 32;
+static_assert(kNoallocWords - kNoallocRecordsAt == (int64_t)BG_NOALLOC_RECORDS, "scratch layout");
+
+static __device__ __align__(256) unsigned long long bg_noalloc_scratch[kNoallocWords];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long *g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+/* Clears what must start at zero for one call and writes the one-input tables. */
+__global__ void bg_noalloc_prologue_kernel(unsigned long long *scratch, int64_t n_bytes,
+                                           int64_t n_tiles, unsigned long long *counts,
+                                           int n_counts) {
+  if (threadIdx.x == 0) {
+    uint32_t *state = reinterpret_cast<uint32_t *>(scratch);
+    state[0] = 0u; /* tile counter */
+    state[1] = 0u; /* status */
+    scratch[1] += 1ull; /* epoch (state[2..3]) */
+    scratch[2] = 0ull;  /* the never-written record (state[4..5]) */
+    scratch[3] = 0ull;  /* match positions written (state[6..7]) */
+    int64_t *t = reinterpret_cast<int64_t *>(scratch + 4);
+    t[0] = 0;       /* in_off */
+    t[1] = n_bytes; /* in_len */
+    t[2] = 0;       /* tile_prefix[0] */
+    t[3] = n_tiles; /* tile_prefix[1] */
+    t[4] = 0;       /* out_off */
+  }
+  if (counts)
+    for (int i = threadIdx.x; i < n_counts; i += blockDim.x) counts[i] = 0ull;
+}
+
+/* Hands the scan's status bits to the caller's word. */
+__global__ void bg_noalloc_epilogue_kernel(const unsigned long long *scratch, uint32_t *status) {
+  *status = reinterpret_cast<const uint32_t *>(scratch)[1];
+}
+
+/* Device address of the array on the current device, looked up once per device. */
+int noalloc_scratch(unsigned long long **out) {
+  int dev = -1;
+  BG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocMaxDevices)
+    return fail(BG_ERR_INVALID, "bg_scan_noalloc: device ordinal beyond 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    unsigned long long *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void **)&ptr, bg_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(BG_ERR_CUDA, std::string("bg_scan_noalloc: cudaGetSymbolAddress of the scratch: ") +
+                                   cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return BG_OK;
+}
+
+}  // namespace
+
+extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int64_t n_bytes,
+                               uint32_t *out_streams, int64_t out_stride,
+                               unsigned long long *counts, uint32_t *status, void *stream) {
+  if (!prog || !prog->kernel || !input || !status || n_bytes < 0)
+    return fail(BG_ERR_INVALID, "bg_scan_noalloc: null program, input or status, or negative size");
+  if (!aligned16(input)) return fail(BG_ERR_ALIGN, "bg_scan_noalloc: input not 16-byte aligned");
+  const int64_t W = (n_bytes + 31) / 32;
+  if (out_streams && out_stride < W)
+    return fail(BG_ERR_INVALID, "bg_scan_noalloc: out_stride shorter than the input's words");
+  const int64_t tile_words =
+      (int64_t)(32 - prog->desc.halo_lanes - prog->desc.tail_lanes) * prog->desc.wpt;
+  const int64_t tiles = std::max<int64_t>(1, (W + tile_words - 1) / tile_words);
+  const int64_t adds = std::max(1, prog->desc.n_adds);
+  if (tiles > (int64_t)BG_NOALLOC_RECORDS / adds) {
+    char msg[320];
+    snprintf(msg, sizeof msg,
+             "bg_scan_noalloc: %lld bytes span %lld tiles of %lld words and need %lld look-back "
+             "records (%lld additions); the fixed %u-byte scratch holds %u records, so at most "
+             "%lld tiles (%lld bytes) for this program",
+             (long long)n_bytes, (long long)tiles, (long long)tile_words,
+             (long long)(tiles * adds), (long long)adds, (unsigned)BG_NOALLOC_SCRATCH_BYTES,
+             (unsigned)BG_NOALLOC_RECORDS, (long long)(BG_NOALLOC_RECORDS / adds),
+             (long long)(BG_NOALLOC_RECORDS / adds) * tile_words * 32);
+    return fail(BG_ERR_CAPACITY, msg);
+  }
+  unsigned long long *scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc != BG_OK) return rc;
+
+  cudaStream_t s = (cudaStream_t)stream;
+  BgParams prm{};
+  prm.in_bytes = input;
+  prm.in_basis = nullptr;
+  const int64_t *tables = reinterpret_cast<const int64_t *>(scratch + 4);
+  prm.in_off = tables;
+  prm.in_len = tables + 1;
+  prm.tile_prefix = tables + 2;
+  prm.out_off = tables + 4;
+  prm.out = out_streams;
+  prm.counts = counts;
+  prm.records = scratch + kNoallocRecordsAt;
+  prm.state = reinterpret_cast<uint32_t *>(scratch);
+  prm.positions = nullptr;
+  prm.pos_capacity = 0;
+  prm.basis_stride = 0;
+  prm.out_stride = out_stride;
+  prm.n_tiles = tiles;
+  prm.spin_limit = 2000000000ll; /* ~1 s at 2 GHz */
+  prm.debug_wait_tile = -1;
+  prm.n_inputs = 1;
+  prm.input_kind = BG_INPUT_BYTES;
+  const int warps_per_block = prog->desc.block / 32;
+  const int64_t need = (tiles + warps_per_block - 1) / warps_per_block;
+  const int grid = (int)std::max<int64_t>(
+      1, std::min<int64_t>(need, (int64_t)sm_count() * prog->blocks_per_sm));
+
+  bg_noalloc_prologue_kernel<<<1, 256, 0, s>>>(scratch, n_bytes, tiles, counts,
+                                               prog->desc.n_outputs);
+  BG_CUDA(cudaGetLastError());
+  void *args[] = {&prm};
+  BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(grid), dim3(prog->desc.block), args, 0, s));
+  bg_noalloc_epilogue_kernel<<<1, 1, 0, s>>>(scratch, status);
+  BG_CUDA(cudaGetLastError());
+  return BG_OK;
+}

@@ -15,6 +15,7 @@
  *                           cuda_kernel.py:35-47,411-427
  *   bg_interp_*          <- the reference's whole-stream semantics of Pablo while/if
  *                           (bitgen/inst/inst_block_while.py:137-153, inst_block_if.py:314-342)
+ *   bg_scan_noalloc      <- no counterpart in the reference (an allocation-free scan, below)
  *
  * All pointers to device memory are plain CUDA device pointers; `stream` is a cudaStream_t
  * (NULL = legacy default stream).  Every function returns a bg_status; none exits the process
@@ -132,6 +133,45 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
 /* Wait for `stream`, then report (and clear) device-side errors of earlier launches. */
 int bg_plan_sync(bg_plan *plan, void *stream);
 int bg_plan_destroy(bg_plan *plan);
+
+/* ---------------------------------------------------------------------------------------
+ * Allocation-free scan of one byte input.  No counterpart in the reference: BitGen always
+ * allocates its outputs and working buffers per call.
+ *
+ * For callers that must not allocate device memory while they scan.  Examples are a process
+ * whose device memory is owned by a pooling allocator with a hard budget, where a stray
+ * cudaMalloc fails or escapes the pool's accounting, and a latency-bound loop, where
+ * cudaFree's implicit device-wide synchronisation would stall every other stream.  The call
+ * enqueues the same fused kernel as bg_plan_launch.  Its look-back records, launch tables and
+ * state live in one fixed device array of BG_NOALLOC_SCRATCH_BYTES inside this library, not
+ * in buffers of a plan.  Nothing is allocated and nothing is freed: no cudaMalloc, no
+ * cudaFree, no memory pool.
+ *
+ *   prog         a program from bg_program_create, created on the current device;
+ *   input        device bytes, 16-byte aligned; exactly n_bytes are read (n_bytes >= 0);
+ *   out_streams  NULL, or n_outputs rows of out_stride >= ceil(n_bytes / 32) words, written in
+ *                the reference bit layout (positions at or beyond n_bytes cleared);
+ *   counts       NULL, or n_outputs uint64 popcounts (zeroed by the call);
+ *   status       device uint32 (required); once the stream reaches the end of this call it
+ *                holds the scan's device status bits: 0 on success, 1 if a carry look-back
+ *                wait ran out of time, 2 if a look-back walked past the first tile.
+ *
+ * Limit: the input may span at most BG_NOALLOC_RECORDS / max(1, additions) tiles of
+ * (32 - halo_lanes - tail_lanes) * wpt words each.  Larger inputs are rejected with
+ * BG_ERR_CAPACITY before anything is enqueued, and bg_last_error() gives the sizes.
+ * The first call on each device looks up the array's device address once
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture begins.
+ * Every call on a device shares the one array.  The call clears what must start at zero and
+ * retags the look-back records.  Two calls whose work overlaps on the GPU (on different
+ * streams, or from different host threads) race on the array and give wrong results.
+ * Serialise them, for example on one stream.
+ * ------------------------------------------------------------------------------------- */
+#define BG_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define BG_NOALLOC_RECORDS (BG_NOALLOC_SCRATCH_BYTES / 8u - 32u)
+int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int64_t n_bytes,
+                    uint32_t *out_streams, int64_t out_stride, unsigned long long *counts,
+                    uint32_t *status, void *stream);
 
 /* ---------------------------------------------------------------------------------------
  * Whole-stream executor for programs that keep while / if blocks (global any-bit semantics).
