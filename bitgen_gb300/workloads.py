@@ -198,15 +198,27 @@ def dna_motifs(n: int = 64, seed: int = 5) -> PatternSet:
     return PatternSet(regexes, wits)
 
 
-def dna_text(n: int, seed: int = 6, gc: float = 0.42, line: int = 80) -> np.ndarray:
+def dna_text(n: int, seed: int = 6, gc: float = 0.42, line: int = 80,
+             chunk: int = 64 << 20) -> np.ndarray:
+    """i.i.d. A/C/G/T with the given GC fraction, runs of N (length 50-5000 at rate 1e-5 per
+    byte) and a line feed after every ``line`` bytes.  Generated in chunks from 16-bit draws
+    against cumulative thresholds, so a 1 GiB text needs no more than the text itself plus one
+    chunk of temporaries."""
     rng = np.random.default_rng(seed)
-    p = np.array([(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2])
-    seq = np.frombuffer(b"ACGT", dtype=np.uint8)[rng.choice(4, size=n, p=p)]
+    cum = np.cumsum([(1 - gc) / 2, gc / 2, gc / 2])
+    thr = (cum * 65536).astype(np.uint32)
+    seq = np.empty(n, dtype=np.uint8)
+    for at in range(0, n, chunk):
+        r = rng.integers(0, 65536, size=min(chunk, n - at), dtype=np.uint16)
+        idx = (r >= thr[0]).astype(np.uint8)
+        idx += r >= thr[1]
+        idx += r >= thr[2]
+        seq[at:at + r.size] = np.frombuffer(b"ACGT", dtype=np.uint8)[idx]
     n_runs = rng.poisson(n * 1e-5)
-    for _ in range(n_runs):
-        s = int(rng.integers(0, n))
-        ln = int(rng.integers(50, 5001))
-        seq[s:s + ln] = ord("N")
+    starts = rng.integers(0, max(n, 1), size=n_runs)
+    lens = rng.integers(50, 5001, size=n_runs)
+    for st, ln in zip(starts.tolist(), lens.tolist()):
+        seq[st:st + ln] = ord("N")
     seq[line::line + 1] = ord("\n")
     return seq
 
