@@ -309,7 +309,8 @@ def main():
     replicas.barrier()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
-    # per-launch kernel time (scan kernel only) for the roofline
+    # per-launch time of one scan (prologue, carry pre-pass and carry scan when the program has
+    # them, main kernel: all on `stream`) for the roofline
     k0 = torch.cuda.Event(enable_timing=True)
     k1 = torch.cuda.Event(enable_timing=True)
     kt = []
@@ -355,6 +356,7 @@ def main():
                    "tuning": {"wpt": info.get("wpt"), "halo_lanes": info.get("halo_lanes"),
                               "block": tuning.block, "skip_interval": tuning.skip_interval},
                    "registers": info.get("registers"), "adds": info.get("adds"),
+                   "pre_pass_adds": info.get("pre_adds"),
                    "compile_s": round(compile_s, 2), "bit_exact_vs_cpu_sample": check},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": recorded_traffic(),
@@ -362,7 +364,7 @@ def main():
                      "kernel_ms": round(kernel_ms, 4)},
         "e2e": {"value": round(total_bytes / (e2e_ms / 1e3) / 1e9, 3), "unit": UNIT,
                 "h2d_bytes_per_step": n, "d2h_bytes_per_step": prog.n_outputs * 8},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": (4 if info.get("pre_adds") else 2) * args.steps,
         "clocks": clk,
     }
     if cb is not None:

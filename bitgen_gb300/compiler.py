@@ -28,7 +28,7 @@ Pipeline
 from __future__ import annotations
 
 import hashlib
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 from typing import Dict, List, Optional, Sequence, Tuple
 
 from .pablo import BASIS, Group, If, Op, While, walk
@@ -322,11 +322,12 @@ class Tuning:
     lockstep: bool = False  # warps of a block run each part together (barrier between parts)
     lookback_width: int = 1  # predecessor records each lane examines per look-back step
     lookback_spin: int = 0   # look-back polls before sleeping
+    carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
-                self.lookback_width, self.lookback_spin)
+                self.lookback_width, self.lookback_spin, self.carry_prepass)
 
 
 @dataclass
@@ -342,6 +343,7 @@ class KernelSpec:
     n_nodes: int
     output_names: List[str] = field(default_factory=list)
     tail_lanes: int = 0
+    n_pre: int = 0          # additions 0..n_pre-1 take their carries from the pre-pass kernel
 
     @property
     def tile_words(self):
@@ -359,6 +361,7 @@ class _Gen:
         self.indent = 2
         self.scopes: List[Dict[int, str]] = [{}]
         self.adds: Dict[int, int] = {}
+        self.pre: Dict[int, int] = {}   # pre-pass additions -> their index (= add index)
         self.uses: Dict[int, int] = {}
         self.tmp = 0
 
@@ -450,9 +453,23 @@ class _Gen:
                 self.uses[a] = self.uses.get(a, 0) + 1
         for o in outputs:
             self.uses[o] = self.uses.get(o, 0) + 1
+        # additions over a wide class whose operands depend on no other addition get their
+        # carries from the pre-pass; they are numbered first
+        pre = []
+        if self.t.carry_prepass:
+            for v in sorted(live):
+                n = d.nodes[v]
+                if n.op in ADD_OPS and self.wide_class(n.args[1]):
+                    anc = self.heavy_ancestors(n.args[0]) | self.heavy_ancestors(n.args[1])
+                    if not any(d.nodes[a].op in ADD_OPS for a in anc):
+                        pre.append(v)
         k = 0
+        for v in pre:
+            self.adds[v] = k
+            self.pre[v] = k
+            k += 1
         for v in sorted(live):
-            if d.nodes[v].op in ADD_OPS:
+            if d.nodes[v].op in ADD_OPS and v not in self.pre:
                 self.adds[v] = k
                 k += 1
 
@@ -572,8 +589,14 @@ class _Gen:
         if n.op in ADD_OPS:
             m = self.mat(n.args[0])
             c = self.mat(n.args[1])
-            fn = "matchstar" if n.op == "matchstar" else "scanthru"
-            self.emit(f"const S {name}_s = {fn}<{self.dl[v]}>(p, t, {self.adds[v]}, {self.pack(m)}, {self.pack(c)});")
+            if v in self.pre:
+                mode = 0 if n.op == "matchstar" else 1
+                args = f"p, t, {self.adds[v]}, {mode}"
+                self.emit(f"const AddState st{v} = add_known<{self.dl[v]}>({args}, {self.pack(m)}, {self.pack(c)});")
+                self.emit(f"const S {name}_s = add_end<{self.dl[v]}>({args}, st{v}, {self.pack(m)}, {self.pack(c)});")
+            else:
+                fn = "matchstar" if n.op == "matchstar" else "scanthru"
+                self.emit(f"const S {name}_s = {fn}<{self.dl[v]}>(p, t, {self.adds[v]}, {self.pack(m)}, {self.pack(c)});")
             for j in range(self.t.wpt):
                 self.emit(f"const uint32_t {name}_{j} = {name}_s.w[{j}];")
             self.scopes[-1][v] = name
@@ -700,6 +723,19 @@ class _Gen:
             stack.extend(self.d.nodes[x].args)
         return out
 
+    def pre_body(self) -> str:
+        """Body of the pre-pass kernel: the operands of every pre-pass addition (with the same
+        zero-skip guards as the main pass) and the publication of its tile aggregate."""
+        self.lines = []
+        self.indent = 4
+        self.scopes = [{}]
+        for v, k in sorted(self.pre.items(), key=lambda x: x[1]):
+            n = self.d.nodes[v]
+            m, c = self.mat(n.args[0]), self.mat(n.args[1])
+            mode = 0 if n.op == "matchstar" else 1
+            self.emit(f"pre_publish<{self.dl[v]}, E>(p, t, {k}, {mode}, {self.pack(m)}, {self.pack(c)});")
+        return "\n".join(self.lines)
+
     def part(self, terms: Sequence[Tuple[int, int]]) -> str:
         """Body of one part function: every (node, output) term OR-ed into the warp's
         shared-memory accumulator of its output.
@@ -735,7 +771,7 @@ class _Gen:
             n = d.nodes[v]
             ha = [a for a in n.args if a in hs]
             late_in[v] = any(late[a] for a in ha)
-            deferred = n.op in ADD_OPS and self.wide_class(n.args[1])
+            deferred = n.op in ADD_OPS and self.wide_class(n.args[1]) and v not in self.pre
             late[v] = deferred or late_in[v]
         for v in heavy:
             n = d.nodes[v]
@@ -823,7 +859,8 @@ class _Gen:
             n = d.nodes[v]
             m, c = self.mat(n.args[0]), self.mat(n.args[1])
             mode = 0 if n.op == "matchstar" else 1
-            self.emit(f"const AddState st{v} = add_begin<{self.dl[v]}, E>(p, t, {self.adds[v]}, {mode}, "
+            fn = "add_known" if v in self.pre else "add_begin"
+            self.emit(f"const AddState st{v} = {fn}<{self.dl[v]}, E>(p, t, {self.adds[v]}, {mode}, "
                       f"{self.pack(m)}, {self.pack(c)});")
             begun.add(v)
 
@@ -1017,11 +1054,16 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     gen = _Gen(dag, tuning)
     gen.analyse(outs)
     n_out = len(outs)
+    per_warp = max(1, n_out) * wpt * 32 * 4
+    if per_warp > SMEM_BUDGET:
+        raise NotFusable(f"{n_out} outputs need {per_warp} bytes of accumulators per warp; "
+                         f"use fewer outputs per program")
+    if (tuning.block // 32) * per_warp > SMEM_BUDGET:
+        # many outputs: fewer warps per block keep the accumulators within the budget
+        block = max(32, (SMEM_BUDGET // per_warp) * 32)
+        tuning = replace(tuning, block=block,
+                         min_blocks=min(32, -(-tuning.min_blocks * tuning.block // block)))
     warps = tuning.block // 32
-    smem_words = warps * n_out * wpt * 32
-    if smem_words * 4 > SMEM_BUDGET:
-        raise NotFusable(f"{n_out} outputs need {smem_words * 4} bytes of accumulators per block; "
-                         f"use fewer outputs per program or a smaller block")
     terms: List[Tuple[int, int]] = []
     for o, v in enumerate(outs):
         for leaf in gen.or_leaves(v):
@@ -1085,7 +1127,30 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"    if (has) acc_store(p, t, acc);\n"
         f"  }}\n"
         f"}}\n")
-    maxreg = max(32, min(255, (65536 // (tuning.block * max(1, tuning.min_blocks))) // 8 * 8))
+    # registers a thread may use so that min_blocks blocks fit: each of the SM's four
+    # sub-partitions holds 16K registers for its share of the resident warps
+    warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
+    maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
+    pre_kernel = ""
+    if gen.pre:
+        basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+        pre_kernel = (
+            f"//@@BG_PART\n"
+            f"/* carry pre-pass: the aggregates of additions 0..{len(gen.pre) - 1} for every tile, no waits;\n"
+            f"   tiles are taken in a fixed stride since nothing here waits on another tile */\n"
+            f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_pre(const __grid_constant__ BgParams p) {{\n'
+            f"  Tile t;\n"
+            f"  init(p, t);\n"
+            f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
+            f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
+            f"    setup_tile(p, t, (unsigned int)g, false);\n"
+            f"    S b[8];\n"
+            f"    load_basis(p, t, b);\n"
+            f"    const uint32_t {basis_decl};\n"
+            f"    constexpr bool E = true;\n"
+            f"{gen.pre_body()}\n"
+            f"  }}\n"
+            f"}}\n")
     src = (
         f"//@@BG_MAXREG {maxreg}\n"
         f"#define BG_WPT {wpt}\n"
@@ -1095,16 +1160,18 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"#define BG_LOOKBACK_INLINE {int(tuning.inline_lookback)}\n"
         f"#define BG_LBK {tuning.lookback_width}\n"
         f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
+        f"#define BG_NPRE {len(gen.pre)}\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"
         f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"
         f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
         f"{comments}\n"
-        + "\n".join(funcs) +
+        + "\n".join(funcs) + pre_kernel +
         f"//@@BG_KERNEL\n{decls}\n"
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
         + (kernel_lockstep if tuning.lockstep else kernel_free)
     )
     return KernelSpec(source=src, name=name, n_outputs=n_out, n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
-                      n_nodes=len(dag.nodes), output_names=names, tail_lanes=gen.tl)
+                      n_nodes=len(dag.nodes), output_names=names, tail_lanes=gen.tl,
+                      n_pre=len(gen.pre))

@@ -19,6 +19,13 @@
  * is needed) publishes its carry-out, first as a (generate, propagate) aggregate and then as
  * an inclusive carry, and this tile reads it with a decoupled look-back.  Every wait is bounded
  * by a clock64 budget; on timeout the kernel records BG_DEV_ERR_TIMEOUT and continues.
+ *
+ * Additions over a wide class (such as '.', which covers whole tiles of text without line
+ * breaks) would make every tile walk the look-back: their carries chain through the entire
+ * input.  The first BG_NPRE additions of a program are of that kind and depend on no other
+ * addition; for them a separate pass (the generated bg_scan_pre kernel, then a scan kernel of
+ * the runtime) computes every tile's carry-in before the main kernel runs, which then reads it
+ * (add_known) instead of waiting.
  */
 #pragma once
 #include "bg_params.h"
@@ -42,6 +49,9 @@
 #ifndef BG_LB_SPIN
 #define BG_LB_SPIN 0 /* look-back polls before the first sleep */
 #endif
+#ifndef BG_NPRE
+#define BG_NPRE 0 /* additions whose carries are computed by the pre-pass (numbered first) */
+#endif
 
 namespace bg {
 
@@ -51,6 +61,8 @@ constexpr int HL = BG_HL;
 constexpr int TL = BG_TL;                   /* tail halo lanes (for Lookahead)     */
 constexpr int SL = 32 - HL - TL;            /* output lanes per tile               */
 constexpr long long SW = (long long)SL * WPT; /* output words per tile             */
+constexpr int NPRE = BG_NPRE;
+constexpr int NPRE_WORDS = NPRE > 0 ? (NPRE + 31) / 32 : 1;
 static_assert(HL >= 0 && TL >= 0 && HL + TL < 32, "halos must leave output lanes");
 
 struct S {
@@ -133,6 +145,7 @@ struct Tile {
   S vm;              /* per word: all ones if the word index is >= 0     */
   S em;              /* per word: the bits of positions before the input end */
   bool edge;         /* the tile has words before the input start or reaches its last word */
+  uint32_t pcin[NPRE_WORDS]; /* bit k: carry entering pre-pass addition k (warp-uniform)   */
 };
 
 /* Advance(x, N): marks move N positions forward; words before the input start read as 0. */
@@ -482,6 +495,72 @@ __device__ __forceinline__ S add_end(const BgParams &p, const Tile &t, int k, in
   return r;
 }
 
+/* Lane generate / propagate masks of X + Y for addition k's operands (lanes below DL cleared):
+ * the part of add_begin that the pre-pass and add_known share. */
+template <int DL, bool E>
+__device__ __forceinline__ void add_masks(const Tile &t, int mode, const S &M, const S &C,
+                                          uint32_t xb[WPT], uint32_t yb[WPT], uint32_t &Gm,
+                                          uint32_t &Pm) {
+  uint32_t G = 0u, P = 1u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const uint32_t x = mode == 0 ? (M.w[j] & C.w[j]) : M.w[j];
+    xb[j] = __brev(E ? (x & t.vm.w[j]) : x);
+    yb[j] = __brev(E ? (C.w[j] & t.vm.w[j]) : C.w[j]);
+    const uint32_t s = xb[j] + yb[j];
+    const uint32_t g = s < xb[j] ? 1u : 0u;
+    const uint32_t pp = s == FULL ? 1u : 0u;
+    G = g | (pp & G);
+    P &= pp;
+  }
+  const uint32_t keep = ~((1u << DL) - 1u);
+  Gm = __ballot_sync(FULL, G) & keep;
+  Pm = __ballot_sync(FULL, P) & keep;
+}
+
+/* Pre-pass: publish this tile's (generate, propagate) aggregate of addition k over its own
+ * lanes [DL, SL + DL), computed with a zero carry entering lane DL.  Written for every tile,
+ * whatever the operands, so that the scan kernel finds a record everywhere. */
+template <int DL, bool E = true>
+__device__ __forceinline__ void pre_publish(const BgParams &p, const Tile &t, int k, int mode,
+                                            const S &M, const S &C) {
+  uint32_t xb[WPT], yb[WPT], Gm, Pm;
+  add_masks<DL, E>(t, mode, M, C, xb, yb, Gm, Pm);
+  constexpr int OUTL = SL + DL;
+  const uint32_t A = Gm | Pm, B = Gm;
+  const uint32_t c0 = (uint32_t)((unsigned long long)A + B) ^ A ^ B;
+  const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
+  const uint32_t Pagg = (((Pm >> DL) & span) == span) ? 1u : 0u;
+  if (t.lane == 0)
+    p.records[(long long)k * p.n_tiles + t.gtile] =
+        (t.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1) | ((c0 >> OUTL) & 1u);
+}
+
+/* Main pass for a pre-pass addition: the carry entering lane DL is known (t.pcin), so the
+ * addition resolves without publishing or waiting.  Its result is formed by add_end. */
+template <int DL, bool E = true>
+__device__ __forceinline__ AddState add_known(const BgParams &p, const Tile &t, int k, int mode,
+                                              const S &M, const S &C) {
+  AddState a;
+  const uint32_t cin = (t.pcin[k >> 5] >> (k & 31)) & 1u;
+  uint32_t mo = 0u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) mo |= M.w[j];
+  if (cin == 0u && !__any_sync(FULL, mo != 0u)) {
+    /* no marker and no carry: the sum is C itself, so the result is zero */
+    a.state = 1u;
+    a.Gm = a.Pm = a.cvec = 0u;
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) a.xb[j] = a.yb[j] = 0u;
+    return a;
+  }
+  add_masks<DL, E>(t, mode, M, C, a.xb, a.yb, a.Gm, a.Pm);
+  const uint32_t A = a.Gm | a.Pm, B = a.Gm;
+  a.cvec = (uint32_t)((unsigned long long)A + B + ((unsigned long long)cin << DL)) ^ A ^ B;
+  a.state = 2u;
+  return a;
+}
+
 /* ---------------------------------------------------------------------------------------
  * Tile scheduling, loads and stores
  * --------------------------------------------------------------------------------------- */
@@ -490,10 +569,27 @@ __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
   t.epoch = *(volatile const unsigned long long *)(p.state + 2);
 }
 
-/* Claim the next tile (tiles are handed out in increasing order, which is what makes the
- * look-back deadlock free: a tile only waits for tiles claimed before it). */
-/* Fill `t` for global tile g. */
-__device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g) {
+/* Carries entering this tile for the pre-pass additions: the scan kernel left the inclusive
+ * carry-out of every tile in its record, so tile g reads tile g-1's (zero for an input's first
+ * tile).  Lane k loads addition k's record; a missing record is reported as a chain error. */
+__device__ __forceinline__ void load_pre_carries(const BgParams &p, Tile &t) {
+#pragma unroll
+  for (int w = 0; w < NPRE_WORDS; ++w) {
+    const int k = w * 32 + t.lane;
+    uint32_t c = 0u;
+    if (NPRE > 0 && k < NPRE && t.gtile > t.first) {
+      const unsigned long long r = __ldg(p.records + (long long)k * p.n_tiles + t.gtile - 1);
+      if ((r >> 4) != t.epoch || ((r >> 2) & 3ull) != 2ull) atomicOr(p.state + 1, BG_DEV_ERR_CHAIN);
+      c = (uint32_t)r & 1u;
+    }
+    t.pcin[w] = __ballot_sync(FULL, c != 0u);
+  }
+}
+
+/* Fill `t` for global tile g.  `main_pass` = false in the carry pre-pass, which neither reads
+ * the pre-pass carries (it is producing them) nor takes part in the wait-limit test. */
+__device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g,
+                                           bool main_pass = true) {
   int lo = 0, hi = p.n_inputs; /* find i: prefix[i] <= g < prefix[i+1] */
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
@@ -513,6 +609,8 @@ __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned 
     t.em.w[j] = rem >= 32 ? FULL : (rem <= 0 ? 0u : (FULL << (32 - rem)));
   }
   t.edge = t.base < 0 || t.base + 32 * WPT >= t.W;
+  if (!main_pass) return;
+  if (NPRE > 0) load_pre_carries(p, t);
   if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
     (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
                       p.spin_limit, p.state, t.lane);

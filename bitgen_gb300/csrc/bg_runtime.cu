@@ -75,6 +75,96 @@ __global__ void bg_prologue_kernel(uint32_t *state) {
   *ep = *ep + 1ull;
 }
 
+/* Carry scan of the pre-pass additions.  Block k handles addition k: its records hold every
+ * tile's (generate, propagate) aggregate, computed with a zero carry entering the tile; they
+ * are replaced by inclusive carry-outs, the carry restarting at zero at each input's first
+ * tile.  Each of the 1024 threads owns a contiguous run of tiles: it folds its run, the folds
+ * are scanned across the block, and a second walk over the run writes the records.
+ * (G, P) pairs compose as (G1, P1) then (G2, P2) = (G2 | (P2 & G1), P1 & P2). */
+__global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long *records,
+                                                             int64_t n_tiles,
+                                                             const int64_t *tile_prefix,
+                                                             int n_inputs, uint32_t *state) {
+  __shared__ uint32_t wg[32], wp[32];
+  unsigned long long *rec = records + (long long)blockIdx.x * n_tiles;
+  const unsigned long long epoch = *reinterpret_cast<volatile unsigned long long *>(state + 2);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t per = (n_tiles + blockDim.x - 1) / blockDim.x;
+  const int64_t lo = (int64_t)tid * per < n_tiles ? (int64_t)tid * per : n_tiles;
+  const int64_t hi = lo + per < n_tiles ? lo + per : n_tiles;
+  int in0 = 0;
+  {
+    int a = 0, b = n_inputs; /* input containing tile lo: prefix[a] <= lo < prefix[a+1] */
+    while (b - a > 1) {
+      const int m = (a + b) >> 1;
+      if (tile_prefix[m] <= lo) a = m; else b = m;
+    }
+    in0 = a;
+  }
+  uint32_t G = 0u, P = 1u;
+  bool bad = false;
+  int in = in0;
+  for (int64_t g = lo; g < hi; ++g) {
+    while (in + 1 < n_inputs && g >= tile_prefix[in + 1]) ++in;
+    const unsigned long long r = rec[g];
+    if ((r >> 4) != epoch || ((r >> 2) & 3ull) != 1ull) bad = true;
+    const uint32_t Gg = (uint32_t)r & 1u, Pg = (uint32_t)(r >> 1) & 1u;
+    if (g == tile_prefix[in]) {
+      G = Gg;
+      P = 0u;
+    } else {
+      G = Gg | (Pg & G);
+      P &= Pg;
+    }
+  }
+  /* inclusive scan of the folds within the warp, then across warps */
+  uint32_t iG = G, iP = P;
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t uG = __shfl_up_sync(0xffffffffu, iG, d), uP = __shfl_up_sync(0xffffffffu, iP, d);
+    if (lane >= d) {
+      iG = iG | (iP & uG);
+      iP &= uP;
+    }
+  }
+  if (lane == 31) {
+    wg[warp] = iG;
+    wp[warp] = iP;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t a = lane < (int)(blockDim.x >> 5) ? wg[lane] : 0u;
+    uint32_t b = lane < (int)(blockDim.x >> 5) ? wp[lane] : 1u;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t uG = __shfl_up_sync(0xffffffffu, a, d), uP = __shfl_up_sync(0xffffffffu, b, d);
+      if (lane >= d) {
+        a = a | (b & uG);
+        b &= uP;
+      }
+    }
+    wg[lane] = a;
+    wp[lane] = b;
+  }
+  __syncthreads();
+  /* exclusive prefix of this thread = (warps before) then (lanes before in this warp) */
+  uint32_t eG = __shfl_up_sync(0xffffffffu, iG, 1), eP = __shfl_up_sync(0xffffffffu, iP, 1);
+  if (lane == 0) {
+    eG = 0u;
+    eP = 1u;
+  }
+  uint32_t c = eG;
+  if (warp > 0) c = eG | (eP & wg[warp - 1]);
+  in = in0;
+  for (int64_t g = lo; g < hi; ++g) {
+    while (in + 1 < n_inputs && g >= tile_prefix[in + 1]) ++in;
+    const unsigned long long r = rec[g];
+    const uint32_t Gg = (uint32_t)r & 1u, Pg = (uint32_t)(r >> 1) & 1u;
+    const uint32_t cin = g == tile_prefix[in] ? 0u : c;
+    c = Gg | (Pg & cin);
+    rec[g] = (epoch << 4) | (2ull << 2) | (unsigned long long)c;
+  }
+  if (bad) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
+}
+
 int sm_count() {
   static int n = -1;
   if (n < 0) {
@@ -107,7 +197,8 @@ struct bg_program {
   std::vector<char> cubin;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t kernel = nullptr;
-  int regs = 0, local_bytes = 0, blocks_per_sm = 1;
+  cudaKernel_t pre_kernel = nullptr; /* carry pre-pass, when desc.n_pre > 0 */
+  int regs = 0, local_bytes = 0, blocks_per_sm = 1, pre_blocks_per_sm = 1;
 };
 
 struct bg_plan {
@@ -333,7 +424,7 @@ int bg_nvrtc_check(const char *source, size_t source_len, const char *name, char
 int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   if (!desc || !out || !desc->source || !desc->name || desc->wpt < 1 || desc->wpt > 8 ||
       desc->halo_lanes < 0 || desc->tail_lanes < 0 || desc->halo_lanes + desc->tail_lanes > 31 ||
-      desc->n_outputs < 0 || desc->n_adds < 0 ||
+      desc->n_outputs < 0 || desc->n_adds < 0 || desc->n_pre < 0 || desc->n_pre > desc->n_adds ||
       desc->block < 32 || desc->block % 32)
     return fail(BG_ERR_INVALID, "bg_program_create: bad descriptor");
   *out = nullptr;
@@ -354,6 +445,8 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   cudaError_t e = cudaLibraryLoadData(&p->lib, p->cubin.data(), nullptr, nullptr, 0, nullptr,
                                       nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&p->kernel, p->lib, p->name.c_str());
+  if (e == cudaSuccess && desc->n_pre > 0)
+    e = cudaLibraryGetKernel(&p->pre_kernel, p->lib, (p->name + "_pre").c_str());
   if (e != cudaSuccess) {
     std::string msg = std::string("loading the compiled program: ") + cudaGetErrorString(e);
     if (p->lib) cudaLibraryUnload(p->lib);
@@ -375,6 +468,14 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
     cudaGetLastError();
     int regs = p->regs > 0 ? p->regs : 128;
     p->blocks_per_sm = std::max(1, 65536 / (regs * desc->block));
+  }
+  if (p->pre_kernel) {
+    nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)p->pre_kernel,
+                                                      desc->block, 0) == cudaSuccess && nb > 0)
+      p->pre_blocks_per_sm = nb;
+    else
+      cudaGetLastError();
   }
   *out = p;
   return BG_OK;
@@ -548,6 +649,31 @@ int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t deb
   return BG_OK;
 }
 
+}  // extern "C"
+
+/* Everything of one scan after its prologue: the carry pre-pass and its scan when the program
+ * has one, then the main kernel.  All launches go to `s`, in this order. */
+static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaStream_t s) {
+  void *args[] = {&prm};
+  if (prog->pre_kernel) {
+    const int warps_per_block = prog->desc.block / 32;
+    const int64_t need = (prm.n_tiles + warps_per_block - 1) / warps_per_block;
+    const int pre_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
+    BG_CUDA(cudaLaunchKernel((const void *)prog->pre_kernel, dim3(pre_grid),
+                             dim3(prog->desc.block), args, 0, s));
+    bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.records, prm.n_tiles,
+                                                            prm.tile_prefix, prm.n_inputs,
+                                                            prm.state);
+    BG_CUDA(cudaGetLastError());
+  }
+  BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(grid), dim3(prog->desc.block), args,
+                           0, s));
+  return BG_OK;
+}
+
+extern "C" {
+
 int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
                    unsigned long long *counts, void *stream) {
   if (!plan || !input) return fail(BG_ERR_INVALID, "bg_plan_launch: null plan or input");
@@ -582,10 +708,7 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
                             sizeof(unsigned long long) * (size_t)plan->prog->desc.n_outputs * n, s));
   bg_prologue_kernel<<<1, 1, 0, s>>>(plan->d_state);
   BG_CUDA(cudaGetLastError());
-  void *args[] = {&prm};
-  BG_CUDA(cudaLaunchKernel((const void *)plan->prog->kernel, dim3(plan->grid),
-                           dim3(plan->prog->desc.block), args, 0, s));
-  return BG_OK;
+  return launch_passes(plan->prog, prm, plan->grid, s);
 }
 
 int bg_plan_sync(bg_plan *plan, void *stream) {
@@ -756,8 +879,8 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   bg_noalloc_prologue_kernel<<<1, 256, 0, s>>>(scratch, n_bytes, tiles, counts,
                                                prog->desc.n_outputs);
   BG_CUDA(cudaGetLastError());
-  void *args[] = {&prm};
-  BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(grid), dim3(prog->desc.block), args, 0, s));
+  const int lrc = launch_passes(prog, prm, grid, s);
+  if (lrc != BG_OK) return lrc;
   bg_noalloc_epilogue_kernel<<<1, 1, 0, s>>>(scratch, status);
   BG_CUDA(cudaGetLastError());
   return BG_OK;

@@ -338,7 +338,7 @@ class Program:
             src = self.spec.source.encode()
             self._desc = N.KernelDesc(src, len(src), name.encode(), self.spec.n_outputs,
                                       self.spec.n_adds, self.spec.halo_lanes, self.spec.wpt,
-                                      self.spec.block, self.spec.tail_lanes)
+                                      self.spec.block, self.spec.tail_lanes, self.spec.n_pre)
             h = C.c_void_p()
             N.check(lib.bg_program_create(C.byref(self._desc), C.byref(h)), "bg_program_create")
             self._handle = h
@@ -365,7 +365,7 @@ class Program:
         N.check(N.lib().bg_program_info(self._handle, C.byref(r), C.byref(l), C.byref(b)), "bg_program_info")
         return {"executor": "fused", "registers": r.value, "local_bytes": l.value,
                 "blocks_per_sm": b.value, "halo_lanes": self.spec.halo_lanes, "wpt": self.spec.wpt,
-                "adds": self.spec.n_adds, "outputs": self.spec.n_outputs}
+                "adds": self.spec.n_adds, "pre_adds": self.spec.n_pre, "outputs": self.spec.n_outputs}
 
     def tiles_for(self, lengths: Sequence[int]) -> int:
         """Tiles one launch over inputs of these lengths needs."""

@@ -75,6 +75,8 @@ typedef struct bg_kernel_desc {
   int32_t wpt;        /* 32-bit words per lane                                          */
   int32_t block;      /* threads per CTA                                                */
   int32_t tail_lanes;
+  int32_t n_pre;      /* additions 0..n_pre-1 get their carries from a pre-pass: the source
+                         then also defines the kernel "<name>_pre" (0 = no pre-pass)      */
 } bg_kernel_desc;
 
 int bg_program_create(const bg_kernel_desc *desc, bg_program **out);

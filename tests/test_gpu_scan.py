@@ -92,9 +92,36 @@ def test_long_carries_across_many_tiles(cuda):
     t2 = np.full(n, ord("a"), np.uint8)  # one 'a' run spanning every tile, 'b' at the end
     t2[-1] = ord("b")
     for tun in (Tuning(wpt=1), Tuning(wpt=4, block=128), Tuning(lockstep=True),
-                Tuning(edge_variants=True)):
+                Tuning(edge_variants=True), Tuning(carry_prepass=False)):
         prog = Program(groups, tuning=tun)
         check(prog, groups, [t, t2, t2[:1000], t[:5]])
+
+
+def test_carry_prepass_matches_lookback_and_oracle(cuda):
+    """Wide-class additions whose operands need no other addition ('.*', '[^x]*') take their
+    carries from the pre-pass and the carry scan; nested ones ('m.*n.*o', second '.*') still use
+    the look-back.  Both forms must agree with the oracle over many inputs in one launch (the
+    carry restarts at every input, including inputs that start inside one scan thread's run of
+    tiles) and over a long input."""
+    groups = [compile_group(["k9.*zz", "q[^x]*r"]), compile_group(["m.*n.*o"]), compile_group(["ab+c"])]
+    rng = np.random.default_rng(5)
+    items = [rand_text(int(n), 100 + i, b"kz9qrmnoabcx ") for i, n in
+             enumerate(rng.integers(0, 3000, size=300))]
+    long = rand_text(2_000_003, 9, b"abcdefghijklmnopqrstuvwyz ")
+    long[10:12] = np.frombuffer(b"k9", np.uint8)
+    long[1_999_990:1_999_992] = np.frombuffer(b"zz", np.uint8)
+    items.append(long)
+    with_pre = Program(groups)
+    without = Program(groups, tuning=Tuning(carry_prepass=False))
+    assert with_pre.spec.n_pre >= 2 and without.spec.n_pre == 0
+    assert with_pre.spec.n_pre < with_pre.spec.n_adds  # the nested '.*' is not pre-passed
+    check(with_pre, groups, items)
+    inp = pack_bytes(items)
+    a, b = with_pre.scan(inp), without.scan(inp)
+    torch.cuda.synchronize()
+    assert torch.equal(a.counts, b.counts)
+    for o, w in zip(a.word_offsets, a.words):  # padding words between inputs are not written
+        assert torch.equal(a.streams[:, o:o + w], b.streams[:, o:o + w])
 
 
 def test_scanthru_and_while_forms(cuda):
