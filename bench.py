@@ -263,7 +263,7 @@ def main():
 
     ps, groups, base, reps = workload(args)
     gs = [compile_group(g) for g in groups]
-    tuning = Tuning(wpt=args.wpt or 2)
+    tuning = Tuning(wpt=args.wpt) if args.wpt else Tuning()
     t0 = time.perf_counter()
     prog = Program(gs, tuning=tuning)
     compile_s = time.perf_counter() - t0

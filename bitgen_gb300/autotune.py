@@ -21,11 +21,11 @@ from .engine import Inputs, Program, _ensure_cache_dir, out_layout
 from .pablo import Group
 
 SPACE = [
-    Tuning(wpt=2, block=256, part_cap=32, window=2, min_blocks=2),
-    Tuning(wpt=2, block=256, part_cap=32, window=2, min_blocks=3),
-    Tuning(wpt=2, block=256, part_cap=64, window=2, min_blocks=2),
-    Tuning(wpt=1, block=256, part_cap=32, window=2, min_blocks=4),
-    Tuning(wpt=4, block=128, part_cap=32, window=2, min_blocks=3),
+    Tuning(),                                              # prefiltered, 1 word per lane
+    Tuning(wpt=1, min_blocks=4, part_cap=8),
+    Tuning(wpt=2, min_blocks=3, part_cap=8),
+    Tuning(wpt=1, min_blocks=4, part_cap=32, prefilter=False),
+    Tuning(wpt=2, min_blocks=3, part_cap=32, prefilter=False),
 ]
 
 

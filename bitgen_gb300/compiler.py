@@ -31,6 +31,7 @@ import hashlib
 from dataclasses import dataclass, field, replace
 from typing import Dict, List, Optional, Sequence, Tuple
 
+from . import prefilter
 from .pablo import BASIS, Group, If, Op, While, walk
 
 CHAIN_OPS = ("and", "advance")
@@ -311,23 +312,24 @@ class Dag:
 
 @dataclass
 class Tuning:
-    wpt: int = 2            # 32-bit words per lane
+    wpt: int = 1            # 32-bit words per lane
     block: int = 256        # threads per CTA
     skip_interval: int = 1  # check for an all-zero marker every k AND steps (0 = never)
-    part_cap: int = 32      # most OR-ed terms one part function computes
+    part_cap: int = 4       # most OR-ed terms one part function computes
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
-    min_blocks: int = 3     # __launch_bounds__ minimum resident blocks per SM (caps registers)
+    min_blocks: int = 4     # __launch_bounds__ minimum resident blocks per SM (caps registers)
     edge_variants: bool = False  # separate unmasked part code for tiles away from input ends
     inline_lookback: bool = False
     lockstep: bool = False  # warps of a block run each part together (barrier between parts)
     lookback_width: int = 1  # predecessor records each lane examines per look-back step
     lookback_spin: int = 0   # look-back polls before sleeping
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
+    prefilter: bool = True   # run a term only in tiles holding one of its trigrams
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
-                self.lookback_width, self.lookback_spin, self.carry_prepass)
+                self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter)
 
 
 @dataclass
@@ -996,6 +998,7 @@ def build_dag(groups: Sequence[Group], per_regex: bool = False) -> Tuple[Dag, Li
 
 
 SMEM_BUDGET = 48 * 1024
+BLOOM_SMEM = (1 << prefilter.BLOOM_BITS) // 8
 
 
 def _cluster_terms(gen: "_Gen", terms: List[Tuple[int, int]], cap: int) -> List[List[Tuple[int, int]]]:
@@ -1054,20 +1057,29 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     gen = _Gen(dag, tuning)
     gen.analyse(outs)
     n_out = len(outs)
-    per_warp = max(1, n_out) * wpt * 32 * 4
-    if per_warp > SMEM_BUDGET:
-        raise NotFusable(f"{n_out} outputs need {per_warp} bytes of accumulators per warp; "
-                         f"use fewer outputs per program")
-    if (tuning.block // 32) * per_warp > SMEM_BUDGET:
-        # many outputs: fewer warps per block keep the accumulators within the budget
-        block = max(32, (SMEM_BUDGET // per_warp) * 32)
-        tuning = replace(tuning, block=block,
-                         min_blocks=min(32, -(-tuning.min_blocks * tuning.block // block)))
-    warps = tuning.block // 32
     terms: List[Tuple[int, int]] = []
     for o, v in enumerate(outs):
         for leaf in gen.or_leaves(v):
             terms.append((leaf, o))
+    filt = None
+    if tuning.prefilter and not tuning.lockstep and not tuning.edge_variants:
+        pre_nodes = [v for v, _ in sorted(gen.pre.items(), key=lambda x: x[1])]
+        filt = prefilter.build(gen, [v for v, _ in terms], pre_nodes)
+        if not filt.enabled:
+            filt = None
+    budget = SMEM_BUDGET - (BLOOM_SMEM if filt else 0)
+    per_warp = max(1, n_out) * wpt * 32 * 4
+    if per_warp > budget:
+        raise NotFusable(f"{n_out} outputs need {per_warp} bytes of accumulators per warp; "
+                         f"use fewer outputs per program")
+    if (tuning.block // 32) * per_warp > budget:
+        # many outputs: fewer warps per block keep the accumulators within the budget
+        block = max(32, (budget // per_warp) * 32)
+        tuning = replace(tuning, block=block,
+                         min_blocks=min(32, -(-tuning.min_blocks * tuning.block // block)))
+    warps = tuning.block // 32
+    if filt is not None:
+        return _generate_filtered(gen, tuning, terms, names, filt, name)
     clusters = _cluster_terms(gen, terms, tuning.part_cap)
     funcs = []
     sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
@@ -1174,4 +1186,184 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     return KernelSpec(source=src, name=name, n_outputs=n_out, n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
                       n_nodes=len(dag.nodes), output_names=names, tail_lanes=gen.tl,
+                      n_pre=len(gen.pre))
+
+
+def _hex_array(vals: Sequence[int], per_line: int = 12) -> str:
+    lines = []
+    for i in range(0, len(vals), per_line):
+        lines.append("  " + ", ".join(f"0x{v:08x}u" for v in vals[i:i + per_line]) + ",")
+    return "\n".join(lines)
+
+
+def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]],
+                       names: List[str], filt: "prefilter.TermFilter", name: str) -> KernelSpec:
+    """The prefiltered form of the kernel.
+
+    Per tile the kernel loads the bytes, scans their trigrams (bg_device.cuh load_scan) and so
+    learns which terms may be non-zero; terms whose additions could take or owe a carry are
+    added (look-back additions whose class is all ones at the carry lane or the successor's
+    carry lane, pre-pass additions with a carry-in when the term's filter holds only through
+    them).  Part functions hold one guarded block per term and are called only when one of
+    their terms runs; each block is the term's full program with its own zero-skip guards.  The
+    carry pre-pass computes a pre-pass addition's marker only when its trigram filter fires."""
+    d = gen.d
+    wpt = tuning.wpt
+    warps = tuning.block // 32
+    nt = len(terms)
+    nw = filt.words
+    always = filt.always_mask()
+    sl = 32 - gen.hl - gen.tl
+    # run conditions -----------------------------------------------------------------------
+    pm_classes: Dict[int, str] = {}          # class node -> name of its all-ones lane mask
+    needs: List[List[str]] = [[] for _ in range(nt)]
+    for r, (v, _) in enumerate(terms):
+        if (always >> r) & 1:
+            continue
+        for a in sorted(gen.heavy_ancestors(v)):
+            n = d.nodes[a]
+            if n.op not in ADD_OPS:
+                continue
+            if a in gen.pre:
+                if filt.term_cond[r]:
+                    k = gen.pre[a]
+                    needs[r].append(f"(t.pcin[{k >> 5}] >> {k & 31}) & 1u")
+                continue
+            c = n.args[1]
+            if not d.is_cc(c):
+                always |= 1 << r
+                break
+            pm = pm_classes.setdefault(c, f"pm{c}")
+            dl = gen.dl[a]
+            needs[r].append(f"(({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u")
+    # kernel-level code: classes for the all-ones masks, then the run bits
+    gen.lines = []
+    gen.indent = 4
+    gen.scopes = [{}]
+    for w in range(nw):
+        m = (always >> (32 * w)) & 0xFFFFFFFF
+        if m:
+            gen.emit(f"t.run[{w}] |= 0x{m:08x}u;")
+    for c, pm in sorted(pm_classes.items()):
+        ref = gen.mat(c)
+        gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
+    for r, conds in enumerate(needs):
+        if conds and not (always >> r) & 1:
+            gen.emit(f"if ({' | '.join(conds)}) t.run[{r >> 5}] |= 0x{1 << (r & 31):08x}u;")
+    run_code = "\n".join(gen.lines)
+    # parts --------------------------------------------------------------------------------
+    # hot terms (run on carries or always) apart from the trigram-gated ones, so that a tile's
+    # calls go to few parts
+    hot = [r for r in range(nt) if (always >> r) & 1 or needs[r]]
+    cold = [r for r in range(nt) if r not in set(hot)]
+    cap = max(1, tuning.part_cap)
+    parts = [hot[i:i + cap] for i in range(0, len(hot), cap)] + \
+            [cold[i:i + cap] for i in range(0, len(cold), cap)]
+    sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
+    funcs = []
+    for ci, rs in enumerate(parts):
+        blocks = []
+        for r in rs:
+            code = gen.part([terms[r]])
+            body = "\n".join("  " + ln for ln in code.split("\n"))
+            blocks.append(f"  if ((t.run[{r >> 5}] >> {r & 31}) & 1u) {{\n{body}\n  }}")
+        funcs.append(f"//@@BG_PART\n"
+                     f'extern "C" __device__ __noinline__ void bg_part_{ci}({sig}) {{\n'
+                     f"  constexpr bool E = true;\n" + "\n".join(blocks) + "\n}\n")
+    decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
+    ba = _basis_args(wpt)
+    calls = []
+    for ci, rs in enumerate(parts):
+        masks = {}
+        for r in rs:
+            masks[r >> 5] = masks.get(r >> 5, 0) | (1 << (r & 31))
+        cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(masks.items()))
+        calls.append(f"    if ({cond}) bg_part_{ci}(p, t, acc, {ba});")
+    # tables -------------------------------------------------------------------------------
+    log2, keys, masks = filt.exact()
+    bloom = filt.bloom()
+    tables = (f"#define BG_EXLOG2 {log2}\n"
+              f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
+              f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
+              f"static __device__ const uint32_t bg_exmasks[{len(masks)}] = {{\n{_hex_array(masks)}\n}};\n")
+    scan = ("    S b[8];\n"
+            "    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
+            f"    const uint32_t {', '.join(f'b{i}_{j} = b[{i}].w[{j}]' for i in range(8) for j in range(wpt))};\n"
+            "    constexpr bool E = true;\n")
+    bloom_init = (f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
+                  f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
+                  f"  __syncthreads();\n")
+    # pre-pass kernel ----------------------------------------------------------------------
+    pre_kernel = ""
+    if gen.pre:
+        gen.lines = []
+        gen.indent = 4
+        gen.scopes = [{}]
+        for v, k in sorted(gen.pre.items(), key=lambda x: x[1]):
+            n = d.nodes[v]
+            bit = nt + k
+            mode = 0 if n.op == "matchstar" else 1
+            gen.emit(f"S m{k} = zero();")
+            gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
+            m = gen.mat(n.args[0])
+            gen.emit(f"m{k} = {gen.pack(m)};")
+            gen.close()
+            c = gen.mat(n.args[1])
+            gen.emit(f"pre_publish<{gen.dl[v]}, E>(p, t, {k}, {mode}, m{k}, {gen.pack(c)});")
+        pre_kernel = (
+            f"//@@BG_PART\n{tables}"
+            f"/* carry pre-pass: the aggregates of additions 0..{len(gen.pre) - 1} for every tile, no waits;\n"
+            f"   tiles are taken in a fixed stride since nothing here waits on another tile */\n"
+            f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_pre(const __grid_constant__ BgParams p) {{\n'
+            + bloom_init +
+            f"  Tile t;\n"
+            f"  init(p, t);\n"
+            f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
+            f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
+            f"    setup_tile(p, t, (unsigned int)g, false);\n"
+            + scan +
+            f"    t.run[{(nt) >> 5}] |= 0u;\n"
+            + "\n".join(
+                f"    t.run[{w}] |= 0x{(always >> (32 * w)) & 0xFFFFFFFF:08x}u;" for w in range(nw)
+                if (always >> (32 * w)) & 0xFFFFFFFF) + "\n"
+            f"{chr(10).join(gen.lines)}\n"
+            f"  }}\n"
+            f"}}\n")
+    warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
+    maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
+    comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
+    src = (
+        f"//@@BG_MAXREG {maxreg}\n"
+        f"#define BG_WPT {wpt}\n"
+        f"#define BG_HL {gen.hl}\n"
+        f"#define BG_TL {gen.tl}\n"
+        f"#define BG_NOUT {len(names)}\n"
+        f"#define BG_LOOKBACK_INLINE {int(tuning.inline_lookback)}\n"
+        f"#define BG_LBK {tuning.lookback_width}\n"
+        f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
+        f"#define BG_NPRE {len(gen.pre)}\n"
+        f"#define BG_NRUN {nw}\n"
+        f"#define BG_PREFILTER 1\n"
+        f'#include "bg_device.cuh"\n'
+        f"using namespace bg;\n"
+        f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"
+        f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
+        f"{comments}\n"
+        + "\n".join(funcs) + pre_kernel +
+        f"//@@BG_KERNEL\n{tables}{decls}\n"
+        f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
+        f"  __shared__ uint32_t bg_acc[{warps} * BG_NOUT * BG_WPT * 32];\n"
+        + bloom_init +
+        f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
+        f"  Tile t;\n"
+        f"  init(p, t);\n"
+        f"  while (next_tile(p, t)) {{\n"
+        f"    acc_clear(acc, t);\n"
+        + scan + run_code + "\n" + "\n".join(calls) + "\n"
+        f"    acc_store(p, t, acc);\n"
+        f"  }}\n"
+        f"}}\n")
+    return KernelSpec(source=src, name=name, n_outputs=len(names), n_adds=len(gen.adds),
+                      halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
+                      n_nodes=len(d.nodes), output_names=names, tail_lanes=gen.tl,
                       n_pre=len(gen.pre))

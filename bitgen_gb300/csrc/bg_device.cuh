@@ -52,6 +52,9 @@
 #ifndef BG_NPRE
 #define BG_NPRE 0 /* additions whose carries are computed by the pre-pass (numbered first) */
 #endif
+#ifndef BG_NRUN
+#define BG_NRUN 1 /* words of the per-tile run mask (trigram prefilter) */
+#endif
 
 namespace bg {
 
@@ -146,6 +149,7 @@ struct Tile {
   S em;              /* per word: the bits of positions before the input end */
   bool edge;         /* the tile has words before the input start or reaches its last word */
   uint32_t pcin[NPRE_WORDS]; /* bit k: carry entering pre-pass addition k (warp-uniform)   */
+  uint32_t run[BG_NRUN];     /* prefilter: bit r = term r (or pre-pass marker) may be set    */
 };
 
 /* Advance(x, N): marks move N positions forward; words before the input start read as 0. */
@@ -636,6 +640,28 @@ __device__ __forceinline__ unsigned int claim_block(const BgParams &p, unsigned 
   return *slot;
 }
 
+/* The 32 bytes of word (lane * WPT + j) of the tile as eight little-endian 32-bit words;
+ * bytes before the input start or at or beyond its end read as zero. */
+__device__ __forceinline__ void load_word_bytes(const BgParams &p, const Tile &t, int j,
+                                                uint32_t u[8]) {
+  const uint8_t *src = p.in_bytes + p.in_off[t.input];
+  const long long w = t.base + t.lane * WPT + j;
+  if (w >= 0 && 32 * w + 32 <= t.n) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(src + 32 * w);
+    const uint4 a = __ldg(q), c = __ldg(q + 1);
+    u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
+    u[4] = c.x; u[5] = c.y; u[6] = c.z; u[7] = c.w;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) u[q] = 0u;
+    if (w >= 0 && w < t.W) {
+      const long long rem = t.n - 32 * w;
+      for (long long k = 0; k < rem; ++k)
+        u[k >> 2] |= (uint32_t)__ldg(src + 32 * w + k) << (8 * (k & 3));
+    }
+  }
+}
+
 __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b[8]) {
   if (p.input_kind == BG_INPUT_BASIS) {
     const uint32_t *src = p.in_basis + p.in_off[t.input];
@@ -648,25 +674,10 @@ __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b
     }
     return;
   }
-  const uint8_t *src = p.in_bytes + p.in_off[t.input];
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
-    const long long w = t.base + t.lane * WPT + j;
     uint32_t u[8];
-    if (w >= 0 && 32 * w + 32 <= t.n) {
-      const uint4 *q = reinterpret_cast<const uint4 *>(src + 32 * w);
-      const uint4 a = __ldg(q), c = __ldg(q + 1);
-      u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
-      u[4] = c.x; u[5] = c.y; u[6] = c.z; u[7] = c.w;
-    } else {
-#pragma unroll
-      for (int q = 0; q < 8; ++q) u[q] = 0u;
-      if (w >= 0 && w < t.W) {
-        const long long rem = t.n - 32 * w;
-        for (long long k = 0; k < rem; ++k)
-          u[k >> 2] |= (uint32_t)__ldg(src + 32 * w + k) << (8 * (k & 3));
-      }
-    }
+    load_word_bytes(p, t, j, u);
     uint32_t o[8];
     transpose32(u, o);
 #pragma unroll
@@ -730,6 +741,90 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
       atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, (unsigned long long)cnt);
   }
 }
+
+#if BG_PREFILTER
+/* Trigram prefilter (tables generated by bitgen_gb300/prefilter.py).  Every trigram lying in
+ * the bytes this warp computes is hashed into the Bloom bitmap `bloom` (2^16 bits, shared
+ * memory); a hit is resolved in the exact open-addressed table (keys: trigram | 1 << 31, 0 =
+ * empty; BG_NRUN mask words per slot), whose mask is OR-ed into the tile's run mask.  The
+ * trigram ending at byte q is byte(q-2) | byte(q-1) << 8 | byte(q) << 16; bytes before the
+ * warp's first byte read as zero. */
+constexpr uint32_t BLOOM_HASH = 0x9E3779B1u, EXACT_HASH = 0x85EBCA6Bu;
+
+static __device__ __noinline__ void trigram_exact(uint32_t key, const uint32_t *keys,
+                                                  const uint32_t *masks, int log2, uint32_t *run) {
+  const uint32_t slots = 1u << log2;
+  uint32_t s = (key * EXACT_HASH) >> (32 - log2);
+  for (uint32_t it = 0; it < slots; ++it) {
+    const uint32_t k = __ldg(keys + s);
+    if (k == 0u) return;
+    if (k == (key | 0x80000000u)) {
+#pragma unroll
+      for (int w = 0; w < BG_NRUN; ++w) run[w] |= __ldg(masks + s * BG_NRUN + w);
+      return;
+    }
+    s = (s + 1u) & (slots - 1u);
+  }
+}
+
+__device__ __forceinline__ void trigram_test(uint32_t key, const uint32_t *bloom,
+                                             const uint32_t *keys, const uint32_t *masks, int log2,
+                                             uint32_t *run) {
+  const uint32_t h = (key * BLOOM_HASH) >> 16;
+  if ((bloom[h >> 5] >> (h & 31u)) & 1u) trigram_exact(key, keys, masks, log2, run);
+}
+
+/* Load the tile's bytes, fill t.run from the trigram scan (warp-uniform) and transpose the bytes
+ * into the basis.  Inputs given as basis planes have no bytes to scan: every term runs. */
+__device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
+                                          const uint32_t *bloom, const uint32_t *keys,
+                                          const uint32_t *masks, int log2) {
+  uint32_t run[BG_NRUN];
+#pragma unroll
+  for (int w = 0; w < BG_NRUN; ++w) run[w] = 0u;
+  if (p.input_kind == BG_INPUT_BASIS) {
+    load_basis(p, t, b);
+#pragma unroll
+    for (int w = 0; w < BG_NRUN; ++w) t.run[w] = FULL;
+    return;
+  }
+  uint32_t raw[WPT][8];
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
+  uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
+  if (t.lane == 0) prev = 0u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t cur = raw[j][i];
+      trigram_test(__byte_perm(prev, cur, 0x0432) & 0xFFFFFFu, bloom, keys, masks, log2, run);
+      trigram_test(__byte_perm(prev, cur, 0x0543) & 0xFFFFFFu, bloom, keys, masks, log2, run);
+      trigram_test(cur & 0xFFFFFFu, bloom, keys, masks, log2, run);
+      trigram_test(cur >> 8, bloom, keys, masks, log2, run);
+      prev = cur;
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < BG_NRUN; ++w) t.run[w] = __reduce_or_sync(FULL, run[w]);
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    uint32_t o[8];
+    transpose32(raw[j], o);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
+  }
+}
+
+/* Lanes whose words of class stream C are all ones (inside the input): an addition over C
+ * with a zero marker can only take or pass on a carry through such lanes. */
+__device__ __forceinline__ uint32_t ones_lanes(const Tile &t, const S &C) {
+  uint32_t a = 1u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) a &= ((C.w[j] & t.vm.w[j]) == FULL) ? 1u : 0u;
+  return __ballot_sync(FULL, a);
+}
+#endif
 
 #ifdef BG_NOUT
 /* Per-warp output accumulators in shared memory, laid out [output][word][lane] so that a warp's

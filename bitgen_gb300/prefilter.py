@@ -1,0 +1,226 @@
+"""Trigram prefilter: which terms of a program can be non-zero in a tile, decided from the
+tile's bytes before any bitstream is computed.
+
+A *trigram node* is a node z whose set bits constrain the bytes at and just before them: if z
+is set at position p, then bytes p-2, p-1 and p lie in sets S0, S1 and S2 (position bounds,
+derived through AND, OR and Advance; see ``position_bounds``).  So when no trigram of
+S0 x S1 x S2 occurs among the bytes a warp computes, z is zero in all of the warp's exact
+lanes.
+
+Zero implication.  Z(v) is the set of trigram nodes whose being zero makes v zero: AND and
+Advance / Lookahead inherit the union of their operands' sets, OR / XOR / SEL the intersection,
+and an addition its marker's set.  The last rule holds only while no carry enters the tile, so
+the kernel also runs a term whenever one of its additions could take or owe a carry: a
+look-back addition whose class is all ones at its carry lane or at its successor's, or a
+pre-pass addition with a carry-in when the term's filter holds only through it.
+
+Each term (an OR-ed leaf of an output) gets the most selective trigram node of Z(term) as its
+filter, preferring one that does not pass through a pre-pass addition; a term without one
+always runs.  Each pre-pass addition gets the filter of its marker,
+so the pre-pass can skip the marker's computation too.
+
+The kernel tests every trigram of the tile against a Bloom bitmap (2^16 bits, in shared memory)
+and resolves the rare hits in an exact open-addressed table that maps a trigram to the bit mask
+of the filters containing it.  Both tables are generated here and compiled into the kernel.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Dict, FrozenSet, List, Optional, Sequence, Tuple
+
+ALL = (1 << 256) - 1
+MAX_SET = 4096          # largest trigram set one filter may carry
+BLOOM_BITS = 16         # log2 of the Bloom bitmap size
+HASH_BLOOM = 0x9E3779B1
+HASH_EXACT = 0x85EBCA6B
+
+
+def bloom_hash(key: int) -> int:
+    return ((key * HASH_BLOOM) & 0xFFFFFFFF) >> (32 - BLOOM_BITS)
+
+
+def exact_hash(key: int, log2_slots: int) -> int:
+    return ((key * HASH_EXACT) & 0xFFFFFFFF) >> (32 - log2_slots)
+
+
+def _bytes(s: int) -> List[int]:
+    return [b for b in range(256) if (s >> b) & 1]
+
+
+def position_bounds(gen, depth: int = 3) -> Dict[int, Tuple[int, ...]]:
+    """PB[v][k]: set of byte values that can stand k positions before a set bit of node v
+    (k < depth; ALL when unconstrained).  AND intersects its operands' bounds, OR / XOR / SEL
+    unite them, Advance(a, s) moves a's bounds s positions back, a class bounds its own position
+    only; additions, NOT of a heavy node and Lookahead bound nothing."""
+    d = gen.d
+    PB: Dict[int, Tuple[int, ...]] = {}
+    free = (ALL,) * depth
+    for v in sorted(gen.live):
+        n = d.nodes[v]
+        if d.is_cc(v):
+            PB[v] = (gen.byteset(v),) + (ALL,) * (depth - 1)
+        elif n.op == "and":
+            a, b = PB[n.args[0]], PB[n.args[1]]
+            PB[v] = tuple(x & y for x, y in zip(a, b))
+        elif n.op in ("or", "xor"):
+            a, b = PB[n.args[0]], PB[n.args[1]]
+            PB[v] = tuple(x | y for x, y in zip(a, b))
+        elif n.op == "sel":
+            a, b = PB[n.args[1]], PB[n.args[2]]
+            PB[v] = tuple(x | y for x, y in zip(a, b))
+        elif n.op == "advance":
+            a, sft = PB[n.args[0]], n.shift
+            PB[v] = tuple(a[k - sft] if k >= sft else ALL for k in range(depth))
+        elif n.op == "zero":
+            PB[v] = (0,) * depth
+        else:
+            PB[v] = free
+    return PB
+
+
+def trigram_nodes(gen, PB: Dict[int, Tuple[int, ...]]) -> Dict[int, Tuple[int, int, int]]:
+    """Trigram nodes of the live program and their byte sets (S0, S1, S2): every heavy node
+    whose bounds at the last three positions are all constrained, with a small product."""
+    d = gen.d
+    out: Dict[int, Tuple[int, int, int]] = {}
+    for z in sorted(gen.live):
+        if d.is_cc(z):
+            continue
+        s2, s1, s0 = PB[z][0], PB[z][1], PB[z][2]
+        if ALL in (s0, s1, s2):
+            continue
+        size = bin(s0).count("1") * bin(s1).count("1") * bin(s2).count("1")
+        if 0 < size <= MAX_SET:
+            out[z] = (s0, s1, s2)
+    return out
+
+
+def zero_sets(gen, tri: Dict[int, Tuple[int, int, int]],
+              blocked=frozenset()) -> Dict[int, FrozenSet[int]]:
+    """Z(v) for every live node.  The result of an addition in `blocked` implies nothing (its
+    carry may be non-zero whatever its marker)."""
+    d = gen.d
+    Z: Dict[int, FrozenSet[int]] = {}
+    empty: FrozenSet[int] = frozenset()
+    for v in sorted(gen.live):
+        n = d.nodes[v]
+        if d.is_cc(v) or n.op in ("basis", "zero", "ones", "not"):
+            z = empty
+        elif n.op == "and":
+            z = Z[n.args[0]] | Z[n.args[1]]
+        elif n.op in ("advance", "lookahead"):
+            z = Z[n.args[0]]
+        elif n.op in ("or", "xor"):
+            z = Z[n.args[0]] & Z[n.args[1]]
+        elif n.op == "sel":
+            z = Z[n.args[1]] & Z[n.args[2]]
+        elif n.op in ("matchstar", "scanthru"):
+            z = empty if v in blocked else Z[n.args[0]]
+        else:
+            z = empty
+        if v in tri:
+            z = z | {v}
+        Z[v] = z
+    return Z
+
+
+def trigram_set(sets: Tuple[int, int, int]) -> List[int]:
+    s0, s1, s2 = (_bytes(s) for s in sets)
+    return [a | (b << 8) | (c << 16) for a in s0 for b in s1 for c in s2]
+
+
+@dataclass
+class TermFilter:
+    """Per-program prefilter: bit r (r < n_terms) = term r may be non-zero, bit n_terms + k =
+    pre-pass addition k's marker may be non-zero.  ``always`` holds the terms without a filter."""
+    n_terms: int
+    n_pre: int
+    term_node: List[Optional[int]]
+    pre_node: List[Optional[int]]
+    term_cond: List[bool] = field(default_factory=list)  # filter implies zero only if no carry
+    table: Dict[int, int] = field(default_factory=dict)   # trigram -> bit mask
+
+    @property
+    def n_bits(self) -> int:
+        return self.n_terms + self.n_pre
+
+    @property
+    def words(self) -> int:
+        return max(1, (self.n_bits + 31) // 32)
+
+    @property
+    def enabled(self) -> bool:
+        return bool(self.table)
+
+    def always_mask(self) -> int:
+        m = 0
+        for r, z in enumerate(self.term_node):
+            if z is None:
+                m |= 1 << r
+        for k, z in enumerate(self.pre_node):
+            if z is None:
+                m |= 1 << (self.n_terms + k)
+        return m
+
+    def bloom(self) -> List[int]:
+        words = [0] * ((1 << BLOOM_BITS) // 32)
+        for key in self.table:
+            h = bloom_hash(key)
+            words[h >> 5] |= 1 << (h & 31)
+        return words
+
+    def exact(self) -> Tuple[int, List[int], List[int]]:
+        """(log2 slots, keys, mask words): open addressing with linear probing; a key slot
+        holds trigram | 1 << 31 (0 = empty); masks are ``words`` words per slot."""
+        n = len(self.table)
+        log2 = 4
+        while (1 << log2) < 2 * max(1, n):
+            log2 += 1
+        slots = 1 << log2
+        keys = [0] * slots
+        masks = [0] * (slots * self.words)
+        for key, m in sorted(self.table.items()):
+            s = exact_hash(key, log2)
+            while keys[s]:
+                s = (s + 1) & (slots - 1)
+            keys[s] = key | (1 << 31)
+            for w in range(self.words):
+                masks[s * self.words + w] = (m >> (32 * w)) & 0xFFFFFFFF
+        return log2, keys, masks
+
+
+def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 16) -> TermFilter:
+    """Filters for `terms` (node ids, in bit order) and pre-pass additions `pre` (node ids, in
+    index order)."""
+    tri = trigram_nodes(gen, position_bounds(gen))
+    Z = zero_sets(gen, tri)
+    # through a pre-pass addition a filter holds only while that addition's carry-in is zero,
+    # which a '.*' after its first match almost never is; other additions are checked anyway
+    Zp = zero_sets(gen, tri, blocked=frozenset(pre))
+    d = gen.d
+
+    def best(zs) -> Optional[int]:
+        cands = sorted(zs, key=lambda z: (len(trigram_set(tri[z])), z))
+        return cands[0] if cands else None
+
+    term_node, term_cond = [], []
+    for v in terms:
+        z = best(Zp.get(v, ()))
+        cond = z is None
+        if z is None:
+            z = best(Z.get(v, ()))
+        term_node.append(z)
+        term_cond.append(cond and z is not None)
+    pre_node = [best(Z.get(d.nodes[a].args[0], ())) for a in pre]
+    f = TermFilter(len(terms), len(pre), term_node, pre_node, term_cond)
+    table: Dict[int, int] = {}
+    for bit, z in list(enumerate(term_node)) + [(len(terms) + k, z) for k, z in enumerate(pre_node)]:
+        if z is None:
+            continue
+        for key in trigram_set(tri[z]):
+            table[key] = table.get(key, 0) | (1 << bit)
+    if len(table) > tri_limit:
+        table = {}
+    f.table = table
+    return f

@@ -58,7 +58,10 @@ def small():
 @pytest.mark.parametrize("wpt,skip,block,extra", [(1, 1, 256, {}), (2, 1, 256, {}), (4, 1, 128, {}),
                                                   (2, 0, 64, {}), (2, 3, 256, {}),
                                                   (2, 1, 256, {"lockstep": True}),
-                                                  (2, 1, 256, {"edge_variants": True, "part_cap": 4})])
+                                                  (2, 1, 256, {"edge_variants": True, "part_cap": 4}),
+                                                  (2, 1, 256, {"prefilter": False}),
+                                                  (1, 1, 256, {"part_cap": 1}),
+                                                  (2, 1, 256, {"carry_prepass": False})])
 def test_small_workload_tunings(cuda, wpt, skip, block, extra):
     ps, text, groups = small()
     prog = Program(groups, tuning=Tuning(wpt=wpt, skip_interval=skip, block=block, **extra))
@@ -92,7 +95,7 @@ def test_long_carries_across_many_tiles(cuda):
     t2 = np.full(n, ord("a"), np.uint8)  # one 'a' run spanning every tile, 'b' at the end
     t2[-1] = ord("b")
     for tun in (Tuning(wpt=1), Tuning(wpt=4, block=128), Tuning(lockstep=True),
-                Tuning(edge_variants=True), Tuning(carry_prepass=False)):
+                Tuning(edge_variants=True), Tuning(carry_prepass=False), Tuning(prefilter=False)):
         prog = Program(groups, tuning=tun)
         check(prog, groups, [t, t2, t2[:1000], t[:5]])
 
@@ -112,7 +115,7 @@ def test_carry_prepass_matches_lookback_and_oracle(cuda):
     long[1_999_990:1_999_992] = np.frombuffer(b"zz", np.uint8)
     items.append(long)
     with_pre = Program(groups)
-    without = Program(groups, tuning=Tuning(carry_prepass=False))
+    without = Program(groups, tuning=Tuning(carry_prepass=False, prefilter=False))
     assert with_pre.spec.n_pre >= 2 and without.spec.n_pre == 0
     assert with_pre.spec.n_pre < with_pre.spec.n_adds  # the nested '.*' is not pre-passed
     check(with_pre, groups, items)

@@ -1,0 +1,96 @@
+"""CPU checks of the trigram prefilter (bitgen_gb300/prefilter.py).
+
+Soundness: a term that is non-zero in a tile's exact lanes must have its bit set by the tile's
+trigram scan.  The scan is simulated here exactly as the kernel does it (every trigram lying
+wholly inside the bytes the warp computes, looked up in the exact table), and the per-regex
+streams come from the C oracle.  Terms behind an addition are excluded, since the kernel runs
+those on its own carry checks.  The Bloom bitmap must contain every key of the exact table
+(the table only removes Bloom false positives), and the table's probes must find every key.
+"""
+
+import numpy as np
+import pytest
+
+from bitgen_gb300 import prefilter, workloads
+from bitgen_gb300.compiler import ADD_OPS, Tuning, _Gen, build_dag
+from bitgen_gb300.regex import compile_group
+from oracle import cpu
+
+
+def _setup(patterns, n_groups, per_regex=True, wpt=2):
+    groups = [compile_group(g) for g in patterns.groups(n_groups)]
+    dag, outs, names = build_dag(groups, per_regex)
+    gen = _Gen(dag, Tuning(wpt=wpt))
+    gen.analyse(outs)
+    terms = [(leaf, o) for o, v in enumerate(outs) for leaf in gen.or_leaves(v)]
+    pre = [v for v, _ in sorted(gen.pre.items(), key=lambda x: x[1])]
+    f = prefilter.build(gen, [v for v, _ in terms], pre)
+    return groups, gen, terms, f
+
+
+def _lookup(f, key, log2, keys, masks):
+    s = prefilter.exact_hash(key, log2)
+    for _ in range(len(keys)):
+        if keys[s] == 0:
+            return 0
+        if keys[s] == key | (1 << 31):
+            return sum(masks[s * f.words + w] << (32 * w) for w in range(f.words))
+        s = (s + 1) & (len(keys) - 1)
+    return 0
+
+
+def test_tables_are_consistent():
+    _, _, _, f = _setup(workloads.throughput_patterns(seed=3, n=64), 4)
+    assert f.enabled
+    bloom = f.bloom()
+    log2, keys, masks = f.exact()
+    for key, m in f.table.items():
+        h = prefilter.bloom_hash(key)
+        assert (bloom[h >> 5] >> (h & 31)) & 1
+        assert _lookup(f, key, log2, keys, masks) == m
+    assert _lookup(f, 0x7f7f7f, log2, keys, masks) == 0 or 0x7f7f7f in f.table
+
+
+@pytest.mark.parametrize("wpt", [1, 2])
+def test_prefilter_is_sound_on_throughput_patterns(wpt):
+    ps = workloads.throughput_patterns(seed=3, n=64)
+    groups, gen, terms, f = _setup(ps, 4, wpt=wpt)
+    n = 300_000
+    text = workloads.plant(workloads.printable_text(n, 41), ps.witnesses, 700, 42)
+    streams, _ = cpu.run_groups(groups, text, per_regex=True)
+    log2, keys, masks = f.exact()
+    hl, tl = gen.hl, gen.tl
+    tile_words = (32 - hl - tl) * wpt
+    W = (n + 31) // 32
+    b = text.astype(np.int64)
+    tri = np.zeros(n, dtype=np.int64)
+    tri[2:] = b[:-2] | (b[1:-1] << 8) | (b[2:] << 16)   # trigram ending at each position
+    hit_bits = np.zeros(n, dtype=object)
+    for p in np.nonzero(np.isin(tri, np.array(sorted(f.table), dtype=np.int64)))[0]:
+        if p >= 2:
+            hit_bits[p] = f.table[int(tri[p])]
+    has_add = [any(gen.d.nodes[a].op in ADD_OPS for a in gen.heavy_ancestors(v)) for v, _ in terms]
+    by_out = {}
+    for r, (v, o) in enumerate(terms):
+        by_out.setdefault(o, []).append(r)
+    checked = 0
+    n_tiles = max(1, -(-W // tile_words))
+    for g in range(n_tiles):
+        base = g * tile_words - hl * wpt               # word index of lane 0, word 0
+        lo_b = max(0, base * 32)
+        hi_b = min(n, (base + 32 * wpt) * 32)
+        cand = 0
+        for p in range(lo_b + 2, hi_b):
+            if hit_bits[p]:
+                cand |= hit_bits[p]
+        cand |= f.always_mask()
+        ex_lo, ex_hi = max(0, g * tile_words), min(W, (g + 1) * tile_words)
+        for o, rs in by_out.items():
+            if any(has_add[r] for r in rs):
+                continue
+            if np.any(streams[o][ex_lo:ex_hi]):
+                assert any((cand >> r) & 1 for r in rs), (g, o)
+                checked += 1
+    assert checked > 10
+    # selective: on this text most tiles flag few terms
+    assert sum(1 for r, z in enumerate(f.term_node) if z is None) < len(terms) // 4
