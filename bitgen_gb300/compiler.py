@@ -346,6 +346,7 @@ class KernelSpec:
     output_names: List[str] = field(default_factory=list)
     tail_lanes: int = 0
     n_pre: int = 0          # additions 0..n_pre-1 take their carries from the pre-pass kernel
+    n_run: int = 0          # split form: run-mask words per tile (0 = single-kernel form)
 
     @property
     def tile_words(self):
@@ -1067,7 +1068,9 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         filt = prefilter.build(gen, [v for v, _ in terms], pre_nodes)
         if not filt.enabled:
             filt = None
-    budget = SMEM_BUDGET - (BLOOM_SMEM if filt else 0)
+    if filt is not None:
+        return _generate_filtered(gen, tuning, terms, names, filt, name)
+    budget = SMEM_BUDGET
     per_warp = max(1, n_out) * wpt * 32 * 4
     if per_warp > budget:
         raise NotFusable(f"{n_out} outputs need {per_warp} bytes of accumulators per warp; "
@@ -1078,8 +1081,6 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         tuning = replace(tuning, block=block,
                          min_blocks=min(32, -(-tuning.min_blocks * tuning.block // block)))
     warps = tuning.block // 32
-    if filt is not None:
-        return _generate_filtered(gen, tuning, terms, names, filt, name)
     clusters = _cluster_terms(gen, terms, tuning.part_cap)
     funcs = []
     sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
@@ -1155,7 +1156,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
             f"  init(p, t);\n"
             f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
             f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
-            f"    setup_tile(p, t, (unsigned int)g, false);\n"
+            f"    setup_tile(p, t, (unsigned int)g, false, false);\n"
             f"    S b[8];\n"
             f"    load_basis(p, t, b);\n"
             f"    const uint32_t {basis_decl};\n"
@@ -1198,36 +1199,41 @@ def _hex_array(vals: Sequence[int], per_line: int = 12) -> str:
 
 def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]],
                        names: List[str], filt: "prefilter.TermFilter", name: str) -> KernelSpec:
-    """The prefiltered form of the kernel.
+    """The split, prefiltered form of the program: two kernels.
 
-    Per tile the kernel loads the bytes, scans their trigrams (bg_device.cuh load_scan) and so
-    learns which terms may be non-zero; terms whose additions could take or owe a carry are
-    added (look-back additions whose class is all ones at the carry lane or the successor's
-    carry lane, pre-pass additions with a carry-in when the term's filter holds only through
-    them).  Part functions hold one guarded block per term and are called only when one of
-    their terms runs; each block is the term's full program with its own zero-skip guards.  The
-    carry pre-pass computes a pre-pass addition's marker only when its trigram filter fires."""
+    ``<name>_cls`` (classify) visits every tile once, with nothing to wait for: it scans the
+    tile's trigrams (bg_device.cuh load_scan), publishes the carry pre-pass aggregates, adds the
+    terms whose look-back additions could take or owe a carry (class all ones at the carry lane
+    or at the successor's) and those whose filter holds only through a pre-pass carry, and
+    writes the tile's run mask (one bit per term) to ``p.runs``.
+
+    ``<name>`` (execute) runs after the carry scan.  Its work items are (part, 32 tiles) pairs
+    in part-major order, handed out by an atomic counter: a warp reads the 32 tiles' run masks
+    with one load, and for each tile where one of the part's terms runs it loads the basis and
+    calls the part.  So at any time the whole GPU executes the same part's code, and the
+    instruction caches stay warm.  Parts hold whole outputs: a part ORs its terms into
+    per-warp accumulators of its own outputs and stores them; outputs of tiles it skips keep
+    the zeros the launch wrote.  Tiles of one part are claimed in increasing order, which keeps
+    the look-back of its additions deadlock free."""
     d = gen.d
     wpt = tuning.wpt
     warps = tuning.block // 32
     nt = len(terms)
     nw = filt.words
     always = filt.always_mask()
+    for r, cond in enumerate(filt.term_cond):
+        if cond:                       # classify runs before the carry scan: no carry-ins yet
+            always |= 1 << r
     sl = 32 - gen.hl - gen.tl
-    # run conditions -----------------------------------------------------------------------
-    pm_classes: Dict[int, str] = {}          # class node -> name of its all-ones lane mask
+    # look-back obligations -----------------------------------------------------------------
+    pm_classes: Dict[int, str] = {}
     needs: List[List[str]] = [[] for _ in range(nt)]
     for r, (v, _) in enumerate(terms):
         if (always >> r) & 1:
             continue
         for a in sorted(gen.heavy_ancestors(v)):
             n = d.nodes[a]
-            if n.op not in ADD_OPS:
-                continue
-            if a in gen.pre:
-                if filt.term_cond[r]:
-                    k = gen.pre[a]
-                    needs[r].append(f"(t.pcin[{k >> 5}] >> {k & 31}) & 1u")
+            if n.op not in ADD_OPS or a in gen.pre:
                 continue
             c = n.args[1]
             if not d.is_cc(c):
@@ -1236,7 +1242,50 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             pm = pm_classes.setdefault(c, f"pm{c}")
             dl = gen.dl[a]
             needs[r].append(f"(({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u")
-    # kernel-level code: classes for the all-ones masks, then the run bits
+    # parts of whole outputs ----------------------------------------------------------------
+    by_out: Dict[int, List[int]] = {}
+    for r, (v, o) in enumerate(terms):
+        by_out.setdefault(o, []).append(r)
+    cap = max(1, tuning.part_cap)
+    parts: List[List[int]] = []          # outputs of each part
+    cur: List[int] = []
+    cur_terms = 0
+    for o in range(len(names)):
+        k = len(by_out.get(o, []))
+        if cur and (cur_terms + k > cap or len(cur) >= 32):
+            parts.append(cur)
+            cur, cur_terms = [], 0
+        cur.append(o)
+        cur_terms += k
+    if cur:
+        parts.append(cur)
+    nacc = max(1, max(len(ps) for ps in parts))
+    sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
+    funcs = []
+    part_masks: List[Dict[int, int]] = []
+    for ci, outs_k in enumerate(parts):
+        blocks = []
+        masks: Dict[int, int] = {}
+        for li, o in enumerate(outs_k):
+            for r in by_out.get(o, []):
+                masks[r >> 5] = masks.get(r >> 5, 0) | (1 << (r & 31))
+                code = gen.part([(terms[r][0], li)])
+                body = "\n".join("  " + ln for ln in code.split("\n"))
+                blocks.append(f"  if ((t.run[{r >> 5}] >> {r & 31}) & 1u) {{\n{body}\n  }}")
+        part_masks.append(masks)
+        stores = "\n".join(f"  store(p, t, {o}, acc_get(acc, t, {li}));" for li, o in enumerate(outs_k))
+        funcs.append(f"//@@BG_PART\n"
+                     f'extern "C" __device__ __noinline__ void bg_part_{ci}({sig}) {{\n'
+                     f"  constexpr bool E = true;\n"
+                     f"  acc_clear_n(acc, t, {len(outs_k)});\n" + "\n".join(blocks) + "\n" + stores + "\n}\n")
+    decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
+    ba = ", ".join(f"b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+    wants = []
+    for ci, masks in enumerate(part_masks):
+        cond = " | ".join(f"(p.runs[{w}LL * p.n_tiles + g] & 0x{m:08x}u)" for w, m in sorted(masks.items())) or "0u"
+        wants.append(f"          case {ci}: want = ({cond}) != 0u; break;")
+    calls = "\n".join(f"        case {ci}: bg_part_{ci}(p, t, acc, {ba}); break;" for ci in range(len(parts)))
+    # classify kernel ------------------------------------------------------------------------
     gen.lines = []
     gen.indent = 4
     gen.scopes = [{}]
@@ -1244,91 +1293,54 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         m = (always >> (32 * w)) & 0xFFFFFFFF
         if m:
             gen.emit(f"t.run[{w}] |= 0x{m:08x}u;")
+    for v, k in sorted(gen.pre.items(), key=lambda x: x[1]):
+        n = d.nodes[v]
+        bit = nt + k
+        mode = 0 if n.op == "matchstar" else 1
+        gen.emit(f"S m{k} = zero();")
+        gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
+        m = gen.mat(n.args[0])
+        gen.emit(f"m{k} = {gen.pack(m)};")
+        gen.close()
+        c = gen.mat(n.args[1])
+        gen.emit(f"pre_publish<{gen.dl[v]}, E>(p, t, {k}, {mode}, m{k}, {gen.pack(c)});")
     for c, pm in sorted(pm_classes.items()):
         ref = gen.mat(c)
         gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
     for r, conds in enumerate(needs):
         if conds and not (always >> r) & 1:
             gen.emit(f"if ({' | '.join(conds)}) t.run[{r >> 5}] |= 0x{1 << (r & 31):08x}u;")
-    run_code = "\n".join(gen.lines)
-    # parts --------------------------------------------------------------------------------
-    # hot terms (run on carries or always) apart from the trigram-gated ones, so that a tile's
-    # calls go to few parts
-    hot = [r for r in range(nt) if (always >> r) & 1 or needs[r]]
-    cold = [r for r in range(nt) if r not in set(hot)]
-    cap = max(1, tuning.part_cap)
-    parts = [hot[i:i + cap] for i in range(0, len(hot), cap)] + \
-            [cold[i:i + cap] for i in range(0, len(cold), cap)]
-    sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
-    funcs = []
-    for ci, rs in enumerate(parts):
-        blocks = []
-        for r in rs:
-            code = gen.part([terms[r]])
-            body = "\n".join("  " + ln for ln in code.split("\n"))
-            blocks.append(f"  if ((t.run[{r >> 5}] >> {r & 31}) & 1u) {{\n{body}\n  }}")
-        funcs.append(f"//@@BG_PART\n"
-                     f'extern "C" __device__ __noinline__ void bg_part_{ci}({sig}) {{\n'
-                     f"  constexpr bool E = true;\n" + "\n".join(blocks) + "\n}\n")
-    decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
-    ba = _basis_args(wpt)
-    calls = []
-    for ci, rs in enumerate(parts):
-        masks = {}
-        for r in rs:
-            masks[r >> 5] = masks.get(r >> 5, 0) | (1 << (r & 31))
-        cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(masks.items()))
-        calls.append(f"    if ({cond}) bg_part_{ci}(p, t, acc, {ba});")
-    # tables -------------------------------------------------------------------------------
-    log2, keys, masks = filt.exact()
+    for w in range(nw):
+        gen.emit(f"if (t.lane == 0) p.runs[{w}LL * p.n_tiles + g] = t.run[{w}];")
+    for ci, outs_k in enumerate(parts):
+        cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
+        gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
+    cls_code = "\n".join(gen.lines)
+    log2, keys, masks_tab = filt.exact()
     bloom = filt.bloom()
     tables = (f"#define BG_EXLOG2 {log2}\n"
               f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
               f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
-              f"static __device__ const uint32_t bg_exmasks[{len(masks)}] = {{\n{_hex_array(masks)}\n}};\n")
-    scan = ("    S b[8];\n"
-            "    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
-            f"    const uint32_t {', '.join(f'b{i}_{j} = b[{i}].w[{j}]' for i in range(8) for j in range(wpt))};\n"
-            "    constexpr bool E = true;\n")
-    bloom_init = (f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
-                  f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
-                  f"  __syncthreads();\n")
-    # pre-pass kernel ----------------------------------------------------------------------
-    pre_kernel = ""
-    if gen.pre:
-        gen.lines = []
-        gen.indent = 4
-        gen.scopes = [{}]
-        for v, k in sorted(gen.pre.items(), key=lambda x: x[1]):
-            n = d.nodes[v]
-            bit = nt + k
-            mode = 0 if n.op == "matchstar" else 1
-            gen.emit(f"S m{k} = zero();")
-            gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
-            m = gen.mat(n.args[0])
-            gen.emit(f"m{k} = {gen.pack(m)};")
-            gen.close()
-            c = gen.mat(n.args[1])
-            gen.emit(f"pre_publish<{gen.dl[v]}, E>(p, t, {k}, {mode}, m{k}, {gen.pack(c)});")
-        pre_kernel = (
-            f"//@@BG_PART\n{tables}"
-            f"/* carry pre-pass: the aggregates of additions 0..{len(gen.pre) - 1} for every tile, no waits;\n"
-            f"   tiles are taken in a fixed stride since nothing here waits on another tile */\n"
-            f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_pre(const __grid_constant__ BgParams p) {{\n'
-            + bloom_init +
-            f"  Tile t;\n"
-            f"  init(p, t);\n"
-            f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
-            f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
-            f"    setup_tile(p, t, (unsigned int)g, false);\n"
-            + scan +
-            f"    t.run[{(nt) >> 5}] |= 0u;\n"
-            + "\n".join(
-                f"    t.run[{w}] |= 0x{(always >> (32 * w)) & 0xFFFFFFFF:08x}u;" for w in range(nw)
-                if (always >> (32 * w)) & 0xFFFFFFFF) + "\n"
-            f"{chr(10).join(gen.lines)}\n"
-            f"  }}\n"
-            f"}}\n")
+              f"static __device__ const uint32_t bg_exmasks[{len(masks_tab)}] = {{\n{_hex_array(masks_tab)}\n}};\n")
+    basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+    cls_kernel = (
+        f"//@@BG_PART\n{tables}"
+        f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_cls(const __grid_constant__ BgParams p) {{\n'
+        f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
+        f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
+        f"  __syncthreads();\n"
+        f"  Tile t;\n"
+        f"  init(p, t);\n"
+        f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
+        f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
+        f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
+        f"    S b[8];\n"
+        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
+        f"    const uint32_t {basis_decl};\n"
+        f"    constexpr bool E = true;\n"
+        f"{cls_code}\n"
+        f"  }}\n"
+        f"}}\n")
     warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
     comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
@@ -1349,21 +1361,42 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"
         f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
         f"{comments}\n"
-        + "\n".join(funcs) + pre_kernel +
-        f"//@@BG_KERNEL\n{tables}{decls}\n"
+        + "\n".join(funcs) + cls_kernel +
+        f"//@@BG_KERNEL\n{decls}\n"
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
-        f"  __shared__ uint32_t bg_acc[{warps} * BG_NOUT * BG_WPT * 32];\n"
-        + bloom_init +
-        f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
+        f"  __shared__ uint32_t bg_acc[{warps} * {nacc} * BG_WPT * 32];\n"
+        f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * ({nacc} * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        f"  while (next_tile(p, t)) {{\n"
-        f"    acc_clear(acc, t);\n"
-        + scan + run_code + "\n" + "\n".join(calls) + "\n"
-        f"    acc_store(p, t, acc);\n"
+        f"  const long long chunks = (p.n_tiles + 31) >> 5;\n"
+        f"  const long long items = chunks * {len(parts)};\n"
+        f"  for (;;) {{\n"
+        f"    unsigned int it = 0u;\n"
+        f"    if (t.lane == 0) it = atomicAdd(p.state, 1u);\n"
+        f"    it = __shfl_sync(FULL, it, 0);\n"
+        f"    if ((long long)it >= items) break;\n"
+        f"    const int k = (int)((long long)it / chunks);\n"
+        f"    const long long g0 = ((long long)it - (long long)k * chunks) * 32;\n"
+        f"    const long long g = g0 + t.lane;\n"
+        f"    bool want = false;\n"
+        f"    if (g < p.n_tiles) {{\n"
+        f"      switch (k) {{\n" + "\n".join(wants) + "\n"
+        f"        default: break;\n"
+        f"      }}\n"
+        f"    }}\n"
+        f"    uint32_t sel = __ballot_sync(FULL, want);\n"
+        f"    while (sel) {{\n"
+        f"      const int l = __ffs(sel) - 1;\n"
+        f"      sel &= sel - 1u;\n"
+        f"      setup_tile(p, t, (unsigned int)(g0 + l), true, false);\n"
+        + "".join(f"      t.run[{w}] = __ldg(p.runs + {w}LL * p.n_tiles + g0 + l);\n" for w in range(nw)) +
+        f"      S b[8];\n"
+        f"      load_basis(p, t, b);\n"
+        f"      switch (k) {{\n{calls}\n        default: break;\n      }}\n"
+        f"    }}\n"
         f"  }}\n"
         f"}}\n")
     return KernelSpec(source=src, name=name, n_outputs=len(names), n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
                       n_nodes=len(d.nodes), output_names=names, tail_lanes=gen.tl,
-                      n_pre=len(gen.pre))
+                      n_pre=len(gen.pre), n_run=nw)

@@ -590,10 +590,11 @@ __device__ __forceinline__ void load_pre_carries(const BgParams &p, Tile &t) {
   }
 }
 
-/* Fill `t` for global tile g.  `main_pass` = false in the carry pre-pass, which neither reads
- * the pre-pass carries (it is producing them) nor takes part in the wait-limit test. */
+/* Fill `t` for global tile g.  `carries`: read the pre-pass carries (false in the passes that
+ * run before the carry scan); `debug_wait`: take part in the wait-limit test (exactly one pass
+ * over every tile does). */
 __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g,
-                                           bool main_pass = true) {
+                                           bool carries = true, bool debug_wait = true) {
   int lo = 0, hi = p.n_inputs; /* find i: prefix[i] <= g < prefix[i+1] */
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
@@ -613,9 +614,8 @@ __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned 
     t.em.w[j] = rem >= 32 ? FULL : (rem <= 0 ? 0u : (FULL << (32 - rem)));
   }
   t.edge = t.base < 0 || t.base + 32 * WPT >= t.W;
-  if (!main_pass) return;
-  if (NPRE > 0) load_pre_carries(p, t);
-  if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
+  if (NPRE > 0 && carries) load_pre_carries(p, t);
+  if (debug_wait && (long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
     (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
                       p.spin_limit, p.state, t.lane);
 }
@@ -843,6 +843,29 @@ __device__ __forceinline__ void acc_or(uint32_t *acc, int o, const S v) {
 #pragma unroll
     for (int j = 0; j < WPT; ++j) acc[(o * WPT + j) * 32 + lane] |= v.w[j];
   }
+}
+
+/* Split form: write zeros to output o's words of this tile (the words `store` would write),
+ * for tiles on which the part computing o does not run. */
+__device__ __forceinline__ void zero_store(const BgParams &p, const Tile &t, int o) {
+  if (!p.out) return;
+  uint32_t *dst = p.out + (long long)o * p.out_stride + p.out_off[t.input];
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) dst[w] = 0u;
+  }
+}
+
+/* Split form: a part's accumulators hold only its own outputs (local index). */
+__device__ __forceinline__ void acc_clear_n(uint32_t *acc, const Tile &t, int n) {
+  for (int i = 0; i < n * WPT; ++i) acc[i * 32 + t.lane] = 0u;
+}
+__device__ __forceinline__ S acc_get(const uint32_t *acc, const Tile &t, int o) {
+  S v;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) v.w[j] = acc[(o * WPT + j) * 32 + t.lane];
+  return v;
 }
 
 __device__ __forceinline__ void acc_store(const BgParams &p, const Tile &t, const uint32_t *acc) {

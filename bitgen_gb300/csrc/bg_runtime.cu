@@ -197,7 +197,8 @@ struct bg_program {
   std::vector<char> cubin;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t kernel = nullptr;
-  cudaKernel_t pre_kernel = nullptr; /* carry pre-pass, when desc.n_pre > 0 */
+  cudaKernel_t pre_kernel = nullptr; /* carry pre-pass, when desc.n_pre > 0 (single form) */
+  cudaKernel_t cls_kernel = nullptr; /* classify pass of the split form (desc.n_run > 0)  */
   int regs = 0, local_bytes = 0, blocks_per_sm = 1, pre_blocks_per_sm = 1;
 };
 
@@ -208,6 +209,7 @@ struct bg_plan {
   int64_t *d_tables = nullptr; /* in_off | in_len | tile_prefix | out_off */
   unsigned long long *d_records = nullptr;
   uint32_t *d_state = nullptr;
+  uint32_t *d_runs = nullptr; /* split form: [n_run][cap_tiles] run masks */
   int grid = 1;
   int64_t debug_wait_tile = -1;
   int64_t spin_limit = 0;
@@ -425,6 +427,7 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   if (!desc || !out || !desc->source || !desc->name || desc->wpt < 1 || desc->wpt > 8 ||
       desc->halo_lanes < 0 || desc->tail_lanes < 0 || desc->halo_lanes + desc->tail_lanes > 31 ||
       desc->n_outputs < 0 || desc->n_adds < 0 || desc->n_pre < 0 || desc->n_pre > desc->n_adds ||
+      desc->n_run < 0 ||
       desc->block < 32 || desc->block % 32)
     return fail(BG_ERR_INVALID, "bg_program_create: bad descriptor");
   *out = nullptr;
@@ -445,7 +448,9 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   cudaError_t e = cudaLibraryLoadData(&p->lib, p->cubin.data(), nullptr, nullptr, 0, nullptr,
                                       nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&p->kernel, p->lib, p->name.c_str());
-  if (e == cudaSuccess && desc->n_pre > 0)
+  if (e == cudaSuccess && desc->n_run > 0)
+    e = cudaLibraryGetKernel(&p->cls_kernel, p->lib, (p->name + "_cls").c_str());
+  else if (e == cudaSuccess && desc->n_pre > 0)
     e = cudaLibraryGetKernel(&p->pre_kernel, p->lib, (p->name + "_pre").c_str());
   if (e != cudaSuccess) {
     std::string msg = std::string("loading the compiled program: ") + cudaGetErrorString(e);
@@ -469,9 +474,9 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
     int regs = p->regs > 0 ? p->regs : 128;
     p->blocks_per_sm = std::max(1, 65536 / (regs * desc->block));
   }
-  if (p->pre_kernel) {
+  if (p->pre_kernel || p->cls_kernel) {
     nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)p->pre_kernel,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)(p->cls_kernel ? p->cls_kernel : p->pre_kernel),
                                                       desc->block, 0) == cudaSuccess && nb > 0)
       p->pre_blocks_per_sm = nb;
     else
@@ -561,6 +566,9 @@ int bg_plan_reserve(bg_program *prog, int32_t input_kind, int32_t max_inputs, in
     return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: look-back records");
   if (cudaMemset(p->d_records, 0, nrec * sizeof(unsigned long long)) != cudaSuccess)
     return cleanup(BG_ERR_CUDA, "bg_plan_reserve: clearing records");
+  if (prog->desc.n_run > 0 &&
+      cudaMalloc(&p->d_runs, (size_t)prog->desc.n_run * (size_t)max_tiles * sizeof(uint32_t)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: run masks");
   if (cudaMalloc(&p->d_state, 8 * sizeof(uint32_t)) != cudaSuccess)
     return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: state");
   if (cudaMemset(p->d_state, 0, 8 * sizeof(uint32_t)) != cudaSuccess)
@@ -655,6 +663,26 @@ int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t deb
  * has one, then the main kernel.  All launches go to `s`, in this order. */
 static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaStream_t s) {
   void *args[] = {&prm};
+  if (prog->cls_kernel) {
+    /* split form: classify every tile (it also zeroes the words of the outputs no part will
+     * write on that tile), scan the pre-pass carries, then run the parts */
+    const int warps_per_block = prog->desc.block / 32;
+    const int64_t need = (prm.n_tiles + warps_per_block - 1) / warps_per_block;
+    const int cls_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
+    BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
+                             dim3(prog->desc.block), args, 0, s));
+    if (prog->desc.n_pre > 0) {
+      bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.records, prm.n_tiles,
+                                                              prm.tile_prefix, prm.n_inputs,
+                                                              prm.state);
+      BG_CUDA(cudaGetLastError());
+    }
+    const int main_grid = (int)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm);
+    BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(main_grid), dim3(prog->desc.block),
+                             args, 0, s));
+    return BG_OK;
+  }
   if (prog->pre_kernel) {
     const int warps_per_block = prog->desc.block / 32;
     const int64_t need = (prm.n_tiles + warps_per_block - 1) / warps_per_block;
@@ -700,6 +728,7 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   prm.debug_wait_tile = plan->debug_wait_tile;
   prm.positions = plan->positions;
   prm.pos_capacity = plan->pos_capacity;
+  prm.runs = plan->d_runs;
   if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
   prm.n_inputs = (int32_t)n;
   prm.input_kind = L.input_kind;
@@ -735,6 +764,7 @@ int bg_plan_destroy(bg_plan *plan) {
   if (plan->d_tables) cudaFree(plan->d_tables);
   if (plan->d_records) cudaFree(plan->d_records);
   if (plan->d_state) cudaFree(plan->d_state);
+  if (plan->d_runs) cudaFree(plan->d_runs);
   if (plan->h_stage) cudaFreeHost(plan->h_stage);
   delete plan;
   return BG_OK;
@@ -755,7 +785,8 @@ int bg_plan_destroy(bg_plan *plan) {
  *   [0, 4)    state: the eight 32-bit slots of a plan's state (tile counter, status, epoch,
  *             a record no kernel writes, match positions written);
  *   [4, 9)    tables of the one input: in_off, in_len, tile_prefix[0..1], out_off;
- *   [32, end) look-back records, [n_adds][n_tiles].
+ *   [32, end) look-back records, [n_adds][n_tiles], then (split form) the run masks,
+ *             [n_run][n_tiles] 32-bit words.
  * The array starts zeroed when the module loads.  Every call then clears the counters and
  * the status, and bumps the epoch.  Records left by an earlier call carry an older epoch, so
  * the look-back reads them as not yet published and they need no clearing.  Calls share the
@@ -833,16 +864,19 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
       (int64_t)(32 - prog->desc.halo_lanes - prog->desc.tail_lanes) * prog->desc.wpt;
   const int64_t tiles = std::max<int64_t>(1, (W + tile_words - 1) / tile_words);
   const int64_t adds = std::max(1, prog->desc.n_adds);
-  if (tiles > (int64_t)BG_NOALLOC_RECORDS / adds) {
-    char msg[320];
+  /* 64-bit scratch words per tile: one look-back record per addition, then the run masks */
+  const int64_t per_tile = adds + (prog->desc.n_run + 1) / 2;
+  if (tiles > (int64_t)BG_NOALLOC_RECORDS / per_tile) {
+    char msg[360];
     snprintf(msg, sizeof msg,
-             "bg_scan_noalloc: %lld bytes span %lld tiles of %lld words and need %lld look-back "
-             "records (%lld additions); the fixed %u-byte scratch holds %u records, so at most "
-             "%lld tiles (%lld bytes) for this program",
+             "bg_scan_noalloc: %lld bytes span %lld tiles of %lld words and need %lld scratch "
+             "words (%lld per tile: %lld additions, %d run-mask words); the fixed %u-byte scratch "
+             "holds %u, so at most %lld tiles (%lld bytes) for this program",
              (long long)n_bytes, (long long)tiles, (long long)tile_words,
-             (long long)(tiles * adds), (long long)adds, (unsigned)BG_NOALLOC_SCRATCH_BYTES,
-             (unsigned)BG_NOALLOC_RECORDS, (long long)(BG_NOALLOC_RECORDS / adds),
-             (long long)(BG_NOALLOC_RECORDS / adds) * tile_words * 32);
+             (long long)(tiles * per_tile), (long long)per_tile, (long long)adds,
+             prog->desc.n_run, (unsigned)BG_NOALLOC_SCRATCH_BYTES, (unsigned)BG_NOALLOC_RECORDS,
+             (long long)(BG_NOALLOC_RECORDS / per_tile),
+             (long long)(BG_NOALLOC_RECORDS / per_tile) * tile_words * 32);
     return fail(BG_ERR_CAPACITY, msg);
   }
   unsigned long long *scratch = nullptr;
@@ -862,6 +896,9 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   prm.counts = counts;
   prm.records = scratch + kNoallocRecordsAt;
   prm.state = reinterpret_cast<uint32_t *>(scratch);
+  prm.runs = prog->desc.n_run > 0
+                 ? reinterpret_cast<uint32_t *>(scratch + kNoallocRecordsAt + adds * tiles)
+                 : nullptr;
   prm.positions = nullptr;
   prm.pos_capacity = 0;
   prm.basis_stride = 0;

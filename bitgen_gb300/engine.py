@@ -338,7 +338,8 @@ class Program:
             src = self.spec.source.encode()
             self._desc = N.KernelDesc(src, len(src), name.encode(), self.spec.n_outputs,
                                       self.spec.n_adds, self.spec.halo_lanes, self.spec.wpt,
-                                      self.spec.block, self.spec.tail_lanes, self.spec.n_pre)
+                                      self.spec.block, self.spec.tail_lanes, self.spec.n_pre,
+                                      self.spec.n_run)
             h = C.c_void_p()
             N.check(lib.bg_program_create(C.byref(self._desc), C.byref(h)), "bg_program_create")
             self._handle = h

@@ -77,6 +77,9 @@ typedef struct bg_kernel_desc {
   int32_t tail_lanes;
   int32_t n_pre;      /* additions 0..n_pre-1 get their carries from a pre-pass: the source
                          then also defines the kernel "<name>_pre" (0 = no pre-pass)      */
+  int32_t n_run;      /* split form (> 0): the source defines "<name>_cls", which writes
+                         n_run run-mask words per tile (and the pre-pass aggregates), and
+                         "<name>" runs the parts on the tiles their masks select           */
 } bg_kernel_desc;
 
 int bg_program_create(const bg_kernel_desc *desc, bg_program **out);
@@ -158,8 +161,8 @@ int bg_plan_destroy(bg_plan *plan);
  *                holds the scan's device status bits: 0 on success, 1 if a carry look-back
  *                wait ran out of time, 2 if a look-back walked past the first tile.
  *
- * Limit: the input may span at most BG_NOALLOC_RECORDS / max(1, additions) tiles of
- * (32 - halo_lanes - tail_lanes) * wpt words each.  Larger inputs are rejected with
+ * Limit: the input may span at most BG_NOALLOC_RECORDS / (max(1, additions) + (n_run + 1) / 2)
+ * tiles of (32 - halo_lanes - tail_lanes) * wpt words each.  Larger inputs are rejected with
  * BG_ERR_CAPACITY before anything is enqueued, and bg_last_error() gives the sizes.
  * The first call on each device looks up the array's device address once
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream

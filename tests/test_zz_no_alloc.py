@@ -98,7 +98,7 @@ def test_two_calls_in_a_row_match_the_plan_path(program, cuda):
 def test_limit_is_exact_and_enforced(program, cuda):
     prog, ps = program
     tile_words = prog.spec.tile_words
-    max_tiles = RECORDS // max(1, prog.spec.n_adds)
+    max_tiles = RECORDS // (max(1, prog.spec.n_adds) + (prog.spec.n_run + 1) // 2)
     n_max = max_tiles * tile_words * 32
     data = torch.from_numpy(_text(n_max + 32, ps, 40)).to(cuda)
     out = torch.empty((prog.n_outputs, n_max // 32 + 1), dtype=torch.int32, device=cuda)
