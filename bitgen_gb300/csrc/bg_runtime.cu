@@ -78,9 +78,36 @@ __global__ void bg_prologue_kernel(uint32_t *state) {
 /* Carry scan of the pre-pass additions.  Block k handles addition k: its records hold every
  * tile's (generate, propagate) aggregate, computed with a zero carry entering the tile; they
  * are replaced by inclusive carry-outs, the carry restarting at zero at each input's first
- * tile.  Each of the 1024 threads owns a contiguous run of tiles: it folds its run, the folds
- * are scanned across the block, and a second walk over the run writes the records.
- * (G, P) pairs compose as (G1, P1) then (G2, P2) = (G2 | (P2 & G1), P1 & P2). */
+ * tile.  The tiles are taken as rows of 32, one coalesced load per row: bit l of the masks
+ * A = generate | propagate and B = generate belongs to tile l of the row, and A + B + carry-in
+ * yields the carry entering every tile of the row at once (the carry that enters lane l is bit
+ * l of (A + B + c) ^ A ^ B, the one that leaves the row is bit 32).  The last tile of each
+ * input gets A = B = 0: its carry-out is read only by the next input's first tile, which must
+ * see zero.  Each of the 32 warps folds a contiguous block of rows into a (generate, propagate)
+ * pair, the pairs are scanned across the warps, and a second walk writes the records. */
+__device__ __forceinline__ void carry_row(const unsigned long long *rec, int64_t n_tiles,
+                                         const int64_t *tile_prefix, int n_inputs, int64_t row,
+                                         unsigned long long epoch, uint32_t &A, uint32_t &B,
+                                         bool &bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t g = row * 32 + lane;
+  uint32_t G = 0u, P = 0u;
+  if (g < n_tiles) {
+    const unsigned long long r = rec[g];
+    if ((r >> 4) != epoch || ((r >> 2) & 3ull) != 1ull) bad = true;
+    G = (uint32_t)r & 1u;
+    P = (uint32_t)(r >> 1) & 1u;
+    int a = 0, b = n_inputs; /* input containing g: prefix[a] <= g < prefix[a+1] */
+    while (b - a > 1) {
+      const int m = (a + b) >> 1;
+      if (tile_prefix[m] <= g) a = m; else b = m;
+    }
+    if (g + 1 == tile_prefix[a + 1]) G = P = 0u; /* last tile of its input */
+  }
+  A = __ballot_sync(0xffffffffu, (G | P) != 0u);
+  B = __ballot_sync(0xffffffffu, G != 0u);
+}
+
 __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long *records,
                                                              int64_t n_tiles,
                                                              const int64_t *tile_prefix,
@@ -88,52 +115,29 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long 
   __shared__ uint32_t wg[32], wp[32];
   unsigned long long *rec = records + (long long)blockIdx.x * n_tiles;
   const unsigned long long epoch = *reinterpret_cast<volatile unsigned long long *>(state + 2);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t per = (n_tiles + blockDim.x - 1) / blockDim.x;
-  const int64_t lo = (int64_t)tid * per < n_tiles ? (int64_t)tid * per : n_tiles;
-  const int64_t hi = lo + per < n_tiles ? lo + per : n_tiles;
-  int in0 = 0;
-  {
-    int a = 0, b = n_inputs; /* input containing tile lo: prefix[a] <= lo < prefix[a+1] */
-    while (b - a > 1) {
-      const int m = (a + b) >> 1;
-      if (tile_prefix[m] <= lo) a = m; else b = m;
-    }
-    in0 = a;
-  }
-  uint32_t G = 0u, P = 1u;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int64_t rows = (n_tiles + 31) / 32;
+  const int64_t per = (rows + nwarps - 1) / nwarps;
+  const int64_t r0 = (int64_t)warp * per < rows ? (int64_t)warp * per : rows;
+  const int64_t r1 = r0 + per < rows ? r0 + per : rows;
   bool bad = false;
-  int in = in0;
-  for (int64_t g = lo; g < hi; ++g) {
-    while (in + 1 < n_inputs && g >= tile_prefix[in + 1]) ++in;
-    const unsigned long long r = rec[g];
-    if ((r >> 4) != epoch || ((r >> 2) & 3ull) != 1ull) bad = true;
-    const uint32_t Gg = (uint32_t)r & 1u, Pg = (uint32_t)(r >> 1) & 1u;
-    if (g == tile_prefix[in]) {
-      G = Gg;
-      P = 0u;
-    } else {
-      G = Gg | (Pg & G);
-      P &= Pg;
-    }
+  /* fold this warp's rows: carry out of the block for carry-in 0 and for carry-in 1 */
+  uint32_t c0 = 0u, c1 = 1u;
+  for (int64_t r = r0; r < r1; ++r) {
+    uint32_t A, B;
+    carry_row(rec, n_tiles, tile_prefix, n_inputs, r, epoch, A, B, bad);
+    c0 = (uint32_t)((((unsigned long long)A + B + c0) >> 32) & 1ull);
+    c1 = (uint32_t)((((unsigned long long)A + B + c1) >> 32) & 1ull);
   }
-  /* inclusive scan of the folds within the warp, then across warps */
-  uint32_t iG = G, iP = P;
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t uG = __shfl_up_sync(0xffffffffu, iG, d), uP = __shfl_up_sync(0xffffffffu, iP, d);
-    if (lane >= d) {
-      iG = iG | (iP & uG);
-      iP &= uP;
-    }
-  }
-  if (lane == 31) {
-    wg[warp] = iG;
-    wp[warp] = iP;
+  uint32_t G = c0, P = c1 & ~c0 & 1u; /* carry-out = G | (P & carry-in) */
+  if (lane == 0) {
+    wg[warp] = G;
+    wp[warp] = P;
   }
   __syncthreads();
   if (warp == 0) {
-    uint32_t a = lane < (int)(blockDim.x >> 5) ? wg[lane] : 0u;
-    uint32_t b = lane < (int)(blockDim.x >> 5) ? wp[lane] : 1u;
+    uint32_t a = lane < nwarps ? wg[lane] : 0u;
+    uint32_t b = lane < nwarps ? wp[lane] : 1u;
     for (int d = 1; d < 32; d <<= 1) {
       const uint32_t uG = __shfl_up_sync(0xffffffffu, a, d), uP = __shfl_up_sync(0xffffffffu, b, d);
       if (lane >= d) {
@@ -141,26 +145,21 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long 
         b &= uP;
       }
     }
-    wg[lane] = a;
+    wg[lane] = a; /* inclusive: carry out of warps 0..lane for carry-in 0 */
     wp[lane] = b;
   }
   __syncthreads();
-  /* exclusive prefix of this thread = (warps before) then (lanes before in this warp) */
-  uint32_t eG = __shfl_up_sync(0xffffffffu, iG, 1), eP = __shfl_up_sync(0xffffffffu, iP, 1);
-  if (lane == 0) {
-    eG = 0u;
-    eP = 1u;
-  }
-  uint32_t c = eG;
-  if (warp > 0) c = eG | (eP & wg[warp - 1]);
-  in = in0;
-  for (int64_t g = lo; g < hi; ++g) {
-    while (in + 1 < n_inputs && g >= tile_prefix[in + 1]) ++in;
-    const unsigned long long r = rec[g];
-    const uint32_t Gg = (uint32_t)r & 1u, Pg = (uint32_t)(r >> 1) & 1u;
-    const uint32_t cin = g == tile_prefix[in] ? 0u : c;
-    c = Gg | (Pg & cin);
-    rec[g] = (epoch << 4) | (2ull << 2) | (unsigned long long)c;
+  uint32_t c = warp > 0 ? wg[warp - 1] : 0u;
+  for (int64_t r = r0; r < r1; ++r) {
+    uint32_t A, B;
+    carry_row(rec, n_tiles, tile_prefix, n_inputs, r, epoch, A, B, bad);
+    const unsigned long long sum = (unsigned long long)A + B + c;
+    /* carry leaving tile l = carry entering tile l+1; tile 31's is the row's carry-out */
+    const uint32_t into = (uint32_t)sum ^ A ^ B;
+    const uint32_t cout = (lane < 31) ? ((into >> (lane + 1)) & 1u) : (uint32_t)((sum >> 32) & 1ull);
+    const int64_t g = r * 32 + lane;
+    if (g < n_tiles) rec[g] = (epoch << 4) | (2ull << 2) | (unsigned long long)cout;
+    c = (uint32_t)((sum >> 32) & 1ull);
   }
   if (bad) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
 }
