@@ -325,11 +325,13 @@ class Tuning:
     lookback_spin: int = 0   # look-back polls before sleeping
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
     prefilter: bool = True   # run a term only in tiles holding one of its trigrams
+    merge_outputs: bool = False  # split form: parts of part_cap terms, outputs merged by atomicOr
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
-                self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter)
+                self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
+                self.merge_outputs)
 
 
 @dataclass
@@ -1227,7 +1229,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     sl = 32 - gen.hl - gen.tl
     # look-back obligations -----------------------------------------------------------------
     pm_classes: Dict[int, str] = {}
-    needs: List[List[str]] = [[] for _ in range(nt)]
+    need_masks: Dict[Tuple[int, int], int] = {}   # (class, carry lane) -> terms to run
+    needs: List[bool] = [False] * nt
     for r, (v, _) in enumerate(terms):
         if (always >> r) & 1:
             continue
@@ -1239,41 +1242,55 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             if not d.is_cc(c):
                 always |= 1 << r
                 break
-            pm = pm_classes.setdefault(c, f"pm{c}")
-            dl = gen.dl[a]
-            needs[r].append(f"(({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u")
+            pm_classes.setdefault(c, f"pm{c}")
+            key = (c, gen.dl[a])
+            need_masks[key] = need_masks.get(key, 0) | (1 << r)
+            needs[r] = True
     # parts of whole outputs ----------------------------------------------------------------
     by_out: Dict[int, List[int]] = {}
     for r, (v, o) in enumerate(terms):
         by_out.setdefault(o, []).append(r)
     cap = max(1, tuning.part_cap)
+    merge = tuning.merge_outputs
+    part_terms: List[List[int]] = []     # terms of each part, in output order
+    if merge:
+        order = [r for o in range(len(names)) for r in by_out.get(o, [])]
+        part_terms = [order[i:i + cap] for i in range(0, len(order), cap)]
+    else:                                # whole outputs per part
+        cur: List[int] = []
+        n_outs = 0
+        for o in range(len(names)):
+            rs = by_out.get(o, [])
+            if cur and (len(cur) + len(rs) > cap or n_outs >= 32):
+                part_terms.append(cur)
+                cur, n_outs = [], 0
+            cur = cur + rs
+            n_outs += 1
+        if cur:
+            part_terms.append(cur)
     parts: List[List[int]] = []          # outputs of each part
-    cur: List[int] = []
-    cur_terms = 0
-    for o in range(len(names)):
-        k = len(by_out.get(o, []))
-        if cur and (cur_terms + k > cap or len(cur) >= 32):
-            parts.append(cur)
-            cur, cur_terms = [], 0
-        cur.append(o)
-        cur_terms += k
-    if cur:
-        parts.append(cur)
+    for rs in part_terms:
+        outs_k: List[int] = []
+        for r in rs:
+            if terms[r][1] not in outs_k:
+                outs_k.append(terms[r][1])
+        parts.append(outs_k)
     nacc = max(1, max(len(ps) for ps in parts))
     sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
     funcs = []
     part_masks: List[Dict[int, int]] = []
-    for ci, outs_k in enumerate(parts):
+    for ci, (rs, outs_k) in enumerate(zip(part_terms, parts)):
         blocks = []
         masks: Dict[int, int] = {}
-        for li, o in enumerate(outs_k):
-            for r in by_out.get(o, []):
-                masks[r >> 5] = masks.get(r >> 5, 0) | (1 << (r & 31))
-                code = gen.part([(terms[r][0], li)])
-                body = "\n".join("  " + ln for ln in code.split("\n"))
-                blocks.append(f"  if ((t.run[{r >> 5}] >> {r & 31}) & 1u) {{\n{body}\n  }}")
+        for r in rs:
+            li = outs_k.index(terms[r][1])
+            masks[r >> 5] = masks.get(r >> 5, 0) | (1 << (r & 31))
+            code = gen.part([(terms[r][0], li)])
+            body = "\n".join("  " + ln for ln in code.split("\n"))
+            blocks.append(f"  if ((t.run[{r >> 5}] >> {r & 31}) & 1u) {{\n{body}\n  }}")
         part_masks.append(masks)
-        stores = "\n".join(f"  store(p, t, {o}, acc_get(acc, t, {li}));" for li, o in enumerate(outs_k))
+        fn = "merge_store" if merge else "store"
+        stores = "\n".join(f"  {fn}(p, t, {o}, acc_get(acc, t, {li}));" for li, o in enumerate(outs_k))
         funcs.append(f"//@@BG_PART\n"
                      f'extern "C" __device__ __noinline__ void bg_part_{ci}({sig}) {{\n'
                      f"  constexpr bool E = true;\n"
@@ -1284,7 +1301,10 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     for ci, masks in enumerate(part_masks):
         cond = " | ".join(f"(p.runs[{w}LL * p.n_tiles + g] & 0x{m:08x}u)" for w, m in sorted(masks.items())) or "0u"
         wants.append(f"          case {ci}: want = ({cond}) != 0u; break;")
-    calls = "\n".join(f"        case {ci}: bg_part_{ci}(p, t, acc, {ba}); break;" for ci in range(len(parts)))
+    calls = "\n".join(
+        f"        case {ci}: "
+        + " ".join(f"t.run[{w}] = __ldg(p.runs + {w}LL * p.n_tiles + g0 + l);" for w in sorted(part_masks[ci]))
+        + f" bg_part_{ci}(p, t, acc, {ba}); break;" for ci in range(len(parts)))
     # classify kernel ------------------------------------------------------------------------
     gen.lines = []
     gen.indent = 4
@@ -1293,28 +1313,45 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         m = (always >> (32 * w)) & 0xFFFFFFFF
         if m:
             gen.emit(f"t.run[{w}] |= 0x{m:08x}u;")
+    # pre-pass aggregates: with a zero marker (no trigram of it in the tile) the aggregate
+    # depends on the class alone
+    pre_classes: Dict[int, str] = {}
     for v, k in sorted(gen.pre.items(), key=lambda x: x[1]):
         n = d.nodes[v]
         bit = nt + k
         mode = 0 if n.op == "matchstar" else 1
-        gen.emit(f"S m{k} = zero();")
+        c = gen.mat(n.args[1])
+        if n.args[1] not in pre_classes:
+            pre_classes[n.args[1]] = f"po{n.args[1]}"
+            gen.emit(f"const uint32_t po{n.args[1]} = ones_lanes(t, {gen.pack(c)});")
         gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
         m = gen.mat(n.args[0])
-        gen.emit(f"m{k} = {gen.pack(m)};")
+        gen.emit(f"pre_publish<{gen.dl[v]}, E>(p, t, {k}, {mode}, {gen.pack(m)}, {gen.pack(c)});")
+        gen.indent -= 2
+        gen.emit("} else {")
+        gen.indent += 2
+        gen.emit(f"pre_publish_zero<{gen.dl[v]}>(p, t, {k}, po{n.args[1]});")
         gen.close()
-        c = gen.mat(n.args[1])
-        gen.emit(f"pre_publish<{gen.dl[v]}, E>(p, t, {k}, {mode}, m{k}, {gen.pack(c)});")
     for c, pm in sorted(pm_classes.items()):
         ref = gen.mat(c)
         gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
-    for r, conds in enumerate(needs):
-        if conds and not (always >> r) & 1:
-            gen.emit(f"if ({' | '.join(conds)}) t.run[{r >> 5}] |= 0x{1 << (r & 31):08x}u;")
+    for (c, dl), mask in sorted(need_masks.items()):
+        mask &= ~always
+        if not mask:
+            continue
+        pm = pm_classes[c]
+        ors = " ".join(f"t.run[{w}] |= 0x{(mask >> (32 * w)) & 0xFFFFFFFF:08x}u;"
+                       for w in range(nw) if (mask >> (32 * w)) & 0xFFFFFFFF)
+        gen.emit(f"if ((({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u) {{ {ors} }}")
     for w in range(nw):
         gen.emit(f"if (t.lane == 0) p.runs[{w}LL * p.n_tiles + g] = t.run[{w}];")
-    for ci, outs_k in enumerate(parts):
-        cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
-        gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
+    if merge:                            # parts OR into the outputs: start every word at zero
+        for o in range(len(names)):
+            gen.emit(f"zero_store(p, t, {o});")
+    else:
+        for ci, outs_k in enumerate(parts):
+            cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
+            gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
     cls_code = "\n".join(gen.lines)
     log2, keys, masks_tab = filt.exact()
     bloom = filt.bloom()
@@ -1389,7 +1426,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"      const int l = __ffs(sel) - 1;\n"
         f"      sel &= sel - 1u;\n"
         f"      setup_tile(p, t, (unsigned int)(g0 + l), true, false);\n"
-        + "".join(f"      t.run[{w}] = __ldg(p.runs + {w}LL * p.n_tiles + g0 + l);\n" for w in range(nw)) +
+        +
         f"      S b[8];\n"
         f"      load_basis(p, t, b);\n"
         f"      switch (k) {{\n{calls}\n        default: break;\n      }}\n"

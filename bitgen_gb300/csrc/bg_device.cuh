@@ -540,6 +540,19 @@ __device__ __forceinline__ void pre_publish(const BgParams &p, const Tile &t, in
         (t.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1) | ((c0 >> OUTL) & 1u);
 }
 
+/* pre_publish for a tile where the marker is known to be zero: nothing is generated, and the
+ * tile propagates a carry exactly when the class is all ones over its own lanes.  `ones` is
+ * ones_lanes() of the class. */
+template <int DL>
+__device__ __forceinline__ void pre_publish_zero(const BgParams &p, const Tile &t, int k,
+                                                 uint32_t ones) {
+  const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
+  const uint32_t Pagg = ((ones >> DL) & span) == span ? 1u : 0u;
+  if (t.lane == 0)
+    p.records[(long long)k * p.n_tiles + t.gtile] =
+        (t.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1);
+}
+
 /* Main pass for a pre-pass addition: the carry entering lane DL is known (t.pcin), so the
  * addition resolves without publishing or waiting.  Its result is formed by add_end. */
 template <int DL, bool E = true>
@@ -685,25 +698,13 @@ __device__ __forceinline__ void load_basis(const BgParams &p, const Tile &t, S b
   }
 }
 
-/* Write output stream o for this tile (lanes >= HL, words inside the input; characters at or
- * beyond n are cleared) and add its popcount to counts[o][input]. */
-static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, const S v) {
+/* Count (and list as sparse positions) the bits of `vals`, this lane's exact words of output o
+ * for this tile (bits at or beyond the input end already cleared). */
+static __device__ __forceinline__ void store_new_bits(const BgParams &p, const Tile &t, int o,
+                                                      const S &vals) {
   uint32_t cnt = 0;
-  uint32_t *dst = p.out ? p.out + (long long)o * p.out_stride + p.out_off[t.input] : nullptr;
-  uint32_t vals[WPT];
 #pragma unroll
-  for (int j = 0; j < WPT; ++j) {
-    const long long w = t.base + t.lane * WPT + j;
-    vals[j] = 0u;
-    if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) {
-      uint32_t val = v.w[j];
-      const long long rem = t.n - 32 * w;
-      if (rem < 32) val &= FULL << (32 - rem);
-      if (dst) dst[w] = val;
-      cnt += __popc(val);
-      vals[j] = val;
-    }
-  }
+  for (int j = 0; j < WPT; ++j) cnt += __popc(vals.w[j]);
   if (p.positions && __any_sync(FULL, cnt != 0u)) {
     /* sparse output: one slot range per warp, then each lane writes its own positions */
     uint32_t incl = cnt;
@@ -721,7 +722,7 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
         ((unsigned long long)o << 52) | ((unsigned long long)t.input << 32);
 #pragma unroll
     for (int j = 0; j < WPT; ++j) {
-      uint32_t val = vals[j];
+      uint32_t val = vals.w[j];
       const long long w = t.base + t.lane * WPT + j;
       while (val) {
         const int b = 31 - __clz(val); /* highest set bit = lowest position */
@@ -740,6 +741,26 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
     if (t.lane == 0 && cnt)
       atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, (unsigned long long)cnt);
   }
+}
+
+/* Write output stream o for this tile (lanes >= HL, words inside the input; characters at or
+ * beyond n are cleared) and add its popcount to counts[o][input]. */
+static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int o, const S v) {
+  uint32_t *dst = p.out ? p.out + (long long)o * p.out_stride + p.out_off[t.input] : nullptr;
+  S vals;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    vals.w[j] = 0u;
+    if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) {
+      uint32_t val = v.w[j];
+      const long long rem = t.n - 32 * w;
+      if (rem < 32) val &= FULL << (32 - rem);
+      if (dst) dst[w] = val;
+      vals.w[j] = val;
+    }
+  }
+  store_new_bits(p, t, o, vals);
 }
 
 #if BG_PREFILTER
@@ -855,6 +876,31 @@ __device__ __forceinline__ void zero_store(const BgParams &p, const Tile &t, int
     const long long w = t.base + t.lane * WPT + j;
     if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) dst[w] = 0u;
   }
+}
+
+/* Split form with outputs shared by several parts: OR this part's value of output o into the
+ * tile's words (which the classify pass zeroed) and count, and list as positions, only the
+ * bits it newly sets, so that counts stay exact whichever parts set a bit first.  Needs the
+ * output streams (p.out). */
+static __device__ __noinline__ void merge_store(const BgParams &p, const Tile &t, int o, const S v) {
+  uint32_t x = 0u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) x |= v.w[j];
+  if (!__any_sync(FULL, x != 0u)) return;
+  uint32_t *dst = p.out + (long long)o * p.out_stride + p.out_off[t.input];
+  S nb;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    nb.w[j] = 0u;
+    if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) {
+      uint32_t val = v.w[j];
+      const long long rem = t.n - 32 * w;
+      if (rem < 32) val &= FULL << (32 - rem);
+      if (val) nb.w[j] = val & ~atomicOr(dst + w, val);
+    }
+  }
+  store_new_bits(p, t, o, nb);
 }
 
 /* Split form: a part's accumulators hold only its own outputs (local index). */

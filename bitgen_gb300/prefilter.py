@@ -5,7 +5,7 @@ A *trigram node* is a node z whose set bits constrain the bytes at and just befo
 is set at position p, then bytes p-2, p-1 and p lie in sets S0, S1 and S2 (position bounds,
 derived through AND, OR and Advance; see ``position_bounds``).  So when no trigram of
 S0 x S1 x S2 occurs among the bytes a warp computes, z is zero in all of the warp's exact
-lanes.
+lanes.  A node that bounds only its last two bytes is a bigram node: S0 is then every byte.
 
 Zero implication.  Z(v) is the set of trigram nodes whose being zero makes v zero: AND and
 Advance / Lookahead inherit the union of their operands' sets, OR / XOR / SEL the intersection,
@@ -88,8 +88,9 @@ def trigram_nodes(gen, PB: Dict[int, Tuple[int, ...]]) -> Dict[int, Tuple[int, i
         if d.is_cc(z):
             continue
         s2, s1, s0 = PB[z][0], PB[z][1], PB[z][2]
-        if ALL in (s0, s1, s2):
+        if ALL in (s1, s2):
             continue
+        # a bigram node (only its last two bytes bounded) is the trigram set ALL x S1 x S2
         size = bin(s0).count("1") * bin(s1).count("1") * bin(s2).count("1")
         if 0 < size <= MAX_SET:
             out[z] = (s0, s1, s2)
@@ -123,6 +124,13 @@ def zero_sets(gen, tri: Dict[int, Tuple[int, int, int]],
             z = z | {v}
         Z[v] = z
     return Z
+
+
+def _set_size(sets: Tuple[int, int, int]) -> int:
+    n = 1
+    for x in sets:
+        n *= bin(x).count("1")
+    return n
 
 
 def trigram_set(sets: Tuple[int, int, int]) -> List[int]:
@@ -201,7 +209,7 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 1
     d = gen.d
 
     def best(zs) -> Optional[int]:
-        cands = sorted(zs, key=lambda z: (len(trigram_set(tri[z])), z))
+        cands = sorted(zs, key=lambda z: (_set_size(tri[z]), z))
         return cands[0] if cands else None
 
     term_node, term_cond = [], []
