@@ -15,6 +15,7 @@ from .build import LIB
 
 BG_OK, BG_ERR_INVALID, BG_ERR_CUDA, BG_ERR_COMPILE, BG_ERR_TIMEOUT, BG_ERR_ALIGN, BG_ERR_NOMEM, BG_ERR_DEVICE, BG_ERR_CAPACITY = range(9)
 BG_INPUT_BYTES, BG_INPUT_BASIS = 0, 1
+BG_PROGRAM_MERGES = 1
 
 _lock = threading.Lock()
 _lib = None
@@ -33,7 +34,7 @@ class KernelDesc(C.Structure):
     _fields_ = [("source", C.c_char_p), ("source_len", C.c_size_t), ("name", C.c_char_p),
                 ("n_outputs", C.c_int32), ("n_adds", C.c_int32), ("halo_lanes", C.c_int32),
                 ("wpt", C.c_int32), ("block", C.c_int32), ("tail_lanes", C.c_int32),
-                ("n_pre", C.c_int32), ("n_run", C.c_int32)]
+                ("n_pre", C.c_int32), ("n_run", C.c_int32), ("flags", C.c_int32)]
 
 
 class Layout(C.Structure):

@@ -325,13 +325,14 @@ class Tuning:
     lookback_spin: int = 0   # look-back polls before sleeping
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
     prefilter: bool = True   # run a term only in tiles holding one of its trigrams
-    merge_outputs: bool = False  # split form: parts of part_cap terms, outputs merged by atomicOr
+    merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
+    chunk_rows: int = 1      # split form: rows of 32 tiles per execute work item
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
-                self.merge_outputs)
+                self.merge_outputs, self.chunk_rows)
 
 
 @dataclass
@@ -349,6 +350,7 @@ class KernelSpec:
     tail_lanes: int = 0
     n_pre: int = 0          # additions 0..n_pre-1 take their carries from the pre-pass kernel
     n_run: int = 0          # split form: run-mask words per tile (0 = single-kernel form)
+    merges: bool = False    # parts OR into shared outputs: launches need the output streams
 
     @property
     def tile_words(self):
@@ -1252,6 +1254,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         by_out.setdefault(o, []).append(r)
     cap = max(1, tuning.part_cap)
     merge = tuning.merge_outputs
+    rows = max(1, tuning.chunk_rows)
     part_terms: List[List[int]] = []     # terms of each part, in output order
     if merge:
         order = [r for o in range(len(names)) for r in by_out.get(o, [])]
@@ -1405,7 +1408,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * ({nacc} * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        f"  const long long chunks = (p.n_tiles + 31) >> 5;\n"
+        f"  const long long chunks = (((p.n_tiles + 31) >> 5) + {rows} - 1) / {rows};\n"
         f"  const long long items = chunks * {len(parts)};\n"
         f"  for (;;) {{\n"
         f"    unsigned int it = 0u;\n"
@@ -1413,7 +1416,10 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"    it = __shfl_sync(FULL, it, 0);\n"
         f"    if ((long long)it >= items) break;\n"
         f"    const int k = (int)((long long)it / chunks);\n"
-        f"    const long long g0 = ((long long)it - (long long)k * chunks) * 32;\n"
+        f"    const long long c = (long long)it - (long long)k * chunks;\n"
+        f"    for (int rr = 0; rr < {rows}; ++rr) {{\n"
+        f"    const long long g0 = (c * {rows} + rr) * 32;\n"
+        f"    if (g0 >= p.n_tiles) break;\n"
         f"    const long long g = g0 + t.lane;\n"
         f"    bool want = false;\n"
         f"    if (g < p.n_tiles) {{\n"
@@ -1431,9 +1437,10 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"      load_basis(p, t, b);\n"
         f"      switch (k) {{\n{calls}\n        default: break;\n      }}\n"
         f"    }}\n"
+        f"    }}\n"
         f"  }}\n"
         f"}}\n")
     return KernelSpec(source=src, name=name, n_outputs=len(names), n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
                       n_nodes=len(d.nodes), output_names=names, tail_lanes=gen.tl,
-                      n_pre=len(gen.pre), n_run=nw)
+                      n_pre=len(gen.pre), n_run=nw, merges=merge)

@@ -85,27 +85,36 @@ __global__ void bg_prologue_kernel(uint32_t *state) {
  * input gets A = B = 0: its carry-out is read only by the next input's first tile, which must
  * see zero.  Each of the 32 warps folds a contiguous block of rows into a (generate, propagate)
  * pair, the pairs are scanned across the warps, and a second walk writes the records. */
-__device__ __forceinline__ void carry_row(const unsigned long long *rec, int64_t n_tiles,
-                                         const int64_t *tile_prefix, int n_inputs, int64_t row,
-                                         unsigned long long epoch, uint32_t &A, uint32_t &B,
-                                         bool &bad) {
+/* Rows of the carry scan are read eight at a time (independent loads in flight); the input
+ * containing each lane's tile is followed with a cursor, since a warp visits rows in order. */
+constexpr int kScanBatch = 8;
+
+__device__ __forceinline__ void carry_rows(const unsigned long long *rec, int64_t n_tiles,
+                                          const int64_t *tile_prefix, int n_inputs, int64_t row,
+                                          int nrows, unsigned long long epoch, int &in,
+                                          uint32_t A[kScanBatch], uint32_t B[kScanBatch],
+                                          bool &bad) {
   const int lane = threadIdx.x & 31;
-  const int64_t g = row * 32 + lane;
-  uint32_t G = 0u, P = 0u;
-  if (g < n_tiles) {
-    const unsigned long long r = rec[g];
-    if ((r >> 4) != epoch || ((r >> 2) & 3ull) != 1ull) bad = true;
-    G = (uint32_t)r & 1u;
-    P = (uint32_t)(r >> 1) & 1u;
-    int a = 0, b = n_inputs; /* input containing g: prefix[a] <= g < prefix[a+1] */
-    while (b - a > 1) {
-      const int m = (a + b) >> 1;
-      if (tile_prefix[m] <= g) a = m; else b = m;
-    }
-    if (g + 1 == tile_prefix[a + 1]) G = P = 0u; /* last tile of its input */
+  unsigned long long r[kScanBatch];
+#pragma unroll
+  for (int i = 0; i < kScanBatch; ++i) {
+    const int64_t g = (row + i) * 32 + lane;
+    r[i] = (i < nrows && g < n_tiles) ? rec[g] : 0ull;
   }
-  A = __ballot_sync(0xffffffffu, (G | P) != 0u);
-  B = __ballot_sync(0xffffffffu, G != 0u);
+#pragma unroll
+  for (int i = 0; i < kScanBatch; ++i) {
+    const int64_t g = (row + i) * 32 + lane;
+    uint32_t G = 0u, P = 0u;
+    if (i < nrows && g < n_tiles) {
+      if ((r[i] >> 4) != epoch || ((r[i] >> 2) & 3ull) != 1ull) bad = true;
+      G = (uint32_t)r[i] & 1u;
+      P = (uint32_t)(r[i] >> 1) & 1u;
+      while (in + 1 < n_inputs && g >= tile_prefix[in + 1]) ++in;
+      if (g + 1 == tile_prefix[in + 1]) G = P = 0u; /* last tile of its input */
+    }
+    A[i] = __ballot_sync(0xffffffffu, (G | P) != 0u);
+    B[i] = __ballot_sync(0xffffffffu, G != 0u);
+  }
 }
 
 __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long *records,
@@ -121,15 +130,32 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long 
   const int64_t r0 = (int64_t)warp * per < rows ? (int64_t)warp * per : rows;
   const int64_t r1 = r0 + per < rows ? r0 + per : rows;
   bool bad = false;
+  int in0 = 0;
+  {
+    const int64_t g = r0 * 32 + lane;
+    int a = 0, b = n_inputs; /* input containing tile g: prefix[a] <= g < prefix[a+1] */
+    while (b - a > 1) {
+      const int m = (a + b) >> 1;
+      if (tile_prefix[m] <= g) a = m; else b = m;
+    }
+    in0 = a;
+  }
   /* fold this warp's rows: carry out of the block for carry-in 0 and for carry-in 1 */
   uint32_t c0 = 0u, c1 = 1u;
-  for (int64_t r = r0; r < r1; ++r) {
-    uint32_t A, B;
-    carry_row(rec, n_tiles, tile_prefix, n_inputs, r, epoch, A, B, bad);
-    c0 = (uint32_t)((((unsigned long long)A + B + c0) >> 32) & 1ull);
-    c1 = (uint32_t)((((unsigned long long)A + B + c1) >> 32) & 1ull);
+  int in = in0;
+  for (int64_t r = r0; r < r1; r += kScanBatch) {
+    uint32_t A[kScanBatch], B[kScanBatch];
+    const int nr = (int)(r1 - r < kScanBatch ? r1 - r : kScanBatch);
+    carry_rows(rec, n_tiles, tile_prefix, n_inputs, r, nr, epoch, in, A, B, bad);
+#pragma unroll
+    for (int i = 0; i < kScanBatch; ++i) {
+      if (i < nr) {
+        c0 = (uint32_t)((((unsigned long long)A[i] + B[i] + c0) >> 32) & 1ull);
+        c1 = (uint32_t)((((unsigned long long)A[i] + B[i] + c1) >> 32) & 1ull);
+      }
+    }
   }
-  uint32_t G = c0, P = c1 & ~c0 & 1u; /* carry-out = G | (P & carry-in) */
+  const uint32_t G = c0, P = c1 & ~c0 & 1u; /* carry-out = G | (P & carry-in) */
   if (lane == 0) {
     wg[warp] = G;
     wp[warp] = P;
@@ -150,16 +176,24 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long 
   }
   __syncthreads();
   uint32_t c = warp > 0 ? wg[warp - 1] : 0u;
-  for (int64_t r = r0; r < r1; ++r) {
-    uint32_t A, B;
-    carry_row(rec, n_tiles, tile_prefix, n_inputs, r, epoch, A, B, bad);
-    const unsigned long long sum = (unsigned long long)A + B + c;
-    /* carry leaving tile l = carry entering tile l+1; tile 31's is the row's carry-out */
-    const uint32_t into = (uint32_t)sum ^ A ^ B;
-    const uint32_t cout = (lane < 31) ? ((into >> (lane + 1)) & 1u) : (uint32_t)((sum >> 32) & 1ull);
-    const int64_t g = r * 32 + lane;
-    if (g < n_tiles) rec[g] = (epoch << 4) | (2ull << 2) | (unsigned long long)cout;
-    c = (uint32_t)((sum >> 32) & 1ull);
+  in = in0;
+  for (int64_t r = r0; r < r1; r += kScanBatch) {
+    uint32_t A[kScanBatch], B[kScanBatch];
+    const int nr = (int)(r1 - r < kScanBatch ? r1 - r : kScanBatch);
+    carry_rows(rec, n_tiles, tile_prefix, n_inputs, r, nr, epoch, in, A, B, bad);
+#pragma unroll
+    for (int i = 0; i < kScanBatch; ++i) {
+      if (i < nr) {
+        const unsigned long long sum = (unsigned long long)A[i] + B[i] + c;
+        /* carry leaving tile l = carry entering tile l+1; tile 31's is the row's carry-out */
+        const uint32_t into = (uint32_t)sum ^ A[i] ^ B[i];
+        const uint32_t cout =
+            (lane < 31) ? ((into >> (lane + 1)) & 1u) : (uint32_t)((sum >> 32) & 1ull);
+        const int64_t g = (r + i) * 32 + lane;
+        if (g < n_tiles) rec[g] = (epoch << 4) | (2ull << 2) | (unsigned long long)cout;
+        c = (uint32_t)((sum >> 32) & 1ull);
+      }
+    }
   }
   if (bad) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
 }
@@ -704,6 +738,9 @@ extern "C" {
 int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
                    unsigned long long *counts, void *stream) {
   if (!plan || !input) return fail(BG_ERR_INVALID, "bg_plan_launch: null plan or input");
+  if (!out_streams && (plan->prog->desc.flags & BG_PROGRAM_MERGES))
+    return fail(BG_ERR_INVALID,
+                "bg_plan_launch: this program merges outputs across parts and needs out_streams");
   const bg_layout &L = plan->layout;
   if (L.input_kind == BG_INPUT_BYTES && !aligned16(input))
     return fail(BG_ERR_ALIGN, "bg_plan_launch: input not 16-byte aligned");
@@ -856,6 +893,9 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   if (!prog || !prog->kernel || !input || !status || n_bytes < 0)
     return fail(BG_ERR_INVALID, "bg_scan_noalloc: null program, input or status, or negative size");
   if (!aligned16(input)) return fail(BG_ERR_ALIGN, "bg_scan_noalloc: input not 16-byte aligned");
+  if (!out_streams && (prog->desc.flags & BG_PROGRAM_MERGES))
+    return fail(BG_ERR_INVALID,
+                "bg_scan_noalloc: this program merges outputs across parts and needs out_streams");
   const int64_t W = (n_bytes + 31) / 32;
   if (out_streams && out_stride < W)
     return fail(BG_ERR_INVALID, "bg_scan_noalloc: out_stride shorter than the input's words");

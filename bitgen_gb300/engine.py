@@ -248,11 +248,14 @@ class Plan:
     def __init__(self, program: "Program", inp: Optional[Inputs], out_offsets: Sequence[int] = (),
                  out_stride: int = 0, _handle=None):
         self.program = program
+        self._scratch: Optional[torch.Tensor] = None
+        self.out_stride = out_stride
         if _handle is not None:
             self._h = _handle
             self.n_inputs = 0
             return
         self.n_inputs = inp.n
+        self._ensure_scratch(inp.data.device)
         lay = N.Layout(inp.kind, inp.n, _i64(inp.offsets), _i64(inp.lengths), inp.basis_stride,
                        _i64(out_offsets), out_stride)
         h = C.c_void_p()
@@ -271,6 +274,17 @@ class Plan:
                        _i64(out_offsets), out_stride)
         N.check(N.lib().bg_plan_set_layout(self._h, C.byref(lay), stream), "bg_plan_set_layout")
         self.n_inputs = inp.n
+        self.out_stride = out_stride
+        self._ensure_scratch(inp.data.device)
+
+    def _ensure_scratch(self, device):
+        """A program that merges outputs across parts needs output streams on every launch;
+        counts-only launches write into this plan-owned buffer instead."""
+        if not self.program.merges:
+            return
+        need = self.program.n_outputs * max(1, self.out_stride)
+        if self._scratch is None or self._scratch.numel() < need:
+            self._scratch = torch.empty(need, dtype=torch.uint32, device=device)
 
     @property
     def tiles(self) -> int:
@@ -290,6 +304,8 @@ class Plan:
         N.check(N.lib().bg_plan_set_wait_limit(self._h, cycles, debug_wait_tile), "bg_plan_set_wait_limit")
 
     def launch(self, data_ptr: int, out_ptr: int, counts_ptr: int, stream: int):
+        if not out_ptr and self._scratch is not None:
+            out_ptr = self._scratch.data_ptr()
         N.check(N.lib().bg_plan_launch(self._h, data_ptr, out_ptr or None, counts_ptr or None,
                                        stream), "bg_plan_launch")
 
@@ -332,6 +348,7 @@ class Program:
                     raise
                 fuse = False
         self.fused = fuse
+        self.merges = bool(fuse and self.spec.merges)
         if fuse:
             _ensure_cache_dir()
             self.n_outputs = self.spec.n_outputs
@@ -339,7 +356,8 @@ class Program:
             self._desc = N.KernelDesc(src, len(src), name.encode(), self.spec.n_outputs,
                                       self.spec.n_adds, self.spec.halo_lanes, self.spec.wpt,
                                       self.spec.block, self.spec.tail_lanes, self.spec.n_pre,
-                                      self.spec.n_run)
+                                      self.spec.n_run,
+                                      N.BG_PROGRAM_MERGES if self.spec.merges else 0)
             h = C.c_void_p()
             N.check(lib.bg_program_create(C.byref(self._desc), C.byref(h)), "bg_program_create")
             self._handle = h

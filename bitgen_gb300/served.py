@@ -73,6 +73,8 @@ class Server:
         self.return_streams = return_streams
         self.max_out = max(p.n_outputs for p in programs.values())
         words = max_batch_bytes // 32 + max_batch_inputs * 4
+        # programs that merge outputs across parts need output streams even for counts
+        dev_streams = return_streams or any(p.merges for p in programs.values())
         self.slots: List[_Slot] = []
         for _ in range(slots):
             plans = {}
@@ -87,7 +89,7 @@ class Server:
                 host_in=torch.empty(max_batch_bytes + max_batch_inputs * ALIGN, dtype=torch.uint8).pin_memory(),
                 dev_counts=torch.empty((self.max_out, max_batch_inputs), dtype=torch.int64, device=device),
                 host_counts=torch.empty((self.max_out, max_batch_inputs), dtype=torch.int64).pin_memory(),
-                dev_out=torch.empty((self.max_out, words), dtype=torch.uint32, device=device) if return_streams else None,
+                dev_out=torch.empty((self.max_out, words), dtype=torch.uint32, device=device) if dev_streams else None,
                 host_out=torch.empty((self.max_out, words), dtype=torch.uint32).pin_memory() if return_streams else None,
                 plans=plans))
         self.in_flight_bytes = 0
@@ -116,7 +118,7 @@ class Server:
             # counts are [n_outputs][n_inputs] with row stride n for this launch
             flat = slot.dev_counts.view(-1)[:prog.n_outputs * n]
             slot.host_counts.view(-1)[:prog.n_outputs * n].copy_(flat, non_blocking=True)
-            if slot.dev_out is not None:
+            if slot.host_out is not None:
                 # streams are written with row stride `total` (this batch's words)
                 m = prog.n_outputs * total
                 slot.host_out.view(-1)[:m].copy_(slot.dev_out.view(-1)[:m], non_blocking=True)

@@ -80,7 +80,11 @@ typedef struct bg_kernel_desc {
   int32_t n_run;      /* split form (> 0): the source defines "<name>_cls", which writes
                          n_run run-mask words per tile (and the pre-pass aggregates), and
                          "<name>" runs the parts on the tiles their masks select           */
+  int32_t flags;      /* BG_PROGRAM_MERGES: parts OR into shared outputs, so every launch
+                         needs out_streams (counts are taken from the bits a part adds)   */
 } bg_kernel_desc;
+
+#define BG_PROGRAM_MERGES 1
 
 int bg_program_create(const bg_kernel_desc *desc, bg_program **out);
 /* Compile only (no device needed): returns BG_OK or BG_ERR_COMPILE, log copied into log_buf. */

@@ -61,6 +61,8 @@ def small():
                                                   (2, 1, 256, {"edge_variants": True, "part_cap": 4}),
                                                   (2, 1, 256, {"prefilter": False}),
                                                   (1, 1, 256, {"part_cap": 1}),
+                                                  (1, 1, 256, {"merge_outputs": False}),
+                                                  (1, 1, 256, {"chunk_rows": 4, "part_cap": 2}),
                                                   (2, 1, 256, {"carry_prepass": False})])
 def test_small_workload_tunings(cuda, wpt, skip, block, extra):
     ps, text, groups = small()
@@ -267,3 +269,26 @@ def test_sparse_positions_match_streams(cuda):
     with pytest.raises(N.BitgenError) as e:
         prog.scan(pack_bytes(items), positions=True, pos_capacity=3)
     assert e.value.status == N.BG_ERR_CAPACITY
+
+
+def test_counts_only_launches_of_merging_programs(cuda):
+    """A program whose parts OR into shared outputs takes its counts from the bits each part
+    adds, so a launch needs the output streams: the C ABI rejects a counts-only launch with
+    BG_ERR_INVALID, and the Python plan supplies its own streams.  Counts equal those of a
+    launch with streams and those of the oracle."""
+    import ctypes as C
+    from bitgen_gb300 import _native as N
+    ps, text, groups = small()
+    prog = Program(groups)
+    assert prog.merges
+    inp = pack_bytes([text])
+    a = prog.scan(inp, streams=False)
+    b = prog.scan(inp)
+    torch.cuda.synchronize()
+    assert torch.equal(a.counts, b.counts)
+    want = [int(np.unpackbits(w.view(np.uint8)).sum()) for w in oracle_streams(groups, text)]
+    assert a.counts[:, 0].tolist() == want
+    plan = prog.plan(inp, b.word_offsets, b.streams.shape[1])
+    rc = N.lib().bg_plan_launch(plan._h, inp.data.data_ptr(), None, b.counts.data_ptr(), None)
+    assert rc == N.BG_ERR_INVALID
+    assert b"needs out_streams" in N.lib().bg_last_error()

@@ -123,9 +123,10 @@ def test_limit_is_exact_and_enforced(program, cuda):
 def test_empty_input(program, cuda):
     prog, _ = program
     data = torch.zeros(32, dtype=torch.uint8, device=cuda)
+    out = torch.zeros((prog.n_outputs, 4), dtype=torch.int32, device=cuda)
     cnt = torch.full((prog.n_outputs,), -1, dtype=torch.int64, device=cuda)
     st = torch.full((1,), -1, dtype=torch.int32, device=cuda)
-    assert _noalloc(prog, data, 0, None, cnt, st) == N.BG_OK
+    assert _noalloc(prog, data, 0, out, cnt, st) == N.BG_OK
     torch.cuda.synchronize()
     assert int(st.item()) == 0
     assert np.all(cnt.cpu().numpy() == 0)
