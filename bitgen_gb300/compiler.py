@@ -740,7 +740,8 @@ class _Gen:
             n = self.d.nodes[v]
             m, c = self.mat(n.args[0]), self.mat(n.args[1])
             mode = 0 if n.op == "matchstar" else 1
-            self.emit(f"pre_publish<{self.dl[v]}, E>(p, t, {k}, {mode}, {self.pack(m)}, {self.pack(c)});")
+            self.emit(f"{{ uint32_t G, P; pre_aggregate<{self.dl[v]}, E>(t, {mode}, {self.pack(m)}, {self.pack(c)}, G, P); "
+                      f"pg[{k >> 5}] |= G << {k & 31}; pp[{k >> 5}] |= P << {k & 31}; }}")
         return "\n".join(self.lines)
 
     def part(self, terms: Sequence[Tuple[int, int]]) -> str:
@@ -1003,6 +1004,24 @@ def build_dag(groups: Sequence[Group], per_regex: bool = False) -> Tuple[Dag, Li
 
 
 SMEM_BUDGET = 48 * 1024
+# Passes that visit every tile once without waiting take chunks of 32 consecutive tiles per warp,
+# so that each pre-pass addition's aggregate bits of a chunk fill one word (pre_collect/flush).
+PRE_CHUNK_OPEN = (
+    "  const long long rows = (p.n_tiles + 31) >> 5;\n"
+    "  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
+    "  for (long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < rows; c += stride) {\n"
+    "   uint32_t gw[NPRE_WORDS], pw[NPRE_WORDS];\n"
+    "   for (int j = 0; j < NPRE_WORDS; ++j) gw[j] = pw[j] = 0u;\n"
+    "   for (int l = 0; l < 32; ++l) {\n"
+    "    const long long g = c * 32 + l;\n"
+    "    if (g >= p.n_tiles) break;\n"
+    "    uint32_t pg[NPRE_WORDS], pp[NPRE_WORDS];\n"
+    "    for (int j = 0; j < NPRE_WORDS; ++j) pg[j] = pp[j] = 0u;\n")
+PRE_CHUNK_CLOSE = (
+    "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
+    "   }\n"
+    "   if (NPRE > 0) pre_flush(p, c, gw, pw, t.lane);\n"
+    "  }\n")
 BLOOM_SMEM = (1 << prefilter.BLOOM_BITS) // 8
 
 
@@ -1158,15 +1177,14 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
             f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_pre(const __grid_constant__ BgParams p) {{\n'
             f"  Tile t;\n"
             f"  init(p, t);\n"
-            f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
-            f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
+            f"{PRE_CHUNK_OPEN}"
             f"    setup_tile(p, t, (unsigned int)g, false, false);\n"
             f"    S b[8];\n"
             f"    load_basis(p, t, b);\n"
             f"    const uint32_t {basis_decl};\n"
             f"    constexpr bool E = true;\n"
             f"{gen.pre_body()}\n"
-            f"  }}\n"
+            f"{PRE_CHUNK_CLOSE}"
             f"}}\n")
     src = (
         f"//@@BG_MAXREG {maxreg}\n"
@@ -1329,11 +1347,12 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             gen.emit(f"const uint32_t po{n.args[1]} = ones_lanes(t, {gen.pack(c)});")
         gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
         m = gen.mat(n.args[0])
-        gen.emit(f"pre_publish<{gen.dl[v]}, E>(p, t, {k}, {mode}, {gen.pack(m)}, {gen.pack(c)});")
+        gen.emit(f"uint32_t G, P; pre_aggregate<{gen.dl[v]}, E>(t, {mode}, {gen.pack(m)}, {gen.pack(c)}, G, P); "
+                 f"pg[{k >> 5}] |= G << {k & 31}; pp[{k >> 5}] |= P << {k & 31};")
         gen.indent -= 2
         gen.emit("} else {")
         gen.indent += 2
-        gen.emit(f"pre_publish_zero<{gen.dl[v]}>(p, t, {k}, po{n.args[1]});")
+        gen.emit(f"pp[{k >> 5}] |= pre_propagates<{gen.dl[v]}>(po{n.args[1]}) << {k & 31};")
         gen.close()
     for c, pm in sorted(pm_classes.items()):
         ref = gen.mat(c)
@@ -1371,15 +1390,14 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  __syncthreads();\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        f"  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
-        f"  for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < p.n_tiles; g += stride) {{\n"
+        f"{PRE_CHUNK_OPEN}"
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
         f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
-        f"  }}\n"
+        f"{PRE_CHUNK_CLOSE}"
         f"}}\n")
     warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))

@@ -23,9 +23,9 @@
  * Additions over a wide class (such as '.', which covers whole tiles of text without line
  * breaks) would make every tile walk the look-back: their carries chain through the entire
  * input.  The first BG_NPRE additions of a program are of that kind and depend on no other
- * addition; for them a separate pass (the generated bg_scan_pre kernel, then a scan kernel of
- * the runtime) computes every tile's carry-in before the main kernel runs, which then reads it
- * (add_known) instead of waiting.
+ * addition; for them a separate pass (the generated pre-pass or classify kernel, then the
+ * runtime's carry scan) computes every tile's carry-in before the main kernel runs, which then
+ * reads it (add_known) instead of waiting.
  */
 #pragma once
 #include "bg_params.h"
@@ -179,6 +179,9 @@ __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long lon
 __device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+
+/* Rows of 32 tiles: the unit of the pre-pass bitmaps (see load_pre_carries). */
+__device__ __forceinline__ long long pre_rows(const BgParams &p) { return (p.n_tiles + 31) >> 5; }
 
 /* record = epoch << 4 | flag << 2 | P << 1 | G ; flag 1 = aggregate, 2 = inclusive carry */
 __device__ __forceinline__ void publish(const BgParams &p, const Tile &t, int k, uint32_t flag,
@@ -522,35 +525,56 @@ __device__ __forceinline__ void add_masks(const Tile &t, int mode, const S &M, c
   Pm = __ballot_sync(FULL, P) & keep;
 }
 
-/* Pre-pass: publish this tile's (generate, propagate) aggregate of addition k over its own
- * lanes [DL, SL + DL), computed with a zero carry entering lane DL.  Written for every tile,
- * whatever the operands, so that the scan kernel finds a record everywhere. */
+/* Pre-pass: this tile's (generate, propagate) aggregate of an addition over its own lanes
+ * [DL, SL + DL), computed with a zero carry entering lane DL (warp-uniform bits). */
 template <int DL, bool E = true>
-__device__ __forceinline__ void pre_publish(const BgParams &p, const Tile &t, int k, int mode,
-                                            const S &M, const S &C) {
+__device__ __forceinline__ void pre_aggregate(const Tile &t, int mode, const S &M, const S &C,
+                                              uint32_t &G, uint32_t &P) {
   uint32_t xb[WPT], yb[WPT], Gm, Pm;
   add_masks<DL, E>(t, mode, M, C, xb, yb, Gm, Pm);
   constexpr int OUTL = SL + DL;
   const uint32_t A = Gm | Pm, B = Gm;
   const uint32_t c0 = (uint32_t)((unsigned long long)A + B) ^ A ^ B;
   const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
-  const uint32_t Pagg = (((Pm >> DL) & span) == span) ? 1u : 0u;
-  if (t.lane == 0)
-    p.records[(long long)k * p.n_tiles + t.gtile] =
-        (t.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1) | ((c0 >> OUTL) & 1u);
+  P = (((Pm >> DL) & span) == span) ? 1u : 0u;
+  G = (c0 >> OUTL) & 1u;
 }
 
-/* pre_publish for a tile where the marker is known to be zero: nothing is generated, and the
+/* pre_aggregate for a tile where the marker is known to be zero: nothing is generated, and the
  * tile propagates a carry exactly when the class is all ones over its own lanes.  `ones` is
  * ones_lanes() of the class. */
 template <int DL>
-__device__ __forceinline__ void pre_publish_zero(const BgParams &p, const Tile &t, int k,
-                                                 uint32_t ones) {
+__device__ __forceinline__ uint32_t pre_propagates(uint32_t ones) {
   const uint32_t span = (SL >= 32) ? FULL : ((1u << SL) - 1u);
-  const uint32_t Pagg = ((ones >> DL) & span) == span ? 1u : 0u;
-  if (t.lane == 0)
-    p.records[(long long)k * p.n_tiles + t.gtile] =
-        (t.epoch << 4) | (1ull << 2) | ((unsigned long long)Pagg << 1);
+  return ((ones >> DL) & span) == span ? 1u : 0u;
+}
+
+/* After tile l of a chunk of 32: move the tile's aggregate bits (bit k of pg / pp = addition k)
+ * into the chunk words that lane k keeps for addition k. */
+__device__ __forceinline__ void pre_collect(const uint32_t pg[NPRE_WORDS], const uint32_t pp[NPRE_WORDS],
+                                            uint32_t gw[NPRE_WORDS], uint32_t pw[NPRE_WORDS],
+                                            int l, int lane) {
+#pragma unroll
+  for (int j = 0; j < NPRE_WORDS; ++j) {
+    gw[j] |= ((pg[j] >> lane) & 1u) << l;
+    pw[j] |= ((pp[j] >> lane) & 1u) << l;
+  }
+}
+
+/* End of chunk c (tiles 32c .. 32c+31): store the chunk words of every pre-pass addition. */
+__device__ __forceinline__ void pre_flush(const BgParams &p, long long c,
+                                          const uint32_t gw[NPRE_WORDS],
+                                          const uint32_t pw[NPRE_WORDS], int lane) {
+  const long long R = pre_rows(p);
+#pragma unroll
+  for (int j = 0; j < NPRE_WORDS; ++j) {
+    const int k = 32 * j + lane;
+    if (k < NPRE) {
+      uint32_t *b = p.pre_bits + 3 * R * k;
+      b[c] = gw[j];
+      b[R + c] = pw[j];
+    }
+  }
 }
 
 /* Main pass for a pre-pass addition: the carry entering lane DL is known (t.pcin), so the
@@ -586,19 +610,19 @@ __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
   t.epoch = *(volatile const unsigned long long *)(p.state + 2);
 }
 
-/* Carries entering this tile for the pre-pass additions: the scan kernel left the inclusive
- * carry-out of every tile in its record, so tile g reads tile g-1's (zero for an input's first
- * tile).  Lane k loads addition k's record; a missing record is reported as a chain error. */
+/* Compact pre-pass data.  For pre-pass addition k, p.pre_bits + 3 * R * k (R = rows of 32 tiles)
+ * holds three bitmaps of R words, bit l of word r standing for tile 32r + l: the tile generates
+ * a carry [0, R), the tile propagates one [R, 2R), a carry enters the tile [2R, 3R).  The first
+ * two are written by the pass that computes the aggregates, the third by the carry scan. */
+/* Carries entering this tile for the pre-pass additions (warp-uniform bit k per addition). */
 __device__ __forceinline__ void load_pre_carries(const BgParams &p, Tile &t) {
+  const long long R = pre_rows(p);
 #pragma unroll
   for (int w = 0; w < NPRE_WORDS; ++w) {
     const int k = w * 32 + t.lane;
     uint32_t c = 0u;
-    if (NPRE > 0 && k < NPRE && t.gtile > t.first) {
-      const unsigned long long r = __ldg(p.records + (long long)k * p.n_tiles + t.gtile - 1);
-      if ((r >> 4) != t.epoch || ((r >> 2) & 3ull) != 2ull) atomicOr(p.state + 1, BG_DEV_ERR_CHAIN);
-      c = (uint32_t)r & 1u;
-    }
+    if (NPRE > 0 && k < NPRE)
+      c = (__ldg(p.pre_bits + 3 * R * k + 2 * R + (t.gtile >> 5)) >> (t.gtile & 31)) & 1u;
     t.pcin[w] = __ballot_sync(FULL, c != 0u);
   }
 }

@@ -48,6 +48,7 @@ typedef struct BgParams {
   int64_t spin_limit;        /* clock64 cycles a look-back wait may take before giving up */
   int64_t debug_wait_tile;   /* tile that first waits on the never-written record, or -1 */
   uint32_t *runs;            /* split form: [n_run][n_tiles] per-tile run masks, or NULL   */
+  uint32_t *pre_bits;        /* pre-pass bitmaps, 3 * ceil(n_tiles / 32) words per addition */
   int32_t n_inputs;
   int32_t input_kind;
 } BgParams;

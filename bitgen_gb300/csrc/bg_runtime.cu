@@ -75,90 +75,67 @@ __global__ void bg_prologue_kernel(uint32_t *state) {
   *ep = *ep + 1ull;
 }
 
-/* Carry scan of the pre-pass additions.  Block k handles addition k: its records hold every
- * tile's (generate, propagate) aggregate, computed with a zero carry entering the tile; they
- * are replaced by inclusive carry-outs, the carry restarting at zero at each input's first
- * tile.  The tiles are taken as rows of 32, one coalesced load per row: bit l of the masks
- * A = generate | propagate and B = generate belongs to tile l of the row, and A + B + carry-in
- * yields the carry entering every tile of the row at once (the carry that enters lane l is bit
- * l of (A + B + c) ^ A ^ B, the one that leaves the row is bit 32).  The last tile of each
- * input gets A = B = 0: its carry-out is read only by the next input's first tile, which must
- * see zero.  Each of the 32 warps folds a contiguous block of rows into a (generate, propagate)
- * pair, the pairs are scanned across the warps, and a second walk writes the records. */
-/* Rows of the carry scan are read eight at a time (independent loads in flight); the input
- * containing each lane's tile is followed with a cursor, since a warp visits rows in order. */
-constexpr int kScanBatch = 8;
-
-__device__ __forceinline__ void carry_rows(const unsigned long long *rec, int64_t n_tiles,
-                                          const int64_t *tile_prefix, int n_inputs, int64_t row,
-                                          int nrows, unsigned long long epoch, int &in,
-                                          uint32_t A[kScanBatch], uint32_t B[kScanBatch],
-                                          bool &bad) {
-  const int lane = threadIdx.x & 31;
-  unsigned long long r[kScanBatch];
-#pragma unroll
-  for (int i = 0; i < kScanBatch; ++i) {
-    const int64_t g = (row + i) * 32 + lane;
-    r[i] = (i < nrows && g < n_tiles) ? rec[g] : 0ull;
+/* Carry scan of the pre-pass additions.  Block k handles addition k, whose bitmaps (see
+ * bg_device.cuh, pre_rows) hold for every row of 32 tiles the tiles that generate (G) and
+ * propagate (P) a carry.  Bit l of A = G | P and B = G belong to tile l of the row, so
+ * A + B + carry-in gives the carry entering every tile of the row at once: bit l of
+ * (A + B + c) ^ A ^ B, and bit 32 of the sum leaves the row.  The last tile of each input gets
+ * A = B = 0: its carry-out only enters the next input's first tile, which must see zero.  Each
+ * thread folds a contiguous run of rows into (carry-out for carry-in 0, for carry-in 1), the
+ * folds are scanned across the block, and a second walk writes the carry-in bitmap. */
+__device__ __forceinline__ uint32_t row_kill(int64_t row, const int64_t *tile_prefix, int n_inputs,
+                                             int &in) {
+  /* inputs whose last tile lies in this row (the cursor only moves forward) */
+  uint32_t kill = 0u;
+  const int64_t lo = row * 32, hi = lo + 32;
+  while (in < n_inputs && tile_prefix[in + 1] <= hi) {
+    const int64_t last = tile_prefix[in + 1] - 1;
+    if (last >= lo) kill |= 1u << (last - lo);
+    ++in;
   }
-#pragma unroll
-  for (int i = 0; i < kScanBatch; ++i) {
-    const int64_t g = (row + i) * 32 + lane;
-    uint32_t G = 0u, P = 0u;
-    if (i < nrows && g < n_tiles) {
-      if ((r[i] >> 4) != epoch || ((r[i] >> 2) & 3ull) != 1ull) bad = true;
-      G = (uint32_t)r[i] & 1u;
-      P = (uint32_t)(r[i] >> 1) & 1u;
-      while (in + 1 < n_inputs && g >= tile_prefix[in + 1]) ++in;
-      if (g + 1 == tile_prefix[in + 1]) G = P = 0u; /* last tile of its input */
-    }
-    A[i] = __ballot_sync(0xffffffffu, (G | P) != 0u);
-    B[i] = __ballot_sync(0xffffffffu, G != 0u);
-  }
+  return kill;
 }
 
-__global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long *records,
-                                                             int64_t n_tiles,
+__global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits, int64_t n_tiles,
                                                              const int64_t *tile_prefix,
-                                                             int n_inputs, uint32_t *state) {
+                                                             int n_inputs) {
   __shared__ uint32_t wg[32], wp[32];
-  unsigned long long *rec = records + (long long)blockIdx.x * n_tiles;
-  const unsigned long long epoch = *reinterpret_cast<volatile unsigned long long *>(state + 2);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int64_t rows = (n_tiles + 31) / 32;
-  const int64_t per = (rows + nwarps - 1) / nwarps;
-  const int64_t r0 = (int64_t)warp * per < rows ? (int64_t)warp * per : rows;
-  const int64_t r1 = r0 + per < rows ? r0 + per : rows;
-  bool bad = false;
+  const int64_t R = (n_tiles + 31) / 32;
+  const uint32_t *Gw = pre_bits + 3 * R * blockIdx.x, *Pw = Gw + R;
+  uint32_t *Cw = pre_bits + 3 * R * blockIdx.x + 2 * R;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int64_t per = (R + blockDim.x - 1) / blockDim.x;
+  const int64_t r0 = (int64_t)tid * per < R ? (int64_t)tid * per : R;
+  const int64_t r1 = r0 + per < R ? r0 + per : R;
   int in0 = 0;
   {
-    const int64_t g = r0 * 32 + lane;
-    int a = 0, b = n_inputs; /* input containing tile g: prefix[a] <= g < prefix[a+1] */
+    int a = 0, b = n_inputs; /* input containing tile 32 * r0 */
     while (b - a > 1) {
       const int m = (a + b) >> 1;
-      if (tile_prefix[m] <= g) a = m; else b = m;
+      if (tile_prefix[m] <= r0 * 32) a = m; else b = m;
     }
     in0 = a;
   }
-  /* fold this warp's rows: carry out of the block for carry-in 0 and for carry-in 1 */
   uint32_t c0 = 0u, c1 = 1u;
   int in = in0;
-  for (int64_t r = r0; r < r1; r += kScanBatch) {
-    uint32_t A[kScanBatch], B[kScanBatch];
-    const int nr = (int)(r1 - r < kScanBatch ? r1 - r : kScanBatch);
-    carry_rows(rec, n_tiles, tile_prefix, n_inputs, r, nr, epoch, in, A, B, bad);
-#pragma unroll
-    for (int i = 0; i < kScanBatch; ++i) {
-      if (i < nr) {
-        c0 = (uint32_t)((((unsigned long long)A[i] + B[i] + c0) >> 32) & 1ull);
-        c1 = (uint32_t)((((unsigned long long)A[i] + B[i] + c1) >> 32) & 1ull);
-      }
+  for (int64_t r = r0; r < r1; ++r) {
+    const uint32_t kill = row_kill(r, tile_prefix, n_inputs, in);
+    const uint32_t A = (Gw[r] | Pw[r]) & ~kill, B = Gw[r] & ~kill;
+    c0 = (uint32_t)((((unsigned long long)A + B + c0) >> 32) & 1ull);
+    c1 = (uint32_t)((((unsigned long long)A + B + c1) >> 32) & 1ull);
+  }
+  /* (G, P) of this thread's run: carry-out = G | (P & carry-in) */
+  uint32_t iG = c0, iP = c1 & ~c0 & 1u;
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t uG = __shfl_up_sync(0xffffffffu, iG, d), uP = __shfl_up_sync(0xffffffffu, iP, d);
+    if (lane >= d) {
+      iG = iG | (iP & uG);
+      iP &= uP;
     }
   }
-  const uint32_t G = c0, P = c1 & ~c0 & 1u; /* carry-out = G | (P & carry-in) */
-  if (lane == 0) {
-    wg[warp] = G;
-    wp[warp] = P;
+  if (lane == 31) {
+    wg[warp] = iG;
+    wp[warp] = iP;
   }
   __syncthreads();
   if (warp == 0) {
@@ -171,31 +148,33 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(unsigned long long 
         b &= uP;
       }
     }
-    wg[lane] = a; /* inclusive: carry out of warps 0..lane for carry-in 0 */
+    wg[lane] = a;
     wp[lane] = b;
   }
   __syncthreads();
-  uint32_t c = warp > 0 ? wg[warp - 1] : 0u;
-  in = in0;
-  for (int64_t r = r0; r < r1; r += kScanBatch) {
-    uint32_t A[kScanBatch], B[kScanBatch];
-    const int nr = (int)(r1 - r < kScanBatch ? r1 - r : kScanBatch);
-    carry_rows(rec, n_tiles, tile_prefix, n_inputs, r, nr, epoch, in, A, B, bad);
-#pragma unroll
-    for (int i = 0; i < kScanBatch; ++i) {
-      if (i < nr) {
-        const unsigned long long sum = (unsigned long long)A[i] + B[i] + c;
-        /* carry leaving tile l = carry entering tile l+1; tile 31's is the row's carry-out */
-        const uint32_t into = (uint32_t)sum ^ A[i] ^ B[i];
-        const uint32_t cout =
-            (lane < 31) ? ((into >> (lane + 1)) & 1u) : (uint32_t)((sum >> 32) & 1ull);
-        const int64_t g = (r + i) * 32 + lane;
-        if (g < n_tiles) rec[g] = (epoch << 4) | (2ull << 2) | (unsigned long long)cout;
-        c = (uint32_t)((sum >> 32) & 1ull);
-      }
-    }
+  /* carry entering this thread's first row: the exclusive prefix (carry-in 0 at tile 0) */
+  uint32_t eG = __shfl_up_sync(0xffffffffu, iG, 1), eP = __shfl_up_sync(0xffffffffu, iP, 1);
+  if (lane == 0) {
+    eG = 0u;
+    eP = 1u;
   }
-  if (bad) atomicOr(state + 1, BG_DEV_ERR_CHAIN);
+  uint32_t c = eG;
+  if (warp > 0) c = eG | (eP & wg[warp - 1]);
+  in = in0;
+  for (int64_t r = r0; r < r1; ++r) {
+    const uint32_t kill = row_kill(r, tile_prefix, n_inputs, in);
+    const uint32_t A = (Gw[r] | Pw[r]) & ~kill, B = Gw[r] & ~kill;
+    const unsigned long long sum = (unsigned long long)A + B + c;
+    Cw[r] = (uint32_t)sum ^ A ^ B;
+    c = (uint32_t)((sum >> 32) & 1ull);
+  }
+}
+
+/* 64-bit words of a records buffer for `tiles` tiles: one look-back record per addition and
+ * tile, then the pre-pass bitmaps (3 words of 32 tiles per pre-pass addition). */
+int64_t record_words(const bg_kernel_desc &d, int64_t tiles) {
+  const int64_t rows = (tiles + 31) / 32;
+  return (int64_t)std::max(1, d.n_adds) * tiles + (3 * (int64_t)d.n_pre * rows + 1) / 2;
 }
 
 int sm_count() {
@@ -594,7 +573,7 @@ int bg_plan_reserve(bg_program *prog, int32_t input_kind, int32_t max_inputs, in
     return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: staging");
   if (cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming) != cudaSuccess)
     return cleanup(BG_ERR_CUDA, "bg_plan_reserve: event");
-  const size_t nrec = (size_t)std::max(1, prog->desc.n_adds) * (size_t)max_tiles;
+  const size_t nrec = (size_t)record_words(prog->desc, max_tiles);
   if (cudaMalloc(&p->d_records, nrec * sizeof(unsigned long long)) != cudaSuccess)
     return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: look-back records");
   if (cudaMemset(p->d_records, 0, nrec * sizeof(unsigned long long)) != cudaSuccess)
@@ -706,9 +685,8 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
                              dim3(prog->desc.block), args, 0, s));
     if (prog->desc.n_pre > 0) {
-      bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.records, prm.n_tiles,
-                                                              prm.tile_prefix, prm.n_inputs,
-                                                              prm.state);
+      bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.pre_bits, prm.n_tiles,
+                                                              prm.tile_prefix, prm.n_inputs);
       BG_CUDA(cudaGetLastError());
     }
     const int main_grid = (int)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm);
@@ -723,9 +701,8 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
         1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
     BG_CUDA(cudaLaunchKernel((const void *)prog->pre_kernel, dim3(pre_grid),
                              dim3(prog->desc.block), args, 0, s));
-    bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.records, prm.n_tiles,
-                                                            prm.tile_prefix, prm.n_inputs,
-                                                            prm.state);
+    bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.pre_bits, prm.n_tiles,
+                                                            prm.tile_prefix, prm.n_inputs);
     BG_CUDA(cudaGetLastError());
   }
   BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(grid), dim3(prog->desc.block), args,
@@ -765,6 +742,8 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   prm.positions = plan->positions;
   prm.pos_capacity = plan->pos_capacity;
   prm.runs = plan->d_runs;
+  prm.pre_bits = reinterpret_cast<uint32_t *>(plan->d_records +
+                                              (int64_t)std::max(1, plan->prog->desc.n_adds) * plan->n_tiles);
   if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
   prm.n_inputs = (int32_t)n;
   prm.input_kind = L.input_kind;
@@ -821,7 +800,8 @@ int bg_plan_destroy(bg_plan *plan) {
  *   [0, 4)    state: the eight 32-bit slots of a plan's state (tile counter, status, epoch,
  *             a record no kernel writes, match positions written);
  *   [4, 9)    tables of the one input: in_off, in_len, tile_prefix[0..1], out_off;
- *   [32, end) look-back records, [n_adds][n_tiles], then (split form) the run masks,
+ *   [32, end) look-back records, [n_adds][n_tiles], the pre-pass bitmaps (3 words of 32
+ *             tiles per pre-pass addition), then (split form) the run masks,
  *             [n_run][n_tiles] 32-bit words.
  * The array starts zeroed when the module loads.  Every call then clears the counters and
  * the status, and bumps the epoch.  Records left by an earlier call carry an older epoch, so
@@ -903,19 +883,25 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
       (int64_t)(32 - prog->desc.halo_lanes - prog->desc.tail_lanes) * prog->desc.wpt;
   const int64_t tiles = std::max<int64_t>(1, (W + tile_words - 1) / tile_words);
   const int64_t adds = std::max(1, prog->desc.n_adds);
-  /* 64-bit scratch words per tile: one look-back record per addition, then the run masks */
-  const int64_t per_tile = adds + (prog->desc.n_run + 1) / 2;
-  if (tiles > (int64_t)BG_NOALLOC_RECORDS / per_tile) {
+  /* 64-bit scratch words: the look-back records and pre-pass bitmaps, then the run masks */
+  auto scratch_words = [&](int64_t n) {
+    return record_words(prog->desc, n) + ((int64_t)prog->desc.n_run * n + 1) / 2;
+  };
+  if (scratch_words(tiles) > (int64_t)BG_NOALLOC_RECORDS) {
+    int64_t lo = 0, hi = tiles; /* largest tile count that fits */
+    while (hi - lo > 1) {
+      const int64_t m = (lo + hi) / 2;
+      if (scratch_words(m) <= (int64_t)BG_NOALLOC_RECORDS) lo = m; else hi = m;
+    }
     char msg[360];
     snprintf(msg, sizeof msg,
              "bg_scan_noalloc: %lld bytes span %lld tiles of %lld words and need %lld scratch "
-             "words (%lld per tile: %lld additions, %d run-mask words); the fixed %u-byte scratch "
-             "holds %u, so at most %lld tiles (%lld bytes) for this program",
+             "words (%lld additions, %d pre-pass, %d run-mask words per tile); the fixed %u-byte "
+             "scratch holds %u, so at most %lld tiles (%lld bytes) for this program",
              (long long)n_bytes, (long long)tiles, (long long)tile_words,
-             (long long)(tiles * per_tile), (long long)per_tile, (long long)adds,
-             prog->desc.n_run, (unsigned)BG_NOALLOC_SCRATCH_BYTES, (unsigned)BG_NOALLOC_RECORDS,
-             (long long)(BG_NOALLOC_RECORDS / per_tile),
-             (long long)(BG_NOALLOC_RECORDS / per_tile) * tile_words * 32);
+             (long long)scratch_words(tiles), (long long)adds, prog->desc.n_pre, prog->desc.n_run,
+             (unsigned)BG_NOALLOC_SCRATCH_BYTES, (unsigned)BG_NOALLOC_RECORDS, (long long)lo,
+             (long long)lo * tile_words * 32);
     return fail(BG_ERR_CAPACITY, msg);
   }
   unsigned long long *scratch = nullptr;
@@ -935,8 +921,10 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   prm.counts = counts;
   prm.records = scratch + kNoallocRecordsAt;
   prm.state = reinterpret_cast<uint32_t *>(scratch);
+  prm.pre_bits = reinterpret_cast<uint32_t *>(scratch + kNoallocRecordsAt + adds * tiles);
   prm.runs = prog->desc.n_run > 0
-                 ? reinterpret_cast<uint32_t *>(scratch + kNoallocRecordsAt + adds * tiles)
+                 ? reinterpret_cast<uint32_t *>(scratch + kNoallocRecordsAt +
+                                                record_words(prog->desc, tiles))
                  : nullptr;
   prm.positions = nullptr;
   prm.pos_capacity = 0;

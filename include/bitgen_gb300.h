@@ -165,9 +165,10 @@ int bg_plan_destroy(bg_plan *plan);
  *                holds the scan's device status bits: 0 on success, 1 if a carry look-back
  *                wait ran out of time, 2 if a look-back walked past the first tile.
  *
- * Limit: the input may span at most BG_NOALLOC_RECORDS / (max(1, additions) + (n_run + 1) / 2)
- * tiles of (32 - halo_lanes - tail_lanes) * wpt words each.  Larger inputs are rejected with
- * BG_ERR_CAPACITY before anything is enqueued, and bg_last_error() gives the sizes.
+ * Limit: for T tiles of (32 - halo_lanes - tail_lanes) * wpt words, the scratch must hold
+ * max(1, additions) * T + ceil(3 * n_pre * ceil(T / 32) / 2) + ceil(n_run * T / 2) 64-bit
+ * words out of BG_NOALLOC_RECORDS.  Larger inputs are rejected with BG_ERR_CAPACITY before
+ * anything is enqueued, and bg_last_error() gives the sizes and the largest input that fits.
  * The first call on each device looks up the array's device address once
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream
  * capture begins.

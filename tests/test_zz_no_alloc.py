@@ -98,7 +98,16 @@ def test_two_calls_in_a_row_match_the_plan_path(program, cuda):
 def test_limit_is_exact_and_enforced(program, cuda):
     prog, ps = program
     tile_words = prog.spec.tile_words
-    max_tiles = RECORDS // (max(1, prog.spec.n_adds) + (prog.spec.n_run + 1) // 2)
+    s = prog.spec
+
+    def words(tiles):   # the scratch rule stated in include/bitgen_gb300.h
+        return (max(1, s.n_adds) * tiles + (3 * s.n_pre * -(-tiles // 32) + 1) // 2
+                + (s.n_run * tiles + 1) // 2)
+    lo, hi = 1, RECORDS
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        lo, hi = (mid, hi) if words(mid) <= RECORDS else (lo, mid)
+    max_tiles = lo
     n_max = max_tiles * tile_words * 32
     data = torch.from_numpy(_text(n_max + 32, ps, 40)).to(cuda)
     out = torch.empty((prog.n_outputs, n_max // 32 + 1), dtype=torch.int32, device=cuda)
