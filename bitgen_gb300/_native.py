@@ -34,7 +34,8 @@ class KernelDesc(C.Structure):
     _fields_ = [("source", C.c_char_p), ("source_len", C.c_size_t), ("name", C.c_char_p),
                 ("n_outputs", C.c_int32), ("n_adds", C.c_int32), ("halo_lanes", C.c_int32),
                 ("wpt", C.c_int32), ("block", C.c_int32), ("tail_lanes", C.c_int32),
-                ("n_pre", C.c_int32), ("n_run", C.c_int32), ("flags", C.c_int32)]
+                ("n_pre", C.c_int32), ("n_run", C.c_int32), ("flags", C.c_int32),
+                ("n_parts", C.c_int32)]
 
 
 class Layout(C.Structure):

@@ -326,13 +326,12 @@ class Tuning:
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
     prefilter: bool = True   # run a term only in tiles holding one of its trigrams
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
-    chunk_rows: int = 1      # split form: rows of 32 tiles per execute work item
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
-                self.merge_outputs, self.chunk_rows)
+                self.merge_outputs)
 
 
 @dataclass
@@ -351,6 +350,7 @@ class KernelSpec:
     n_pre: int = 0          # additions 0..n_pre-1 take their carries from the pre-pass kernel
     n_run: int = 0          # split form: run-mask words per tile (0 = single-kernel form)
     merges: bool = False    # parts OR into shared outputs: launches need the output streams
+    n_parts: int = 0        # split form: part functions
 
     @property
     def tile_words(self):
@@ -1272,7 +1272,6 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         by_out.setdefault(o, []).append(r)
     cap = max(1, tuning.part_cap)
     merge = tuning.merge_outputs
-    rows = max(1, tuning.chunk_rows)
     part_terms: List[List[int]] = []     # terms of each part, in output order
     if merge:
         order = [r for o in range(len(names)) for r in by_out.get(o, [])]
@@ -1318,6 +1317,12 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
                      f"  acc_clear_n(acc, t, {len(outs_k)});\n" + "\n".join(blocks) + "\n" + stores + "\n}\n")
     decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
     ba = ", ".join(f"b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+    pmw = max(1, max(len(m) for m in part_masks))
+    pm_table = []
+    for masks in part_masks:
+        items_ = sorted(masks.items()) + [(0, 0)] * (pmw - len(masks))
+        for w, m in items_:
+            pm_table += [w, m]
     wants = []
     for ci, masks in enumerate(part_masks):
         cond = " | ".join(f"(p.runs[{w}LL * p.n_tiles + g] & 0x{m:08x}u)" for w, m in sorted(masks.items())) or "0u"
@@ -1384,20 +1389,26 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
     cls_kernel = (
         f"//@@BG_PART\n{tables}"
+        f"/* per part: {pmw} (run-mask word, mask) pairs; read by the runtime's work-list kernel */\n"
+        f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}] = {{\n{_hex_array(pm_table)}\n}};\n'
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_cls(const __grid_constant__ BgParams p) {{\n'
         f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
         f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
         f"  __syncthreads();\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        f"{PRE_CHUNK_OPEN}"
+        + PRE_CHUNK_OPEN +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
         f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
-        f"{PRE_CHUNK_CLOSE}"
+        f"    if (t.lane == 0) {{ /* row summaries for the work list (zeroed by the launch) */\n"
+        f"      uint32_t *rowrun = p.work + 1 + {len(parts)}LL * (1 + rows);\n"
+        + "".join(f"      if (t.run[{w}]) atomicOr(rowrun + {w}LL * rows + c, t.run[{w}]);\n" for w in range(nw)) +
+        f"    }}\n"
+        + PRE_CHUNK_CLOSE +
         f"}}\n")
     warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
@@ -1426,18 +1437,32 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * ({nacc} * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        f"  const long long chunks = (((p.n_tiles + 31) >> 5) + {rows} - 1) / {rows};\n"
-        f"  const long long items = chunks * {len(parts)};\n"
+        f"  __shared__ unsigned int bg_pref[{len(parts) + 1}];\n"
+        f"  if (threadIdx.x < 32) {{\n"
+        f"    /* part-major order: exclusive prefix of the parts' row counts */\n"
+        f"    const int per = ({len(parts)} + 31) / 32, lo = threadIdx.x * per;\n"
+        f"    unsigned int sum = 0u;\n"
+        f"    for (int i = lo; i < lo + per && i < {len(parts)}; ++i) sum += __ldg(p.work + 1 + i);\n"
+        f"    unsigned int incl = sum;\n"
+        f"    for (int d = 1; d < 32; d <<= 1) {{\n"
+        f"      const unsigned int y = __shfl_up_sync(FULL, incl, d);\n"
+        f"      if ((int)threadIdx.x >= d) incl += y;\n"
+        f"    }}\n"
+        f"    unsigned int at = incl - sum;\n"
+        f"    for (int i = lo; i < lo + per && i < {len(parts)}; ++i) {{ bg_pref[i] = at; at += __ldg(p.work + 1 + i); }}\n"
+        f"    if (threadIdx.x == 31) bg_pref[{len(parts)}] = incl;\n"
+        f"  }}\n"
+        f"  __syncthreads();\n"
+        f"  const unsigned int items = bg_pref[{len(parts)}];\n"
+        f"  const long long rows = (p.n_tiles + 31) >> 5;\n"
         f"  for (;;) {{\n"
         f"    unsigned int it = 0u;\n"
         f"    if (t.lane == 0) it = atomicAdd(p.state, 1u);\n"
         f"    it = __shfl_sync(FULL, it, 0);\n"
-        f"    if ((long long)it >= items) break;\n"
-        f"    const int k = (int)((long long)it / chunks);\n"
-        f"    const long long c = (long long)it - (long long)k * chunks;\n"
-        f"    for (int rr = 0; rr < {rows}; ++rr) {{\n"
-        f"    const long long g0 = (c * {rows} + rr) * 32;\n"
-        f"    if (g0 >= p.n_tiles) break;\n"
+        f"    if (it >= items) break;\n"
+        f"    int k = 0, hi = {len(parts)};\n"
+        f"    while (hi - k > 1) {{ const int m = (k + hi) >> 1; if (bg_pref[m] <= it) k = m; else hi = m; }}\n"
+        f"    const long long g0 = (long long)__ldg(p.work + 1 + {len(parts)} + (long long)k * rows + (it - bg_pref[k])) * 32;\n"
         f"    const long long g = g0 + t.lane;\n"
         f"    bool want = false;\n"
         f"    if (g < p.n_tiles) {{\n"
@@ -1455,10 +1480,9 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"      load_basis(p, t, b);\n"
         f"      switch (k) {{\n{calls}\n        default: break;\n      }}\n"
         f"    }}\n"
-        f"    }}\n"
         f"  }}\n"
         f"}}\n")
     return KernelSpec(source=src, name=name, n_outputs=len(names), n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
                       n_nodes=len(d.nodes), output_names=names, tail_lanes=gen.tl,
-                      n_pre=len(gen.pre), n_run=nw, merges=merge)
+                      n_pre=len(gen.pre), n_run=nw, merges=merge, n_parts=len(parts))

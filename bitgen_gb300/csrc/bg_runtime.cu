@@ -170,6 +170,61 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits,
   }
 }
 
+/* Work list of the split form's execute pass: the (part, tile row) pairs where the part has
+ * something to run, a row being 32 consecutive tiles.  The classify pass leaves, for every row
+ * and run-mask word, the OR of the row's 32 masks (`rowrun`, [n_run][rows]); part p has work in
+ * a row when one of its (word, mask) pairs (`pmask`) meets it.  Block p lists part p's rows in
+ * increasing order at work + 1 + n_parts + p * rows and stores their count at work[1 + p]:
+ * each warp takes a contiguous block of rows, 32 rows per step (one per lane, coalesced loads,
+ * a ballot to keep them in order), and the warps' counts are scanned across the block.  The
+ * execute pass orders the parts one after the other (part-major, so that the whole GPU runs one
+ * part at a time) and claims a part's rows in increasing order. */
+__global__ void __launch_bounds__(256) bg_work_list_kernel(const uint32_t *rowrun,
+                                                           const uint32_t *pmask, int pmw,
+                                                           uint32_t *work, int n_parts,
+                                                           int64_t rows) {
+  __shared__ uint32_t wsum[8];
+  const int p = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
+  uint32_t *out = work + 1 + n_parts + (int64_t)p * rows;
+  const int64_t steps = (rows + 31) / 32;
+  const int64_t per = (steps + nwarps - 1) / nwarps;
+  const int64_t s0 = (int64_t)warp * per < steps ? (int64_t)warp * per : steps;
+  const int64_t s1 = s0 + per < steps ? s0 + per : steps;
+  auto present = [&](int64_t step) -> uint32_t {
+    const int64_t r = step * 32 + lane;
+    uint32_t any = 0u;
+    if (r < rows)
+      for (int e = 0; e < pmw; ++e) {
+        const uint32_t m = pm[2 * e + 1];
+        if (m) any |= rowrun[(int64_t)pm[2 * e] * rows + r] & m;
+      }
+    return __ballot_sync(0xffffffffu, any != 0u);
+  };
+  uint32_t cnt = 0;
+  for (int64_t st = s0; st < s1; ++st) cnt += __popc(present(st));
+  if (lane == 0) wsum[warp] = cnt;
+  __syncthreads();
+  uint32_t pos = 0, total = 0;
+  for (int w = 0; w < nwarps; ++w) {
+    if (w < warp) pos += wsum[w];
+    total += wsum[w];
+  }
+  for (int64_t st = s0; st < s1; ++st) {
+    const uint32_t b = present(st);
+    if ((b >> lane) & 1u) out[pos + __popc(b & ((1u << lane) - 1u))] = (uint32_t)(st * 32 + lane);
+    pos += __popc(b);
+  }
+  if (threadIdx.x == 0) work[1 + p] = total;
+}
+
+/* 32-bit words of the split form's work list (counts, rows per part, row summaries). */
+int64_t work_words(const bg_kernel_desc &d, int64_t tiles) {
+  const int64_t rows = (tiles + 31) / 32;
+  return d.n_run > 0 ? 1 + (int64_t)d.n_parts * (1 + rows) + (int64_t)d.n_run * rows : 0;
+}
+
 /* 64-bit words of a records buffer for `tiles` tiles: one look-back record per addition and
  * tile, then the pre-pass bitmaps (3 words of 32 tiles per pre-pass addition). */
 int64_t record_words(const bg_kernel_desc &d, int64_t tiles) {
@@ -211,6 +266,8 @@ struct bg_program {
   cudaKernel_t kernel = nullptr;
   cudaKernel_t pre_kernel = nullptr; /* carry pre-pass, when desc.n_pre > 0 (single form) */
   cudaKernel_t cls_kernel = nullptr; /* classify pass of the split form (desc.n_run > 0)  */
+  const uint32_t *pmask = nullptr;   /* split form: per part, pmw (word, mask) pairs        */
+  int pmw = 0;
   int regs = 0, local_bytes = 0, blocks_per_sm = 1, pre_blocks_per_sm = 1;
 };
 
@@ -222,6 +279,7 @@ struct bg_plan {
   unsigned long long *d_records = nullptr;
   uint32_t *d_state = nullptr;
   uint32_t *d_runs = nullptr; /* split form: [n_run][cap_tiles] run masks */
+  uint32_t *d_work = nullptr; /* split form: work list */
   int grid = 1;
   int64_t debug_wait_tile = -1;
   int64_t spin_limit = 0;
@@ -460,8 +518,16 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   cudaError_t e = cudaLibraryLoadData(&p->lib, p->cubin.data(), nullptr, nullptr, 0, nullptr,
                                       nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&p->kernel, p->lib, p->name.c_str());
-  if (e == cudaSuccess && desc->n_run > 0)
+  if (e == cudaSuccess && desc->n_run > 0) {
     e = cudaLibraryGetKernel(&p->cls_kernel, p->lib, (p->name + "_cls").c_str());
+    void *pm = nullptr;
+    size_t pm_bytes = 0;
+    if (e == cudaSuccess) e = cudaLibraryGetGlobal(&pm, &pm_bytes, p->lib, "bg_pmask");
+    if (e == cudaSuccess) {
+      p->pmask = static_cast<const uint32_t *>(pm);
+      p->pmw = (int)(pm_bytes / (sizeof(uint32_t) * 2 * (size_t)std::max(1, desc->n_parts)));
+    }
+  }
   else if (e == cudaSuccess && desc->n_pre > 0)
     e = cudaLibraryGetKernel(&p->pre_kernel, p->lib, (p->name + "_pre").c_str());
   if (e != cudaSuccess) {
@@ -581,6 +647,9 @@ int bg_plan_reserve(bg_program *prog, int32_t input_kind, int32_t max_inputs, in
   if (prog->desc.n_run > 0 &&
       cudaMalloc(&p->d_runs, (size_t)prog->desc.n_run * (size_t)max_tiles * sizeof(uint32_t)) != cudaSuccess)
     return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: run masks");
+  if (prog->desc.n_run > 0 &&
+      cudaMalloc(&p->d_work, (size_t)work_words(prog->desc, max_tiles) * sizeof(uint32_t)) != cudaSuccess)
+    return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: work list");
   if (cudaMalloc(&p->d_state, 8 * sizeof(uint32_t)) != cudaSuccess)
     return cleanup(BG_ERR_NOMEM, "bg_plan_reserve: state");
   if (cudaMemset(p->d_state, 0, 8 * sizeof(uint32_t)) != cudaSuccess)
@@ -679,7 +748,13 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     /* split form: classify every tile (it also zeroes the words of the outputs no part will
      * write on that tile), scan the pre-pass carries, then run the parts */
     const int warps_per_block = prog->desc.block / 32;
-    const int64_t need = (prm.n_tiles + warps_per_block - 1) / warps_per_block;
+    const int64_t rows = (prm.n_tiles + 31) / 32;
+    if (!prog->pmask || prog->desc.n_parts > 4096)
+      return fail(BG_ERR_INVALID, "split-form launch: no part table or more than 4096 parts");
+    /* the row summaries start at zero; classify ORs every tile's run masks into its row */
+    BG_CUDA(cudaMemsetAsync(prm.work + 1 + (int64_t)prog->desc.n_parts * (1 + rows), 0,
+                            sizeof(uint32_t) * (size_t)prog->desc.n_run * (size_t)rows, s));
+    const int64_t need = (rows + warps_per_block - 1) / warps_per_block;
     const int cls_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
     BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
@@ -689,6 +764,10 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
                                                               prm.tile_prefix, prm.n_inputs);
       BG_CUDA(cudaGetLastError());
     }
+    bg_work_list_kernel<<<std::max(1, prog->desc.n_parts), 256, 0, s>>>(
+        prm.work + 1 + (int64_t)prog->desc.n_parts * (1 + rows), prog->pmask, prog->pmw, prm.work,
+        prog->desc.n_parts, rows);
+    BG_CUDA(cudaGetLastError());
     const int main_grid = (int)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm);
     BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(main_grid), dim3(prog->desc.block),
                              args, 0, s));
@@ -744,6 +823,7 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   prm.runs = plan->d_runs;
   prm.pre_bits = reinterpret_cast<uint32_t *>(plan->d_records +
                                               (int64_t)std::max(1, plan->prog->desc.n_adds) * plan->n_tiles);
+  prm.work = plan->d_work;
   if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
   prm.n_inputs = (int32_t)n;
   prm.input_kind = L.input_kind;
@@ -780,6 +860,7 @@ int bg_plan_destroy(bg_plan *plan) {
   if (plan->d_records) cudaFree(plan->d_records);
   if (plan->d_state) cudaFree(plan->d_state);
   if (plan->d_runs) cudaFree(plan->d_runs);
+  if (plan->d_work) cudaFree(plan->d_work);
   if (plan->h_stage) cudaFreeHost(plan->h_stage);
   delete plan;
   return BG_OK;
@@ -802,7 +883,7 @@ int bg_plan_destroy(bg_plan *plan) {
  *   [4, 9)    tables of the one input: in_off, in_len, tile_prefix[0..1], out_off;
  *   [32, end) look-back records, [n_adds][n_tiles], the pre-pass bitmaps (3 words of 32
  *             tiles per pre-pass addition), then (split form) the run masks,
- *             [n_run][n_tiles] 32-bit words.
+ *             [n_run][n_tiles] 32-bit words, and the work list.
  * The array starts zeroed when the module loads.  Every call then clears the counters and
  * the status, and bumps the epoch.  Records left by an earlier call carry an older epoch, so
  * the look-back reads them as not yet published and they need no clearing.  Calls share the
@@ -885,7 +966,8 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   const int64_t adds = std::max(1, prog->desc.n_adds);
   /* 64-bit scratch words: the look-back records and pre-pass bitmaps, then the run masks */
   auto scratch_words = [&](int64_t n) {
-    return record_words(prog->desc, n) + ((int64_t)prog->desc.n_run * n + 1) / 2;
+    return record_words(prog->desc, n) + ((int64_t)prog->desc.n_run * n + 1) / 2 +
+           (work_words(prog->desc, n) + 1) / 2;
   };
   if (scratch_words(tiles) > (int64_t)BG_NOALLOC_RECORDS) {
     int64_t lo = 0, hi = tiles; /* largest tile count that fits */
@@ -925,6 +1007,11 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   prm.runs = prog->desc.n_run > 0
                  ? reinterpret_cast<uint32_t *>(scratch + kNoallocRecordsAt +
                                                 record_words(prog->desc, tiles))
+                 : nullptr;
+  prm.work = prog->desc.n_run > 0
+                 ? reinterpret_cast<uint32_t *>(scratch + kNoallocRecordsAt +
+                                                record_words(prog->desc, tiles) +
+                                                ((int64_t)prog->desc.n_run * tiles + 1) / 2)
                  : nullptr;
   prm.positions = nullptr;
   prm.pos_capacity = 0;

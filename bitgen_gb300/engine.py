@@ -357,7 +357,8 @@ class Program:
                                       self.spec.n_adds, self.spec.halo_lanes, self.spec.wpt,
                                       self.spec.block, self.spec.tail_lanes, self.spec.n_pre,
                                       self.spec.n_run,
-                                      N.BG_PROGRAM_MERGES if self.spec.merges else 0)
+                                      N.BG_PROGRAM_MERGES if self.spec.merges else 0,
+                                      self.spec.n_parts)
             h = C.c_void_p()
             N.check(lib.bg_program_create(C.byref(self._desc), C.byref(h)), "bg_program_create")
             self._handle = h

@@ -82,6 +82,7 @@ typedef struct bg_kernel_desc {
                          "<name>" runs the parts on the tiles their masks select           */
   int32_t flags;      /* BG_PROGRAM_MERGES: parts OR into shared outputs, so every launch
                          needs out_streams (counts are taken from the bits a part adds)   */
+  int32_t n_parts;    /* split form: part functions (work items are (part, 32 tiles))      */
 } bg_kernel_desc;
 
 #define BG_PROGRAM_MERGES 1
@@ -165,9 +166,10 @@ int bg_plan_destroy(bg_plan *plan);
  *                holds the scan's device status bits: 0 on success, 1 if a carry look-back
  *                wait ran out of time, 2 if a look-back walked past the first tile.
  *
- * Limit: for T tiles of (32 - halo_lanes - tail_lanes) * wpt words, the scratch must hold
- * max(1, additions) * T + ceil(3 * n_pre * ceil(T / 32) / 2) + ceil(n_run * T / 2) 64-bit
- * words out of BG_NOALLOC_RECORDS.  Larger inputs are rejected with BG_ERR_CAPACITY before
+ * Limit: for T tiles of (32 - halo_lanes - tail_lanes) * wpt words and R = ceil(T / 32), the
+ * scratch must hold max(1, additions) * T + ceil(3 * n_pre * R / 2) + ceil(n_run * T / 2) +
+ * ceil(w / 2) 64-bit words out of BG_NOALLOC_RECORDS, where w = n_parts * (R + 1) + 1 +
+ * n_run * R for the split form (n_run > 0) and 0 otherwise.  Larger inputs are rejected with BG_ERR_CAPACITY before
  * anything is enqueued, and bg_last_error() gives the sizes and the largest input that fits.
  * The first call on each device looks up the array's device address once
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream

@@ -62,7 +62,7 @@ def small():
                                                   (2, 1, 256, {"prefilter": False}),
                                                   (1, 1, 256, {"part_cap": 1}),
                                                   (1, 1, 256, {"merge_outputs": False}),
-                                                  (1, 1, 256, {"chunk_rows": 4, "part_cap": 2}),
+                                                  (1, 1, 256, {"part_cap": 2}),
                                                   (2, 1, 256, {"carry_prepass": False})])
 def test_small_workload_tunings(cuda, wpt, skip, block, extra):
     ps, text, groups = small()

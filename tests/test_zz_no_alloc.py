@@ -101,8 +101,10 @@ def test_limit_is_exact_and_enforced(program, cuda):
     s = prog.spec
 
     def words(tiles):   # the scratch rule stated in include/bitgen_gb300.h
-        return (max(1, s.n_adds) * tiles + (3 * s.n_pre * -(-tiles // 32) + 1) // 2
-                + (s.n_run * tiles + 1) // 2)
+        rows = -(-tiles // 32)
+        w = s.n_parts * (rows + 1) + 1 + s.n_run * rows if s.n_run else 0
+        return (max(1, s.n_adds) * tiles + (3 * s.n_pre * rows + 1) // 2
+                + (s.n_run * tiles + 1) // 2 + (w + 1) // 2)
     lo, hi = 1, RECORDS
     while hi - lo > 1:
         mid = (lo + hi) // 2
