@@ -1341,23 +1341,29 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             gen.emit(f"t.run[{w}] |= 0x{m:08x}u;")
     # pre-pass aggregates: with a zero marker (no trigram of it in the tile) the aggregate
     # depends on the class alone
-    pre_classes: Dict[int, str] = {}
+    # additions sharing a class and carry lane have the same zero-marker aggregate: one test
+    # per group; an addition whose marker filter fired (rare) replaces its bits
+    groups_: Dict[Tuple[int, int], int] = {}
+    for v, k in gen.pre.items():
+        key = (d.nodes[v].args[1], gen.dl[v])
+        groups_[key] = groups_.get(key, 0) | (1 << k)
+    for (cnode, dl), kmask in sorted(groups_.items()):
+        c = gen.mat(cnode)
+        gen.emit(f"{{ const uint32_t pz = pre_propagates<{dl}>(ones_lanes(t, {gen.pack(c)})) ? 0xffffffffu : 0u;")
+        for j in range(-(-len(gen.pre) // 32)):
+            m = (kmask >> (32 * j)) & 0xFFFFFFFF
+            if m:
+                gen.emit(f"  pp[{j}] |= pz & 0x{m:08x}u;")
+        gen.emit("}")
     for v, k in sorted(gen.pre.items(), key=lambda x: x[1]):
         n = d.nodes[v]
         bit = nt + k
         mode = 0 if n.op == "matchstar" else 1
-        c = gen.mat(n.args[1])
-        if n.args[1] not in pre_classes:
-            pre_classes[n.args[1]] = f"po{n.args[1]}"
-            gen.emit(f"const uint32_t po{n.args[1]} = ones_lanes(t, {gen.pack(c)});")
         gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
         m = gen.mat(n.args[0])
+        c = gen.mat(n.args[1])
         gen.emit(f"uint32_t G, P; pre_aggregate<{gen.dl[v]}, E>(t, {mode}, {gen.pack(m)}, {gen.pack(c)}, G, P); "
-                 f"pg[{k >> 5}] |= G << {k & 31}; pp[{k >> 5}] |= P << {k & 31};")
-        gen.indent -= 2
-        gen.emit("} else {")
-        gen.indent += 2
-        gen.emit(f"pp[{k >> 5}] |= pre_propagates<{gen.dl[v]}>(po{n.args[1]}) << {k & 31};")
+                 f"pg[{k >> 5}] |= G << {k & 31}; pp[{k >> 5}] = (pp[{k >> 5}] & ~(1u << {k & 31})) | (P << {k & 31});")
         gen.close()
     for c, pm in sorted(pm_classes.items()):
         ref = gen.mat(c)
@@ -1373,8 +1379,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     for w in range(nw):
         gen.emit(f"if (t.lane == 0) p.runs[{w}LL * p.n_tiles + g] = t.run[{w}];")
     if merge:                            # parts OR into the outputs: start every word at zero
-        for o in range(len(names)):
-            gen.emit(f"zero_store(p, t, {o});")
+        gen.emit(f"zero_outputs(p, t, {len(names)});")
     else:
         for ci, outs_k in enumerate(parts):
             cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"

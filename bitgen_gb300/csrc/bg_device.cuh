@@ -927,6 +927,25 @@ static __device__ __noinline__ void merge_store(const BgParams &p, const Tile &t
   store_new_bits(p, t, o, nb);
 }
 
+/* Split form with merged outputs: zero this tile's words of outputs 0..n-1 (the words `store`
+ * would write), so that the parts can OR into them. */
+__device__ __forceinline__ void zero_outputs(const BgParams &p, const Tile &t, int n) {
+  if (!p.out) return;
+  uint32_t *dst = p.out + p.out_off[t.input];
+  bool ok[WPT];
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    ok[j] = t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W;
+  }
+  const long long w0 = t.base + t.lane * WPT;
+  for (int o = 0; o < n; ++o, dst += p.out_stride) {
+#pragma unroll
+    for (int j = 0; j < WPT; ++j)
+      if (ok[j]) dst[w0 + j] = 0u;
+  }
+}
+
 /* Split form: a part's accumulators hold only its own outputs (local index). */
 __device__ __forceinline__ void acc_clear_n(uint32_t *acc, const Tile &t, int n) {
   for (int i = 0; i < n * WPT; ++i) acc[i * 32 + t.lane] = 0u;

@@ -179,11 +179,11 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits,
  * a ballot to keep them in order), and the warps' counts are scanned across the block.  The
  * execute pass orders the parts one after the other (part-major, so that the whole GPU runs one
  * part at a time) and claims a part's rows in increasing order. */
-__global__ void __launch_bounds__(256) bg_work_list_kernel(const uint32_t *rowrun,
+__global__ void __launch_bounds__(1024) bg_work_list_kernel(const uint32_t *rowrun,
                                                            const uint32_t *pmask, int pmw,
                                                            uint32_t *work, int n_parts,
                                                            int64_t rows) {
-  __shared__ uint32_t wsum[8];
+  __shared__ uint32_t wsum[32];
   const int p = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
@@ -764,7 +764,7 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
                                                               prm.tile_prefix, prm.n_inputs);
       BG_CUDA(cudaGetLastError());
     }
-    bg_work_list_kernel<<<std::max(1, prog->desc.n_parts), 256, 0, s>>>(
+    bg_work_list_kernel<<<std::max(1, prog->desc.n_parts), 1024, 0, s>>>(
         prm.work + 1 + (int64_t)prog->desc.n_parts * (1 + rows), prog->pmask, prog->pmw, prm.work,
         prog->desc.n_parts, rows);
     BG_CUDA(cudaGetLastError());
