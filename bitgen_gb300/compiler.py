@@ -325,13 +325,14 @@ class Tuning:
     lookback_spin: int = 0   # look-back polls before sleeping
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
     prefilter: bool = True   # run a term only in tiles holding one of its trigrams
+    bloom_bits: int = 18     # prefilter: log2 of the Bloom bitmap's size (shared memory)
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
-                self.merge_outputs)
+                self.merge_outputs, self.bloom_bits)
 
 
 @dataclass
@@ -1022,7 +1023,6 @@ PRE_CHUNK_CLOSE = (
     "   }\n"
     "   if (NPRE > 0) pre_flush(p, c, gw, pw, t.lane);\n"
     "  }\n")
-BLOOM_SMEM = (1 << prefilter.BLOOM_BITS) // 8
 
 
 def _cluster_terms(gen: "_Gen", terms: List[Tuple[int, int]], cap: int) -> List[List[Tuple[int, int]]]:
@@ -1386,7 +1386,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
     cls_code = "\n".join(gen.lines)
     log2, keys, masks_tab = filt.exact()
-    bloom = filt.bloom()
+    bloom = filt.bloom(tuning.bloom_bits)
     tables = (f"#define BG_EXLOG2 {log2}\n"
               f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
               f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
@@ -1429,6 +1429,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
         f"#define BG_NPRE {len(gen.pre)}\n"
         f"#define BG_NRUN {nw}\n"
+        f"#define BG_BLOOM_BITS {tuning.bloom_bits}\n"
         f"#define BG_PREFILTER 1\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"

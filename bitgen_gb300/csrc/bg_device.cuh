@@ -55,6 +55,9 @@
 #ifndef BG_NRUN
 #define BG_NRUN 1 /* words of the per-tile run mask (trigram prefilter) */
 #endif
+#ifndef BG_BLOOM_BITS
+#define BG_BLOOM_BITS 16 /* log2 of the prefilter's Bloom bitmap size */
+#endif
 
 namespace bg {
 
@@ -789,8 +792,8 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
 
 #if BG_PREFILTER
 /* Trigram prefilter (tables generated by bitgen_gb300/prefilter.py).  Every trigram lying in
- * the bytes this warp computes is hashed into the Bloom bitmap `bloom` (2^16 bits, shared
- * memory); a hit is resolved in the exact open-addressed table (keys: trigram | 1 << 31, 0 =
+ * the bytes this warp computes is hashed into the Bloom bitmap `bloom` (2^BG_BLOOM_BITS bits,
+ * shared memory); a hit is resolved in the exact open-addressed table (keys: trigram | 1 << 31, 0 =
  * empty; BG_NRUN mask words per slot), whose mask is OR-ed into the tile's run mask.  The
  * trigram ending at byte q is byte(q-2) | byte(q-1) << 8 | byte(q) << 16; bytes before the
  * warp's first byte read as zero. */
@@ -815,7 +818,7 @@ static __device__ __noinline__ void trigram_exact(uint32_t key, const uint32_t *
 __device__ __forceinline__ void trigram_test(uint32_t key, const uint32_t *bloom,
                                              const uint32_t *keys, const uint32_t *masks, int log2,
                                              uint32_t *run) {
-  const uint32_t h = (key * BLOOM_HASH) >> 16;
+  const uint32_t h = (key * BLOOM_HASH) >> (32 - BG_BLOOM_BITS);
   if ((bloom[h >> 5] >> (h & 31u)) & 1u) trigram_exact(key, keys, masks, log2, run);
 }
 

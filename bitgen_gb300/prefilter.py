@@ -19,8 +19,9 @@ filter, preferring one that does not pass through a pre-pass addition; a term wi
 always runs.  Each pre-pass addition gets the filter of its marker,
 so the pre-pass can skip the marker's computation too.
 
-The kernel tests every trigram of the tile against a Bloom bitmap (2^16 bits, in shared memory)
-and resolves the rare hits in an exact open-addressed table that maps a trigram to the bit mask
+The kernel tests every trigram of the tile against a Bloom bitmap (2^18 bits by default, in
+shared memory: a warp takes the slow path whenever any of its 32 lanes hits, so the bitmap is
+sized for a per-lane false-hit rate well below 1/32) and resolves the rare hits in an exact open-addressed table that maps a trigram to the bit mask
 of the filters containing it.  Both tables are generated here and compiled into the kernel.
 """
 
@@ -31,13 +32,13 @@ from typing import Dict, FrozenSet, List, Optional, Sequence, Tuple
 
 ALL = (1 << 256) - 1
 MAX_SET = 4096          # largest trigram set one filter may carry
-BLOOM_BITS = 16         # log2 of the Bloom bitmap size
+BLOOM_BITS = 18         # log2 of the Bloom bitmap size (32 KB of shared memory)
 HASH_BLOOM = 0x9E3779B1
 HASH_EXACT = 0x85EBCA6B
 
 
-def bloom_hash(key: int) -> int:
-    return ((key * HASH_BLOOM) & 0xFFFFFFFF) >> (32 - BLOOM_BITS)
+def bloom_hash(key: int, bits: int = BLOOM_BITS) -> int:
+    return ((key * HASH_BLOOM) & 0xFFFFFFFF) >> (32 - bits)
 
 
 def exact_hash(key: int, log2_slots: int) -> int:
@@ -171,10 +172,10 @@ class TermFilter:
                 m |= 1 << (self.n_terms + k)
         return m
 
-    def bloom(self) -> List[int]:
-        words = [0] * ((1 << BLOOM_BITS) // 32)
+    def bloom(self, bits: int = BLOOM_BITS) -> List[int]:
+        words = [0] * ((1 << bits) // 32)
         for key in self.table:
-            h = bloom_hash(key)
+            h = bloom_hash(key, bits)
             words[h >> 5] |= 1 << (h & 31)
         return words
 
