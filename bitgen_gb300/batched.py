@@ -29,7 +29,9 @@ class BatchScanner:
         self.inp = pack_bytes(items, device=device)
         self.offs, self.words, self.total = out_layout(self.inp.lengths)
         n_out = program.n_outputs
-        self.out = torch.empty((n_out, self.total), dtype=torch.uint32, device=device) if streams else None
+        # a program that merges outputs across parts needs output streams even for counts
+        self.out = (torch.empty((n_out, self.total), dtype=torch.uint32, device=device)
+                    if streams or program.merges else None)
         self.counts = torch.empty((n_out, self.inp.n), dtype=torch.int64, device=device)
         self.plan = Plan(program, self.inp, self.offs, self.total)
         self.stream = torch.cuda.Stream(device=device)
@@ -69,7 +71,9 @@ class PerInputScanner:
         self.inp = pack_bytes(items, device=device)
         self.offs, self.words, self.total = out_layout(self.inp.lengths)
         n_out = program.n_outputs
-        self.out = torch.empty((n_out, self.total), dtype=torch.uint32, device=device) if streams else None
+        # one shared output (each input's launch writes its own words), also for counts only
+        self.out = (torch.empty((n_out, self.total), dtype=torch.uint32, device=device)
+                    if streams or program.merges else None)
         self.counts = torch.empty((n_out, self.inp.n), dtype=torch.int64, device=device)
         self.stream = torch.cuda.Stream(device=device)
         self.plans: List[Plan] = []

@@ -250,12 +250,13 @@ class Plan:
         self.program = program
         self._scratch: Optional[torch.Tensor] = None
         self.out_stride = out_stride
+        self._device = None
         if _handle is not None:
             self._h = _handle
             self.n_inputs = 0
             return
         self.n_inputs = inp.n
-        self._ensure_scratch(inp.data.device)
+        self._device = inp.data.device
         lay = N.Layout(inp.kind, inp.n, _i64(inp.offsets), _i64(inp.lengths), inp.basis_stride,
                        _i64(out_offsets), out_stride)
         h = C.c_void_p()
@@ -275,16 +276,15 @@ class Plan:
         N.check(N.lib().bg_plan_set_layout(self._h, C.byref(lay), stream), "bg_plan_set_layout")
         self.n_inputs = inp.n
         self.out_stride = out_stride
-        self._ensure_scratch(inp.data.device)
+        self._device = inp.data.device
 
-    def _ensure_scratch(self, device):
+    def _ensure_scratch(self):
         """A program that merges outputs across parts needs output streams on every launch;
-        counts-only launches write into this plan-owned buffer instead."""
-        if not self.program.merges:
-            return
+        counts-only launches write into this plan-owned buffer, made on the first of them (so
+        before any graph capture that replays the launch)."""
         need = self.program.n_outputs * max(1, self.out_stride)
         if self._scratch is None or self._scratch.numel() < need:
-            self._scratch = torch.empty(need, dtype=torch.uint32, device=device)
+            self._scratch = torch.empty(need, dtype=torch.uint32, device=self._device)
 
     @property
     def tiles(self) -> int:
@@ -304,7 +304,8 @@ class Plan:
         N.check(N.lib().bg_plan_set_wait_limit(self._h, cycles, debug_wait_tile), "bg_plan_set_wait_limit")
 
     def launch(self, data_ptr: int, out_ptr: int, counts_ptr: int, stream: int):
-        if not out_ptr and self._scratch is not None:
+        if not out_ptr and self.program.merges:
+            self._ensure_scratch()
             out_ptr = self._scratch.data_ptr()
         N.check(N.lib().bg_plan_launch(self._h, data_ptr, out_ptr or None, counts_ptr or None,
                                        stream), "bg_plan_launch")
