@@ -4,12 +4,17 @@ Workload (one step = one scan of the whole input): 256 seeded synthetic regexes 
 30% with an unbounded repetition), 16 groups of 16, over 1 MiB of printable ASCII with ~1
 planted match per 4 KiB, tiled to 256 MiB.  Each step writes the 16 per-group match streams
 (the reference's result shape) and the per-group match counts.  The input (256 MiB) is larger
-than L2 (129 MB), so no flush is needed between steps.
+than L2 (129 MB), so no flush is needed between steps.  The CPU evaluator scans the same
+256 MiB once (a few seconds on the host's cores); its counts must equal the GPU's.
+
+Further legs on the same line: ``batched`` (4096 small inputs, one graph launch vs one launch
+per input), ``dna`` (64 IUPAC motifs over 1 GiB of DNA text, its own CPU check) and ``served``
+(Poisson request arrivals over three resident pattern sets, p50/p99 latency).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-``--impl reference`` times the CPU evaluator (``oracle/bg_cpu.c``, all host threads) on a bounded
-sample of the same workload: the reference's own GPU path cannot execute these programs (its
+``--impl reference`` times the CPU evaluator (``oracle/bg_cpu.c``, all host threads) on the same
+workload, one scan of the 256 MiB input per step: the reference's own GPU path cannot execute these programs (its
 parser rejects MatchStar, ``bitgen/bitparser/bitstream_parser.py:202-211``) and its CPU
 comparison point, icgrep, is not part of the reference tree.
 """
@@ -42,10 +47,12 @@ def parse():
     ap.add_argument("--regexes", type=int, default=256)
     ap.add_argument("--groups", type=int, default=16)
     ap.add_argument("--wpt", type=int, default=0, help="words per lane (0 = autotuned default)")
-    ap.add_argument("--cpu-sample", type=int, default=4 << 20, help="bytes of the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="bytes of the CPU baseline sample (0 = the whole input, a few seconds)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-modes", action="store_true", help="skip the batched / served legs")
     ap.add_argument("--served-requests", type=int, default=600)
+    ap.add_argument("--dna-bytes", type=int, default=1 << 30, help="DNA text of the dna leg")
     return ap.parse_args()
 
 
@@ -125,14 +132,15 @@ class Clocks:
 
 
 def cpu_baseline(groups, base, sample_bytes):
-    """C evaluator on the host: all 16 groups on their own threads over a bounded sample."""
+    """C evaluator on the host: all groups on their own threads over a bounded sample (the
+    first `sample_bytes` of `base` tiled).  Its counts are the bit-exact check of the GPU run."""
     import numpy as np
     from oracle import cpu
     from bitgen_gb300.regex import compile_group
 
-    gs = [compile_group(g) for g in groups]
+    gs = [compile_group(g) if isinstance(g, list) else g for g in groups]
     reps = -(-sample_bytes // base.size)
-    data = np.tile(base, reps)[:sample_bytes]
+    data = np.tile(base, reps)[:sample_bytes] if reps > 1 else base[:sample_bytes]
     threads = min(os.cpu_count() or 1, len(gs))
     cpu.run_groups(gs, data[:1 << 16], threads=threads)  # warm
     t0 = time.perf_counter()
@@ -176,6 +184,59 @@ def batched_leg(prog, ps, dev):
             "batched_GBps": round(total / tb / 1e6, 3), "plain_GBps": round(total / tp / 1e6, 3),
             "batched_ms": round(tb, 4), "plain_ms": round(tp, 4), "speedup": round(tp / tb, 2),
             "bit_exact": exact, "median_len": int(np.median(lens))}
+
+
+def dna_leg(dev, n_bytes, steps, check_bytes):
+    """64 IUPAC motifs (6-20 bases, every fourth split by a gap .{a,b}, 3 <= a <= 5, b <= a + 4) in 4 groups over DNA text
+    (i.i.d. A/C/G/T, GC 42%, N runs, 80-column lines, 2^16 planted motif instances); per-group
+    streams and counts, the program's default tuning (on a 4-letter text the trigram filter
+    passes nearly every tile, so the compiler picks the single-kernel form)."""
+    import torch
+    from bitgen_gb300 import workloads
+    from bitgen_gb300.engine import Program, bytes_input, out_layout
+    from bitgen_gb300.regex import compile_group
+
+    t0 = time.perf_counter()
+    ps = workloads.dna_motifs(64, seed=5)
+    text = workloads.plant(workloads.dna_text(n_bytes, seed=6), ps.witnesses, 1 << 16, 7)
+    gen_s = time.perf_counter() - t0
+    groups = [compile_group(g) for g in ps.groups(4)]
+    prog = Program(groups)
+    data = torch.from_numpy(text).to(dev)
+    inp = bytes_input(data)
+    offs, words, total = out_layout([n_bytes])
+    out = torch.empty((prog.n_outputs, total), dtype=torch.uint32, device=dev)
+    counts = torch.empty((prog.n_outputs, 1), dtype=torch.int64, device=dev)
+    plan = prog.plan(inp, offs, total)
+    s = torch.cuda.current_stream(dev)
+    sp = int(s.cuda_stream)
+    for _ in range(3):
+        plan.launch(data.data_ptr(), out.data_ptr(), counts.data_ptr(), sp)
+    plan.sync(sp)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        plan.launch(data.data_ptr(), out.data_ptr(), counts.data_ptr(), sp)
+    e1.record(s)
+    plan.sync(sp)
+    ms = e0.elapsed_time(e1) / steps
+    res = {"bytes": n_bytes, "regexes": len(ps.regexes), "groups": len(groups), "steps": steps,
+           "GBps": round(n_bytes / ms / 1e6, 3), "ms": round(ms, 4),
+           "form": "split" if prog.spec.n_parts else "single-kernel",
+           "matches": int(counts.sum()), "text_gen_s": round(gen_s, 1)}
+    if check_bytes is not None:
+        check_bytes = min(check_bytes or n_bytes, n_bytes)
+        cb, cpu_counts = cpu_baseline(groups, text, check_bytes)
+        if check_bytes == n_bytes:          # the counts of the timed launches themselves
+            got = counts[:, 0].tolist()
+        else:
+            got = prog.scan(bytes_input(data[:check_bytes].contiguous()), streams=False,
+                            counts=True).counts[:, 0].tolist()
+        res["bit_exact_vs_cpu_sample"] = [int(x) for x in got] == list(cpu_counts)
+        res["cpu_baseline"] = cb
+    prog.close()
+    del out, data
+    return res
 
 
 def served_leg(dev, n_req, load_GBps):
@@ -227,7 +288,7 @@ def run_reference(args):
     ps, groups, base, reps = workload(args)
     vals = []
     for i in range(args.warmup + args.steps):
-        cb, _ = cpu_baseline(groups, base, args.cpu_sample)
+        cb, _ = cpu_baseline(groups, base, args.cpu_sample or args.bytes)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)
@@ -236,7 +297,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded)",
             "config": {"workload": f"throughput: {args.regexes} synthetic regexes, {args.groups} groups, "
-                                   f"CPU sample of {args.cpu_sample} bytes"},
+                                   f"CPU sample of {args.cpu_sample or args.bytes} bytes"},
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -287,10 +348,14 @@ def main():
     # bit-exact self-check of this very configuration against the CPU evaluator (rank 0, sample)
     check = None
     if rank == 0 and not args.no_cpu:
-        cb, cpu_counts = cpu_baseline(groups, base, args.cpu_sample)
-        sub = bytes_input(data[:args.cpu_sample].contiguous())
-        r = prog.scan(sub, streams=False, counts=True)
-        gpu_counts = [int(x) for x in r.counts[:, 0].tolist()]
+        sample = min(args.cpu_sample or n, n)
+        cb, cpu_counts = cpu_baseline(groups, base, sample)
+        if sample == n:                     # the counts of the warm-up launches themselves
+            gpu_counts = [int(x) for x in counts[:, 0].tolist()]
+        else:
+            sub = bytes_input(data[:sample].contiguous())
+            r = prog.scan(sub, streams=False, counts=True)
+            gpu_counts = [int(x) for x in r.counts[:, 0].tolist()]
         check = gpu_counts == list(cpu_counts)
     else:
         cb = None
@@ -364,7 +429,7 @@ def main():
                      "kernel_ms": round(kernel_ms, 4)},
         "e2e": {"value": round(total_bytes / (e2e_ms / 1e3) / 1e9, 3), "unit": UNIT,
                 "h2d_bytes_per_step": n, "d2h_bytes_per_step": prog.n_outputs * 8},
-        "gpu_launches": (4 if info.get("pre_adds") else 2) * args.steps,
+        "gpu_launches": info.get("kernels_per_scan", 0) * args.steps,
         "clocks": clk,
     }
     if cb is not None:
@@ -374,6 +439,10 @@ def main():
             line["batched"] = batched_leg(prog, ps, dev)
         except Exception as e:  # a failed leg is reported, it does not void the main line
             line["batched"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        try:
+            line["dna"] = dna_leg(dev, args.dna_bytes, 5, None if args.no_cpu else args.cpu_sample)
+        except Exception as e:
+            line["dna"] = {"error": f"{type(e).__name__}: {e}"[:300]}
         try:
             load = line["batched"].get("batched_GBps", value)
             line["served"] = served_leg(dev, args.served_requests, load)

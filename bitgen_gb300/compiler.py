@@ -315,7 +315,8 @@ class Tuning:
     wpt: int = 1            # 32-bit words per lane
     block: int = 256        # threads per CTA
     skip_interval: int = 1  # check for an all-zero marker every k AND steps (0 = never)
-    part_cap: int = 4       # most OR-ed terms one part function computes
+    part_cap: int = 0       # most OR-ed terms one part function computes (0: 4 in the split
+                            # form, 32 in the single-kernel form)
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
     min_blocks: int = 4     # __launch_bounds__ minimum resident blocks per SM (caps registers)
     edge_variants: bool = False  # separate unmasked part code for tiles away from input ends
@@ -326,13 +327,16 @@ class Tuning:
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
     prefilter: bool = True   # run a term only in tiles holding one of its trigrams
     bloom_bits: int = 18     # prefilter: log2 of the Bloom bitmap's size (shared memory)
+    prefilter_limit: float = 0.25  # prefilter only while a tile is expected to run fewer than
+                                   # this fraction of the terms (text taken as uniform over
+                                   # the bytes the filters name)
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
-                self.merge_outputs, self.bloom_bits)
+                self.merge_outputs, self.bloom_bits, self.prefilter_limit)
 
 
 @dataclass
@@ -1089,8 +1093,10 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     if tuning.prefilter and not tuning.lockstep and not tuning.edge_variants:
         pre_nodes = [v for v, _ in sorted(gen.pre.items(), key=lambda x: x[1])]
         filt = prefilter.build(gen, [v for v, _ in terms], pre_nodes)
-        if not filt.enabled:
-            filt = None
+        positions = 32 * 32 * tuning.wpt
+        if not filt.enabled or (filt.expected_per_tile(positions) >
+                                tuning.prefilter_limit * len(terms)):
+            filt = None                  # the filter would pass most terms: single-kernel form
     if filt is not None:
         return _generate_filtered(gen, tuning, terms, names, filt, name)
     budget = SMEM_BUDGET
@@ -1104,7 +1110,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         tuning = replace(tuning, block=block,
                          min_blocks=min(32, -(-tuning.min_blocks * tuning.block // block)))
     warps = tuning.block // 32
-    clusters = _cluster_terms(gen, terms, tuning.part_cap)
+    clusters = _cluster_terms(gen, terms, tuning.part_cap or 32)
     funcs = []
     sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
     args = f"p, t, acc, {', '.join(f'b{i}_{j}' for i in range(8) for j in range(wpt))}"
@@ -1270,7 +1276,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     by_out: Dict[int, List[int]] = {}
     for r, (v, o) in enumerate(terms):
         by_out.setdefault(o, []).append(r)
-    cap = max(1, tuning.part_cap)
+    cap = max(1, tuning.part_cap or 4)
     merge = tuning.merge_outputs
     part_terms: List[List[int]] = []     # terms of each part, in output order
     if merge:

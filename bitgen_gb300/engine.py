@@ -386,7 +386,18 @@ class Program:
         N.check(N.lib().bg_program_info(self._handle, C.byref(r), C.byref(l), C.byref(b)), "bg_program_info")
         return {"executor": "fused", "registers": r.value, "local_bytes": l.value,
                 "blocks_per_sm": b.value, "halo_lanes": self.spec.halo_lanes, "wpt": self.spec.wpt,
-                "adds": self.spec.n_adds, "pre_adds": self.spec.n_pre, "outputs": self.spec.n_outputs}
+                "adds": self.spec.n_adds, "pre_adds": self.spec.n_pre, "outputs": self.spec.n_outputs,
+                "form": "split" if self.spec.n_parts else "single-kernel",
+                "kernels_per_scan": self.kernels_per_scan()}
+
+    def kernels_per_scan(self) -> int:
+        """Kernels one ``Plan.launch`` starts: the prologue; in the split form classify, the carry
+        scan (with pre-pass additions), the work list and execute; else the pre-pass and carry
+        scan (with pre-pass additions) and the main kernel."""
+        pre = self.spec.n_pre > 0
+        if self.spec.n_parts:
+            return 1 + 3 + int(pre)
+        return 1 + 1 + 2 * int(pre)
 
     def tiles_for(self, lengths: Sequence[int]) -> int:
         """Tiles one launch over inputs of these lengths needs."""

@@ -162,6 +162,27 @@ class TermFilter:
     def enabled(self) -> bool:
         return bool(self.table)
 
+    alphabet: int = 0                                     # estimated text alphabet (bit set)
+    sets: List[Optional[Tuple[int, int, int]]] = field(default_factory=list)
+
+    def expected_per_tile(self, positions: int) -> float:
+        """Terms a tile of `positions` bytes is expected to run, taking the text to be uniform
+        over the estimated alphabet (the bytes of the program's narrow classes)."""
+        a = self.alphabet
+        na = bin(a).count("1")
+        if na == 0:
+            return 0.0
+        e = 0.0
+        for r, z in enumerate(self.term_node):
+            if z is None or self.sets[r] is None:
+                e += 1.0
+                continue
+            p = 1.0
+            for s in self.sets[r]:
+                p *= bin(s & a).count("1") / na
+            e += min(1.0, p * positions)
+        return e
+
     def always_mask(self) -> int:
         m = 0
         for r, z in enumerate(self.term_node):
@@ -223,6 +244,14 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 1
         term_cond.append(cond and z is not None)
     pre_node = [best(Z.get(d.nodes[a].args[0], ())) for a in pre]
     f = TermFilter(len(terms), len(pre), term_node, pre_node, term_cond)
+    f.sets = [tri[z] if z is not None else None for z in term_node]
+    # the text's alphabet, as the program sees it: the bytes its filters name
+    alpha = 0
+    for s in f.sets:
+        for x in s or ():
+            if x != ALL:
+                alpha |= x
+    f.alphabet = alpha
     table: Dict[int, int] = {}
     for bit, z in list(enumerate(term_node)) + [(len(terms) + k, z) for k, z in enumerate(pre_node)]:
         if z is None:

@@ -94,3 +94,16 @@ def test_prefilter_is_sound_on_throughput_patterns(wpt):
     assert checked > 10
     # selective: on this text most tiles flag few terms
     assert sum(1 for r, z in enumerate(f.term_node) if z is None) < len(terms) // 4
+
+
+def test_form_follows_expected_selectivity():
+    """On printable text the 256-regex program's filters pass few terms per tile (split form);
+    on a 4-letter DNA text nearly every motif's trigrams occur in every tile (single form)."""
+    from bitgen_gb300.compiler import generate_kernel
+    thr = [compile_group(g) for g in workloads.throughput_patterns(seed=3, n=256).groups(16)]
+    dna = [compile_group(g) for g in workloads.dna_motifs(64, seed=5).groups(4)]
+    assert generate_kernel(thr, Tuning()).n_parts > 0
+    assert generate_kernel(dna, Tuning()).n_parts == 0
+    # the limit can force either form
+    assert generate_kernel(dna, Tuning(prefilter_limit=2.0)).n_parts > 0
+    assert generate_kernel(thr, Tuning(prefilter_limit=0.0)).n_parts == 0
