@@ -1022,6 +1022,25 @@ PRE_CHUNK_OPEN = (
     "    if (g >= p.n_tiles) break;\n"
     "    uint32_t pg[NPRE_WORDS], pp[NPRE_WORDS];\n"
     "    for (int j = 0; j < NPRE_WORDS; ++j) pg[j] = pp[j] = 0u;\n")
+CLS_CHUNK_OPEN = (                   # classify: PRE_CHUNK_OPEN plus the chunk's output zeroing
+    "  const long long rows = (p.n_tiles + 31) >> 5;\n"
+    "  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
+    "  for (long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < rows; c += stride) {\n"
+    "   uint32_t gw[NPRE_WORDS], pw[NPRE_WORDS];\n"
+    "   for (int j = 0; j < NPRE_WORDS; ++j) gw[j] = pw[j] = 0u;\n"
+    "   const int zin = chunk_input(p, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles);\n"
+    "   if (zin >= 0) { @ZERO@ }\n"
+    "   for (int l = 0; l < 32; ++l) {\n"
+    "    const long long g = c * 32 + l;\n"
+    "    if (g >= p.n_tiles) break;\n"
+    "    uint32_t pg[NPRE_WORDS], pp[NPRE_WORDS];\n"
+    "    for (int j = 0; j < NPRE_WORDS; ++j) pg[j] = pp[j] = 0u;\n")
+CLS_CHUNK_CLOSE = (
+    "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
+    "   }\n"
+    "   if (NPRE > 0) pre_flush(p, c, gw, pw, t.lane);\n"
+    "   flush_runs(p, c, runs_s, @ROWRUN@, t.lane);\n"
+    "  }\n")
 PRE_CHUNK_CLOSE = (
     "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
     "   }\n"
@@ -1361,16 +1380,38 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             if m:
                 gen.emit(f"  pp[{j}] |= pz & 0x{m:08x}u;")
         gen.emit("}")
-    for v, k in sorted(gen.pre.items(), key=lambda x: x[1]):
-        n = d.nodes[v]
-        bit = nt + k
-        mode = 0 if n.op == "matchstar" else 1
-        gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
-        m = gen.mat(n.args[0])
-        c = gen.mat(n.args[1])
-        gen.emit(f"uint32_t G, P; pre_aggregate<{gen.dl[v]}, E>(t, {mode}, {gen.pack(m)}, {gen.pack(c)}, G, P); "
-                 f"pg[{k >> 5}] |= G << {k & 31}; pp[{k >> 5}] = (pp[{k >> 5}] & ~(1u << {k & 31})) | (P << {k & 31});")
-        gen.close()
+    # additions whose marker filter fired (a few percent of tiles): out of line, one function per
+    # word of 32 additions, so that the common path stays short in the instruction caches
+    cand_funcs = []
+    saved = (gen.lines, gen.indent, gen.scopes)
+    pre_sorted = sorted(gen.pre.items(), key=lambda x: x[1])
+    for j in range(-(-len(gen.pre) // 32)):
+        gen.lines, gen.indent, gen.scopes = [], 2, [{}]
+        run_bits: Dict[int, int] = {}
+        for v, k in pre_sorted:
+            if k >> 5 != j:
+                continue
+            n = d.nodes[v]
+            bit = nt + k
+            run_bits[bit >> 5] = run_bits.get(bit >> 5, 0) | (1 << (bit & 31))
+            mode = 0 if n.op == "matchstar" else 1
+            gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
+            m = gen.mat(n.args[0])
+            c = gen.mat(n.args[1])
+            gen.emit(f"uint32_t G, P; pre_aggregate<{gen.dl[v]}, E>(t, {mode}, {gen.pack(m)}, {gen.pack(c)}, G, P); "
+                     f"pg |= G << {k & 31}; pm |= 1u << {k & 31}; pv |= P << {k & 31};")
+            gen.close()
+        cand_funcs.append(
+            f"static __device__ __noinline__ uint3 bg_cand_{j}(const Tile &t, {_basis_params(wpt)}) {{\n"
+            f"  constexpr bool E = true;\n"
+            f"  uint32_t pg = 0u, pm = 0u, pv = 0u;\n" + "\n".join(gen.lines) + "\n"
+            f"  return make_uint3(pg, pm, pv);\n}}\n")
+        cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(run_bits.items()))
+        basis_names = ", ".join(f"b{i}_{jj}" for i in range(8) for jj in range(wpt))
+        saved[0].append(" " * saved[1] +
+                        f"if ({cond}) {{ const uint3 cr = bg_cand_{j}(t, {basis_names}); "
+                        f"pg[{j}] |= cr.x; pp[{j}] = (pp[{j}] & ~cr.y) | cr.z; }}")
+    gen.lines, gen.indent, gen.scopes = saved
     for c, pm in sorted(pm_classes.items()):
         ref = gen.mat(c)
         gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
@@ -1382,10 +1423,10 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         ors = " ".join(f"t.run[{w}] |= 0x{(mask >> (32 * w)) & 0xFFFFFFFF:08x}u;"
                        for w in range(nw) if (mask >> (32 * w)) & 0xFFFFFFFF)
         gen.emit(f"if ((({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u) {{ {ors} }}")
-    for w in range(nw):
-        gen.emit(f"if (t.lane == 0) p.runs[{w}LL * p.n_tiles + g] = t.run[{w}];")
+    # run masks: kept in the warp's shared words, stored per chunk (flush_runs)
+    gen.emit("if (t.lane == 0) {" + " ".join(f"runs_s[{w * 32} + l] = t.run[{w}];" for w in range(nw)) + " }")
     if merge:                            # parts OR into the outputs: start every word at zero
-        gen.emit(f"zero_outputs(p, t, {len(names)});")
+        gen.emit(f"if (zin < 0) zero_outputs(p, t, {len(names)});   /* else zeroed per chunk */")
     else:
         for ci, outs_k in enumerate(parts):
             cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
@@ -1402,24 +1443,23 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"//@@BG_PART\n{tables}"
         f"/* per part: {pmw} (run-mask word, mask) pairs; read by the runtime's work-list kernel */\n"
         f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}] = {{\n{_hex_array(pm_table)}\n}};\n'
+        + "".join(cand_funcs) +
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_cls(const __grid_constant__ BgParams p) {{\n'
         f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
+        f"  __shared__ uint32_t bg_runs_s[{warps * nw * 32}];\n"
         f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
         f"  __syncthreads();\n"
+        f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        + PRE_CHUNK_OPEN +
+        + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
         f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
-        f"    if (t.lane == 0) {{ /* row summaries for the work list (zeroed by the launch) */\n"
-        f"      uint32_t *rowrun = p.work + 1 + {len(parts)}LL * (1 + rows);\n"
-        + "".join(f"      if (t.run[{w}]) atomicOr(rowrun + {w}LL * rows + c, t.run[{w}]);\n" for w in range(nw)) +
-        f"    }}\n"
-        + PRE_CHUNK_CLOSE +
+        + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + 1 + {len(parts)}LL * (1 + rows)") +
         f"}}\n")
     warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))

@@ -949,6 +949,62 @@ __device__ __forceinline__ void zero_outputs(const BgParams &p, const Tile &t, i
   }
 }
 
+/* Split form, classify: the input holding all of tiles g0 .. g1-1, or -1 when they span
+ * several inputs. */
+__device__ __forceinline__ int chunk_input(const BgParams &p, long long g0, long long g1) {
+  int lo = 0, hi = p.n_inputs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (p.tile_prefix[mid] <= g0) lo = mid; else hi = mid;
+  }
+  return p.tile_prefix[lo + 1] >= g1 ? lo : -1;
+}
+
+/* Zero words [lo, hi) of dst with the warp: scalar stores up to a 16-byte boundary, then
+ * 16-byte stores, then the scalar tail. */
+__device__ __forceinline__ void zero_span(uint32_t *dst, long long lo, long long hi, int lane) {
+  if (hi <= lo) return;
+  const unsigned mis = (unsigned)(((16u - ((unsigned)(unsigned long long)(dst + lo) & 15u)) & 15u) >> 2);
+  const long long head = lo + mis < hi ? lo + mis : hi;
+  if (lo + lane < head) dst[lo + lane] = 0u;
+  const long long nv = (hi - head) >> 2;
+  uint4 *v = reinterpret_cast<uint4 *>(dst + head);
+  for (long long i = lane; i < nv; i += 32) v[i] = make_uint4(0u, 0u, 0u, 0u);
+  const long long tail = head + 4 * nv;
+  if (tail + lane < hi) dst[tail + lane] = 0u;
+}
+
+/* Split form with merged outputs, classify: zero the words of outputs 0..n-1 that tiles
+ * g0 .. g1-1 of input `in` write (what zero_outputs does tile by tile). */
+__device__ __forceinline__ void zero_chunk(const BgParams &p, int in, long long g0, long long g1,
+                                           int n, int lane) {
+  if (!p.out) return;
+  const long long first = p.tile_prefix[in];
+  const long long W = (p.in_len[in] + 31) >> 5;
+  long long lo = (g0 - first) * SW, hi = (g1 - first) * SW;
+  if (hi > W) hi = W;
+  uint32_t *dst = p.out + p.out_off[in];
+  for (int o = 0; o < n; ++o, dst += p.out_stride) zero_span(dst, lo, hi, lane);
+}
+
+/* Split form, classify: store the run masks of chunk c's tiles (kept by lane 0 in the warp's
+ * shared words rs[w * 32 + l]) with one coalesced store per mask word, and the chunk's row
+ * summary (OR over its tiles) that the work-list kernel reads. */
+__device__ __forceinline__ void flush_runs(const BgParams &p, long long c, const uint32_t *rs,
+                                           uint32_t *rowrun, int lane) {
+  __syncwarp();
+  const long long rows = (p.n_tiles + 31) >> 5;
+  const long long g = c * 32 + lane;
+#pragma unroll
+  for (int w = 0; w < BG_NRUN; ++w) {
+    const uint32_t v = g < p.n_tiles ? rs[w * 32 + lane] : 0u;
+    if (g < p.n_tiles) p.runs[(long long)w * p.n_tiles + g] = v;
+    const uint32_t s = __reduce_or_sync(FULL, v);
+    if (lane == 0) rowrun[(long long)w * rows + c] = s;
+  }
+  __syncwarp();
+}
+
 /* Split form: a part's accumulators hold only its own outputs (local index). */
 __device__ __forceinline__ void acc_clear_n(uint32_t *acc, const Tile &t, int n) {
   for (int i = 0; i < n * WPT; ++i) acc[i * 32 + t.lane] = 0u;

@@ -745,15 +745,13 @@ int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t deb
 static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaStream_t s) {
   void *args[] = {&prm};
   if (prog->cls_kernel) {
-    /* split form: classify every tile (it also zeroes the words of the outputs no part will
-     * write on that tile), scan the pre-pass carries, then run the parts */
+    /* split form: classify every tile (it also zeroes the output words the parts OR into, and
+     * writes every row's summary of run masks), scan the pre-pass carries, list each part's
+     * rows with work, then run the parts */
     const int warps_per_block = prog->desc.block / 32;
     const int64_t rows = (prm.n_tiles + 31) / 32;
     if (!prog->pmask || prog->desc.n_parts > 4096)
       return fail(BG_ERR_INVALID, "split-form launch: no part table or more than 4096 parts");
-    /* the row summaries start at zero; classify ORs every tile's run masks into its row */
-    BG_CUDA(cudaMemsetAsync(prm.work + 1 + (int64_t)prog->desc.n_parts * (1 + rows), 0,
-                            sizeof(uint32_t) * (size_t)prog->desc.n_run * (size_t)rows, s));
     const int64_t need = (rows + warps_per_block - 1) / warps_per_block;
     const int cls_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
