@@ -21,9 +21,9 @@ from .engine import Inputs, Program, _ensure_cache_dir, out_layout
 from .pablo import Group
 
 SPACE = [
-    Tuning(),                                              # split form, merged 4-term parts
-    Tuning(part_cap=2),
-    Tuning(part_cap=8),
+    Tuning(),                                              # split form, merged 2-term parts
+    Tuning(part_cap=1),
+    Tuning(part_cap=4, exec_groups=8),
     Tuning(merge_outputs=False, part_cap=32),              # parts of whole outputs
     Tuning(wpt=2, min_blocks=3),
     Tuning(wpt=1, min_blocks=4, part_cap=32, prefilter=False),

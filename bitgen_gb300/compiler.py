@@ -314,8 +314,10 @@ class Dag:
 class Tuning:
     wpt: int = 1            # 32-bit words per lane
     block: int = 256        # threads per CTA
-    skip_interval: int = 1  # check for an all-zero marker every k AND steps (0 = never)
-    part_cap: int = 0       # most OR-ed terms one part function computes (0: 4 in the split
+    skip_interval: int = -1  # check for an all-zero marker every k AND steps (0 = never; -1:
+                             # never in the split form, whose tiles mostly hold the marker's
+                             # trigram, every AND in the single-kernel form)
+    part_cap: int = 0       # most OR-ed terms one part function computes (0: 2 in the split
                             # form, 32 in the single-kernel form)
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
     min_blocks: int = 4     # __launch_bounds__ minimum resident blocks per SM (caps registers)
@@ -331,12 +333,13 @@ class Tuning:
                                    # this fraction of the terms (text taken as uniform over
                                    # the bytes the filters name)
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
+    exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
-                self.merge_outputs, self.bloom_bits, self.prefilter_limit)
+                self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups)
 
 
 @dataclass
@@ -1116,6 +1119,9 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         if not filt.enabled or (filt.expected_per_tile(positions) >
                                 tuning.prefilter_limit * len(terms)):
             filt = None                  # the filter would pass most terms: single-kernel form
+    if tuning.skip_interval < 0:
+        tuning = replace(tuning, skip_interval=0 if filt is not None else 1)
+        gen.t = tuning
     if filt is not None:
         return _generate_filtered(gen, tuning, terms, names, filt, name)
     budget = SMEM_BUDGET
@@ -1295,7 +1301,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     by_out: Dict[int, List[int]] = {}
     for r, (v, o) in enumerate(terms):
         by_out.setdefault(o, []).append(r)
-    cap = max(1, tuning.part_cap or 4)
+    cap = max(1, tuning.part_cap or 2)
     merge = tuning.merge_outputs
     part_terms: List[List[int]] = []     # terms of each part, in output order
     if merge:
@@ -1341,6 +1347,14 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
                      f"  constexpr bool E = true;\n"
                      f"  acc_clear_n(acc, t, {len(outs_k)});\n" + "\n".join(blocks) + "\n" + stores + "\n}\n")
     decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
+    # execute order: part k belongs to group k % ngroups; groups one after the other
+    ngroups = max(1, min(16, tuning.exec_groups, len(parts)))
+    ord_ = [k for gi in range(ngroups) for k in range(gi, len(parts), ngroups)]
+    gpos = [0]
+    for gi in range(ngroups):
+        gpos.append(gpos[-1] + len(range(gi, len(parts), ngroups)))
+    decls += (f"\n__constant__ int bg_ord[{len(parts)}] = {{{', '.join(map(str, ord_))}}};"
+              f"\n__constant__ int bg_gpos[{ngroups + 1}] = {{{', '.join(map(str, gpos))}}};")
     ba = ", ".join(f"b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
     pmw = max(1, max(len(m) for m in part_masks))
     pm_table = []
@@ -1432,12 +1446,13 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
             gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
     cls_code = "\n".join(gen.lines)
-    log2, keys, masks_tab = filt.exact()
+    log2, keys, masks_tab, ext_tab = filt.exact()
     bloom = filt.bloom(tuning.bloom_bits)
     tables = (f"#define BG_EXLOG2 {log2}\n"
               f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
               f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
-              f"static __device__ const uint32_t bg_exmasks[{len(masks_tab)}] = {{\n{_hex_array(masks_tab)}\n}};\n")
+              f"static __device__ const uint32_t bg_exmasks[{len(masks_tab)}] = {{\n{_hex_array(masks_tab)}\n}};\n"
+              f"static __device__ const uint32_t bg_exext[{len(ext_tab)}] = {{\n{_hex_array(ext_tab)}\n}};\n")
     basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
     cls_kernel = (
         f"//@@BG_PART\n{tables}"
@@ -1447,7 +1462,9 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_cls(const __grid_constant__ BgParams p) {{\n'
         f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
         f"  __shared__ uint32_t bg_runs_s[{warps * nw * 32}];\n"
+        f"  __shared__ uint32_t bg_exkeys_s[{len(keys)}];\n"
         f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
+        f"  for (int i = threadIdx.x; i < {len(keys)}; i += blockDim.x) bg_exkeys_s[i] = bg_exkeys[i];\n"
         f"  __syncthreads();\n"
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
         f"  Tile t;\n"
@@ -1455,11 +1472,11 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
-        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys, bg_exmasks, BG_EXLOG2);\n"
+        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exmasks, bg_exext, BG_EXLOG2);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
-        + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + 1 + {len(parts)}LL * (1 + rows)") +
+        + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + BG_WORK_HEAD + {len(parts)}LL * (1 + rows)") +
         f"}}\n")
     warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
@@ -1491,30 +1508,40 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  init(p, t);\n"
         f"  __shared__ unsigned int bg_pref[{len(parts) + 1}];\n"
         f"  if (threadIdx.x < 32) {{\n"
-        f"    /* part-major order: exclusive prefix of the parts' row counts */\n"
+        f"    /* group-major, then part-major order (bg_ord): exclusive prefix of the row counts */\n"
         f"    const int per = ({len(parts)} + 31) / 32, lo = threadIdx.x * per;\n"
         f"    unsigned int sum = 0u;\n"
-        f"    for (int i = lo; i < lo + per && i < {len(parts)}; ++i) sum += __ldg(p.work + 1 + i);\n"
+        f"    for (int i = lo; i < lo + per && i < {len(parts)}; ++i) sum += __ldg(p.work + BG_WORK_HEAD + bg_ord[i]);\n"
         f"    unsigned int incl = sum;\n"
         f"    for (int d = 1; d < 32; d <<= 1) {{\n"
         f"      const unsigned int y = __shfl_up_sync(FULL, incl, d);\n"
         f"      if ((int)threadIdx.x >= d) incl += y;\n"
         f"    }}\n"
         f"    unsigned int at = incl - sum;\n"
-        f"    for (int i = lo; i < lo + per && i < {len(parts)}; ++i) {{ bg_pref[i] = at; at += __ldg(p.work + 1 + i); }}\n"
+        f"    for (int i = lo; i < lo + per && i < {len(parts)}; ++i) {{ bg_pref[i] = at; at += __ldg(p.work + BG_WORK_HEAD + bg_ord[i]); }}\n"
         f"    if (threadIdx.x == 31) bg_pref[{len(parts)}] = incl;\n"
         f"  }}\n"
         f"  __syncthreads();\n"
-        f"  const unsigned int items = bg_pref[{len(parts)}];\n"
         f"  const long long rows = (p.n_tiles + 31) >> 5;\n"
+        f"  /* the warps of an SM start on their group's parts (fewer part bodies per SM in the\n"
+        f"     instruction caches) and take other groups' items once their own run out */\n"
+        f"  unsigned int smid;\n"
+        f"  asm(\"mov.u32 %0, %%smid;\" : \"=r\"(smid));\n"
+        f"  int grp = (int)(smid % {ngroups}u), tried = 0;\n"
         f"  for (;;) {{\n"
+        f"    const unsigned int gb = bg_pref[bg_gpos[grp]], ge = bg_pref[bg_gpos[grp + 1]];\n"
         f"    unsigned int it = 0u;\n"
-        f"    if (t.lane == 0) it = atomicAdd(p.state, 1u);\n"
+        f"    if (t.lane == 0) it = gb < ge ? gb + atomicAdd(p.work + grp, 1u) : ge;\n"
         f"    it = __shfl_sync(FULL, it, 0);\n"
-        f"    if (it >= items) break;\n"
-        f"    int k = 0, hi = {len(parts)};\n"
-        f"    while (hi - k > 1) {{ const int m = (k + hi) >> 1; if (bg_pref[m] <= it) k = m; else hi = m; }}\n"
-        f"    const long long g0 = (long long)__ldg(p.work + 1 + {len(parts)} + (long long)k * rows + (it - bg_pref[k])) * 32;\n"
+        f"    if (it >= ge) {{\n"
+        f"      if (++tried >= {ngroups}) break;\n"
+        f"      grp = grp + 1 < {ngroups} ? grp + 1 : 0;\n"
+        f"      continue;\n"
+        f"    }}\n"
+        f"    int j = bg_gpos[grp], hi = bg_gpos[grp + 1];\n"
+        f"    while (hi - j > 1) {{ const int m = (j + hi) >> 1; if (bg_pref[m] <= it) j = m; else hi = m; }}\n"
+        f"    const int k = bg_ord[j];\n"
+        f"    const long long g0 = (long long)__ldg(p.work + BG_WORK_HEAD + {len(parts)} + (long long)k * rows + (it - bg_pref[j])) * 32;\n"
         f"    const long long g = g0 + t.lane;\n"
         f"    bool want = false;\n"
         f"    if (g < p.n_tiles) {{\n"

@@ -793,40 +793,56 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
 #if BG_PREFILTER
 /* Trigram prefilter (tables generated by bitgen_gb300/prefilter.py).  Every trigram lying in
  * the bytes this warp computes is hashed into the Bloom bitmap `bloom` (2^BG_BLOOM_BITS bits,
- * shared memory); a hit is resolved in the exact open-addressed table (keys: trigram | 1 << 31, 0 =
- * empty; BG_NRUN mask words per slot), whose mask is OR-ed into the tile's run mask.  The
+ * shared memory); a hit is resolved in the exact open-addressed table (keys in shared memory:
+ * trigram | 1 << 31, 0 = empty; BG_NRUN mask words per slot in global memory), whose mask is
+ * OR-ed into the tile's run mask.  The
  * trigram ending at byte q is byte(q-2) | byte(q-1) << 8 | byte(q) << 16; bytes before the
  * warp's first byte read as zero. */
 constexpr uint32_t BLOOM_HASH = 0x9E3779B1u, EXACT_HASH = 0x85EBCA6Bu;
 
-static __device__ __noinline__ void trigram_exact(uint32_t key, const uint32_t *keys,
-                                                  const uint32_t *masks, int log2, uint32_t *run) {
+/* Exact lookup of a trigram whose Bloom bit is set.  `pre3` holds the three bytes before the
+ * trigram (3 back in bits 0-7, 4 back in 8-15, 5 back in 16-23).  A slot has BG_NRUN + 1 words
+ * in `masks`: the bits the trigram sets by itself, then ext_start << 8 | ext_count; extension
+ * record i is ext[2i] = bytes | count << 24 and ext[2i + 1] = the bit it sets when the first
+ * `count` bytes of pre3 equal `bytes`. */
+static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
+                                                  const uint32_t *keys, const uint32_t *masks,
+                                                  const uint32_t *ext, int log2, uint32_t *run) {
   const uint32_t slots = 1u << log2;
   uint32_t s = (key * EXACT_HASH) >> (32 - log2);
   for (uint32_t it = 0; it < slots; ++it) {
-    const uint32_t k = __ldg(keys + s);
+    const uint32_t k = keys[s]; /* keys: shared memory */
     if (k == 0u) return;
     if (k == (key | 0x80000000u)) {
+      const uint32_t *m = masks + s * (BG_NRUN + 1);
 #pragma unroll
-      for (int w = 0; w < BG_NRUN; ++w) run[w] |= __ldg(masks + s * BG_NRUN + w);
+      for (int w = 0; w < BG_NRUN; ++w) run[w] |= __ldg(m + w);
+      const uint32_t e = __ldg(m + BG_NRUN);
+      for (uint32_t i = e >> 8, n = e & 255u; n > 0u; --n, ++i) {
+        const uint32_t r = __ldg(ext + 2 * i), bit = __ldg(ext + 2 * i + 1);
+        const uint32_t cmp = (1u << (8u * (r >> 24))) - 1u; /* count <= 3 */
+        if (((pre3 ^ r) & cmp) == 0u && bit < 32u * BG_NRUN) run[bit >> 5] |= 1u << (bit & 31u);
+      }
       return;
     }
     s = (s + 1u) & (slots - 1u);
   }
 }
 
-__device__ __forceinline__ void trigram_test(uint32_t key, const uint32_t *bloom,
-                                             const uint32_t *keys, const uint32_t *masks, int log2,
-                                             uint32_t *run) {
-  const uint32_t h = (key * BLOOM_HASH) >> (32 - BG_BLOOM_BITS);
-  if ((bloom[h >> 5] >> (h & 31u)) & 1u) trigram_exact(key, keys, masks, log2, run);
+/* The Bloom bit of `key`, moved to bit q (a rotation, so that the probes of several keys OR
+ * into one word of hits).  Bit h of the bitmap, h = the top BG_BLOOM_BITS bits of
+ * key * BLOOM_HASH, is bit h % 32 of word h / 32. */
+__device__ __forceinline__ uint32_t bloom_probe(uint32_t key, const uint32_t *bloom, int q) {
+  const uint32_t h = key * BLOOM_HASH;
+  const uint32_t w = bloom[h >> (37 - BG_BLOOM_BITS)];
+  return __funnelshift_r(w, w, (h >> (32 - BG_BLOOM_BITS)) - (uint32_t)q) & (1u << q);
 }
 
 /* Load the tile's bytes, fill t.run from the trigram scan (warp-uniform) and transpose the bytes
  * into the basis.  Inputs given as basis planes have no bytes to scan: every term runs. */
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
                                           const uint32_t *bloom, const uint32_t *keys,
-                                          const uint32_t *masks, int log2) {
+                                          const uint32_t *masks, const uint32_t *ext, int log2) {
   uint32_t run[BG_NRUN];
 #pragma unroll
   for (int w = 0; w < BG_NRUN; ++w) run[w] = 0u;
@@ -840,17 +856,42 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
 #pragma unroll
   for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
   uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
-  if (t.lane == 0) prev = 0u;
+  uint32_t pprev = __shfl_up_sync(FULL, raw[WPT - 1][6], 1);
+  if (t.lane == 0) prev = pprev = 0u;
+  /* eight trigrams (two words) per step: all Bloom probes first, then the rare exact lookups.
+   * Trigram q ends at byte 8 + q of the window pprev, prev, c0, c1 (bytes 0-15); its pre3 is
+   * bytes 5 + q, 4 + q, 3 + q of the window. */
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t cur = raw[j][i];
-      trigram_test(__byte_perm(prev, cur, 0x0432) & 0xFFFFFFu, bloom, keys, masks, log2, run);
-      trigram_test(__byte_perm(prev, cur, 0x0543) & 0xFFFFFFu, bloom, keys, masks, log2, run);
-      trigram_test(cur & 0xFFFFFFu, bloom, keys, masks, log2, run);
-      trigram_test(cur >> 8, bloom, keys, masks, log2, run);
-      prev = cur;
+    for (int i = 0; i < 8; i += 2) {
+      const uint32_t c0 = raw[j][i], c1 = raw[j][i + 1];
+      uint32_t k[8];
+      k[0] = __byte_perm(prev, c0, 0x0432) & 0xFFFFFFu;
+      k[1] = __byte_perm(prev, c0, 0x0543) & 0xFFFFFFu;
+      k[2] = c0 & 0xFFFFFFu;
+      k[3] = c0 >> 8;
+      k[4] = __byte_perm(c0, c1, 0x0432) & 0xFFFFFFu;
+      k[5] = __byte_perm(c0, c1, 0x0543) & 0xFFFFFFu;
+      k[6] = c1 & 0xFFFFFFu;
+      k[7] = c1 >> 8;
+      uint32_t hb = 0u;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) hb |= bloom_probe(k[q], bloom, q);
+      if (hb) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if ((hb >> q) & 1u) {
+            const uint32_t sel = q < 3 ? 0x0345u + 0x111u * q : q == 3 || q == 7 ? 0x0234u
+                                                               : 0x0345u + 0x111u * (q - 4);
+            const uint32_t lo = q < 3 ? pprev : q < 7 ? prev : c0;
+            const uint32_t hi = q < 3 ? prev : q < 7 ? c0 : c1;
+            const uint32_t pre3 = __byte_perm(lo, hi, sel) & 0xFFFFFFu;
+            trigram_exact(k[q], pre3, keys, masks, ext, log2, run);
+          }
+      }
+      pprev = c0;
+      prev = c1;
     }
   }
 #pragma unroll

@@ -49,12 +49,16 @@ typedef struct BgParams {
   int64_t debug_wait_tile;   /* tile that first waits on the never-written record, or -1 */
   uint32_t *runs;            /* split form: [n_run][n_tiles] per-tile run masks, or NULL   */
   uint32_t *pre_bits;        /* pre-pass bitmaps, 3 * ceil(n_tiles / 32) words per addition */
-  uint32_t *work;            /* split form, R = ceil(n_tiles / 32) rows of 32 tiles:
-                                [1 + p] = number of rows part p runs on; at 1 + n_parts + p * R
-                                those rows (ascending); at 1 + n_parts * (1 + R) the OR of each
-                                row's run masks, [n_run][R]                                    */
+  uint32_t *work;            /* split form, R = ceil(n_tiles / 32) rows of 32 tiles, H =
+                                BG_WORK_HEAD: [0, H) the execute pass's claim counters (one
+                                per group of SMs); [H + p] = number of rows part p runs on; at
+                                H + n_parts + p * R those rows (ascending); at
+                                H + n_parts * (1 + R) the OR of each row's run masks, [n_run][R] */
   int32_t n_inputs;
   int32_t input_kind;
 } BgParams;
+
+/* Words before the part counts in BgParams.work: the execute pass's claim counters. */
+#define BG_WORK_HEAD 16
 
 #endif

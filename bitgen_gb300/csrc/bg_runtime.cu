@@ -174,7 +174,8 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits,
  * something to run, a row being 32 consecutive tiles.  The classify pass leaves, for every row
  * and run-mask word, the OR of the row's 32 masks (`rowrun`, [n_run][rows]); part p has work in
  * a row when one of its (word, mask) pairs (`pmask`) meets it.  Block p lists part p's rows in
- * increasing order at work + 1 + n_parts + p * rows and stores their count at work[1 + p]:
+ * increasing order at work + H + n_parts + p * rows and stores their count at work[H + p]
+ * (H = BG_WORK_HEAD; block 0 also zeroes the execute pass's claim counters, work[0, H)):
  * each warp takes a contiguous block of rows, 32 rows per step (one per lane, coalesced loads,
  * a ballot to keep them in order), and the warps' counts are scanned across the block.  The
  * execute pass orders the parts one after the other (part-major, so that the whole GPU runs one
@@ -187,7 +188,8 @@ __global__ void __launch_bounds__(1024) bg_work_list_kernel(const uint32_t *rowr
   const int p = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
-  uint32_t *out = work + 1 + n_parts + (int64_t)p * rows;
+  uint32_t *out = work + BG_WORK_HEAD + n_parts + (int64_t)p * rows;
+  if (p == 0 && threadIdx.x < BG_WORK_HEAD) work[threadIdx.x] = 0u;
   const int64_t steps = (rows + 31) / 32;
   const int64_t per = (steps + nwarps - 1) / nwarps;
   const int64_t s0 = (int64_t)warp * per < steps ? (int64_t)warp * per : steps;
@@ -216,13 +218,14 @@ __global__ void __launch_bounds__(1024) bg_work_list_kernel(const uint32_t *rowr
     if ((b >> lane) & 1u) out[pos + __popc(b & ((1u << lane) - 1u))] = (uint32_t)(st * 32 + lane);
     pos += __popc(b);
   }
-  if (threadIdx.x == 0) work[1 + p] = total;
+  if (threadIdx.x == 0) work[BG_WORK_HEAD + p] = total;
 }
 
 /* 32-bit words of the split form's work list (counts, rows per part, row summaries). */
 int64_t work_words(const bg_kernel_desc &d, int64_t tiles) {
   const int64_t rows = (tiles + 31) / 32;
-  return d.n_run > 0 ? 1 + (int64_t)d.n_parts * (1 + rows) + (int64_t)d.n_run * rows : 0;
+  return d.n_run > 0 ? BG_WORK_HEAD + (int64_t)d.n_parts * (1 + rows) + (int64_t)d.n_run * rows
+                    : 0;
 }
 
 /* 64-bit words of a records buffer for `tiles` tiles: one look-back record per addition and
@@ -763,7 +766,8 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
       BG_CUDA(cudaGetLastError());
     }
     bg_work_list_kernel<<<std::max(1, prog->desc.n_parts), 1024, 0, s>>>(
-        prm.work + 1 + (int64_t)prog->desc.n_parts * (1 + rows), prog->pmask, prog->pmw, prm.work,
+        prm.work + BG_WORK_HEAD + (int64_t)prog->desc.n_parts * (1 + rows), prog->pmask, prog->pmw,
+        prm.work,
         prog->desc.n_parts, rows);
     BG_CUDA(cudaGetLastError());
     const int main_grid = (int)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm);

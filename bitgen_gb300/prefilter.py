@@ -19,6 +19,12 @@ filter, preferring one that does not pass through a pre-pass addition; a term wi
 always runs.  Each pre-pass addition gets the filter of its marker,
 so the pre-pass can skip the marker's computation too.
 
+Extensions.  Where the filter node's bounds also fix single bytes 3, 4 and 5 positions back,
+the trigram alone would pass the term on every chance occurrence of its last three bytes; the
+table then holds, under the trigram, an extension record (those bytes and the term's bit), and
+the kernel sets the bit only when the bytes before the trigram match.  On printable text this
+makes the chance hits of literal filters about a hundred times rarer per byte of extension.
+
 The kernel tests every trigram of the tile against a Bloom bitmap (2^18 bits by default, in
 shared memory: a warp takes the slow path whenever any of its 32 lanes hits, so the bitmap is
 sized for a per-lane false-hit rate well below 1/32) and resolves the rare hits in an exact open-addressed table that maps a trigram to the bit mask
@@ -32,6 +38,8 @@ from typing import Dict, FrozenSet, List, Optional, Sequence, Tuple
 
 ALL = (1 << 256) - 1
 MAX_SET = 4096          # largest trigram set one filter may carry
+MAX_EXT = 3             # bytes before the trigram an extension record may fix
+EXT_DEPTH = 3 + MAX_EXT
 BLOOM_BITS = 18         # log2 of the Bloom bitmap size (32 KB of shared memory)
 HASH_BLOOM = 0x9E3779B1
 HASH_EXACT = 0x85EBCA6B
@@ -148,7 +156,10 @@ class TermFilter:
     term_node: List[Optional[int]]
     pre_node: List[Optional[int]]
     term_cond: List[bool] = field(default_factory=list)  # filter implies zero only if no carry
-    table: Dict[int, int] = field(default_factory=dict)   # trigram -> bit mask
+    table: Dict[int, int] = field(default_factory=dict)   # trigram -> bits it sets by itself
+    # trigram -> extension records (bytes 3, 4, 5 positions back packed low byte first, their
+    # number, bit): the bit is set when those bytes precede the trigram
+    ext: Dict[int, List[Tuple[int, int, int]]] = field(default_factory=dict)
 
     @property
     def n_bits(self) -> int:
@@ -183,6 +194,16 @@ class TermFilter:
             e += min(1.0, p * positions)
         return e
 
+    def match(self, trigram: int, pre3: int) -> int:
+        """Bits set by `trigram` when the three bytes before it, packed like the records
+        (byte 3 back in bits 0-7), are `pre3`."""
+        m = self.table.get(trigram, 0)
+        for b, n, bit in self.ext.get(trigram, ()):
+            mask = (1 << (8 * n)) - 1
+            if (pre3 ^ b) & mask == 0:
+                m |= 1 << bit
+        return m
+
     def always_mask(self) -> int:
         m = 0
         for r, z in enumerate(self.term_node):
@@ -200,24 +221,33 @@ class TermFilter:
             words[h >> 5] |= 1 << (h & 31)
         return words
 
-    def exact(self) -> Tuple[int, List[int], List[int]]:
-        """(log2 slots, keys, mask words): open addressing with linear probing; a key slot
-        holds trigram | 1 << 31 (0 = empty); masks are ``words`` words per slot."""
+    def exact(self) -> Tuple[int, List[int], List[int], List[int]]:
+        """(log2 slots, keys, mask words, extension words): open addressing with linear
+        probing; a key slot holds trigram | 1 << 31 (0 = empty); per slot ``words`` mask words
+        and one word ext_start << 8 | ext_count; an extension record is two words, bytes |
+        count << 24 and the bit."""
         n = len(self.table)
         log2 = 4
         while (1 << log2) < 2 * max(1, n):
             log2 += 1
         slots = 1 << log2
+        stride = self.words + 1
         keys = [0] * slots
-        masks = [0] * (slots * self.words)
+        masks = [0] * (slots * stride)
+        ext: List[int] = []
         for key, m in sorted(self.table.items()):
             s = exact_hash(key, log2)
             while keys[s]:
                 s = (s + 1) & (slots - 1)
             keys[s] = key | (1 << 31)
             for w in range(self.words):
-                masks[s * self.words + w] = (m >> (32 * w)) & 0xFFFFFFFF
-        return log2, keys, masks
+                masks[s * stride + w] = (m >> (32 * w)) & 0xFFFFFFFF
+            recs = self.ext.get(key, [])
+            assert len(recs) < 256 and len(ext) // 2 < (1 << 24)
+            masks[s * stride + self.words] = ((len(ext) // 2) << 8) | len(recs)
+            for b, cnt, bit in recs:
+                ext += [b | (cnt << 24), bit]
+        return log2, keys, masks, ext or [0, 0]
 
 
 def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 16) -> TermFilter:
@@ -229,9 +259,22 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 1
     # which a '.*' after its first match almost never is; other additions are checked anyway
     Zp = zero_sets(gen, tri, blocked=frozenset(pre))
     d = gen.d
+    deep = position_bounds(gen, depth=EXT_DEPTH)
+
+    def fixed_before(z) -> List[int]:
+        """Single bytes that the bounds of z fix 3, 4, 5 positions back (stopping at the
+        first position that is not a single byte)."""
+        out = []
+        for k in range(3, EXT_DEPTH):
+            s = deep[z][k]
+            if s == ALL or bin(s).count("1") != 1:
+                break
+            out.append(s.bit_length() - 1)
+        return out
 
     def best(zs) -> Optional[int]:
-        cands = sorted(zs, key=lambda z: (_set_size(tri[z]), z))
+        # smallest trigram set, then the longest extension (fewest chance hits)
+        cands = sorted(zs, key=lambda z: (_set_size(tri[z]), -len(fixed_before(z)), z))
         return cands[0] if cands else None
 
     term_node, term_cond = [], []
@@ -253,12 +296,20 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 1
                 alpha |= x
     f.alphabet = alpha
     table: Dict[int, int] = {}
+    ext: Dict[int, List[Tuple[int, int, int]]] = {}
     for bit, z in list(enumerate(term_node)) + [(len(terms) + k, z) for k, z in enumerate(pre_node)]:
         if z is None:
             continue
+        fixed = fixed_before(z)
+        packed = sum(b << (8 * i) for i, b in enumerate(fixed))
         for key in trigram_set(tri[z]):
-            table[key] = table.get(key, 0) | (1 << bit)
-    if len(table) > tri_limit:
-        table = {}
+            if fixed:
+                table.setdefault(key, 0)
+                ext.setdefault(key, []).append((packed, len(fixed), bit))
+            else:
+                table[key] = table.get(key, 0) | (1 << bit)
+    if len(table) > tri_limit or any(len(r) > 255 for r in ext.values()):
+        table, ext = {}, {}
     f.table = table
+    f.ext = ext
     return f
