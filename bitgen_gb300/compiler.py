@@ -328,7 +328,9 @@ class Tuning:
     lookback_spin: int = 0   # look-back polls before sleeping
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
     prefilter: bool = True   # run a term only in tiles holding one of its trigrams
-    bloom_bits: int = 18     # prefilter: log2 of the Bloom bitmap's size (shared memory)
+    bloom_bits: int = 20     # prefilter: log2 of the Bloom bitmap's size (shared memory)
+    cls_block: int = 1024    # split form: threads per classify block (one block per SM holds
+                             # the Bloom bitmap, the exact keys and the warps' run masks)
     prefilter_limit: float = 0.25  # prefilter only while a tile is expected to run fewer than
                                    # this fraction of the terms (text taken as uniform over
                                    # the bytes the filters name)
@@ -339,7 +341,8 @@ class Tuning:
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
-                self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups)
+                self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
+                self.cls_block)
 
 
 @dataclass
@@ -1454,15 +1457,23 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
               f"static __device__ const uint32_t bg_exmasks[{len(masks_tab)}] = {{\n{_hex_array(masks_tab)}\n}};\n"
               f"static __device__ const uint32_t bg_exext[{len(ext_tab)}] = {{\n{_hex_array(ext_tab)}\n}};\n")
     basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+    cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
+    cls_warps = cls_block // 32
+    cls_smem = 4 * (len(bloom) + len(keys) + cls_warps * nw * 32)
+    if cls_smem > 227 * 1024:
+        raise NotFusable(f"classify needs {cls_smem} bytes of shared memory; lower bloom_bits or cls_block")
     cls_kernel = (
         f"//@@BG_PART\n{tables}"
         f"/* per part: {pmw} (run-mask word, mask) pairs; read by the runtime's work-list kernel */\n"
         f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}] = {{\n{_hex_array(pm_table)}\n}};\n'
         + "".join(cand_funcs) +
-        f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}_cls(const __grid_constant__ BgParams p) {{\n'
-        f"  __shared__ uint32_t bg_bloom_s[{len(bloom)}];\n"
-        f"  __shared__ uint32_t bg_runs_s[{warps * nw * 32}];\n"
-        f"  __shared__ uint32_t bg_exkeys_s[{len(keys)}];\n"
+        f"/* classify launch: threads per block, bytes of dynamic shared memory (read by the runtime) */\n"
+        f'extern "C" __device__ const uint32_t bg_cls_cfg[2] = {{{cls_block}u, {cls_smem}u}};\n'
+        f'extern "C" __global__ void __launch_bounds__({cls_block}, 1) {name}_cls(const __grid_constant__ BgParams p) {{\n'
+        f"  extern __shared__ uint32_t bg_dyn_s[];\n"
+        f"  uint32_t *bg_bloom_s = bg_dyn_s;                            /* {len(bloom)} words */\n"
+        f"  uint32_t *bg_exkeys_s = bg_dyn_s + {len(bloom)};            /* {len(keys)} words */\n"
+        f"  uint32_t *bg_runs_s = bg_dyn_s + {len(bloom) + len(keys)};  /* {cls_warps * nw * 32} words */\n"
         f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
         f"  for (int i = threadIdx.x; i < {len(keys)}; i += blockDim.x) bg_exkeys_s[i] = bg_exkeys[i];\n"
         f"  __syncthreads();\n"

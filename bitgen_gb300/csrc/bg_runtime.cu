@@ -272,6 +272,7 @@ struct bg_program {
   const uint32_t *pmask = nullptr;   /* split form: per part, pmw (word, mask) pairs        */
   int pmw = 0;
   int regs = 0, local_bytes = 0, blocks_per_sm = 1, pre_blocks_per_sm = 1;
+  int cls_block = 0, cls_smem = 0; /* classify launch (bg_cls_cfg of the program)          */
 };
 
 struct bg_plan {
@@ -530,6 +531,27 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
       p->pmask = static_cast<const uint32_t *>(pm);
       p->pmw = (int)(pm_bytes / (sizeof(uint32_t) * 2 * (size_t)std::max(1, desc->n_parts)));
     }
+    /* classify's block size and dynamic shared memory; programs without the table use the
+     * program's block and static shared memory */
+    void *cfg = nullptr;
+    size_t cfg_bytes = 0;
+    p->cls_block = desc->block;
+    if (e == cudaSuccess &&
+        cudaLibraryGetGlobal(&cfg, &cfg_bytes, p->lib, "bg_cls_cfg") == cudaSuccess &&
+        cfg_bytes >= 2 * sizeof(uint32_t)) {
+      uint32_t c[2] = {0, 0};
+      e = cudaMemcpy(c, cfg, sizeof c, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess && (c[0] == 0 || c[0] > 1024 || c[0] % 32 != 0 || c[1] > 227u * 1024u))
+        e = cudaErrorInvalidValue;
+      if (e == cudaSuccess) {
+        p->cls_block = (int)c[0];
+        p->cls_smem = (int)c[1];
+        e = cudaFuncSetAttribute((const void *)p->cls_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, p->cls_smem);
+      }
+    } else {
+      cudaGetLastError();
+    }
   }
   else if (e == cudaSuccess && desc->n_pre > 0)
     e = cudaLibraryGetKernel(&p->pre_kernel, p->lib, (p->name + "_pre").c_str());
@@ -557,8 +579,10 @@ int bg_program_create(const bg_kernel_desc *desc, bg_program **out) {
   }
   if (p->pre_kernel || p->cls_kernel) {
     nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)(p->cls_kernel ? p->cls_kernel : p->pre_kernel),
-                                                      desc->block, 0) == cudaSuccess && nb > 0)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, (const void *)(p->cls_kernel ? p->cls_kernel : p->pre_kernel),
+            p->cls_kernel ? p->cls_block : desc->block, p->cls_kernel ? (size_t)p->cls_smem : 0) ==
+            cudaSuccess && nb > 0)
       p->pre_blocks_per_sm = nb;
     else
       cudaGetLastError();
@@ -751,7 +775,7 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     /* split form: classify every tile (it also zeroes the output words the parts OR into, and
      * writes every row's summary of run masks), scan the pre-pass carries, list each part's
      * rows with work, then run the parts */
-    const int warps_per_block = prog->desc.block / 32;
+    const int warps_per_block = prog->cls_block / 32;
     const int64_t rows = (prm.n_tiles + 31) / 32;
     if (!prog->pmask || prog->desc.n_parts > 4096)
       return fail(BG_ERR_INVALID, "split-form launch: no part table or more than 4096 parts");
@@ -759,7 +783,7 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     const int cls_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
     BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
-                             dim3(prog->desc.block), args, 0, s));
+                             dim3(prog->cls_block), args, (size_t)prog->cls_smem, s));
     if (prog->desc.n_pre > 0) {
       bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.pre_bits, prm.n_tiles,
                                                               prm.tile_prefix, prm.n_inputs);

@@ -25,7 +25,7 @@ table then holds, under the trigram, an extension record (those bytes and the te
 the kernel sets the bit only when the bytes before the trigram match.  On printable text this
 makes the chance hits of literal filters about a hundred times rarer per byte of extension.
 
-The kernel tests every trigram of the tile against a Bloom bitmap (2^18 bits by default, in
+The kernel tests every trigram of the tile against a Bloom bitmap (2^20 bits by default, in
 shared memory: a warp takes the slow path whenever any of its 32 lanes hits, so the bitmap is
 sized for a per-lane false-hit rate well below 1/32) and resolves the rare hits in an exact open-addressed table that maps a trigram to the bit mask
 of the filters containing it.  Both tables are generated here and compiled into the kernel.
@@ -40,7 +40,7 @@ ALL = (1 << 256) - 1
 MAX_SET = 4096          # largest trigram set one filter may carry
 MAX_EXT = 3             # bytes before the trigram an extension record may fix
 EXT_DEPTH = 3 + MAX_EXT
-BLOOM_BITS = 18         # log2 of the Bloom bitmap size (32 KB of shared memory)
+BLOOM_BITS = 20         # log2 of the Bloom bitmap size (128 KB of shared memory)
 HASH_BLOOM = 0x9E3779B1
 HASH_EXACT = 0x85EBCA6B
 
