@@ -1263,14 +1263,16 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     or at the successor's) and those whose filter holds only through a pre-pass carry, and
     writes the tile's run mask (one bit per term) to ``p.runs``.
 
-    ``<name>`` (execute) runs after the carry scan.  Its work items are (part, 32 tiles) pairs
-    in part-major order, handed out by an atomic counter: a warp reads the 32 tiles' run masks
-    with one load, and for each tile where one of the part's terms runs it loads the basis and
-    calls the part.  So at any time the whole GPU executes the same part's code, and the
-    instruction caches stay warm.  Parts hold whole outputs: a part ORs its terms into
-    per-warp accumulators of its own outputs and stores them; outputs of tiles it skips keep
-    the zeros the launch wrote.  Tiles of one part are claimed in increasing order, which keeps
-    the look-back of its additions deadlock free."""
+    ``<name>`` (execute) runs after the carry scan and the runtime's work-list kernel.  Its work
+    items are (part, row of 32 tiles) pairs where the part has work.  Part k belongs to SM group
+    k % exec_groups; the warps of an SM claim their group's items (part-major, rows increasing)
+    from the group's counter, then help the other groups, so an SM keeps few part bodies in its
+    instruction caches.  A warp reads the row's 32 run masks with one load, and for each tile
+    where one of the part's terms runs it loads the basis and calls the part, which ORs its
+    terms into per-warp accumulators and merges them into the outputs (atomicOr over the zeros
+    classify wrote, counting only newly set bits) or, without merging, stores whole outputs.
+    Tiles of one part are claimed in increasing order, which keeps the look-back of its
+    additions deadlock free."""
     d = gen.d
     wpt = tuning.wpt
     warps = tuning.block // 32
