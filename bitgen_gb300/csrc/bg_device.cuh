@@ -829,13 +829,18 @@ static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
   }
 }
 
-/* The Bloom bit of `key`, moved to bit q (a rotation, so that the probes of several keys OR
- * into one word of hits).  Bit h of the bitmap, h = the top BG_BLOOM_BITS bits of
- * key * BLOOM_HASH, is bit h % 32 of word h / 32. */
-__device__ __forceinline__ uint32_t bloom_probe(uint32_t key, const uint32_t *bloom, int q) {
-  const uint32_t h = key * BLOOM_HASH;
-  const uint32_t w = bloom[h >> (37 - BG_BLOOM_BITS)];
-  return __funnelshift_r(w, w, (h >> (32 - BG_BLOOM_BITS)) - (uint32_t)q) & (1u << q);
+/* The Bloom bit of trigram t (bits 0-23 of x; the top byte of x is ignored), moved to bit q (a
+ * rotation, so that the probes of several keys OR into one word of hits).  The bit index is
+ * the top BG_BLOOM_BITS bits of the 24-bit product t * BLOOM_HASH mod 2^24 (word = index / 32,
+ * bit = index % 32).  Multiplying x by the constant shifted left by 8 gives that product in the
+ * top 24 bits whatever the top byte of x; subtracting q before the bit field is shifted down
+ * makes the rotation put the bit at position q. */
+__device__ __forceinline__ uint32_t bloom_probe(uint32_t x, const uint32_t *bloom, int q) {
+  constexpr uint32_t M = BLOOM_HASH << 8;
+  constexpr int S = 32 - BG_BLOOM_BITS;
+  const uint32_t w = bloom[(x * M) >> (S + 5)];
+  const uint32_t a = (x * M - ((uint32_t)q << S)) >> S;
+  return __funnelshift_r(w, w, a) & (1u << q);
 }
 
 /* Load the tile's bytes, fill t.run from the trigram scan (warp-uniform) and transpose the bytes
@@ -866,14 +871,14 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
 #pragma unroll
     for (int i = 0; i < 8; i += 2) {
       const uint32_t c0 = raw[j][i], c1 = raw[j][i + 1];
-      uint32_t k[8];
-      k[0] = __byte_perm(prev, c0, 0x0432) & 0xFFFFFFu;
-      k[1] = __byte_perm(prev, c0, 0x0543) & 0xFFFFFFu;
-      k[2] = c0 & 0xFFFFFFu;
+      uint32_t k[8]; /* trigram q in bits 0-23, any top byte */
+      k[0] = __byte_perm(prev, c0, 0x0432);
+      k[1] = __byte_perm(prev, c0, 0x0543);
+      k[2] = c0;
       k[3] = c0 >> 8;
-      k[4] = __byte_perm(c0, c1, 0x0432) & 0xFFFFFFu;
-      k[5] = __byte_perm(c0, c1, 0x0543) & 0xFFFFFFu;
-      k[6] = c1 & 0xFFFFFFu;
+      k[4] = __byte_perm(c0, c1, 0x0432);
+      k[5] = __byte_perm(c0, c1, 0x0543);
+      k[6] = c1;
       k[7] = c1 >> 8;
       uint32_t hb = 0u;
 #pragma unroll
@@ -887,7 +892,7 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
             const uint32_t lo = q < 3 ? pprev : q < 7 ? prev : c0;
             const uint32_t hi = q < 3 ? prev : q < 7 ? c0 : c1;
             const uint32_t pre3 = __byte_perm(lo, hi, sel) & 0xFFFFFFu;
-            trigram_exact(k[q], pre3, keys, masks, ext, log2, run);
+            trigram_exact(k[q] & 0xFFFFFFu, pre3, keys, masks, ext, log2, run);
           }
       }
       pprev = c0;

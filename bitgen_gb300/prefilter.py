@@ -46,7 +46,9 @@ HASH_EXACT = 0x85EBCA6B
 
 
 def bloom_hash(key: int, bits: int = BLOOM_BITS) -> int:
-    return ((key * HASH_BLOOM) & 0xFFFFFFFF) >> (32 - bits)
+    """Bit index of trigram `key` in a 2^bits-bit Bloom bitmap: the top `bits` bits of the 24-bit
+    product key * HASH_BLOOM mod 2^24 (the kernel's bg_device.cuh bloom_probe)."""
+    return ((key * HASH_BLOOM) & 0xFFFFFF) >> (24 - bits)
 
 
 def exact_hash(key: int, log2_slots: int) -> int:
@@ -215,6 +217,7 @@ class TermFilter:
         return m
 
     def bloom(self, bits: int = BLOOM_BITS) -> List[int]:
+        assert 5 < bits <= 24, "the Bloom index comes from a 24-bit product"
         words = [0] * ((1 << bits) // 32)
         for key in self.table:
             h = bloom_hash(key, bits)
