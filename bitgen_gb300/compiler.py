@@ -1367,13 +1367,17 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         items_ = sorted(masks.items()) + [(0, 0)] * (pmw - len(masks))
         for w, m in items_:
             pm_table += [w, m]
+    # each lane loads its tile's run words of the part (rw0, rw1, ...); a tile's words reach the
+    # part through shuffles, so no load sits between the bytes and the call
     wants = []
     for ci, masks in enumerate(part_masks):
-        cond = " | ".join(f"(p.runs[{w}LL * p.n_tiles + g] & 0x{m:08x}u)" for w, m in sorted(masks.items())) or "0u"
-        wants.append(f"          case {ci}: want = ({cond}) != 0u; break;")
+        ws = sorted(masks.items())
+        loads = " ".join(f"rw{i} = p.runs[{w}LL * p.n_tiles + g];" for i, (w, m) in enumerate(ws))
+        cond = " | ".join(f"(rw{i} & 0x{m:08x}u)" for i, (w, m) in enumerate(ws)) or "0u"
+        wants.append(f"          case {ci}: {loads} want = ({cond}) != 0u; break;")
     calls = "\n".join(
         f"        case {ci}: "
-        + " ".join(f"t.run[{w}] = __ldg(p.runs + {w}LL * p.n_tiles + g0 + l);" for w in sorted(part_masks[ci]))
+        + " ".join(f"t.run[{w}] = __shfl_sync(FULL, rw{i}, l);" for i, w in enumerate(sorted(part_masks[ci])))
         + f" bg_part_{ci}(p, t, acc, {ba}); break;" for ci in range(len(parts)))
     # classify kernel ------------------------------------------------------------------------
     gen.lines = []
@@ -1464,8 +1468,9 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     cls_smem = 4 * (len(bloom) + len(keys) + cls_warps * nw * 32)
     if cls_smem > 227 * 1024:
         raise NotFusable(f"classify needs {cls_smem} bytes of shared memory; lower bloom_bits or cls_block")
+    cls_maxreg = max(32, min(255, 65536 // cls_block // 8 * 8))
     cls_kernel = (
-        f"//@@BG_PART\n{tables}"
+        f"//@@BG_PART\n//@@BG_UNITREG {cls_maxreg}\n{tables}"
         f"/* per part: {pmw} (run-mask word, mask) pairs; read by the runtime's work-list kernel */\n"
         f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}] = {{\n{_hex_array(pm_table)}\n}};\n'
         + "".join(cand_funcs) +
@@ -1557,6 +1562,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"    const long long g0 = (long long)__ldg(p.work + BG_WORK_HEAD + {len(parts)} + (long long)k * rows + (it - bg_pref[j])) * 32;\n"
         f"    const long long g = g0 + t.lane;\n"
         f"    bool want = false;\n"
+        f"    uint32_t {', '.join(f'rw{i} = 0u' for i in range(pmw))};\n"
         f"    if (g < p.n_tiles) {{\n"
         f"      switch (k) {{\n" + "\n".join(wants) + "\n"
         f"        default: break;\n"

@@ -343,10 +343,15 @@ int bg_transpose(const uint8_t *bytes, uint32_t *basis, int64_t n_bytes_padded, 
 static int nvrtc_one(const std::string &src, const std::string &name, bool rdc, std::string &log,
                      std::vector<char> &cubin) {
   /* "//@@BG_MAXREG n" in the source caps registers in every translation unit (the linker
-   * requires callees of a __launch_bounds__ kernel to fit its register budget) */
+   * requires callees of a __launch_bounds__ kernel to fit its register budget); a unit whose
+   * kernel calls only functions of its own unit may set its own cap with "//@@BG_UNITREG n" */
   std::string maxreg;
+  const size_t up = src.find("//@@BG_UNITREG ");
   const size_t mp = src.find("//@@BG_MAXREG ");
-  if (mp != std::string::npos) maxreg = "--maxrregcount=" + std::to_string(atoi(src.c_str() + mp + 14));
+  if (up != std::string::npos)
+    maxreg = "--maxrregcount=" + std::to_string(atoi(src.c_str() + up + 15));
+  else if (mp != std::string::npos)
+    maxreg = "--maxrregcount=" + std::to_string(atoi(src.c_str() + mp + 14));
   std::vector<const char *> base = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
                                     "--device-as-default-execution-space"};
   if (rdc) base.push_back("--relocatable-device-code=true");
