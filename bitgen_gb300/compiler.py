@@ -1455,17 +1455,17 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
             gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
     cls_code = "\n".join(gen.lines)
-    log2, keys, masks_tab, ext_tab = filt.exact()
+    log2, keys, info_tab, rec_tab = filt.exact()
     bloom = filt.bloom(tuning.bloom_bits)
     tables = (f"#define BG_EXLOG2 {log2}\n"
               f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
               f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
-              f"static __device__ const uint32_t bg_exmasks[{len(masks_tab)}] = {{\n{_hex_array(masks_tab)}\n}};\n"
-              f"static __device__ const uint32_t bg_exext[{len(ext_tab)}] = {{\n{_hex_array(ext_tab)}\n}};\n")
+              f"static __device__ const uint32_t bg_exinfo[{len(info_tab)}] = {{\n{_hex_array(info_tab)}\n}};\n"
+              f"static __device__ const uint32_t bg_exrecs[{len(rec_tab)}] = {{\n{_hex_array(rec_tab)}\n}};\n")
     basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
     cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
     cls_warps = cls_block // 32
-    cls_smem = 4 * (len(bloom) + len(keys) + cls_warps * nw * 32)
+    cls_smem = 4 * (len(bloom) + len(keys) + len(info_tab) + len(rec_tab) + cls_warps * nw * 32)
     if cls_smem > 227 * 1024:
         raise NotFusable(f"classify needs {cls_smem} bytes of shared memory; lower bloom_bits or cls_block")
     cls_maxreg = max(32, min(255, 65536 // cls_block // 8 * 8))
@@ -1480,8 +1480,12 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  extern __shared__ uint32_t bg_dyn_s[];\n"
         f"  uint32_t *bg_bloom_s = bg_dyn_s;                            /* {len(bloom)} words */\n"
         f"  uint32_t *bg_exkeys_s = bg_dyn_s + {len(bloom)};            /* {len(keys)} words */\n"
-        f"  uint32_t *bg_runs_s = bg_dyn_s + {len(bloom) + len(keys)};  /* {cls_warps * nw * 32} words */\n"
+        f"  uint32_t *bg_exinfo_s = bg_exkeys_s + {len(keys)};         /* {len(info_tab)} words */\n"
+        f"  uint32_t *bg_exrecs_s = bg_exinfo_s + {len(info_tab)};     /* {len(rec_tab)} words */\n"
+        f"  uint32_t *bg_runs_s = bg_exrecs_s + {len(rec_tab)};        /* {cls_warps * nw * 32} words */\n"
         f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
+        f"  for (int i = threadIdx.x; i < {len(info_tab)}; i += blockDim.x) bg_exinfo_s[i] = bg_exinfo[i];\n"
+        f"  for (int i = threadIdx.x; i < {len(rec_tab)}; i += blockDim.x) bg_exrecs_s[i] = bg_exrecs[i];\n"
         f"  for (int i = threadIdx.x; i < {len(keys)}; i += blockDim.x) bg_exkeys_s[i] = bg_exkeys[i];\n"
         f"  __syncthreads();\n"
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
@@ -1490,7 +1494,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
-        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exmasks, bg_exext, BG_EXLOG2);\n"
+        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"

@@ -793,34 +793,30 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
 #if BG_PREFILTER
 /* Trigram prefilter (tables generated by bitgen_gb300/prefilter.py).  Every trigram lying in
  * the bytes this warp computes is hashed into the Bloom bitmap `bloom` (2^BG_BLOOM_BITS bits,
- * shared memory); a hit is resolved in the exact open-addressed table (keys in shared memory:
- * trigram | 1 << 31, 0 = empty; BG_NRUN mask words per slot in global memory), whose mask is
- * OR-ed into the tile's run mask.  The
+ * shared memory); a hit is resolved in the exact open-addressed table (also in shared memory),
+ * whose records set bits of the tile's run mask.  The
  * trigram ending at byte q is byte(q-2) | byte(q-1) << 8 | byte(q) << 16; bytes before the
  * warp's first byte read as zero. */
 constexpr uint32_t BLOOM_HASH = 0x9E3779B1u, EXACT_HASH = 0x85EBCA6Bu;
 
-/* Exact lookup of a trigram whose Bloom bit is set.  `pre3` holds the three bytes before the
- * trigram (3 back in bits 0-7, 4 back in 8-15, 5 back in 16-23).  A slot has BG_NRUN + 1 words
- * in `masks`: the bits the trigram sets by itself, then ext_start << 8 | ext_count; extension
- * record i is ext[2i] = bytes | count << 24 and ext[2i + 1] = the bit it sets when the first
- * `count` bytes of pre3 equal `bytes`. */
+/* Exact lookup of a trigram whose Bloom bit is set (all tables in shared memory).  `pre3`
+ * holds the three bytes before the trigram (3 back in bits 0-7, 4 back in 8-15, 5 back in
+ * 16-23).  Slot s holds the key trigram | 1 << 31 (0 = empty) and info[s] = start << 8 | count
+ * of its records; record i is recs[2i] = bytes | n << 24 and recs[2i + 1] = the bit it sets when
+ * the first n bytes of pre3 equal `bytes` (n = 0: always). */
 static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
-                                                  const uint32_t *keys, const uint32_t *masks,
-                                                  const uint32_t *ext, int log2, uint32_t *run) {
+                                                  const uint32_t *keys, const uint32_t *info,
+                                                  const uint32_t *recs, int log2, uint32_t *run) {
   const uint32_t slots = 1u << log2;
   uint32_t s = (key * EXACT_HASH) >> (32 - log2);
   for (uint32_t it = 0; it < slots; ++it) {
-    const uint32_t k = keys[s]; /* keys: shared memory */
+    const uint32_t k = keys[s];
     if (k == 0u) return;
     if (k == (key | 0x80000000u)) {
-      const uint32_t *m = masks + s * (BG_NRUN + 1);
-#pragma unroll
-      for (int w = 0; w < BG_NRUN; ++w) run[w] |= __ldg(m + w);
-      const uint32_t e = __ldg(m + BG_NRUN);
+      const uint32_t e = info[s];
       for (uint32_t i = e >> 8, n = e & 255u; n > 0u; --n, ++i) {
-        const uint32_t r = __ldg(ext + 2 * i), bit = __ldg(ext + 2 * i + 1);
-        const uint32_t cmp = (1u << (8u * (r >> 24))) - 1u; /* count <= 3 */
+        const uint32_t r = recs[2 * i], bit = recs[2 * i + 1];
+        const uint32_t cmp = (1u << (8u * (r >> 24))) - 1u; /* n <= 3 */
         if (((pre3 ^ r) & cmp) == 0u && bit < 32u * BG_NRUN) run[bit >> 5] |= 1u << (bit & 31u);
       }
       return;
@@ -847,7 +843,7 @@ __device__ __forceinline__ uint32_t bloom_probe(uint32_t x, const uint32_t *bloo
  * into the basis.  Inputs given as basis planes have no bytes to scan: every term runs. */
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
                                           const uint32_t *bloom, const uint32_t *keys,
-                                          const uint32_t *masks, const uint32_t *ext, int log2) {
+                                          const uint32_t *info, const uint32_t *recs, int log2) {
   uint32_t run[BG_NRUN];
 #pragma unroll
   for (int w = 0; w < BG_NRUN; ++w) run[w] = 0u;
@@ -892,7 +888,7 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
             const uint32_t lo = q < 3 ? pprev : q < 7 ? prev : c0;
             const uint32_t hi = q < 3 ? prev : q < 7 ? c0 : c1;
             const uint32_t pre3 = __byte_perm(lo, hi, sel) & 0xFFFFFFu;
-            trigram_exact(k[q] & 0xFFFFFFu, pre3, keys, masks, ext, log2, run);
+            trigram_exact(k[q] & 0xFFFFFFu, pre3, keys, info, recs, log2, run);
           }
       }
       pprev = c0;

@@ -224,34 +224,37 @@ class TermFilter:
             words[h >> 5] |= 1 << (h & 31)
         return words
 
+    def records(self, key: int) -> List[Tuple[int, int, int]]:
+        """The records of trigram `key`: (bytes, count, bit), the bit set when the first
+        `count` bytes before the trigram equal `bytes` (count 0: always)."""
+        m = self.table.get(key, 0)
+        base = [(0, 0, b) for b in range(self.n_bits) if (m >> b) & 1]
+        return base + list(self.ext.get(key, []))
+
     def exact(self) -> Tuple[int, List[int], List[int], List[int]]:
-        """(log2 slots, keys, mask words, extension words): open addressing with linear
-        probing; a key slot holds trigram | 1 << 31 (0 = empty); per slot ``words`` mask words
-        and one word ext_start << 8 | ext_count; an extension record is two words, bytes |
-        count << 24 and the bit."""
+        """(log2 slots, keys, slot info, records): open addressing with linear probing; a key
+        slot holds trigram | 1 << 31 (0 = empty) and its info word record_start << 8 |
+        record_count; a record is two words, bytes | count << 24 and the bit it sets (see
+        `records`).  All of it fits the kernel's shared memory."""
         n = len(self.table)
         log2 = 4
         while (1 << log2) < 2 * max(1, n):
             log2 += 1
         slots = 1 << log2
-        stride = self.words + 1
         keys = [0] * slots
-        masks = [0] * (slots * stride)
-        ext: List[int] = []
-        for key, m in sorted(self.table.items()):
+        info = [0] * slots
+        recs: List[int] = []
+        for key in sorted(self.table):
             s = exact_hash(key, log2)
             while keys[s]:
                 s = (s + 1) & (slots - 1)
             keys[s] = key | (1 << 31)
-            for w in range(self.words):
-                masks[s * stride + w] = (m >> (32 * w)) & 0xFFFFFFFF
-            recs = self.ext.get(key, [])
-            assert len(recs) < 256 and len(ext) // 2 < (1 << 24)
-            masks[s * stride + self.words] = ((len(ext) // 2) << 8) | len(recs)
-            for b, cnt, bit in recs:
-                ext += [b | (cnt << 24), bit]
-        return log2, keys, masks, ext or [0, 0]
-
+            rs = self.records(key)
+            assert len(rs) < 256 and len(recs) // 2 < (1 << 23)
+            info[s] = ((len(recs) // 2) << 8) | len(rs)
+            for b, cnt, bit in rs:
+                recs += [b | (cnt << 24), bit]
+        return log2, keys, info, recs or [0, 0]
 
 def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 16) -> TermFilter:
     """Filters for `terms` (node ids, in bit order) and pre-pass additions `pre` (node ids, in
@@ -311,7 +314,8 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 1
                 ext.setdefault(key, []).append((packed, len(fixed), bit))
             else:
                 table[key] = table.get(key, 0) | (1 << bit)
-    if len(table) > tri_limit or any(len(r) > 255 for r in ext.values()):
+    if len(table) > tri_limit or any(
+            bin(table.get(k, 0)).count("1") + len(ext.get(k, [])) > 255 for k in table):
         table, ext = {}, {}
     f.table = table
     f.ext = ext

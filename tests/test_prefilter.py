@@ -28,18 +28,17 @@ def _setup(patterns, n_groups, per_regex=True, wpt=2):
     return groups, gen, terms, f
 
 
-def _lookup(f, key, pre3, log2, keys, masks, ext):
+def _lookup(f, key, pre3, log2, keys, info, recs):
     """The kernel's exact lookup (bg_device.cuh trigram_exact), over the generated tables."""
-    stride = f.words + 1
     s = prefilter.exact_hash(key, log2)
     for _ in range(len(keys)):
         if keys[s] == 0:
             return 0
         if keys[s] == key | (1 << 31):
-            m = sum(masks[s * stride + w] << (32 * w) for w in range(f.words))
-            e = masks[s * stride + f.words]
+            m = 0
+            e = info[s]
             for i in range(e >> 8, (e >> 8) + (e & 255)):
-                r, bit = ext[2 * i], ext[2 * i + 1]
+                r, bit = recs[2 * i], recs[2 * i + 1]
                 cmp = (1 << (8 * (r >> 24))) - 1
                 if (pre3 ^ r) & cmp == 0:
                     m |= 1 << bit
