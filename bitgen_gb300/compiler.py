@@ -1456,18 +1456,30 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
     cls_code = "\n".join(gen.lines)
     log2, keys, info_tab, rec_tab = filt.exact()
-    bloom = filt.bloom(tuning.bloom_bits)
+    # classify's shared memory: Bloom bitmap, exact table, the warps' run masks.  Programs with
+    # many terms (long run masks) get fewer warps per block, then a smaller bitmap.
+    bloom_bits = tuning.bloom_bits
+    cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
+
+    def cls_bytes(bits, block):
+        return 4 * ((1 << bits) // 32 + len(keys) + len(info_tab) + len(rec_tab) + (block // 32) * nw * 32)
+
+    while cls_bytes(bloom_bits, cls_block) > 227 * 1024:
+        if cls_block > 256:
+            cls_block //= 2
+        elif bloom_bits > 16:
+            bloom_bits -= 1
+        else:
+            raise NotFusable(f"classify needs {cls_bytes(bloom_bits, cls_block)} bytes of shared memory")
+    bloom = filt.bloom(bloom_bits)
     tables = (f"#define BG_EXLOG2 {log2}\n"
               f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
               f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
               f"static __device__ const uint32_t bg_exinfo[{len(info_tab)}] = {{\n{_hex_array(info_tab)}\n}};\n"
               f"static __device__ const uint32_t bg_exrecs[{len(rec_tab)}] = {{\n{_hex_array(rec_tab)}\n}};\n")
     basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
-    cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
     cls_warps = cls_block // 32
-    cls_smem = 4 * (len(bloom) + len(keys) + len(info_tab) + len(rec_tab) + cls_warps * nw * 32)
-    if cls_smem > 227 * 1024:
-        raise NotFusable(f"classify needs {cls_smem} bytes of shared memory; lower bloom_bits or cls_block")
+    cls_smem = cls_bytes(bloom_bits, cls_block)
     cls_maxreg = max(32, min(255, 65536 // cls_block // 8 * 8))
     cls_kernel = (
         f"//@@BG_PART\n//@@BG_UNITREG {cls_maxreg}\n{tables}"
@@ -1514,7 +1526,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
         f"#define BG_NPRE {len(gen.pre)}\n"
         f"#define BG_NRUN {nw}\n"
-        f"#define BG_BLOOM_BITS {tuning.bloom_bits}\n"
+        f"#define BG_BLOOM_BITS {bloom_bits}\n"
         f"#define BG_PREFILTER 1\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"

@@ -292,3 +292,26 @@ def test_counts_only_launches_of_merging_programs(cuda):
     rc = N.lib().bg_plan_launch(plan._h, inp.data.data_ptr(), None, b.counts.data_ptr(), None)
     assert rc == N.BG_ERR_INVALID
     assert b"needs out_streams" in N.lib().bg_last_error()
+
+
+def test_large_pattern_set_matches_c_oracle(cuda):
+    """1024 regexes in 16 groups (the classify block and Bloom bitmap shrink to fit shared
+    memory) over 1 MiB of printable text with planted matches, two ragged inputs."""
+    from oracle import cpu
+    ps = workloads.throughput_patterns(seed=83, n=1024)
+    groups = [compile_group(g) for g in ps.groups(16)]
+    prog = Program(groups)
+    assert prog.fused and prog.spec.n_parts > 0
+    a = workloads.plant(workloads.printable_text((1 << 20) + 77, 84), ps.witnesses, 2048, 85)
+    b = a[: 50_001].copy()
+    res = prog.scan(pack_bytes([a, b]))
+    torch.cuda.synchronize()
+    got = res.streams.cpu().numpy().view(np.uint32)
+    for i, data in enumerate((a, b)):
+        want, wc = cpu.run_groups(groups, data)
+        o, W = res.word_offsets[i], res.words[i]
+        for k, w in enumerate(want):
+            d = first_diff(got[k, o:o + W], w)
+            assert d is None, (i, k, d)
+        assert res.counts[:, i].cpu().tolist() == wc
+    assert int(res.counts.sum()) > 0

@@ -127,3 +127,14 @@ def test_form_follows_expected_selectivity():
     # the limit can force either form
     assert generate_kernel(dna, Tuning(prefilter_limit=2.0)).n_parts > 0
     assert generate_kernel(thr, Tuning(prefilter_limit=0.0)).n_parts == 0
+
+
+def test_large_programs_fit_classify_shared_memory():
+    """1024 regexes: the classify block shrinks (and then the Bloom bitmap) until its shared
+    memory fits one block."""
+    import re
+    from bitgen_gb300.compiler import generate_kernel
+    gs = [compile_group(g) for g in workloads.throughput_patterns(seed=83, n=1024).groups(16)]
+    spec = generate_kernel(gs, Tuning())
+    block, smem = map(int, re.search(r"bg_cls_cfg\[2\] = \{(\d+)u, (\d+)u\}", spec.source).groups())
+    assert smem <= 227 * 1024 and block % 32 == 0 and spec.n_parts > 0
