@@ -1506,7 +1506,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
-        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2);\n"
+        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"

@@ -803,7 +803,8 @@ constexpr uint32_t BLOOM_HASH = 0x9E3779B1u, EXACT_HASH = 0x85EBCA6Bu;
  * holds the three bytes before the trigram (3 back in bits 0-7, 4 back in 8-15, 5 back in
  * 16-23).  Slot s holds the key trigram | 1 << 31 (0 = empty) and info[s] = start << 8 | count
  * of its records; record i is recs[2i] = bytes | n << 24 and recs[2i + 1] = the bit it sets when
- * the first n bytes of pre3 equal `bytes` (n = 0: always). */
+ * the first n bytes of pre3 equal `bytes` (n = 0: always).  Bit b goes to run[(b / 32) * 32]
+ * (the tile's run words in the warp's shared memory, 32 words apart). */
 static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
                                                   const uint32_t *keys, const uint32_t *info,
                                                   const uint32_t *recs, int log2, uint32_t *run) {
@@ -817,7 +818,7 @@ static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
       for (uint32_t i = e >> 8, n = e & 255u; n > 0u; --n, ++i) {
         const uint32_t r = recs[2 * i], bit = recs[2 * i + 1];
         const uint32_t cmp = (1u << (8u * (r >> 24))) - 1u; /* n <= 3 */
-        if (((pre3 ^ r) & cmp) == 0u && bit < 32u * BG_NRUN) run[bit >> 5] |= 1u << (bit & 31u);
+        if (((pre3 ^ r) & cmp) == 0u && bit < 32u * BG_NRUN) atomicOr(run + (bit >> 5) * 32u, 1u << (bit & 31u));
       }
       return;
     }
@@ -843,16 +844,20 @@ __device__ __forceinline__ uint32_t bloom_probe(uint32_t x, const uint32_t *bloo
  * into the basis.  Inputs given as basis planes have no bytes to scan: every term runs. */
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
                                           const uint32_t *bloom, const uint32_t *keys,
-                                          const uint32_t *info, const uint32_t *recs, int log2) {
-  uint32_t run[BG_NRUN];
-#pragma unroll
-  for (int w = 0; w < BG_NRUN; ++w) run[w] = 0u;
+                                          const uint32_t *info, const uint32_t *recs, int log2,
+                                          uint32_t *run) {
+  /* run: the tile's run words in shared memory (word w at run[32 w]); hits OR into them */
   if (p.input_kind == BG_INPUT_BASIS) {
     load_basis(p, t, b);
 #pragma unroll
     for (int w = 0; w < BG_NRUN; ++w) t.run[w] = FULL;
     return;
   }
+  if (t.lane == 0) {
+#pragma unroll
+    for (int w = 0; w < BG_NRUN; ++w) run[32 * w] = 0u;
+  }
+  __syncwarp();
   uint32_t raw[WPT][8];
 #pragma unroll
   for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
@@ -895,8 +900,9 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
       prev = c1;
     }
   }
+  __syncwarp();
 #pragma unroll
-  for (int w = 0; w < BG_NRUN; ++w) t.run[w] = __reduce_or_sync(FULL, run[w]);
+  for (int w = 0; w < BG_NRUN; ++w) t.run[w] = run[32 * w];
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
     uint32_t o[8];
