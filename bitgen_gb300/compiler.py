@@ -1017,42 +1017,40 @@ def build_dag(groups: Sequence[Group], per_regex: bool = False) -> Tuple[Dag, Li
 SMEM_BUDGET = 48 * 1024
 # Passes that visit every tile once without waiting take chunks of 32 consecutive tiles per warp,
 # so that each pre-pass addition's aggregate bits of a chunk fill one word (pre_collect/flush).
-PRE_CHUNK_OPEN = (
+_CHUNK_HEAD = (
     "  const long long rows = (p.n_tiles + 31) >> 5;\n"
+    "  /* chunks of CT consecutive tiles (1..32, a power of two, so a chunk stays in one row of\n"
+    "     32 tiles): small launches use short chunks, so that every warp has work */\n"
+    "  const int CT = p.chunk_tiles > 0 ? p.chunk_tiles : 32;\n"
+    "  const long long chunks = (p.n_tiles + CT - 1) / CT;\n"
     "  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
-    "  for (long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < rows; c += stride) {\n"
+    "  for (long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += stride) {\n"
+    "   const long long g0 = c * CT, g1 = g0 + CT < p.n_tiles ? g0 + CT : p.n_tiles, row = g0 >> 5;\n"
+    "   const int l0 = (int)(g0 & 31);\n"
     "   uint32_t gw[NPRE_WORDS], pw[NPRE_WORDS];\n"
-    "   for (int j = 0; j < NPRE_WORDS; ++j) gw[j] = pw[j] = 0u;\n"
-    "   for (int l = 0; l < 32; ++l) {\n"
-    "    const long long g = c * 32 + l;\n"
+    "   for (int j = 0; j < NPRE_WORDS; ++j) gw[j] = pw[j] = 0u;\n")
+_TILE_LOOP = (
+    "   for (int l = l0; l < l0 + CT; ++l) {\n"
+    "    const long long g = row * 32 + l;\n"
     "    if (g >= p.n_tiles) break;\n"
     "    uint32_t pg[NPRE_WORDS], pp[NPRE_WORDS];\n"
     "    for (int j = 0; j < NPRE_WORDS; ++j) pg[j] = pp[j] = 0u;\n")
+PRE_CHUNK_OPEN = _CHUNK_HEAD + _TILE_LOOP
 CLS_CHUNK_OPEN = (                   # classify: PRE_CHUNK_OPEN plus the chunk's output zeroing
-    "  const long long rows = (p.n_tiles + 31) >> 5;\n"
-    "  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);\n"
-    "  for (long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < rows; c += stride) {\n"
-    "   uint32_t gw[NPRE_WORDS], pw[NPRE_WORDS];\n"
-    "   for (int j = 0; j < NPRE_WORDS; ++j) gw[j] = pw[j] = 0u;\n"
-    "   const int zin = chunk_input(p, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles);\n"
-    "   if (zin >= 0) { @ZERO@ }\n"
-    "   for (int l = 0; l < 32; ++l) {\n"
-    "    const long long g = c * 32 + l;\n"
-    "    if (g >= p.n_tiles) break;\n"
-    "    uint32_t pg[NPRE_WORDS], pp[NPRE_WORDS];\n"
-    "    for (int j = 0; j < NPRE_WORDS; ++j) pg[j] = pp[j] = 0u;\n")
+    _CHUNK_HEAD +
+    "   const int zin = chunk_input(p, g0, g1);\n"
+    "   if (zin >= 0) { @ZERO@ }\n" + _TILE_LOOP)
 CLS_CHUNK_CLOSE = (
     "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
     "   }\n"
-    "   if (NPRE > 0) pre_flush(p, c, gw, pw, t.lane);\n"
-    "   flush_runs(p, c, runs_s, @ROWRUN@, t.lane);\n"
+    "   if (NPRE > 0) pre_flush(p, row, gw, pw, t.lane, CT < 32);\n"
+    "   flush_runs(p, row, l0, CT, runs_s, @ROWRUN@, t.lane);\n"
     "  }\n")
 PRE_CHUNK_CLOSE = (
     "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
     "   }\n"
-    "   if (NPRE > 0) pre_flush(p, c, gw, pw, t.lane);\n"
+    "   if (NPRE > 0) pre_flush(p, row, gw, pw, t.lane, CT < 32);\n"
     "  }\n")
-
 
 def _cluster_terms(gen: "_Gen", terms: List[Tuple[int, int]], cap: int) -> List[List[Tuple[int, int]]]:
     """Union terms that share a non-character-class node (a common prefix chain, an addition),
@@ -1503,7 +1501,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, c * 32, c * 32 + 32 < p.n_tiles ? c * 32 + 32 : p.n_tiles, {len(names)}, t.lane);" if merge else "") +
+        + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
         f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l);\n"

@@ -564,18 +564,25 @@ __device__ __forceinline__ void pre_collect(const uint32_t pg[NPRE_WORDS], const
   }
 }
 
-/* End of chunk c (tiles 32c .. 32c+31): store the chunk words of every pre-pass addition. */
-__device__ __forceinline__ void pre_flush(const BgParams &p, long long c,
+/* End of a chunk of row `row` (tiles 32 row .. 32 row + 31): store the row words of every
+ * pre-pass addition; a chunk shorter than the row ORs its tiles' bits into words the launch
+ * zeroed. */
+__device__ __forceinline__ void pre_flush(const BgParams &p, long long row,
                                           const uint32_t gw[NPRE_WORDS],
-                                          const uint32_t pw[NPRE_WORDS], int lane) {
+                                          const uint32_t pw[NPRE_WORDS], int lane, bool partial) {
   const long long R = pre_rows(p);
 #pragma unroll
   for (int j = 0; j < NPRE_WORDS; ++j) {
     const int k = 32 * j + lane;
     if (k < NPRE) {
       uint32_t *b = p.pre_bits + 3 * R * k;
-      b[c] = gw[j];
-      b[R + c] = pw[j];
+      if (!partial) {
+        b[row] = gw[j];
+        b[R + row] = pw[j];
+      } else {
+        if (gw[j]) atomicOr(b + row, gw[j]);
+        if (pw[j]) atomicOr(b + R + row, pw[j]);
+      }
     }
   }
 }
@@ -1035,20 +1042,25 @@ __device__ __forceinline__ void zero_chunk(const BgParams &p, int in, long long 
   for (int o = 0; o < n; ++o, dst += p.out_stride) zero_span(dst, lo, hi, lane);
 }
 
-/* Split form, classify: store the run masks of chunk c's tiles (kept by lane 0 in the warp's
- * shared words rs[w * 32 + l]) with one coalesced store per mask word, and the chunk's row
- * summary (OR over its tiles) that the work-list kernel reads. */
-__device__ __forceinline__ void flush_runs(const BgParams &p, long long c, const uint32_t *rs,
-                                           uint32_t *rowrun, int lane) {
+/* Split form, classify: store the run masks of a chunk's tiles (row `row`, positions
+ * l0 .. l0 + ct - 1, kept by lane 0 in the warp's shared words rs[w * 32 + l]) with one
+ * coalesced store per mask word, and the row summary (OR over its tiles) that the work-list
+ * kernel reads: stored for a whole-row chunk, ORed into words the launch zeroed otherwise. */
+__device__ __forceinline__ void flush_runs(const BgParams &p, long long row, int l0, int ct,
+                                           const uint32_t *rs, uint32_t *rowrun, int lane) {
   __syncwarp();
   const long long rows = (p.n_tiles + 31) >> 5;
-  const long long g = c * 32 + lane;
+  const long long g = row * 32 + lane;
+  const bool mine = lane >= l0 && lane < l0 + ct && g < p.n_tiles;
 #pragma unroll
   for (int w = 0; w < BG_NRUN; ++w) {
-    const uint32_t v = g < p.n_tiles ? rs[w * 32 + lane] : 0u;
-    if (g < p.n_tiles) p.runs[(long long)w * p.n_tiles + g] = v;
+    const uint32_t v = mine ? rs[w * 32 + lane] : 0u;
+    if (mine) p.runs[(long long)w * p.n_tiles + g] = v;
     const uint32_t s = __reduce_or_sync(FULL, v);
-    if (lane == 0) rowrun[(long long)w * rows + c] = s;
+    if (lane == 0) {
+      if (ct >= 32) rowrun[(long long)w * rows + row] = s;
+      else if (s) atomicOr(rowrun + (long long)w * rows + row, s);
+    }
   }
   __syncwarp();
 }

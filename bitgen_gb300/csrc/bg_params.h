@@ -56,6 +56,8 @@ typedef struct BgParams {
                                 H + n_parts * (1 + R) the OR of each row's run masks, [n_run][R] */
   int32_t n_inputs;
   int32_t input_kind;
+  int32_t chunk_tiles;       /* tiles per warp chunk in the classify / pre-pass kernels:
+                                1..32, a power of two (the runtime's choice per launch)       */
 } BgParams;
 
 /* Words before the part counts in BgParams.work: the execute pass's claim counters. */

@@ -774,19 +774,53 @@ int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t deb
 
 /* Everything of one scan after its prologue: the carry pre-pass and its scan when the program
  * has one, then the main kernel.  All launches go to `s`, in this order. */
+/* Tiles per warp chunk of the classify / pre-pass kernels for a launch of `tiles` tiles on
+ * `warps` resident warps: whole rows of 32 tiles while they keep at least half of the warps
+ * busy, else the longest shorter chunk (a power of two) that does, so that small launches
+ * spread over the whole GPU instead of walking 32 tiles per warp. */
+static int chunk_tiles_for(int64_t tiles, int64_t warps) {
+  int ct = 32;
+  while (ct > 1 && 2 * tiles < warps * ct) ct >>= 1;
+  return ct;
+}
+
+/* Launch grid and chunk length of a classify / pre-pass kernel; with chunks shorter than a row
+ * the row words they OR into (pre-pass bitmaps, and in the split form the row summaries) are
+ * zeroed first. */
+static int chunk_launch(const bg_program *prog, BgParams &prm, int block, int blocks_per_sm,
+                        uint32_t *rowrun, cudaStream_t s, int &grid) {
+  const int warps_per_block = block / 32;
+  const int64_t resident = (int64_t)sm_count() * blocks_per_sm;
+  prm.chunk_tiles = chunk_tiles_for(prm.n_tiles, resident * warps_per_block);
+  const int64_t rows = (prm.n_tiles + 31) / 32;
+  if (prm.chunk_tiles < 32) {
+    if (prog->desc.n_pre > 0)
+      BG_CUDA(cudaMemsetAsync(prm.pre_bits, 0,
+                              sizeof(uint32_t) * 3 * (size_t)rows * (size_t)prog->desc.n_pre, s));
+    if (rowrun)
+      BG_CUDA(cudaMemsetAsync(rowrun, 0, sizeof(uint32_t) * (size_t)prog->desc.n_run * (size_t)rows,
+                              s));
+  }
+  const int64_t chunks = (prm.n_tiles + prm.chunk_tiles - 1) / prm.chunk_tiles;
+  const int64_t need = (chunks + warps_per_block - 1) / warps_per_block;
+  grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, resident));
+  return BG_OK;
+}
+
 static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaStream_t s) {
   void *args[] = {&prm};
   if (prog->cls_kernel) {
     /* split form: classify every tile (it also zeroes the output words the parts OR into, and
      * writes every row's summary of run masks), scan the pre-pass carries, list each part's
      * rows with work, then run the parts */
-    const int warps_per_block = prog->cls_block / 32;
     const int64_t rows = (prm.n_tiles + 31) / 32;
     if (!prog->pmask || prog->desc.n_parts > 4096)
       return fail(BG_ERR_INVALID, "split-form launch: no part table or more than 4096 parts");
-    const int64_t need = (rows + warps_per_block - 1) / warps_per_block;
-    const int cls_grid = (int)std::max<int64_t>(
-        1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
+    int cls_grid = 1;
+    const int rc = chunk_launch(prog, prm, prog->cls_block, prog->pre_blocks_per_sm,
+                                prm.work + BG_WORK_HEAD + (int64_t)prog->desc.n_parts * (1 + rows),
+                                s, cls_grid);
+    if (rc != BG_OK) return rc;
     BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
                              dim3(prog->cls_block), args, (size_t)prog->cls_smem, s));
     if (prog->desc.n_pre > 0) {
@@ -805,10 +839,10 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     return BG_OK;
   }
   if (prog->pre_kernel) {
-    const int warps_per_block = prog->desc.block / 32;
-    const int64_t need = (prm.n_tiles + warps_per_block - 1) / warps_per_block;
-    const int pre_grid = (int)std::max<int64_t>(
-        1, std::min<int64_t>(need, (int64_t)sm_count() * prog->pre_blocks_per_sm));
+    int pre_grid = 1;
+    const int rc = chunk_launch(prog, prm, prog->desc.block, prog->pre_blocks_per_sm, nullptr, s,
+                                pre_grid);
+    if (rc != BG_OK) return rc;
     BG_CUDA(cudaLaunchKernel((const void *)prog->pre_kernel, dim3(pre_grid),
                              dim3(prog->desc.block), args, 0, s));
     bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.pre_bits, prm.n_tiles,
