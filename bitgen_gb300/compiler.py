@@ -1333,15 +1333,21 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
     funcs = []
     part_masks: List[Dict[int, int]] = []
+    # a part receives the tile's run words it tests as r0, r1, ... (its words in increasing order)
+    pmw = max(1, max(len({r >> 5 for r in rs}) for rs in part_terms))
+    sig = (f"const BgParams &p, const Tile &t, uint32_t *acc, "
+           + "".join(f"uint32_t r{i}, " for i in range(pmw)) + _basis_params(wpt))
     for ci, (rs, outs_k) in enumerate(zip(part_terms, parts)):
         blocks = []
         masks: Dict[int, int] = {}
         for r in rs:
-            li = outs_k.index(terms[r][1])
             masks[r >> 5] = masks.get(r >> 5, 0) | (1 << (r & 31))
+        words = sorted(masks)
+        for r in rs:
+            li = outs_k.index(terms[r][1])
             code = gen.part([(terms[r][0], li)])
             body = "\n".join("  " + ln for ln in code.split("\n"))
-            blocks.append(f"  if ((t.run[{r >> 5}] >> {r & 31}) & 1u) {{\n{body}\n  }}")
+            blocks.append(f"  if ((r{words.index(r >> 5)} >> {r & 31}) & 1u) {{\n{body}\n  }}")
         part_masks.append(masks)
         fn = "merge_store" if merge else "store"
         stores = "\n".join(f"  {fn}(p, t, {o}, acc_get(acc, t, {li}));" for li, o in enumerate(outs_k))
@@ -1365,18 +1371,11 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         items_ = sorted(masks.items()) + [(0, 0)] * (pmw - len(masks))
         for w, m in items_:
             pm_table += [w, m]
-    # each lane loads its tile's run words of the part (rw0, rw1, ...); a tile's words reach the
-    # part through shuffles, so no load sits between the bytes and the call
-    wants = []
-    for ci, masks in enumerate(part_masks):
-        ws = sorted(masks.items())
-        loads = " ".join(f"rw{i} = p.runs[{w}LL * p.n_tiles + g];" for i, (w, m) in enumerate(ws))
-        cond = " | ".join(f"(rw{i} & 0x{m:08x}u)" for i, (w, m) in enumerate(ws)) or "0u"
-        wants.append(f"          case {ci}: {loads} want = ({cond}) != 0u; break;")
-    calls = "\n".join(
-        f"        case {ci}: "
-        + " ".join(f"t.run[{w}] = __shfl_sync(FULL, rw{i}, l);" for i, w in enumerate(sorted(part_masks[ci])))
-        + f" bg_part_{ci}(p, t, acc, {ba}); break;" for ci in range(len(parts)))
+    # execute dispatch: the parts' (run word, mask) pairs in shared memory and a table of the
+    # part functions, so that one call site serves every part
+    fn_tab = (f"typedef void (*bg_part_fn)({sig});\n"
+              f"__device__ bg_part_fn bg_part_tab[{len(parts)}] = {{{', '.join(f'bg_part_{ci}' for ci in range(len(parts)))}}};\n"
+              f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}];\n')
     # classify kernel ------------------------------------------------------------------------
     gen.lines = []
     gen.indent = 4
@@ -1532,8 +1531,10 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define EM(j) (E ? t.em.w[j] : 0xffffffffu)\n"
         f"{comments}\n"
         + "\n".join(funcs) + cls_kernel +
-        f"//@@BG_KERNEL\n{decls}\n"
+        f"//@@BG_KERNEL\n{decls}\n{fn_tab}"
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
+        f"  __shared__ uint32_t bg_pm_s[{len(pm_table)}];\n"
+        f"  for (int i = threadIdx.x; i < {len(pm_table)}; i += blockDim.x) bg_pm_s[i] = bg_pmask[i];\n"
         f"  __shared__ uint32_t bg_acc[{warps} * {nacc} * BG_WPT * 32];\n"
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * ({nacc} * BG_WPT * 32);\n"
         f"  Tile t;\n"
@@ -1575,22 +1576,21 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"    const int k = bg_ord[j];\n"
         f"    const long long g0 = (long long)__ldg(p.work + BG_WORK_HEAD + {len(parts)} + (long long)k * rows + (it - bg_pref[j])) * 32;\n"
         f"    const long long g = g0 + t.lane;\n"
-        f"    bool want = false;\n"
+        f"    /* each lane loads its tile's run words of the part */\n"
+        f"    uint32_t want = 0u;\n"
         f"    uint32_t {', '.join(f'rw{i} = 0u' for i in range(pmw))};\n"
-        f"    if (g < p.n_tiles) {{\n"
-        f"      switch (k) {{\n" + "\n".join(wants) + "\n"
-        f"        default: break;\n"
-        f"      }}\n"
-        f"    }}\n"
-        f"    uint32_t sel = __ballot_sync(FULL, want);\n"
+        + "".join(f"    {{ const uint32_t w = bg_pm_s[(k * {pmw} + {i}) * 2], m = bg_pm_s[(k * {pmw} + {i}) * 2 + 1];\n"
+                  f"      if (m && g < p.n_tiles) rw{i} = p.runs[(long long)w * p.n_tiles + g];\n"
+                  f"      want |= rw{i} & m; }}\n" for i in range(pmw)) +
+        f"    uint32_t sel = __ballot_sync(FULL, want != 0u);\n"
+        f"    const bg_part_fn fn = bg_part_tab[k];\n"
         f"    while (sel) {{\n"
         f"      const int l = __ffs(sel) - 1;\n"
         f"      sel &= sel - 1u;\n"
         f"      setup_tile(p, t, (unsigned int)(g0 + l), true, false);\n"
-        +
         f"      S b[8];\n"
         f"      load_basis(p, t, b);\n"
-        f"      switch (k) {{\n{calls}\n        default: break;\n      }}\n"
+        f"      fn(p, t, acc, {''.join(f'__shfl_sync(FULL, rw{i}, l), ' for i in range(pmw))}{ba});\n"
         f"    }}\n"
         f"  }}\n"
         f"}}\n")
