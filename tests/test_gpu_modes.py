@@ -84,3 +84,29 @@ def test_autotuner_choice_is_exact(cuda, tmp_path, monkeypatch):
     ref = Program(groups).scan(inp)
     got = Program(groups, tuning=best).scan(inp)
     assert torch.equal(ref.streams, got.streams) and torch.equal(ref.counts, got.counts)
+
+
+def test_streamed_scans_equal_program_scan(cuda):
+    """StreamScanner: five different inputs through the double-buffered copy/scan pipeline give
+    the counts (and, for the last one, the streams) of Program.scan on each input."""
+    from bitgen_gb300.streaming import StreamScanner
+    ps = workloads.throughput_patterns(seed=3, n=64)
+    prog = Program([compile_group(g) for g in ps.groups(4)])
+    n = (1 << 20) + 96
+    hosts = [torch.from_numpy(workloads.plant(workloads.printable_text(n, 70 + i), ps.witnesses, 300, 80 + i)).pin_memory()
+             for i in range(5)]
+    sc = StreamScanner(prog, n, cuda, copy_streams=3)
+    handles = []
+    got = []
+    for h in hosts:
+        handles.append(sc.submit(h))
+        if len(handles) >= 2:
+            got.append(sc.counts(handles[-2]))
+    got.append(sc.counts(handles[-1]))
+    for h, c in zip(hosts, got):
+        want = prog.scan(pack_bytes([h.numpy()]))
+        assert c == [int(x) for x in want.counts[:, 0].tolist()]
+    last = prog.scan(pack_bytes([hosts[-1].numpy()]))
+    W = last.words[0]
+    assert torch.equal(sc.out[:, :W], last.streams[:, last.word_offsets[0]:last.word_offsets[0] + W])
+    assert sum(got[-1]) > 0
