@@ -617,6 +617,7 @@ __device__ __forceinline__ AddState add_known(const BgParams &p, const Tile &t, 
  * --------------------------------------------------------------------------------------- */
 __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
   t.lane = threadIdx.x & 31;
+  t.input = 0;
   t.epoch = *(volatile const unsigned long long *)(p.state + 2);
 }
 
@@ -642,10 +643,17 @@ __device__ __forceinline__ void load_pre_carries(const BgParams &p, Tile &t) {
  * over every tile does). */
 __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g,
                                            bool carries = true, bool debug_wait = true) {
-  int lo = 0, hi = p.n_inputs; /* find i: prefix[i] <= g < prefix[i+1] */
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (p.tile_prefix[mid] <= (long long)g) lo = mid; else hi = mid;
+  /* find i: prefix[i] <= g < prefix[i+1]; a warp's tiles mostly stay in the input of its
+   * previous tile, so that one is tried first */
+  int lo = t.input;
+  if (!(lo >= 0 && lo < p.n_inputs && p.tile_prefix[lo] <= (long long)g &&
+        (long long)g < p.tile_prefix[lo + 1])) {
+    lo = 0;
+    int hi = p.n_inputs;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (p.tile_prefix[mid] <= (long long)g) lo = mid; else hi = mid;
+    }
   }
   t.input = lo;
   t.gtile = g;
