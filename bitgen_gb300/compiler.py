@@ -1540,6 +1540,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  Tile t;\n"
         f"  init(p, t);\n"
         f"  __shared__ unsigned int bg_pref[{len(parts) + 1}];\n"
+        f"  __shared__ unsigned int bg_spent;  /* bit g: the block saw group g's items run out */\n"
+        f"  if (threadIdx.x == 0) bg_spent = 0u;\n"
         f"  if (threadIdx.x < 32) {{\n"
         f"    /* group-major, then part-major order (bg_ord): exclusive prefix of the row counts */\n"
         f"    const int per = ({len(parts)} + 31) / 32, lo = threadIdx.x * per;\n"
@@ -1564,9 +1566,11 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  for (;;) {{\n"
         f"    const unsigned int gb = bg_pref[bg_gpos[grp]], ge = bg_pref[bg_gpos[grp + 1]];\n"
         f"    unsigned int it = 0u;\n"
-        f"    if (t.lane == 0) it = gb < ge ? gb + atomicAdd(p.work + grp, 1u) : ge;\n"
+        f"    if (t.lane == 0)\n"
+        f"      it = gb < ge && !((*(volatile unsigned int *)&bg_spent >> grp) & 1u) ? gb + atomicAdd(p.work + grp, 1u) : ge;\n"
         f"    it = __shfl_sync(FULL, it, 0);\n"
         f"    if (it >= ge) {{\n"
+        f"      if (t.lane == 0) atomicOr(&bg_spent, 1u << grp);\n"
         f"      if (++tried >= {ngroups}) break;\n"
         f"      grp = grp + 1 < {ngroups} ? grp + 1 : 0;\n"
         f"      continue;\n"
