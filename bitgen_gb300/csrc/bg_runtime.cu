@@ -221,7 +221,8 @@ __global__ void __launch_bounds__(1024) bg_work_list_kernel(const uint32_t *rowr
   if (threadIdx.x == 0) work[BG_WORK_HEAD + p] = total;
 }
 
-/* 32-bit words of the split form's work list (counts, rows per part, row summaries). */
+/* 32-bit words of the split form's work list (claim counters, counts, rows per part, row
+ * summaries). */
 int64_t work_words(const bg_kernel_desc &d, int64_t tiles) {
   const int64_t rows = (tiles + 31) / 32;
   return d.n_run > 0 ? BG_WORK_HEAD + (int64_t)d.n_parts * (1 + rows) + (int64_t)d.n_run * rows
