@@ -336,13 +336,16 @@ class Tuning:
                                    # the bytes the filters name)
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
+    single_wpt: int = 2      # words per lane (and blocks per SM below) when the compiler falls
+    single_min_blocks: int = 3   # back to the single-kernel form because the filters are
+                                 # unselective (0: keep wpt / min_blocks)
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
-                self.cls_block)
+                self.cls_block, self.single_wpt, self.single_min_blocks)
 
 
 @dataclass
@@ -1119,7 +1122,13 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         positions = 32 * 32 * tuning.wpt
         if not filt.enabled or (filt.expected_per_tile(positions) >
                                 tuning.prefilter_limit * len(terms)):
-            filt = None                  # the filter would pass most terms: single-kernel form
+            # the filter would pass most terms: single-kernel form, with its own tile shape
+            # (programs whose terms have no filter at all keep the requested shape)
+            if filt.enabled and tuning.single_wpt and tuning.single_wpt != tuning.wpt:
+                return generate_kernel(groups, replace(tuning, prefilter=False, wpt=tuning.single_wpt,
+                                                       min_blocks=tuning.single_min_blocks),
+                                       per_regex, name)
+            filt = None
     if tuning.skip_interval < 0:
         tuning = replace(tuning, skip_interval=0 if filt is not None else 1)
         gen.t = tuning
