@@ -1441,17 +1441,35 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
                         f"if ({cond}) {{ const uint3 cr = bg_cand_{j}(t, {basis_names}); "
                         f"pg[{j}] |= cr.x; pp[{j}] = (pp[{j}] & ~cr.y) | cr.z; }}")
     gen.lines, gen.indent, gen.scopes = saved
+    live_needs = [(c, dl, mask & ~always) for (c, dl), mask in sorted(need_masks.items())
+                  if mask & ~always]
+    # when one class contains all the others, a lane that is not all ones in it is not all ones
+    # in any: test that class at the carry lanes first and skip the rest (the common case)
+    guard = None
+    if len({c for c, _, _ in live_needs}) > 1:
+        sup = max((c for c, _, _ in live_needs), key=lambda c: (bin(gen.byteset(c)).count("1"), c))
+        if all(gen.byteset(c) & ~gen.byteset(sup) == 0 for c, _, _ in live_needs):
+            lanes = 0
+            for _, dl, _ in live_needs:
+                lanes |= 1 << dl
+                if sl + dl < 32:
+                    lanes |= 1 << (sl + dl)
+            guard = sup
+            ref = gen.mat(sup)
+            gen.emit(f"const uint32_t {pm_classes[sup]} = ones_lanes(t, {gen.pack(ref)});")
+            gen.open(f"{pm_classes[sup]} & 0x{lanes:08x}u")
     for c, pm in sorted(pm_classes.items()):
+        if c == guard:
+            continue
         ref = gen.mat(c)
         gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
-    for (c, dl), mask in sorted(need_masks.items()):
-        mask &= ~always
-        if not mask:
-            continue
+    for c, dl, mask in live_needs:
         pm = pm_classes[c]
         ors = " ".join(f"t.run[{w}] |= 0x{(mask >> (32 * w)) & 0xFFFFFFFF:08x}u;"
                        for w in range(nw) if (mask >> (32 * w)) & 0xFFFFFFFF)
         gen.emit(f"if ((({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u) {{ {ors} }}")
+    if guard is not None:
+        gen.close()
     # run masks: kept in the warp's shared words, stored per chunk (flush_runs)
     gen.emit("if (t.lane == 0) {" + " ".join(f"runs_s[{w * 32} + l] = t.run[{w}];" for w in range(nw)) + " }")
     if merge:                            # parts OR into the outputs: start every word at zero
