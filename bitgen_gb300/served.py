@@ -13,8 +13,10 @@ latency runs from its arrival to the moment its counts are back on the host.
 
 from __future__ import annotations
 
+import os
 import time
 from collections import deque
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence
 
@@ -93,6 +95,8 @@ class Server:
                 host_out=torch.empty((self.max_out, words), dtype=torch.uint32).pin_memory() if return_streams else None,
                 plans=plans))
         self.in_flight_bytes = 0
+        self.copy_threads = max(1, min(8, os.cpu_count() or 1))
+        self.pool = ThreadPoolExecutor(max_workers=self.copy_threads)
 
     # --------------------------------------------------------------------------------------
     def _launch(self, slot: _Slot, pset: str, batch: List[Request], footprint: int):
@@ -101,8 +105,19 @@ class Server:
         host = slot.host_in.numpy()
         for r in batch:
             offs.append(pos)
-            host[pos:pos + r.data.size] = r.data
             pos += -(-r.data.size // ALIGN) * ALIGN
+        # gather the requests into the pinned staging buffer, on several host threads for
+        # large batches (numpy copies release the GIL)
+        def gather(lo: int, hi: int):
+            for i in range(lo, hi):
+                d = batch[i].data
+                host[offs[i]:offs[i] + d.size] = d
+        if pos >= (8 << 20) and len(batch) > 1:
+            k = min(self.copy_threads, len(batch))
+            step = -(-len(batch) // k)
+            list(self.pool.map(lambda a: gather(a, min(len(batch), a + step)), range(0, len(batch), step)))
+        else:
+            gather(0, len(batch))
         lens = [int(r.data.size) for r in batch]
         out_offs, words, total = out_layout(lens)
         s = slot.stream
