@@ -20,7 +20,7 @@ from typing import List, Optional
 
 import torch
 
-from .engine import Program, bytes_input, out_layout
+from .engine import Plan, Program, bytes_input, out_layout
 
 
 class StreamScanner:
@@ -38,7 +38,9 @@ class StreamScanner:
         self.d_counts = torch.empty((program.n_outputs, 1), dtype=torch.int64, device=self.dev)
         self.h_counts = [torch.empty((program.n_outputs, 1), dtype=torch.int64).pin_memory()
                          for _ in range(2)]
-        self.plan = program.plan(bytes_input(self.bufs[0]), offs, total)
+        # its own plan (look-back records, run masks, work list): scans of the same layout
+        # elsewhere do not share this scratch
+        self.plan = Plan(program, bytes_input(self.bufs[0]), offs, total)
         self.compute = torch.cuda.Stream(device=self.dev)
         self.copies = [torch.cuda.Stream(device=self.dev) for _ in range(max(1, copy_streams))]
         self.copied = [[torch.cuda.Event() for _ in self.copies] for _ in range(2)]
