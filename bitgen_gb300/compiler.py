@@ -1514,6 +1514,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f'extern "C" __device__ const uint32_t bg_cls_cfg[2] = {{{cls_block}u, {cls_smem}u}};\n'
         f'extern "C" __global__ void __launch_bounds__({cls_block}, 1) {name}_cls(const __grid_constant__ BgParams p) {{\n'
         f"  extern __shared__ uint32_t bg_dyn_s[];\n"
+        f"  cls_prologue(p, {len(names)});\n"
         f"  uint32_t *bg_bloom_s = bg_dyn_s;                            /* {len(bloom)} words */\n"
         f"  uint32_t *bg_exkeys_s = bg_dyn_s + {len(bloom)};            /* {len(keys)} words */\n"
         f"  uint32_t *bg_exinfo_s = bg_exkeys_s + {len(keys)};         /* {len(info_tab)} words */\n"

@@ -1012,6 +1012,25 @@ __device__ __forceinline__ void zero_outputs(const BgParams &p, const Tile &t, i
   }
 }
 
+/* Split form, classify: the launch's prologue, which the runtime's prologue kernel and counts
+ * memset do for the other forms.  Block 0 clears the tile and match-position counters and
+ * advances the launch epoch (only the execute pass reads it); all blocks clear the counts. */
+__device__ __forceinline__ void cls_prologue(const BgParams &p, int n_out) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.state[0] = 0u;
+    p.state[6] = 0u;
+    p.state[7] = 0u;
+    unsigned long long *ep = reinterpret_cast<unsigned long long *>(p.state + 2);
+    *ep = *ep + 1ull;
+  }
+  if (p.counts) {
+    const long long nc = (long long)n_out * p.n_inputs;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc;
+         i += (long long)gridDim.x * blockDim.x)
+      p.counts[i] = 0ull;
+  }
+}
+
 /* Split form, classify: the input holding all of tiles g0 .. g1-1, or -1 when they span
  * several inputs. */
 __device__ __forceinline__ int chunk_input(const BgParams &p, long long g0, long long g1) {

@@ -96,13 +96,12 @@ __device__ __forceinline__ uint32_t row_kill(int64_t row, const int64_t *tile_pr
   return kill;
 }
 
-__global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits, int64_t n_tiles,
-                                                             const int64_t *tile_prefix,
-                                                             int n_inputs) {
+__device__ __forceinline__ void carry_scan_block(int k, uint32_t *pre_bits, int64_t n_tiles,
+                                                 const int64_t *tile_prefix, int n_inputs) {
   __shared__ uint32_t wg[32], wp[32];
   const int64_t R = (n_tiles + 31) / 32;
-  const uint32_t *Gw = pre_bits + 3 * R * blockIdx.x, *Pw = Gw + R;
-  uint32_t *Cw = pre_bits + 3 * R * blockIdx.x + 2 * R;
+  const uint32_t *Gw = pre_bits + 3 * R * k, *Pw = Gw + R;
+  uint32_t *Cw = pre_bits + 3 * R * k + 2 * R;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int64_t per = (R + blockDim.x - 1) / blockDim.x;
   const int64_t r0 = (int64_t)tid * per < R ? (int64_t)tid * per : R;
@@ -170,6 +169,12 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits,
   }
 }
 
+__global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits, int64_t n_tiles,
+                                                             const int64_t *tile_prefix,
+                                                             int n_inputs) {
+  carry_scan_block(blockIdx.x, pre_bits, n_tiles, tile_prefix, n_inputs);
+}
+
 /* Work list of the split form's execute pass: the (part, tile row) pairs where the part has
  * something to run, a row being 32 consecutive tiles.  The classify pass leaves, for every row
  * and run-mask word, the OR of the row's 32 masks (`rowrun`, [n_run][rows]); part p has work in
@@ -180,12 +185,10 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits,
  * a ballot to keep them in order), and the warps' counts are scanned across the block.  The
  * execute pass orders the parts one after the other (part-major, so that the whole GPU runs one
  * part at a time) and claims a part's rows in increasing order. */
-__global__ void __launch_bounds__(1024) bg_work_list_kernel(const uint32_t *rowrun,
-                                                           const uint32_t *pmask, int pmw,
-                                                           uint32_t *work, int n_parts,
-                                                           int64_t rows) {
+__device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
+                                                const uint32_t *pmask, int pmw, uint32_t *work,
+                                                int n_parts, int64_t rows) {
   __shared__ uint32_t wsum[32];
-  const int p = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
   uint32_t *out = work + BG_WORK_HEAD + n_parts + (int64_t)p * rows;
@@ -219,6 +222,20 @@ __global__ void __launch_bounds__(1024) bg_work_list_kernel(const uint32_t *rowr
     pos += __popc(b);
   }
   if (threadIdx.x == 0) work[BG_WORK_HEAD + p] = total;
+}
+
+/* The split form's row-level work between classify and execute in one launch: blocks
+ * [0, n_pre) scan the pre-pass carries (one addition each), blocks [n_pre, n_pre + n_parts)
+ * list the parts' rows. */
+__global__ void __launch_bounds__(1024) bg_rows_kernel(uint32_t *pre_bits, int64_t n_tiles,
+                                                       const int64_t *tile_prefix, int n_inputs,
+                                                       int n_pre, const uint32_t *rowrun,
+                                                       const uint32_t *pmask, int pmw,
+                                                       uint32_t *work, int n_parts, int64_t rows) {
+  if ((int)blockIdx.x < n_pre)
+    carry_scan_block(blockIdx.x, pre_bits, n_tiles, tile_prefix, n_inputs);
+  else
+    work_list_block(blockIdx.x - n_pre, rowrun, pmask, pmw, work, n_parts, rows);
 }
 
 /* 32-bit words of the split form's work list (claim counters, counts, rows per part, row
@@ -811,9 +828,9 @@ static int chunk_launch(const bg_program *prog, BgParams &prm, int block, int bl
 static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaStream_t s) {
   void *args[] = {&prm};
   if (prog->cls_kernel) {
-    /* split form: classify every tile (it also zeroes the output words the parts OR into, and
-     * writes every row's summary of run masks), scan the pre-pass carries, list each part's
-     * rows with work, then run the parts */
+    /* split form: classify every tile (it also does the launch prologue, zeroes the output
+     * words the parts OR into and writes every row's summary of run masks), scan the pre-pass
+     * carries and list each part's rows with work (one launch), then run the parts */
     const int64_t rows = (prm.n_tiles + 31) / 32;
     if (!prog->pmask || prog->desc.n_parts > 4096)
       return fail(BG_ERR_INVALID, "split-form launch: no part table or more than 4096 parts");
@@ -824,15 +841,10 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     if (rc != BG_OK) return rc;
     BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
                              dim3(prog->cls_block), args, (size_t)prog->cls_smem, s));
-    if (prog->desc.n_pre > 0) {
-      bg_carry_scan_kernel<<<prog->desc.n_pre, 1024, 0, s>>>(prm.pre_bits, prm.n_tiles,
-                                                              prm.tile_prefix, prm.n_inputs);
-      BG_CUDA(cudaGetLastError());
-    }
-    bg_work_list_kernel<<<std::max(1, prog->desc.n_parts), 1024, 0, s>>>(
+    bg_rows_kernel<<<prog->desc.n_pre + std::max(1, prog->desc.n_parts), 1024, 0, s>>>(
+        prm.pre_bits, prm.n_tiles, prm.tile_prefix, prm.n_inputs, prog->desc.n_pre,
         prm.work + BG_WORK_HEAD + (int64_t)prog->desc.n_parts * (1 + rows), prog->pmask, prog->pmw,
-        prm.work,
-        prog->desc.n_parts, rows);
+        prm.work, std::max(1, prog->desc.n_parts), rows);
     BG_CUDA(cudaGetLastError());
     const int main_grid = (int)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm);
     BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(main_grid), dim3(prog->desc.block),
@@ -893,11 +905,13 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
   prm.n_inputs = (int32_t)n;
   prm.input_kind = L.input_kind;
-  if (counts)
-    BG_CUDA(cudaMemsetAsync(counts, 0,
-                            sizeof(unsigned long long) * (size_t)plan->prog->desc.n_outputs * n, s));
-  bg_prologue_kernel<<<1, 1, 0, s>>>(plan->d_state);
-  BG_CUDA(cudaGetLastError());
+  if (!plan->prog->cls_kernel) { /* the split form's classify kernel does this itself */
+    if (counts)
+      BG_CUDA(cudaMemsetAsync(counts, 0,
+                              sizeof(unsigned long long) * (size_t)plan->prog->desc.n_outputs * n, s));
+    bg_prologue_kernel<<<1, 1, 0, s>>>(plan->d_state);
+    BG_CUDA(cudaGetLastError());
+  }
   return launch_passes(plan->prog, prm, plan->grid, s);
 }
 

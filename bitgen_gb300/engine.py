@@ -391,13 +391,12 @@ class Program:
                 "kernels_per_scan": self.kernels_per_scan()}
 
     def kernels_per_scan(self) -> int:
-        """Kernels one ``Plan.launch`` starts: the prologue; in the split form classify, the carry
-        scan (with pre-pass additions), the work list and execute; else the pre-pass and carry
-        scan (with pre-pass additions) and the main kernel."""
-        pre = self.spec.n_pre > 0
+        """Kernels one ``Plan.launch`` starts: in the split form classify (which also does the
+        launch prologue), the row kernel (carry scan and work list) and execute; else the
+        prologue, the pre-pass and carry scan (with pre-pass additions) and the main kernel."""
         if self.spec.n_parts:
-            return 1 + 3 + int(pre)
-        return 1 + 1 + 2 * int(pre)
+            return 3
+        return 1 + 1 + 2 * int(self.spec.n_pre > 0)
 
     def tiles_for(self, lengths: Sequence[int]) -> int:
         """Tiles one launch over inputs of these lengths needs."""
