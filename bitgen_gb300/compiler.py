@@ -1563,6 +1563,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f'extern "C" __global__ void __launch_bounds__({tuning.block}, {tuning.min_blocks}) {name}(const __grid_constant__ BgParams p) {{\n'
         f"  __shared__ uint32_t bg_pm_s[{len(pm_table)}];\n"
         f"  for (int i = threadIdx.x; i < {len(pm_table)}; i += blockDim.x) bg_pm_s[i] = bg_pmask[i];\n"
+        f"  asm volatile(\"griddepcontrol.wait;\" ::: \"memory\"); /* launched as a programmatic dependent of the row kernel */\n"
         f"  __shared__ uint32_t bg_acc[{warps} * {nacc} * BG_WPT * 32];\n"
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * ({nacc} * BG_WPT * 32);\n"
         f"  Tile t;\n"

@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(1024) bg_rows_kernel(uint32_t *pre_bits, int64
                                                        int n_pre, const uint32_t *rowrun,
                                                        const uint32_t *pmask, int pmw,
                                                        uint32_t *work, int n_parts, int64_t rows) {
+  asm volatile("griddepcontrol.wait;" ::: "memory"); /* classify's results */
   if ((int)blockIdx.x < n_pre)
     carry_scan_block(blockIdx.x, pre_bits, n_tiles, tile_prefix, n_inputs);
   else
@@ -841,14 +842,27 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     if (rc != BG_OK) return rc;
     BG_CUDA(cudaLaunchKernel((const void *)prog->cls_kernel, dim3(cls_grid),
                              dim3(prog->cls_block), args, (size_t)prog->cls_smem, s));
-    bg_rows_kernel<<<prog->desc.n_pre + std::max(1, prog->desc.n_parts), 1024, 0, s>>>(
-        prm.pre_bits, prm.n_tiles, prm.tile_prefix, prm.n_inputs, prog->desc.n_pre,
-        prm.work + BG_WORK_HEAD + (int64_t)prog->desc.n_parts * (1 + rows), prog->pmask, prog->pmw,
-        prm.work, std::max(1, prog->desc.n_parts), rows);
-    BG_CUDA(cudaGetLastError());
-    const int main_grid = (int)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm);
-    BG_CUDA(cudaLaunchKernel((const void *)prog->kernel, dim3(main_grid), dim3(prog->desc.block),
-                             args, 0, s));
+    /* the row kernel and execute are launched as programmatic dependents: each may be set up
+     * while its predecessor drains, and waits (griddepcontrol.wait) before reading its results */
+    cudaLaunchAttribute pdl;
+    pdl.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.stream = s;
+    cfg.attrs = &pdl;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(prog->desc.n_pre + std::max(1, prog->desc.n_parts));
+    cfg.blockDim = dim3(1024);
+    BG_CUDA(cudaLaunchKernelEx(&cfg, bg_rows_kernel, prm.pre_bits, prm.n_tiles,
+                               (const int64_t *)prm.tile_prefix, (int)prm.n_inputs,
+                               (int)prog->desc.n_pre,
+                               (const uint32_t *)(prm.work + BG_WORK_HEAD +
+                                                  (int64_t)prog->desc.n_parts * (1 + rows)),
+                               prog->pmask, prog->pmw, prm.work,
+                               (int)std::max(1, prog->desc.n_parts), (int64_t)rows));
+    cfg.gridDim = dim3((unsigned)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm));
+    cfg.blockDim = dim3(prog->desc.block);
+    BG_CUDA(cudaLaunchKernelExC(&cfg, (const void *)prog->kernel, args));
     return BG_OK;
   }
   if (prog->pre_kernel) {
