@@ -1497,9 +1497,9 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             raise NotFusable(f"classify needs {cls_bytes(bloom_bits, cls_block)} bytes of shared memory")
     bloom = filt.bloom(bloom_bits)
     tables = (f"#define BG_EXLOG2 {log2}\n"
-              f"static __device__ const uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
-              f"static __device__ const uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
-              f"static __device__ const uint32_t bg_exinfo[{len(info_tab)}] = {{\n{_hex_array(info_tab)}\n}};\n"
+              f"static __device__ const __align__(16) uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
+              f"static __device__ const __align__(16) uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
+              f"static __device__ const __align__(16) uint32_t bg_exinfo[{len(info_tab)}] = {{\n{_hex_array(info_tab)}\n}};\n"
               f"static __device__ const uint32_t bg_exrecs[{len(rec_tab)}] = {{\n{_hex_array(rec_tab)}\n}};\n")
     basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
     cls_warps = cls_block // 32
@@ -1513,17 +1513,22 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"/* classify launch: threads per block, bytes of dynamic shared memory (read by the runtime) */\n"
         f'extern "C" __device__ const uint32_t bg_cls_cfg[2] = {{{cls_block}u, {cls_smem}u}};\n'
         f'extern "C" __global__ void __launch_bounds__({cls_block}, 1) {name}_cls(const __grid_constant__ BgParams p) {{\n'
-        f"  extern __shared__ uint32_t bg_dyn_s[];\n"
+        f"  extern __shared__ __align__(16) uint32_t bg_dyn_s[];\n"
         f"  cls_prologue(p, {len(names)});\n"
         f"  uint32_t *bg_bloom_s = bg_dyn_s;                            /* {len(bloom)} words */\n"
         f"  uint32_t *bg_exkeys_s = bg_dyn_s + {len(bloom)};            /* {len(keys)} words */\n"
         f"  uint32_t *bg_exinfo_s = bg_exkeys_s + {len(keys)};         /* {len(info_tab)} words */\n"
         f"  uint32_t *bg_exrecs_s = bg_exinfo_s + {len(info_tab)};     /* {len(rec_tab)} words */\n"
         f"  uint32_t *bg_runs_s = bg_exrecs_s + {len(rec_tab)};        /* {cls_warps * nw * 32} words */\n"
-        f"  for (int i = threadIdx.x; i < {len(bloom)}; i += blockDim.x) bg_bloom_s[i] = bg_bloom_g[i];\n"
-        f"  for (int i = threadIdx.x; i < {len(info_tab)}; i += blockDim.x) bg_exinfo_s[i] = bg_exinfo[i];\n"
+        f"  /* the tables, 16 bytes per load with several loads in flight (sizes are multiples of 4 words) */\n"
+        f"#pragma unroll 4\n"
+        f"  for (int i = threadIdx.x; i < {len(bloom) // 4}; i += blockDim.x)\n"
+        f"    reinterpret_cast<uint4 *>(bg_bloom_s)[i] = reinterpret_cast<const uint4 *>(bg_bloom_g)[i];\n"
+        f"  for (int i = threadIdx.x; i < {len(info_tab) // 4}; i += blockDim.x)\n"
+        f"    reinterpret_cast<uint4 *>(bg_exinfo_s)[i] = reinterpret_cast<const uint4 *>(bg_exinfo)[i];\n"
         f"  for (int i = threadIdx.x; i < {len(rec_tab)}; i += blockDim.x) bg_exrecs_s[i] = bg_exrecs[i];\n"
-        f"  for (int i = threadIdx.x; i < {len(keys)}; i += blockDim.x) bg_exkeys_s[i] = bg_exkeys[i];\n"
+        f"  for (int i = threadIdx.x; i < {len(keys) // 4}; i += blockDim.x)\n"
+        f"    reinterpret_cast<uint4 *>(bg_exkeys_s)[i] = reinterpret_cast<const uint4 *>(bg_exkeys)[i];\n"
         f"  __syncthreads();\n"
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
         f"  Tile t;\n"
