@@ -25,8 +25,8 @@ SPACE = [
     Tuning(part_cap=1),
     Tuning(part_cap=4, exec_groups=8),
     Tuning(merge_outputs=False, part_cap=32),              # parts of whole outputs
-    Tuning(wpt=2, min_blocks=3),
-    Tuning(wpt=1, min_blocks=4, part_cap=32, prefilter=False),
+    Tuning(single_wpt=4, single_min_blocks=2),             # unselective sets: 4 words per lane
+    Tuning(wpt=1, min_blocks=4, prefilter=False),          # single-kernel form forced
 ]
 
 

@@ -318,7 +318,7 @@ class Tuning:
                              # never in the split form, whose tiles mostly hold the marker's
                              # trigram, every AND in the single-kernel form)
     part_cap: int = 0       # most OR-ed terms one part function computes (0: 2 in the split
-                            # form, 32 in the single-kernel form)
+                            # form, 64 in the single-kernel form)
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
     min_blocks: int = 4     # __launch_bounds__ minimum resident blocks per SM (caps registers)
     edge_variants: bool = False  # separate unmasked part code for tiles away from input ends
@@ -1145,7 +1145,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         tuning = replace(tuning, block=block,
                          min_blocks=min(32, -(-tuning.min_blocks * tuning.block // block)))
     warps = tuning.block // 32
-    clusters = _cluster_terms(gen, terms, tuning.part_cap or 32)
+    clusters = _cluster_terms(gen, terms, tuning.part_cap or 64)
     funcs = []
     sig = f"const BgParams &p, const Tile &t, uint32_t *acc, {_basis_params(wpt)}"
     args = f"p, t, acc, {', '.join(f'b{i}_{j}' for i in range(8) for j in range(wpt))}"
