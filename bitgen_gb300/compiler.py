@@ -316,7 +316,8 @@ class Tuning:
     block: int = 256        # threads per CTA
     skip_interval: int = -1  # check for an all-zero marker every k AND steps (0 = never; -1:
                              # never in the split form, whose tiles mostly hold the marker's
-                             # trigram, every AND in the single-kernel form)
+                             # trigram, nor when unselective filters choose the single-kernel
+                             # form; every AND when the single-kernel form is forced)
     part_cap: int = 0       # most OR-ed terms one part function computes (0: 2 in the split
                             # form, 64 in the single-kernel form)
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
@@ -1124,10 +1125,14 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
                                 tuning.prefilter_limit * len(terms)):
             # the filter would pass most terms: single-kernel form, with its own tile shape
             # (programs whose terms have no filter at all keep the requested shape)
+            # (the terms run on every tile and mostly stay non-zero for several steps, so
+            # zero-block skipping costs more branches than it saves: off by default)
             if filt.enabled and tuning.single_wpt and tuning.single_wpt != tuning.wpt:
-                return generate_kernel(groups, replace(tuning, prefilter=False, wpt=tuning.single_wpt,
-                                                       min_blocks=tuning.single_min_blocks),
-                                       per_regex, name)
+                return generate_kernel(groups, replace(
+                    tuning, prefilter=False, wpt=tuning.single_wpt,
+                    min_blocks=tuning.single_min_blocks,
+                    skip_interval=0 if tuning.skip_interval < 0 else tuning.skip_interval),
+                    per_regex, name)
             filt = None
     if tuning.skip_interval < 0:
         tuning = replace(tuning, skip_interval=0 if filt is not None else 1)
