@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-modes", action="store_true", help="skip the batched / served legs")
     ap.add_argument("--served-requests", type=int, default=600)
     ap.add_argument("--dna-bytes", type=int, default=1 << 30, help="DNA text of the dna leg")
+    ap.add_argument("--dna-only", action="store_true",
+                    help="run only the dna leg and print its JSON (profiling the DNA kernel)")
     return ap.parse_args()
 
 
@@ -311,6 +313,11 @@ def main():
     import numpy as np
     import torch
     import torch.distributed as dist
+
+    if args.dna_only:
+        print(json.dumps(dna_leg(torch.device("cuda", 0), args.dna_bytes, max(1, args.steps),
+                                 None if args.no_cpu else args.cpu_sample)), flush=True)
+        return
 
     from bitgen_gb300.compiler import Tuning
     from bitgen_gb300.engine import Program, bytes_input, out_layout
