@@ -323,7 +323,7 @@ class Tuning:
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
     min_blocks: int = 4     # __launch_bounds__ minimum resident blocks per SM (caps registers)
     edge_variants: bool = False  # separate unmasked part code for tiles away from input ends
-    inline_lookback: bool = False
+    inline_lookback: bool = False  # look-back code inlined at each addition (else one shared function)
     lockstep: bool = False  # warps of a block run each part together (barrier between parts)
     lookback_width: int = 1  # predecessor records each lane examines per look-back step
     lookback_spin: int = 0   # look-back polls before sleeping
