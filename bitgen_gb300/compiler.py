@@ -1490,8 +1490,12 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     bloom_bits = tuning.bloom_bits
     cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
 
+    def cls_words(bits, block):     # up to the warps' byte buffers (16-byte aligned)
+        w = (1 << bits) // 32 + len(keys) + len(info_tab) + len(rec_tab) + (block // 32) * nw * 32
+        return -(-w // 4) * 4
+
     def cls_bytes(bits, block):
-        return 4 * ((1 << bits) // 32 + len(keys) + len(info_tab) + len(rec_tab) + (block // 32) * nw * 32)
+        return 4 * cls_words(bits, block) + (block // 32) * 1024 * wpt
 
     while cls_bytes(bloom_bits, cls_block) > 227 * 1024:
         if cls_block > 256:
@@ -1536,12 +1540,13 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"    reinterpret_cast<uint4 *>(bg_exkeys_s)[i] = reinterpret_cast<const uint4 *>(bg_exkeys)[i];\n"
         f"  __syncthreads();\n"
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
+        f"  uint8_t *bytes_s = reinterpret_cast<uint8_t *>(bg_dyn_s + {cls_words(bloom_bits, cls_block)}) + (threadIdx.x >> 5) * {1024 * wpt};\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
         + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    S b[8];\n"
-        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l);\n"
+        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l, bytes_s);\n"
         f"    const uint32_t {basis_decl};\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"

@@ -860,7 +860,7 @@ __device__ __forceinline__ uint32_t bloom_probe(uint32_t x, const uint32_t *bloo
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
                                           const uint32_t *bloom, const uint32_t *keys,
                                           const uint32_t *info, const uint32_t *recs, int log2,
-                                          uint32_t *run) {
+                                          uint32_t *run, uint8_t *bytes_s) {
   /* run: the tile's run words in shared memory (word w at run[32 w]); hits OR into them */
   if (p.input_kind == BG_INPUT_BASIS) {
     load_basis(p, t, b);
@@ -879,11 +879,12 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
   uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
   uint32_t pprev = __shfl_up_sync(FULL, raw[WPT - 1][6], 1);
   if (t.lane == 0) prev = pprev = 0u;
-  /* eight trigrams (two words) per step: all Bloom probes first, then the rare exact lookups.
-   * Trigram q ends at byte 8 + q of the window pprev, prev, c0, c1 (bytes 0-15); its pre3 is
-   * bytes 5 + q, 4 + q, 3 + q of the window. */
+  /* eight trigrams (two words) per step, all Bloom probes; bit 8 g + q of hits[j] = trigram q
+   * of step g (ending at byte 32 j + 8 g + q of the lane's bytes) may be a key */
+  uint32_t hits[WPT];
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
+    hits[j] = 0u;
 #pragma unroll
     for (int i = 0; i < 8; i += 2) {
       const uint32_t c0 = raw[j][i], c1 = raw[j][i + 1];
@@ -899,25 +900,23 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
       uint32_t hb = 0u;
 #pragma unroll
       for (int q = 0; q < 8; ++q) hb |= bloom_probe(k[q], bloom, q);
-      if (hb) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if ((hb >> q) & 1u) {
-            const uint32_t sel = q < 3 ? 0x0345u + 0x111u * q : q == 3 || q == 7 ? 0x0234u
-                                                               : 0x0345u + 0x111u * (q - 4);
-            const uint32_t lo = q < 3 ? pprev : q < 7 ? prev : c0;
-            const uint32_t hi = q < 3 ? prev : q < 7 ? c0 : c1;
-            const uint32_t pre3 = __byte_perm(lo, hi, sel) & 0xFFFFFFu;
-            trigram_exact(k[q] & 0xFFFFFFu, pre3, keys, info, recs, log2, run);
-          }
-      }
+      hits[j] |= hb << (4 * i);
       pprev = c0;
       prev = c1;
     }
   }
-  __syncwarp();
+  uint32_t any = 0u;
 #pragma unroll
-  for (int w = 0; w < BG_NRUN; ++w) t.run[w] = run[32 * w];
+  for (int j = 0; j < WPT; ++j) any |= hits[j];
+  const bool look = __any_sync(FULL, any != 0u);
+  if (look) { /* the warp's bytes in shared memory, for the lookups below */
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      uint4 *d = reinterpret_cast<uint4 *>(bytes_s + 32 * (t.lane * WPT + j));
+      d[0] = make_uint4(raw[j][0], raw[j][1], raw[j][2], raw[j][3]);
+      d[1] = make_uint4(raw[j][4], raw[j][5], raw[j][6], raw[j][7]);
+    }
+  }
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
     uint32_t o[8];
@@ -925,6 +924,25 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
 #pragma unroll
     for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
   }
+  if (look) {
+    /* the rare Bloom hits: the trigram ending at byte e of the warp's bytes and the three bytes
+     * before it (bytes before the warp's first byte read as zero); one lookup call site */
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      for (uint32_t m = hits[j]; m; m &= m - 1u) {
+        const int e = 32 * (t.lane * WPT + j) + __ffs(m) - 1;
+        uint32_t v[6];
+#pragma unroll
+        for (int d = 0; d < 6; ++d) v[d] = e - d >= 0 ? bytes_s[e - d] : 0u;
+        trigram_exact(v[2] | v[1] << 8 | v[0] << 16, v[3] | v[4] << 8 | v[5] << 16, keys, info,
+                      recs, log2, run);
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int w = 0; w < BG_NRUN; ++w) t.run[w] = run[32 * w];
 }
 
 /* Lanes whose words of class stream C are all ones (inside the input): an addition over C
