@@ -337,6 +337,7 @@ class Tuning:
                                    # the bytes the filters name)
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
+    inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
     single_wpt: int = 2      # words per lane (and blocks per SM below) when the compiler falls
     single_min_blocks: int = 3   # back to the single-kernel form because the filters are
                                  # unselective (0: keep wpt / min_blocks)
@@ -346,7 +347,7 @@ class Tuning:
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
-                self.cls_block, self.single_wpt, self.single_min_blocks)
+                self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts)
 
 
 @dataclass
@@ -1365,11 +1366,24 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         part_masks.append(masks)
         fn = "merge_store" if merge else "store"
         stores = "\n".join(f"  {fn}(p, t, {o}, acc_get(acc, t, {li}));" for li, o in enumerate(outs_k))
-        funcs.append(f"//@@BG_PART\n"
-                     f'extern "C" __device__ __noinline__ void bg_part_{ci}({sig}) {{\n'
+        funcs.append(f"{{PART}}"
+                     f'{{QUAL}} void bg_part_{ci}({sig}) {{\n'
                      f"  constexpr bool E = true;\n"
                      f"  acc_clear_n(acc, t, {len(outs_k)});\n" + "\n".join(blocks) + "\n" + stores + "\n}\n")
-    decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
+    # up to inline_parts parts are inlined into the execute kernel (one translation unit, no call
+    # per tile: the call would save the item loop's registers and pass the tile by memory);
+    # more parts are separate translation units compiled in parallel and called through a table
+    inline = 0 < len(parts) <= tuning.inline_parts
+    if inline:
+        # one whole-program compile of classify and execute (two sections): relocatable code
+        # measured slower for the inlined kernel
+        funcs = ["".join(f.replace("{PART}", "").replace("{QUAL}", "static __device__ __forceinline__")
+                         for f in funcs)]
+        decls = ""
+    else:
+        funcs = [f.replace("{PART}", "//@@BG_PART\n").replace("{QUAL}", 'extern "C" __device__ __noinline__')
+                 for f in funcs]
+        decls = "\n".join(f'extern "C" __device__ void bg_part_{ci}({sig});' for ci in range(len(parts)))
     # execute order: part k belongs to group k % ngroups; groups one after the other
     ngroups = max(1, min(16, tuning.exec_groups, len(parts)))
     ord_ = [k for gi in range(ngroups) for k in range(gi, len(parts), ngroups)]
@@ -1387,9 +1401,16 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             pm_table += [w, m]
     # execute dispatch: the parts' (run word, mask) pairs in shared memory and a table of the
     # part functions, so that one call site serves every part
-    fn_tab = (f"typedef void (*bg_part_fn)({sig});\n"
-              f"__device__ bg_part_fn bg_part_tab[{len(parts)}] = {{{', '.join(f'bg_part_{ci}' for ci in range(len(parts)))}}};\n"
-              f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}];\n')
+    fn_tab = ((f"typedef void (*bg_part_fn)({sig});\n"
+               f"__device__ bg_part_fn bg_part_tab[{len(parts)}] = {{{', '.join(f'bg_part_{ci}' for ci in range(len(parts)))}}};\n")
+              if not inline else "") + f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}];\n'
+    part_args = f"p, t, acc, {''.join(f'__shfl_sync(FULL, rw{i}, l), ' for i in range(pmw))}{ba}"
+    if inline:
+        dispatch = ("      switch (k) {\n" + "".join(f"        case {ci}: bg_part_{ci}({part_args}); break;\n"
+                                                 for ci in range(len(parts)))
+                    + "        default: break;\n      }\n")
+    else:
+        dispatch = f"      bg_part_tab[k]({part_args});\n"
     # classify kernel ------------------------------------------------------------------------
     gen.lines = []
     gen.indent = 4
@@ -1515,7 +1536,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     cls_smem = cls_bytes(bloom_bits, cls_block)
     cls_maxreg = max(32, min(255, 65536 // cls_block // 8 * 8))
     cls_kernel = (
-        f"//@@BG_PART\n//@@BG_UNITREG {cls_maxreg}\n{tables}"
+        f"//@@BG_PART\n" + ("" if inline else f"//@@BG_UNITREG {cls_maxreg}\n") + f"{tables}"
         f"/* per part: {pmw} (run-mask word, mask) pairs; read by the runtime's work-list kernel */\n"
         f'extern "C" __device__ const uint32_t bg_pmask[{len(pm_table)}] = {{\n{_hex_array(pm_table)}\n}};\n'
         + "".join(cand_funcs) +
@@ -1556,7 +1577,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
     comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
     src = (
-        f"//@@BG_MAXREG {maxreg}\n"
+        f"//@@BG_MAXREG {min(maxreg, cls_maxreg) if inline else maxreg}\n"
         f"#define BG_WPT {wpt}\n"
         f"#define BG_HL {gen.hl}\n"
         f"#define BG_TL {gen.tl}\n"
@@ -1631,14 +1652,13 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
                   f"      if (m && g < p.n_tiles) rw{i} = p.runs[(long long)w * p.n_tiles + g];\n"
                   f"      want |= rw{i} & m; }}\n" for i in range(pmw)) +
         f"    uint32_t sel = __ballot_sync(FULL, want != 0u);\n"
-        f"    const bg_part_fn fn = bg_part_tab[k];\n"
         f"    while (sel) {{\n"
         f"      const int l = __ffs(sel) - 1;\n"
         f"      sel &= sel - 1u;\n"
         f"      setup_tile(p, t, (unsigned int)(g0 + l), true, false);\n"
         f"      S b[8];\n"
         f"      load_basis(p, t, b);\n"
-        f"      fn(p, t, acc, {''.join(f'__shfl_sync(FULL, rw{i}, l), ' for i in range(pmw))}{ba});\n"
+        + dispatch +
         f"    }}\n"
         f"  }}\n"
         f"}}\n")
