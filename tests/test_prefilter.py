@@ -138,3 +138,17 @@ def test_large_programs_fit_classify_shared_memory():
     spec = generate_kernel(gs, Tuning())
     block, smem = map(int, re.search(r"bg_cls_cfg\[2\] = \{(\d+)u, (\d+)u\}", spec.source).groups())
     assert smem <= 227 * 1024 and block % 32 == 0 and spec.n_parts > 0
+
+
+def test_parts_inline_up_to_the_threshold():
+    """Up to Tuning.inline_parts parts are inlined into the execute kernel (one whole-program
+    compile: no part sections, a switch); more parts are separate sections called through a
+    table."""
+    from bitgen_gb300.compiler import generate_kernel
+    gs = [compile_group(g) for g in workloads.throughput_patterns(seed=3, n=64).groups(4)]
+    inl = generate_kernel(gs, Tuning())
+    assert 0 < inl.n_parts <= Tuning().inline_parts
+    assert inl.source.count("//@@BG_PART") == 1 and "bg_part_tab" not in inl.source
+    assert "static __device__ __forceinline__ void bg_part_0(" in inl.source
+    sep = generate_kernel(gs, Tuning(inline_parts=0))
+    assert sep.source.count("//@@BG_PART") == sep.n_parts + 1 and "bg_part_tab[k](" in sep.source
