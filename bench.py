@@ -393,6 +393,12 @@ def main():
         torch.cuda.synchronize(dev)
         kt.append(k0.elapsed_time(k1))
     kernel_ms = statistics.median(kt)
+    # work counters of the last launch (read back after the timed region)
+    st = plan.stats(sp)
+    work = {"form": st["form"], "tiles": st["tiles"]}
+    if st["form"] == "split":
+        work.update(parts=len(st["tiles_run"]), rows_listed=sum(st["rows"]),
+                    part_runs_per_tile=round(sum(st["tiles_run"]) / max(1, st["tiles"]), 4))
 
     # end to end through the public API: pinned host bytes in, counts out, every step.  Serial:
     # copy, scan, read back one after another on one stream.  Streamed (StreamScanner, the
@@ -444,7 +450,8 @@ def main():
                               "block": tuning.block, "skip_interval": tuning.skip_interval},
                    "registers": info.get("registers"), "adds": info.get("adds"),
                    "pre_pass_adds": info.get("pre_adds"),
-                   "compile_s": round(compile_s, 2), "bit_exact_vs_cpu_sample": check},
+                   "compile_s": round(compile_s, 2), "bit_exact_vs_cpu_sample": check,
+                   "work": work},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": recorded_traffic(),
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg,

@@ -69,6 +69,8 @@ SIGNATURES = {
     "bg_plan_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "bg_plan_set_positions": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "bg_plan_positions_written": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "bg_plan_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int64),
+                              C.POINTER(C.c_int64)]),
     "bg_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "bg_plan_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
     "bg_plan_destroy": (C.c_int, [C.c_void_p]),

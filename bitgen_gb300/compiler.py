@@ -367,6 +367,7 @@ class KernelSpec:
     n_run: int = 0          # split form: run-mask words per tile (0 = single-kernel form)
     merges: bool = False    # parts OR into shared outputs: launches need the output streams
     n_parts: int = 0        # split form: part functions
+    part_outputs: List[List[int]] = field(default_factory=list)  # split form: outputs of each part
 
     @property
     def tile_words(self):
@@ -1665,4 +1666,5 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     return KernelSpec(source=src, name=name, n_outputs=len(names), n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,
                       n_nodes=len(d.nodes), output_names=names, tail_lanes=gen.tl,
-                      n_pre=len(gen.pre), n_run=nw, merges=merge, n_parts=len(parts))
+                      n_pre=len(gen.pre), n_run=nw, merges=merge, n_parts=len(parts),
+                      part_outputs=[list(o) for o in parts])

@@ -782,6 +782,44 @@ int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written) {
   return BG_OK;
 }
 
+int bg_plan_stats(bg_plan *plan, void *stream, int32_t n_parts, int64_t *tiles_run, int64_t *rows) {
+  if (!plan || n_parts < 0 || (n_parts > 0 && (!tiles_run || !rows)))
+    return fail(BG_ERR_INVALID, "bg_plan_stats: bad arguments");
+  const bg_program *prog = plan->prog;
+  if (prog->desc.n_run <= 0 || !prog->pmask || !plan->d_runs || !plan->d_work)
+    return fail(BG_ERR_INVALID, "bg_plan_stats: single-kernel program (every tile runs every term)");
+  if (n_parts != prog->desc.n_parts) return fail(BG_ERR_INVALID, "bg_plan_stats: n_parts differs");
+  const int64_t T = plan->n_tiles, NR = prog->desc.n_run, pmw = prog->pmw;
+  std::vector<uint32_t> runs((size_t)(NR * T)), pm((size_t)(n_parts * pmw * 2)), cnt((size_t)n_parts);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!runs.empty())
+    BG_CUDA(cudaMemcpyAsync(runs.data(), plan->d_runs, runs.size() * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+  if (n_parts > 0) {
+    BG_CUDA(cudaMemcpyAsync(pm.data(), prog->pmask, pm.size() * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+    BG_CUDA(cudaMemcpyAsync(cnt.data(), plan->d_work + BG_WORK_HEAD, cnt.size() * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, s));
+  }
+  BG_CUDA(cudaStreamSynchronize(s));
+  /* the execute pass runs part k on tile g when one of k's (word, mask) pairs meets the tile's
+     run word, and walks the rows the work list holds for k */
+  for (int32_t k = 0; k < n_parts; ++k) {
+    int64_t n = 0;
+    for (int64_t g = 0; g < T; ++g) {
+      bool any = false;
+      for (int64_t e = 0; e < pmw && !any; ++e) {
+        const uint32_t w = pm[(size_t)((k * pmw + e) * 2)], m = pm[(size_t)((k * pmw + e) * 2 + 1)];
+        any = m != 0u && w < (uint32_t)NR && (runs[(size_t)(w * T + g)] & m) != 0u;
+      }
+      n += any;
+    }
+    tiles_run[k] = n;
+    rows[k] = (int64_t)cnt[(size_t)k];
+  }
+  return BG_OK;
+}
+
 int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t debug_wait_tile) {
   if (!plan) return fail(BG_ERR_INVALID, "bg_plan_set_wait_limit: null plan");
   plan->spin_limit = spin_limit_cycles;

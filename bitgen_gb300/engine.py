@@ -214,6 +214,7 @@ class ScanResult:
     word_offsets: List[int]
     words: List[int]
     positions: Optional["np.ndarray"] = None  # sorted u64 (output << 52 | input << 32 | pos)
+    stats: Optional[dict] = None  # work counters of the launch (Program.scan(stats=True))
 
     def stream(self, output: int, input_index: int = 0) -> torch.Tensor:
         o = self.word_offsets[input_index]
@@ -299,6 +300,22 @@ class Plan:
         v = C.c_int64()
         N.check(N.lib().bg_plan_positions_written(self._h, stream, C.byref(v)), "bg_plan_positions_written")
         return int(v.value)
+
+    def stats(self, stream: int) -> dict:
+        """Work counters of the last launch (waits for `stream`), the counterpart of the
+        reference's optional ``dyn_stats`` buffer: the tiles of the launch and, for a split-form
+        program, per part the tiles the execute pass ran it on (``tiles_run``), the 32-tile rows
+        of its work list (``rows``) and the outputs it writes (``part_outputs``).  A
+        single-kernel program runs every term on every tile."""
+        spec = self.program.spec
+        st = {"form": "split" if spec.n_parts else "single-kernel", "tiles": self.tiles}
+        if spec.n_parts:
+            k = spec.n_parts
+            tiles_run, rows = (C.c_int64 * k)(), (C.c_int64 * k)()
+            N.check(N.lib().bg_plan_stats(self._h, stream, k, tiles_run, rows), "bg_plan_stats")
+            st.update(tiles_run=list(tiles_run), rows=list(rows),
+                      part_outputs=[list(o) for o in spec.part_outputs])
+        return st
 
     def set_wait_limit(self, cycles: int, debug_wait_tile: int = -1):
         N.check(N.lib().bg_plan_set_wait_limit(self._h, cycles, debug_wait_tile), "bg_plan_set_wait_limit")
@@ -416,7 +433,7 @@ class Program:
              out: Optional[torch.Tensor] = None, out_offsets: Optional[Sequence[int]] = None,
              out_stride: Optional[int] = None, stream: Optional[torch.cuda.Stream] = None,
              sync: bool = True, max_iterations: Optional[int] = None,
-             positions: bool = False, pos_capacity: int = 1 << 22) -> ScanResult:
+             positions: bool = False, pos_capacity: int = 1 << 22, stats: bool = False) -> ScanResult:
         dev = inp.data.device
         if out_offsets is None:
             offs, words, total = out_layout(inp.lengths)
@@ -431,7 +448,7 @@ class Program:
         out_ptr = out.data_ptr() if streams else 0
         cnt_ptr = cnt.data_ptr() if counts else 0
         stride = out_stride if out_stride is not None else total
-        pos = None
+        pos = st = None
         if self.fused:
             plan = self.plan(inp, offs, stride)
             pbuf = torch.empty(pos_capacity, dtype=torch.int64, device=dev) if positions else None
@@ -444,6 +461,8 @@ class Program:
                 n = plan.positions_written(sp)
                 pos = np.sort(pbuf[:min(n, pos_capacity)].cpu().numpy().view(np.uint64))
                 plan.set_positions(None)
+            if stats:
+                st = plan.stats(sp)
         else:
             if max_iterations is None:  # a monotone Pablo loop settles within n iterations
                 max_iterations = 4 * max(inp.lengths + [0]) + 64
@@ -452,7 +471,7 @@ class Program:
             N.check(N.lib().bg_interp_run(self._interp, C.byref(lay), inp.data.data_ptr(),
                                           out_ptr or None, cnt_ptr or None, max_iterations, sp),
                     "bg_interp_run")
-        return ScanResult(out if streams else None, cnt, offs, words, pos)
+        return ScanResult(out if streams else None, cnt, offs, words, pos, st)
 
     def close(self):
         for p in self._plans.values():

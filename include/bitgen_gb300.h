@@ -133,6 +133,14 @@ int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t deb
 int bg_plan_set_positions(bg_plan *plan, unsigned long long *positions, int64_t capacity);
 /* Number of positions the last launch on `stream` produced (waits for the stream). */
 int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written);
+/* Work counters of the last launch on `stream` (waits for the stream); replaces the optional
+ * `dyn_stats` buffer of the reference's generated kernel (backend/cuda/template/
+ * template_dyn_stat.py:39-87, filled at codegen/gen_cuda.py:152-170), whose per-tile loop
+ * counters have no meaning in this engine.  For each of the n_parts parts of a split-form
+ * program: tiles_run[k] = tiles the execute pass ran part k on, rows[k] = 32-tile rows of its
+ * work list.  Reads the plan's run masks back to the host (4 * n_run bytes per tile): not for
+ * timed loops.  BG_ERR_INVALID for a single-kernel program, where every tile runs every term. */
+int bg_plan_stats(bg_plan *plan, void *stream, int32_t n_parts, int64_t *tiles_run, int64_t *rows);
 /* Enqueue one scan on `stream`: input is the device base of the bytes / basis planes;
  * out_streams (may be NULL) receives n_outputs streams in the reference bit layout, positions at
  * or beyond an input's length cleared; counts (may be NULL) receives uint64 popcounts

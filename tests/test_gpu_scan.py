@@ -315,3 +315,46 @@ def test_large_pattern_set_matches_c_oracle(cuda):
             assert d is None, (i, k, d)
         assert res.counts[:, i].cpu().tolist() == wc
     assert int(res.counts.sum()) > 0
+
+
+def test_work_counters(cuda):
+    """`scan(stats=True)` reports, per part of a split-form program, the tiles the execute pass
+    ran it on and the rows of its work list.  Every tile holding a match of an output ran a part
+    that writes that output; a listed row has at least one such tile; the trigram filter keeps
+    most parts off most tiles of printable text; a single-kernel program reports only its tiles."""
+    ps = workloads.throughput_patterns(seed=91, n=64)
+    groups = [compile_group(g) for g in ps.groups(4)]
+    prog = Program(groups)
+    assert prog.fused and prog.spec.n_parts > 0
+    data = workloads.plant(workloads.printable_text((1 << 19) + 333, 92), ps.witnesses, 4096, 93)
+    inp = pack_bytes([data])
+    res = prog.scan(inp, stats=True)
+    st = res.stats
+    T = prog.tiles_for([data.size])
+    R = -(-T // 32)
+    assert st["form"] == "split" and st["tiles"] == T
+    assert len(st["tiles_run"]) == len(st["rows"]) == len(st["part_outputs"]) == prog.spec.n_parts
+    for k, (n, r) in enumerate(zip(st["tiles_run"], st["rows"])):
+        assert 0 <= r <= R and r <= n <= min(T, 32 * r), (k, n, r)
+    tw = prog.spec.tile_words
+    streams = res.streams.cpu().numpy()
+    for o in range(prog.n_outputs):
+        bits = np.unpackbits(streams[o, :res.words[0]].astype(">u4").view(np.uint8))
+        need = np.unique(np.nonzero(bits)[0] // 32 // tw).size
+        ran = sum(n for n, outs in zip(st["tiles_run"], st["part_outputs"]) if o in outs)
+        assert ran >= need, (o, ran, need)
+    assert int(res.counts.sum()) > 0
+    assert sum(st["tiles_run"]) <= 0.5 * T * prog.spec.n_parts
+    # the counters read back do not disturb the next launch, which reports the same work
+    again = prog.scan(inp, stats=True)
+    assert again.stats == st
+    assert all(torch.equal(again.stream(o), res.stream(o)) for o in range(prog.n_outputs))
+    # several ragged inputs in one launch
+    items = [data[:0], data[:5], data[: 70_001], data]
+    many = prog.scan(pack_bytes(items), stats=True).stats
+    assert many["tiles"] == prog.tiles_for([len(x) for x in items])
+    for n, r in zip(many["tiles_run"], many["rows"]):
+        assert r <= n <= min(many["tiles"], 32 * r)
+    single = Program(groups, tuning=Tuning(prefilter=False))
+    assert single.spec.n_parts == 0
+    assert single.scan(inp, stats=True).stats == {"form": "single-kernel", "tiles": single.tiles_for([data.size])}

@@ -152,3 +152,16 @@ def test_parts_inline_up_to_the_threshold():
     assert "static __device__ __forceinline__ void bg_part_0(" in inl.source
     sep = generate_kernel(gs, Tuning(inline_parts=0))
     assert sep.source.count("//@@BG_PART") == sep.n_parts + 1 and "bg_part_tab[k](" in sep.source
+
+
+def test_split_form_part_outputs():
+    """The split form records which outputs each part writes (read with the work counters):
+    every output is written by some part, every part writes at least one output, and with
+    merged outputs each part holds at most part_cap terms, so at most that many outputs."""
+    from bitgen_gb300.compiler import generate_kernel
+    gs = [compile_group(g) for g in workloads.throughput_patterns(seed=3, n=256).groups(16)]
+    spec = generate_kernel(gs, Tuning())
+    assert spec.n_parts == len(spec.part_outputs) > 0
+    assert sorted({o for outs in spec.part_outputs for o in outs}) == list(range(spec.n_outputs))
+    assert all(0 < len(outs) <= 2 for outs in spec.part_outputs)
+    assert generate_kernel(gs, Tuning(prefilter_limit=0.0)).part_outputs == []
