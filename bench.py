@@ -437,6 +437,18 @@ def main():
     b_alg = n + prog.n_outputs * ((n + 31) // 32) * 4   # input once + each output stream once
     achieved = b_alg / (kernel_ms / 1e3) / 1e9
     info = prog.info()
+    # integer work: Pablo IR operations of the compiled groups per 32-bit word (before any
+    # tile skipping) x input words, against the dense ALU rate of 64 32-bit logical results per
+    # clock per SM at the maximum SM clock
+    from bitgen_gb300.pablo import Op, walk
+    ir_ops = sum(1 for g in gs for s in walk(g.stmts) if isinstance(s, Op) and s.op != "assign")
+    ops_launch = ir_ops * ((n + 31) // 32)
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    alu_peak = sm_count * 64 * float((clk or {}).get("sm_max_mhz") or 2070.0) * 1e6
+    int_ops = {"ir_ops_per_word": ir_ops, "ops_per_launch": ops_launch,
+               "achieved_Tops": round(ops_launch / (kernel_ms / 1e3) / 1e12, 2),
+               "dense_alu_peak_Tops": round(alu_peak / 1e12, 2),
+               "frac_of_dense_alu": round(ops_launch / (kernel_ms / 1e3) / alu_peak, 3)}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -455,7 +467,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "traffic": recorded_traffic(),
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg,
-                     "kernel_ms": round(kernel_ms, 4)},
+                     "kernel_ms": round(kernel_ms, 4), "int_ops": int_ops},
         "e2e": {"value": round(total_bytes / (e2e_ms / 1e3) / 1e9, 3), "unit": UNIT,
                 "h2d_bytes_per_step": n, "d2h_bytes_per_step": prog.n_outputs * 8,
                 "mode": "streamed (StreamScanner: copy of step i+1 beside the scan of step i, "
