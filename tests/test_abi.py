@@ -44,6 +44,8 @@ def test_bad_arguments_are_reported(native):
     bad = (N.Instr * 1)(N.Instr(0, 3, 0, 1, -1, 0))  # writes a basis slot
     assert native.bg_interp_create(bad, 1, 12, None, 0, C.byref(out)) == N.BG_ERR_INVALID
     assert native.bg_plan_launch(None, None, None, None, None) == N.BG_ERR_INVALID
+    assert native.bg_plan_stats(None, None, 0, None, None) == N.BG_ERR_INVALID
+    assert b"bg_plan_stats" in native.bg_last_error()
     assert b"bg_" in native.bg_last_error() or native.bg_last_error()
 
 
