@@ -12,8 +12,14 @@ names, argument meaning and return shapes:
   that ``bitgen/from_icgrep.py:169-193`` imports.  It returns
   ``(result, tmp_streams, kernel_handle, run_fn, dyn_stats)``: ``result`` is
   ``uint32 [S, M, G, W]``; ``run_fn(basis)`` scans the basis tensor and writes ``result``;
-  ``kernel_handle.free()`` releases the program.  ``tmp_streams`` and ``dyn_stats`` are ``None``
-  (the fused engine needs no global scratch streams).  The reference kernel ORs into ``result``
+  ``kernel_handle.free()`` releases the program.  ``tmp_streams`` is ``None`` (the fused engine
+  needs no global scratch streams).  ``dyn_stats`` is ``None`` unless the configuration sets
+  ``pass_inst_stats_dyn`` (the reference then builds from ``template_dyn_stat.py:39-87`` and its
+  runner sums ``dyn_stats[..., :1]`` and ``dyn_stats[..., 1:]``, ``from_icgrep.py:619-640``):
+  here it is ``int64 [S, 1, P, 2]``, refreshed by every ``run_fn`` call, with per part of the
+  program (P = 1 for a single-kernel program) ``[..., 0]`` = the tiles it ran on (the
+  reference: tile-loop iterations) and ``[..., 1]`` = the 32-tile rows of its work list (the
+  reference: per-iteration advance offsets).  The reference kernel ORs into ``result``
   and relies on the caller zeroing it (``from_icgrep.py:546-552``); this engine writes it with
   plain stores, so zeroing is harmless but not needed.
 
@@ -53,6 +59,20 @@ class KernelHandle:
             self.program = None
 
 
+def _cfg_flag(cfg, key: str) -> bool:
+    """A flag of the runner's configuration: the reference's config module
+    (``bitgen/config.py:19``, ``get_config(key)`` gives None for an unset key), any object with
+    such a ``get_config``, or a plain dict."""
+    if cfg is None:
+        return False
+    if hasattr(cfg, "get_config"):
+        try:
+            return bool(cfg.get_config(key))
+        except (KeyError, AttributeError):
+            return False
+    return bool(cfg.get(key)) if isinstance(cfg, dict) else False
+
+
 def init_kernel(regex_func_num: int, input_stream_tensor, basic_stream_tensor: torch.Tensor,
                 cfg: Optional[dict] = None, groups: Optional[Sequence[Group]] = None,
                 tuning: Optional[Tuning] = None):
@@ -70,14 +90,23 @@ def init_kernel(regex_func_num: int, input_stream_tensor, basic_stream_tensor: t
     program = Program(list(groups), tuning=tuning)
     result = torch.zeros((S, M, G, W), dtype=torch.uint32, device=basic_stream_tensor.device)
     out_offsets = [m * G * W for m in range(M)]
+    dyn_stats = None
+    if _cfg_flag(cfg, "pass_inst_stats_dyn"):
+        P = max(1, program.spec.n_parts) if program.fused else 1
+        dyn_stats = torch.zeros((S, 1, P, 2), dtype=torch.int64, device=basic_stream_tensor.device)
 
     def run_fn(basis: torch.Tensor):
         inp = basis_input(basis)
-        program.scan(inp, streams=True, counts=False, out=result, out_offsets=out_offsets,
-                     out_stride=W)
+        res = program.scan(inp, streams=True, counts=False, out=result, out_offsets=out_offsets,
+                           out_stride=W, stats=dyn_stats is not None)
+        st = res.stats
+        if st is not None and st["form"] == "split":
+            dyn_stats[0, 0].copy_(torch.tensor(list(zip(st["tiles_run"], st["rows"])), dtype=torch.int64))
+        elif st is not None:
+            dyn_stats[0, 0, 0, 0] = st["tiles"]
         return None
 
-    return result, None, KernelHandle(program), run_fn, None
+    return result, None, KernelHandle(program), run_fn, dyn_stats
 
 
 _MODULE = '''"""Generated by bitgen_gb300.backend.write_kernel_module (drop-in kernels/kernel_0.py)."""

@@ -58,3 +58,61 @@ def test_generated_kernels_compile_for_sm103a(native, wpt):
     src = spec.source.encode()
     rc = native.bg_nvrtc_check(src, len(src), b"bg_scan", buf, len(buf))
     assert rc == N.BG_OK, buf.value.decode()
+
+
+def test_runner_configuration_flags():
+    """init_kernel reads flags from an object with get_config (the reference's config module
+    returns None for an unset key; this one raises KeyError) or from a plain dict."""
+    from bitgen_gb300.backend import _cfg_flag
+
+    class Cfg:
+        def __init__(self, **kw):
+            self.kw = kw
+
+        def get_config(self, key):
+            return self.kw[key]
+
+    assert _cfg_flag(Cfg(pass_inst_stats_dyn=1), "pass_inst_stats_dyn")
+    assert not _cfg_flag(Cfg(pass_inst_stats_dyn=0), "pass_inst_stats_dyn")
+    assert not _cfg_flag(Cfg(), "pass_inst_stats_dyn")
+    assert _cfg_flag({"pass_inst_stats_dyn": True}, "pass_inst_stats_dyn")
+    assert not _cfg_flag({}, "pass_inst_stats_dyn") and not _cfg_flag(None, "pass_inst_stats_dyn")
+
+
+@pytest.mark.parametrize("n_parts", [0, 3])
+def test_dyn_stats_filled_from_scan_counters(monkeypatch, n_parts):
+    """run_fn copies the scan's work counters into the dyn_stats tensor init_kernel returned:
+    per part (tiles run, rows) for a split-form program, (tiles, 0) for a single kernel.  The
+    program is a stand-in here (no device)."""
+    from types import SimpleNamespace
+    import torch
+    import bitgen_gb300.backend as B
+
+    stats = ({"form": "split", "tiles": 10, "tiles_run": [1, 0, 7], "rows": [1, 0, 2],
+              "part_outputs": [[0], [1], [1]]} if n_parts else {"form": "single-kernel", "tiles": 10})
+
+    class Prog:
+        fused = True
+        spec = SimpleNamespace(n_parts=n_parts)
+
+        def __init__(self, groups, tuning=None):
+            pass
+
+        def scan(self, inp, **kw):
+            assert kw["stats"] and kw["out_stride"] == 4
+            return SimpleNamespace(stats=stats)
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(B, "Program", Prog)
+    monkeypatch.setattr(B, "basis_input", lambda basis: None)
+    basis = torch.zeros((1, 1, 8, 4), dtype=torch.uint32)
+    result, tmp, handle, run_fn, dyn = B.init_kernel(2, None, basis, {"pass_inst_stats_dyn": 1},
+                                                     groups=[object(), object()])
+    assert tuple(result.shape) == (1, 1, 2, 4) and tmp is None
+    assert tuple(dyn.shape) == (1, 1, max(1, n_parts), 2) and int(dyn.sum()) == 0
+    run_fn(basis)
+    want = [[1, 1], [0, 0], [7, 2]] if n_parts else [[10, 0]]
+    assert dyn[0, 0].tolist() == want
+    handle.free()
