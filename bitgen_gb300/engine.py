@@ -214,7 +214,7 @@ class ScanResult:
     word_offsets: List[int]
     words: List[int]
     positions: Optional["np.ndarray"] = None  # sorted u64 (output << 52 | input << 32 | pos)
-    stats: Optional[dict] = None  # work counters of the launch (Program.scan(stats=True))
+    stats: Optional[dict] = None  # work counters (scan(stats=True); None on the whole-stream executor)
 
     def stream(self, output: int, input_index: int = 0) -> torch.Tensor:
         o = self.word_offsets[input_index]
