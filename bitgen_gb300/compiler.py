@@ -341,13 +341,16 @@ class Tuning:
     single_wpt: int = 2      # words per lane (and blocks per SM below) when the compiler falls
     single_min_blocks: int = 3   # back to the single-kernel form because the filters are
                                  # unselective (0: keep wpt / min_blocks)
+    basis_filter: bool = False   # split form: rebuild the bytes of basis-plane inputs and run
+                                 # the trigram filter on them (else every term runs there)
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
                 self.min_blocks, self.edge_variants, self.inline_lookback, self.lockstep,
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
-                self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts)
+                self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
+                self.basis_filter)
 
 
 @dataclass
@@ -1590,6 +1593,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_NRUN {nw}\n"
         f"#define BG_BLOOM_BITS {bloom_bits}\n"
         f"#define BG_PREFILTER 1\n"
+        f"#define BG_BASIS_FILTER {int(tuning.basis_filter)}\n"
         f'#include "bg_device.cuh"\n'
         f"using namespace bg;\n"
         f"#define VM(j) (E ? t.vm.w[j] : 0xffffffffu)\n"

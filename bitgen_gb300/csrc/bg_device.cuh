@@ -855,27 +855,44 @@ __device__ __forceinline__ uint32_t bloom_probe(uint32_t x, const uint32_t *bloo
   return __funnelshift_r(w, w, a) & (1u << q);
 }
 
+#ifndef BG_BASIS_FILTER
+#define BG_BASIS_FILTER 0
+#endif
 /* Load the tile's bytes, fill t.run from the trigram scan (warp-uniform) and transpose the bytes
- * into the basis.  Inputs given as basis planes have no bytes to scan: every term runs. */
+ * into the basis.  Inputs given as basis planes: every term runs, or, with BG_BASIS_FILTER, the
+ * bytes are rebuilt from the planes and scanned the same way (bytes at or beyond the input's
+ * length are the planes' padding there, which can only add hits). */
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
                                           const uint32_t *bloom, const uint32_t *keys,
                                           const uint32_t *info, const uint32_t *recs, int log2,
                                           uint32_t *run, uint8_t *bytes_s) {
   /* run: the tile's run words in shared memory (word w at run[32 w]); hits OR into them */
-  if (p.input_kind == BG_INPUT_BASIS) {
+  if (!BG_BASIS_FILTER && p.input_kind == BG_INPUT_BASIS) {
     load_basis(p, t, b);
 #pragma unroll
     for (int w = 0; w < BG_NRUN; ++w) t.run[w] = FULL;
     return;
   }
+  const bool from_basis = BG_BASIS_FILTER && p.input_kind == BG_INPUT_BASIS;
   if (t.lane == 0) {
 #pragma unroll
     for (int w = 0; w < BG_NRUN; ++w) run[32 * w] = 0u;
   }
   __syncwarp();
   uint32_t raw[WPT][8];
+  if (from_basis) {
+    load_basis(p, t, b);
 #pragma unroll
-  for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
+    for (int j = 0; j < WPT; ++j) {
+      uint32_t o[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) o[i] = b[i].w[j];
+      untranspose32(o, raw[j]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
+  }
   uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
   uint32_t pprev = __shfl_up_sync(FULL, raw[WPT - 1][6], 1);
   if (t.lane == 0) prev = pprev = 0u;
@@ -917,12 +934,14 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
       d[1] = make_uint4(raw[j][4], raw[j][5], raw[j][6], raw[j][7]);
     }
   }
+  if (!from_basis) {
 #pragma unroll
-  for (int j = 0; j < WPT; ++j) {
-    uint32_t o[8];
-    transpose32(raw[j], o);
+    for (int j = 0; j < WPT; ++j) {
+      uint32_t o[8];
+      transpose32(raw[j], o);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
+      for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
+    }
   }
   if (look) {
     /* the rare Bloom hits: the trigram ending at byte e of the warp's bytes and the three bytes

@@ -54,4 +54,33 @@ __device__ __forceinline__ void transpose32(const uint32_t u[8], uint32_t out[8]
   }
 }
 
+/* The inverse: 8 plane words back to 32 bytes.  Byte m of plane word i (i < 4) is byte i of
+ * the flipped piece L[3 - m] (of H[3 - m] for plane word 4 + i), a 4x4 byte transpose that the
+ * same two byte-permute stages undo; the anti-diagonal flip is its own inverse. */
+__device__ __forceinline__ void untranspose32(const uint32_t in[8], uint32_t u[8]) {
+  uint32_t L[4], H[4];
+  {
+    const uint32_t P = __byte_perm(in[0], in[1], 0x5140), Q = __byte_perm(in[0], in[1], 0x7362);
+    const uint32_t R = __byte_perm(in[2], in[3], 0x5140), T = __byte_perm(in[2], in[3], 0x7362);
+    L[3] = __byte_perm(P, R, 0x5410);
+    L[2] = __byte_perm(P, R, 0x7632);
+    L[1] = __byte_perm(Q, T, 0x5410);
+    L[0] = __byte_perm(Q, T, 0x7632);
+  }
+  {
+    const uint32_t P = __byte_perm(in[4], in[5], 0x5140), Q = __byte_perm(in[4], in[5], 0x7362);
+    const uint32_t R = __byte_perm(in[6], in[7], 0x5140), T = __byte_perm(in[6], in[7], 0x7362);
+    H[3] = __byte_perm(P, R, 0x5410);
+    H[2] = __byte_perm(P, R, 0x7632);
+    H[1] = __byte_perm(Q, T, 0x5410);
+    H[0] = __byte_perm(Q, T, 0x7632);
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const unsigned long long x = flip_anti_diag((unsigned long long)L[r] | ((unsigned long long)H[r] << 32));
+    u[2 * r] = (uint32_t)x;
+    u[2 * r + 1] = (uint32_t)(x >> 32);
+  }
+}
+
 }  // namespace bg

@@ -49,11 +49,13 @@ def test_bad_arguments_are_reported(native):
     assert b"bg_" in native.bg_last_error() or native.bg_last_error()
 
 
-@pytest.mark.parametrize("wpt", [1, 2, 4])
-def test_generated_kernels_compile_for_sm103a(native, wpt):
+@pytest.mark.parametrize("wpt,basis_filter", [(1, False), (2, False), (4, False), (1, True),
+                                               (2, True)])
+def test_generated_kernels_compile_for_sm103a(native, wpt, basis_filter):
     ps = workloads.throughput_patterns(seed=3, n=32)
     groups = [compile_group(g) for g in ps.groups(2)]
-    spec = generate_kernel(groups, Tuning(wpt=wpt))
+    spec = generate_kernel(groups, Tuning(wpt=wpt, basis_filter=basis_filter))
+    assert spec.n_parts > 0 and f"#define BG_BASIS_FILTER {int(basis_filter)}" in spec.source
     buf = C.create_string_buffer(1 << 16)
     src = spec.source.encode()
     rc = native.bg_nvrtc_check(src, len(src), b"bg_scan", buf, len(buf))
