@@ -14,9 +14,14 @@ parts of the reference are what pin the oracle:
   ``datasets_small/snort_10KB.input``, 4 groups, published count 16;
 * ``parser.json``    - the reference parser's instruction list (type, operands, result) for the
   hand-written fixture bitgen/bitparser/xml_lexical_parsing.pablo and for Pablo emitted by this
-  project (while-loop form), to pin the dialect this project's parser accepts.
+  project (while-loop form), to pin the dialect this project's parser accepts;
+* ``grouping.json``  - the reference entry script's regex grouping (``group_regex_in_list`` /
+  ``balance_regex_groups`` / ``regex_custom_length``, scripts/run_bitgen.py:71-116) on the
+  README regexes, the synthetic workloads' pattern sets and edge cases.  The script's module
+  imports the GPU runner, so only those three function definitions are taken from its source
+  and executed.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [grouping]   (``grouping``: only grouping.json)
 """
 
 from __future__ import annotations
@@ -52,7 +57,49 @@ def import_reference():
     return cfg
 
 
+def reference_grouping():
+    """The three grouping functions of scripts/run_bitgen.py, from its source."""
+    import ast
+    import re
+    path = os.path.join(REF, "scripts", "run_bitgen.py")
+    with open(path) as f:
+        tree = ast.parse(f.read(), path)
+    keep = {"regex_custom_length", "balance_regex_groups", "group_regex_in_list"}
+    mod = ast.Module([n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in keep],
+                     type_ignores=[])
+    ns = {"re": re}
+    exec(compile(mod, path, "exec"), ns)
+    assert keep <= set(ns)
+    return ns
+
+
+def write_grouping():
+    ref = reference_grouping()
+    sys.path.insert(0, REPO)
+    from bitgen_gb300 import workloads
+    from bitgen_gb300.grouping import read_regex_file
+    readme = read_regex_file(os.path.join(REF, "datasets_small/snort_small.regex"))
+    thr = list(workloads.throughput_patterns(seed=3, n=256).regexes)
+    dna = list(workloads.dna_motifs(64, seed=5).regexes)
+    hand = [r"\x41\x42", "abc", "[a-z]+q", "hello.*world", "x", "yy", "zzz[0-9]", r"[\x00-\x1f]z",
+            "q[^a]{2,4}", r"\x2f\x2a.*\x2a\x2f"]
+    cases = []
+    for name, rx, ns in (("readme", readme, (4, 1, 0, 3, 20)), ("throughput", thr, (16, 3)),
+                         ("dna", dna, (4,)), ("hand", hand, (3, 5, 1, 0, -1, 100))):
+        for n in ns:
+            groups = ref["group_regex_in_list"](list(rx), n, 1)
+            cases.append({"set": name, "regexes": rx, "n_groups": n, "groups": groups,
+                          "lengths": [ref["regex_custom_length"](r) for r in rx]})
+    with open(os.path.join(HERE, "grouping.json"), "w") as f:
+        json.dump({"cases": cases}, f, indent=0)
+
+
 def main():
+    if sys.argv[1:] == ["grouping"]:
+        write_grouping()
+        print("grouping.json written to", HERE)
+        return
+    write_grouping()
     cfg = import_reference()
     import torch
     from bitgen import bitstream as ref_bs

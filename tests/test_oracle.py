@@ -180,8 +180,20 @@ def test_grouping_follows_reference_rule():
     assert sorted(sum(groups, [])) == sorted(rx)
     loads = [sum(regex_custom_length(r) for r in g) for g in groups]
     assert max(loads) - min(loads) <= max(regex_custom_length(r) for r in rx)
-    assert group_regex_in_list(rx[:2], 5) == [[r"\x41\x42"], ["abc"]] or len(group_regex_in_list(rx[:2], 5)) == 2
+    assert group_regex_in_list(rx[:2], 5) == [[r"\x41\x42"], ["abc"]]   # both length 3, stable
     assert group_regex_in_list(rx, 0) == [[r] for r in rx]
+
+
+def test_grouping_matches_reference_vectors():
+    """Groups (and custom lengths) equal those of the reference entry script's own functions
+    (scripts/run_bitgen.py:71-116, run by tests/golden/make_golden.py) on the README regexes,
+    the synthetic workloads' sets and edge-case group counts."""
+    with open(os.path.join(GOLDEN, "grouping.json")) as f:
+        cases = json.load(f)["cases"]
+    assert len(cases) >= 10
+    for c in cases:
+        assert [regex_custom_length(r) for r in c["regexes"]] == c["lengths"], c["set"]
+        assert group_regex_in_list(c["regexes"], c["n_groups"]) == c["groups"], (c["set"], c["n_groups"])
 
 
 def test_readme_known_answer_count_16():
