@@ -15,6 +15,9 @@ parts of the reference are what pin the oracle:
 * ``parser.json``    - the reference parser's instruction list (type, operands, result) for the
   hand-written fixture bitgen/bitparser/xml_lexical_parsing.pablo and for Pablo emitted by this
   project (while-loop form), to pin the dialect this project's parser accepts;
+* ``bitstream.npz``  - ``Bitstream`` (bitgen/bitstream.py:27-73), the runner's result reader, on
+  seeded uint32 streams: set-bit positions of 1-D streams and ``get_count_array`` of
+  ``[S, M, G, W]`` results, to pin the bit order this project's outputs are read with;
 * ``grouping.json``  - the reference entry script's regex grouping (``group_regex_in_list`` /
   ``balance_regex_groups`` / ``regex_custom_length``, scripts/run_bitgen.py:71-116) on the
   README regexes, the synthetic workloads' pattern sets and edge cases.  The script's module
@@ -139,6 +142,20 @@ def main():
         ops[f"add{i}"] = ref_tpl.bs_add(m.copy(), c.copy())
         ops[f"ms{i}"] = ref_tpl.bs_match_star(m.copy(), c.copy())
     np.savez_compressed(os.path.join(HERE, "ops.npz"), **ops)
+
+    # ---- result reader -------------------------------------------------------------------
+    bsv = {}
+    for i, W in enumerate((1, 2, 7, 33)):
+        words = rng.integers(0, 1 << 32, size=W, dtype=np.uint64).astype(np.uint32)
+        words[0] |= 1 << 31            # position 0 set
+        bsv[f"w{i}"] = words.copy()
+        pos = ref_bs.Bitstream(words.copy()).get_ones_pos()
+        bsv[f"pos{i}"] = np.asarray(pos, dtype=np.int64)
+        bsv[f"count{i}"] = np.int64(ref_bs.Bitstream(words.copy()).get_count())
+    res4 = rng.integers(0, 1 << 32, size=(1, 2, 3, 5), dtype=np.uint64).astype(np.uint32)
+    bsv["res4"] = res4.copy()
+    bsv["res4_count_array"] = np.asarray(ref_bs.Bitstream(res4.copy()).get_count_array(), np.int64)
+    np.savez_compressed(os.path.join(HERE, "bitstream.npz"), **bsv)
 
     # ---- README quick-start known answer ----------------------------------------------
     from bitgen.tool.pcre import read_regex_from_pcre_file

@@ -184,6 +184,28 @@ def test_grouping_follows_reference_rule():
     assert group_regex_in_list(rx, 0) == [[r] for r in rx]
 
 
+def test_result_bit_order_matches_reference_reader():
+    """Position p of a stream is bit 31 - p % 32 of word p // 32, as the runner's result reader
+    (bitgen/bitstream.py:27-73, golden vectors) sees it: the oracle's word conversion, the
+    big-endian unpacking the GPU tests read outputs with, and the per-group counts of a
+    [S, M, G, W] result."""
+    z = np.load(os.path.join(GOLDEN, "bitstream.npz"))
+    i = 0
+    while f"w{i}" in z:
+        words, pos = z[f"w{i}"], z[f"pos{i}"]
+        x = words_to_int(words)
+        assert [p for p in range(32 * words.size) if (x >> p) & 1] == pos.tolist()
+        assert np.array_equal(np.nonzero(np.unpackbits(words.astype(">u4").view(np.uint8)))[0], pos)
+        assert bin(x).count("1") == int(z[f"count{i}"]) and pos[0] == 0
+        assert np.array_equal(int_to_words(x, words.size), words)
+        i += 1
+    assert i == 4
+    res = z["res4"]
+    per_group = [sum(bin(words_to_int(res[0, m, g])).count("1") for m in range(res.shape[1]))
+                 for g in range(res.shape[2])]
+    assert per_group == z["res4_count_array"].tolist()
+
+
 def test_grouping_matches_reference_vectors():
     """Groups (and custom lengths) equal those of the reference entry script's own functions
     (scripts/run_bitgen.py:71-116, run by tests/golden/make_golden.py) on the README regexes,
