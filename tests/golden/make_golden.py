@@ -60,14 +60,14 @@ def import_reference():
     return cfg
 
 
-def reference_grouping():
-    """The three grouping functions of scripts/run_bitgen.py, from its source."""
+def reference_functions(rel: str, keep: set) -> dict:
+    """Function definitions `keep` of the reference file `rel`, executed from its source (the
+    files' own imports pull in the GPU runner)."""
     import ast
     import re
-    path = os.path.join(REF, "scripts", "run_bitgen.py")
+    path = os.path.join(REF, rel)
     with open(path) as f:
         tree = ast.parse(f.read(), path)
-    keep = {"regex_custom_length", "balance_regex_groups", "group_regex_in_list"}
     mod = ast.Module([n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in keep],
                      type_ignores=[])
     ns = {"re": re}
@@ -76,12 +76,20 @@ def reference_grouping():
     return ns
 
 
+def reference_grouping():
+    """The three grouping functions of scripts/run_bitgen.py and the PCRE file reader of
+    bitgen/tool/pcre.py."""
+    ns = reference_functions("scripts/run_bitgen.py",
+                             {"regex_custom_length", "balance_regex_groups", "group_regex_in_list"})
+    ns.update(reference_functions("bitgen/tool/pcre.py", {"read_regex_from_pcre_file"}))
+    return ns
+
+
 def write_grouping():
     ref = reference_grouping()
     sys.path.insert(0, REPO)
     from bitgen_gb300 import workloads
-    from bitgen_gb300.grouping import read_regex_file
-    readme = read_regex_file(os.path.join(REF, "datasets_small/snort_small.regex"))
+    readme = ref["read_regex_from_pcre_file"](os.path.join(REF, "datasets_small/snort_small.regex"))
     thr = list(workloads.throughput_patterns(seed=3, n=256).regexes)
     dna = list(workloads.dna_motifs(64, seed=5).regexes)
     hand = [r"\x41\x42", "abc", "[a-z]+q", "hello.*world", "x", "yy", "zzz[0-9]", r"[\x00-\x1f]z",
@@ -93,8 +101,22 @@ def write_grouping():
             groups = ref["group_regex_in_list"](list(rx), n, 1)
             cases.append({"set": name, "regexes": rx, "n_groups": n, "groups": groups,
                           "lengths": [ref["regex_custom_length"](r) for r in rx]})
+    # the PCRE file reader on edge-case lines (blank lines, spaces, flags, inner slashes)
+    import tempfile
+    text = "/abc/\n\n   /a\\/b[/]c/i  \n/x//\n/p/q/r/sm\n\t/\\x2f\\x2a/\n"
+    with tempfile.NamedTemporaryFile("w", suffix=".regex", delete=False) as f:
+        f.write(text)
+    pcre = {"text": text, "regexes": ref["read_regex_from_pcre_file"](f.name), "bad": []}
+    for bad in ("abc", "/abc", "x/abc/", "/"):
+        with open(f.name, "w") as g:
+            g.write(bad + "\n")
+        try:
+            ref["read_regex_from_pcre_file"](f.name)
+        except ValueError:
+            pcre["bad"].append(bad)
+    os.unlink(f.name)
     with open(os.path.join(HERE, "grouping.json"), "w") as f:
-        json.dump({"cases": cases}, f, indent=0)
+        json.dump({"cases": cases, "pcre": pcre}, f, indent=0)
 
 
 def main():

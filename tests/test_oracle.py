@@ -218,6 +218,23 @@ def test_grouping_matches_reference_vectors():
         assert group_regex_in_list(c["regexes"], c["n_groups"]) == c["groups"], (c["set"], c["n_groups"])
 
 
+def test_pcre_reader_matches_reference_vectors(tmp_path):
+    """`read_regex_file` reads a /regex/flags file as bitgen/tool/pcre.py:5-27 does (golden
+    vectors from that function): blank lines skipped, text between the first and last slash,
+    lines without a leading slash pair rejected."""
+    from bitgen_gb300.grouping import read_regex_file
+    with open(os.path.join(GOLDEN, "grouping.json")) as f:
+        pcre = json.load(f)["pcre"]
+    path = tmp_path / "set.regex"
+    path.write_text(pcre["text"])
+    assert read_regex_file(str(path)) == pcre["regexes"]
+    assert len(pcre["bad"]) == 4
+    for bad in pcre["bad"]:
+        path.write_text(bad + "\n")
+        with pytest.raises(ValueError):
+            read_regex_file(str(path))
+
+
 def test_readme_known_answer_count_16():
     """The reference's only published known answer (README.md:124-142): 8 Snort regexes over the
     first 10 000 bytes of snort_10KB.input in 4 groups give count 16."""
