@@ -188,6 +188,50 @@ def batched_leg(prog, ps, dev):
             "bit_exact": exact, "median_len": int(np.median(lens))}
 
 
+def transpose_leg(dev, n_bytes=1 << 30, reps=20, check_bytes=1 << 20, cpu_bytes=4 << 20):
+    """The stand-alone transpose (the reference's byte_stream_transpose, kernel.cu:102-124):
+    uint8 [1, 1, n] -> uint32 [1, 1, 8, n/32] on the device, 2n bytes of HBM traffic per call;
+    the first `check_bytes` compared with the oracle's restatement of bitstream.py:228-258,
+    which is also timed on the host over `cpu_bytes` (one thread, numpy)."""
+    import numpy as np
+    import torch
+    from bitgen_gb300.engine import transpose
+    from oracle.pablo_ref import transpose_ref
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(6)
+    src = torch.randint(0, 256, (1, 1, n_bytes), dtype=torch.uint8, device=dev, generator=g)
+    dst = torch.empty((1, 1, 8, n_bytes // 32), dtype=torch.uint32, device=dev)
+    s = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        transpose(src, dst, s)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        transpose(src, dst, s)
+    e1.record(s)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / reps
+    head = src[0, 0, :check_bytes].cpu().numpy()
+    want = transpose_ref(head)
+    got = dst[0, 0, :, :check_bytes // 32].cpu().numpy()
+    sample = src[0, 0, :cpu_bytes].cpu().numpy()
+    t0 = time.perf_counter()
+    transpose_ref(sample)
+    cpu_s = time.perf_counter() - t0
+    peak, peak_kind = peaks()
+    return {"bytes": n_bytes, "reps": reps, "ms": round(ms, 4),
+            "GBps": round(n_bytes / ms / 1e6, 3),
+            "roofline": {"bound": "hbm", "achieved": round(2 * n_bytes / ms / 1e6, 2), "peak": peak,
+                         "unit": "GB/s", "frac": round(2 * n_bytes / ms / 1e6 / peak, 4),
+                         "peak_kind": peak_kind, "algorithmic_bytes_per_launch": 2 * n_bytes},
+            "bit_exact_vs_oracle_first_bytes": check_bytes if np.array_equal(got, want) else False,
+            "cpu_baseline": {"value": round(sample.size / cpu_s / 1e9, 6), "unit": "GB/s", "cores": 1,
+                             "kind": "port", "sample": f"{sample.size} bytes, numpy restatement of "
+                                                       f"bitstream.py:228-258, {cpu_s:.2f} s"}}
+
+
 def dna_leg(dev, n_bytes, steps, check_bytes):
     """64 IUPAC motifs (6-20 bases, every fourth split by a gap .{a,b}, 3 <= a <= 5, b <= a + 4) in 4 groups over DNA text
     (i.i.d. A/C/G/T, GC 42%, N runs, 80-column lines, 2^16 planted motif instances); per-group
@@ -489,6 +533,10 @@ def main():
             line["batched"] = batched_leg(prog, ps, dev)
         except Exception as e:  # a failed leg is reported, it does not void the main line
             line["batched"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        try:
+            line["transpose"] = transpose_leg(dev)
+        except Exception as e:
+            line["transpose"] = {"error": f"{type(e).__name__}: {e}"[:300]}
         try:
             line["dna"] = dna_leg(dev, args.dna_bytes, 5, None if args.no_cpu else args.cpu_sample)
         except Exception as e:
