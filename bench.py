@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="bytes of the CPU baseline sample (0 = the whole input, a few seconds)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-modes", action="store_true", help="skip the batched / served legs")
+    ap.add_argument("--no-modes", action="store_true", help="skip the batched / transpose / DNA / served legs")
     ap.add_argument("--served-requests", type=int, default=600)
     ap.add_argument("--dna-bytes", type=int, default=1 << 30, help="DNA text of the dna leg")
     ap.add_argument("--dna-only", action="store_true",
