@@ -23,7 +23,7 @@ from bitgen_gb300.pablo import Op, While, parse_pablo, PabloSyntaxError
 from bitgen_gb300.refir import group_from_ir
 from bitgen_gb300.regex import UnsupportedRegex, compile_group, compile_regex
 from oracle import cpu
-from oracle.nfa_ref import match_ends
+from oracle.nfa_ref import group_match_ends, match_ends
 from oracle.pablo_ref import (advance, int_to_words, matchstar, run_group, transpose_ref,
                               words_to_int)
 
@@ -112,6 +112,23 @@ def test_emitter_matches_nfa_and_python_re(matchstar_form):
                 if any(pr.fullmatch(data, s, e + 1) for s in range(e + 1)):
                     want_re |= 1 << e
             assert run_group(g, data) == match_ends(r, data) == want_re, (r, data)
+
+
+def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
+    """The genomic motif grammar (IUPAC classes, gapped `.{lo,hi}` motifs) over DNA text with N
+    runs, line feeds and planted motifs: emitter + big-int oracle == NFA == C evaluator."""
+    from bitgen_gb300 import workloads
+    ps = workloads.dna_motifs(24, seed=5)
+    text = workloads.plant(workloads.dna_text(6000, seed=6), ps.witnesses, 400, 9)
+    text[1000:1300] = ord("N")
+    data = text.tobytes()
+    groups = [compile_group(g) for g in ps.groups(3)]
+    for g, rx in zip(groups, ps.groups(3)):
+        want = run_group(g, text)
+        assert want == group_match_ends(rx, data) != 0
+        code, ns, outs = lower_interp([g])
+        st, cnt = cpu.run_code(code, ns, outs, text, block_words=64)
+        assert words_to_int(st[0]) == want and int(cnt[0]) == bin(want).count("1")
 
 
 def test_emitter_rejects_unsupported():
