@@ -118,3 +118,42 @@ def test_dyn_stats_filled_from_scan_counters(monkeypatch, n_parts):
     want = [[1, 1], [0, 0], [7, 2]] if n_parts else [[10, 0]]
     assert dyn[0, 0].tolist() == want
     handle.free()
+
+
+C_HOST = r"""
+#include "bitgen_gb300.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+  char log[8192];
+  const char *src = "extern \"C\" __global__ void k(unsigned int *x) { x[threadIdx.x] = 1u; }";
+  int rc = bg_nvrtc_check(src, strlen(src), "k", log, sizeof log);
+  if (rc != BG_OK) { printf("nvrtc %d %s\n", rc, log); return 1; }
+  if (bg_plan_stats(NULL, NULL, 0, NULL, NULL) != BG_ERR_INVALID) return 2;
+  if (strcmp(bg_status_string(BG_ERR_TIMEOUT), "bounded device wait timed out") != 0) return 3;
+  if (bg_transpose(NULL, NULL, 32, 1, NULL) != BG_ERR_INVALID) return 4;
+  if (bg_plan_launch(NULL, NULL, NULL, NULL, NULL) != BG_ERR_INVALID) return 5;
+  puts("ok");
+  return 0;
+}
+"""
+
+
+def test_c_host_builds_and_calls_the_abi(native, tmp_path):
+    """A plain C99 host includes include/bitgen_gb300.h, links the library and calls the entry
+    points that need no device (compile-only NVRTC check, argument checks, status strings)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "bitgen_gb300")
+    src = tmp_path / "host.c"
+    src.write_text(C_HOST)
+    exe = tmp_path / "host"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", f"-I{os.path.join(root, 'include')}", str(src),
+                    f"-L{libdir}", "-lbitgen_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", (out.returncode, out.stdout, out.stderr)
