@@ -64,12 +64,18 @@ def test_tables_are_consistent():
     assert _lookup(f, 0x7f7f7f, 0, *tabs) == 0 or 0x7f7f7f in f.table
 
 
-@pytest.mark.parametrize("wpt", [1, 2])
-def test_prefilter_is_sound_on_throughput_patterns(wpt):
-    ps = workloads.throughput_patterns(seed=3, n=64)
-    groups, gen, terms, f = _setup(ps, 4, wpt=wpt)
+@pytest.mark.parametrize("wpt,kind", [(1, "throughput"), (2, "throughput"), (2, "dna")])
+def test_prefilter_is_sound(wpt, kind):
+    """Also on IUPAC motifs over DNA text (the filter the split form would use there if forced;
+    the compiler picks the single-kernel form for it)."""
     n = 300_000
-    text = workloads.plant(workloads.printable_text(n, 41), ps.witnesses, 700, 42)
+    if kind == "dna":
+        ps = workloads.dna_motifs(24, seed=5)
+        text = workloads.plant(workloads.dna_text(n, seed=43), ps.witnesses, 700, 42)
+    else:
+        ps = workloads.throughput_patterns(seed=3, n=64)
+        text = workloads.plant(workloads.printable_text(n, 41), ps.witnesses, 700, 42)
+    groups, gen, terms, f = _setup(ps, 4, wpt=wpt)
     streams, _ = cpu.run_groups(groups, text, per_regex=True)
     hl, tl = gen.hl, gen.tl
     tile_words = (32 - hl - tl) * wpt
