@@ -14,8 +14,9 @@ names, argument meaning and return shapes:
   ``uint32 [S, M, G, W]``; ``run_fn(basis)`` scans the basis tensor and writes ``result``;
   ``kernel_handle.free()`` releases the program.  ``tmp_streams`` is ``None`` (the fused engine
   needs no global scratch streams).  ``dyn_stats`` is ``None`` unless the configuration sets
-  ``pass_inst_stats_dyn`` (the reference then builds from ``template_dyn_stat.py:39-87`` and its
-  runner sums ``dyn_stats[..., :1]`` and ``dyn_stats[..., 1:]``, ``from_icgrep.py:619-640``):
+  ``pass_inst_stats_dyn`` (the reference then builds from
+  ``bitgen/backend/cuda/template/template_dyn_stat.py:39-87`` and its runner sums
+  ``dyn_stats[..., :1]`` and ``dyn_stats[..., 1:]``, ``from_icgrep.py:619-640``):
   here it is ``int64 [S, 1, P, 2]``, refreshed by every ``run_fn`` call, with per part of the
   program (P = 1 for a single-kernel program) ``[..., 0]`` = the tiles it ran on (the
   reference: tile-loop iterations) and ``[..., 1]`` = the 32-tile rows of its work list (the

@@ -13,6 +13,8 @@
  *                           template.py:116-121, cuda_kernel.py:411-427
  *   bg_plan_sync         <- the cuStreamSynchronize + checkCudaErrors after each run
  *                           cuda_kernel.py:35-47,411-427
+ *   bg_plan_stats        <- the optional dyn_stats buffer of the generated kernel
+ *                           bitgen/backend/cuda/template/template_dyn_stat.py:39-87
  *   bg_interp_*          <- the reference's whole-stream semantics of Pablo while/if
  *                           (bitgen/inst/inst_block_while.py:137-153, inst_block_if.py:314-342)
  *   bg_scan_noalloc      <- no counterpart in the reference (an allocation-free scan, below)
@@ -134,8 +136,8 @@ int bg_plan_set_positions(bg_plan *plan, unsigned long long *positions, int64_t 
 /* Number of positions the last launch on `stream` produced (waits for the stream). */
 int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written);
 /* Work counters of the last launch on `stream` (waits for the stream); replaces the optional
- * `dyn_stats` buffer of the reference's generated kernel (backend/cuda/template/
- * template_dyn_stat.py:39-87, filled at codegen/gen_cuda.py:152-170), whose per-tile loop
+ * `dyn_stats` buffer of the reference's generated kernel (bitgen/backend/cuda/template/
+ * template_dyn_stat.py:39-87, filled at bitgen/codegen/gen_cuda.py:152-170), whose per-tile loop
  * counters have no meaning in this engine.  For each of the n_parts parts of a split-form
  * program: tiles_run[k] = tiles the execute pass ran part k on, rows[k] = 32-tile rows of its
  * work list.  Reads the plan's run masks back to the host (4 * n_run bytes per tile): not for
