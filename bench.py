@@ -75,18 +75,6 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def recorded_traffic():
-    """DRAM bytes per launch of the scan kernel from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "bg_scan_throughput_256re.md")
-    try:
-        for line in open(p):
-            if line.startswith("dram_bytes_per_full_launch:"):
-                return int(float(line.split(":", 1)[1].split()[0]))
-    except OSError:
-        pass
-    return None
-
-
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -134,23 +122,39 @@ class Clocks:
 
 
 def cpu_baseline(groups, base, sample_bytes):
-    """C evaluator on the host: all groups on their own threads over a bounded sample (the
-    first `sample_bytes` of `base` tiled).  Its counts are the bit-exact check of the GPU run."""
+    """C evaluator on the host over a bounded sample (the first `sample_bytes` of `base` tiled),
+    on every host core: one group per thread, or, for programs of bounded reach (no additions
+    or loops), one byte range per thread.  Its streams and counts are the bit-exact check of
+    the GPU run.  Returns (baseline record, streams, counts)."""
     import numpy as np
     from oracle import cpu
+    from bitgen_gb300.engine import lower_interp
     from bitgen_gb300.regex import compile_group
 
     gs = [compile_group(g) if isinstance(g, list) else g for g in groups]
     reps = -(-sample_bytes // base.size)
     data = np.tile(base, reps)[:sample_bytes] if reps > 1 else base[:sample_bytes]
-    threads = min(os.cpu_count() or 1, len(gs))
+    cores = os.cpu_count() or 1
+    split = all(cpu.reach(lower_interp([g])[0]) is not None for g in gs) and len(gs) < cores
+    threads = cores if split else min(cores, len(gs))
     cpu.run_groups(gs, data[:1 << 16], threads=threads)  # warm
     t0 = time.perf_counter()
-    _, counts = cpu.run_groups(gs, data, threads=threads)
+    streams, counts = cpu.run_groups(gs, data, threads=threads, split=split)
     dt = time.perf_counter() - t0
+    how = (f"one byte range per thread ({threads} ranges)" if split else "one group per thread")
     return {"value": round(sample_bytes / dt / 1e9, 6), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{sample_bytes} bytes of the same input, all {len(gs)} groups, one group per thread "
-                      f"(C word-parallel evaluator, oracle/bg_cpu.c), {dt:.2f} s"}, counts
+            "sample": f"{sample_bytes} bytes of the same input, all {len(gs)} groups, {how} "
+                      f"(C word-parallel evaluator, oracle/bg_cpu.c), {dt:.2f} s"}, streams, counts
+
+
+def streams_equal(out, cpu_streams, words: int) -> bool:
+    """Every output stream of a GPU launch (device uint32 [n_out, >= words]) equals the CPU
+    evaluator's over all `words` words."""
+    import numpy as np
+    got = out[:, :words].cpu().numpy().view(np.uint32)
+    return len(cpu_streams) == got.shape[0] and all(
+        np.array_equal(got[k], np.asarray(cpu_streams[k][:words], dtype=np.uint32))
+        for k in range(got.shape[0]))
 
 
 def batched_leg(prog, ps, dev):
@@ -272,13 +276,16 @@ def dna_leg(dev, n_bytes, steps, check_bytes):
            "matches": int(counts.sum()), "text_gen_s": round(gen_s, 1)}
     if check_bytes is not None:
         check_bytes = min(check_bytes or n_bytes, n_bytes)
-        cb, cpu_counts = cpu_baseline(groups, text, check_bytes)
-        if check_bytes == n_bytes:          # the counts of the timed launches themselves
-            got = counts[:, 0].tolist()
+        cb, cpu_streams, cpu_counts = cpu_baseline(groups, text, check_bytes)
+        if check_bytes == n_bytes:          # the streams and counts of the timed launches
+            got, got_out = counts[:, 0].tolist(), out
         else:
-            got = prog.scan(bytes_input(data[:check_bytes].contiguous()), streams=False,
-                            counts=True).counts[:, 0].tolist()
-        res["bit_exact_vs_cpu_sample"] = [int(x) for x in got] == list(cpu_counts)
+            r = prog.scan(bytes_input(data[:check_bytes].contiguous()))
+            got, got_out = r.counts[:, 0].tolist(), r.streams
+        res["bit_exact_vs_cpu"] = {
+            "bytes": check_bytes, "counts": [int(x) for x in got] == list(cpu_counts),
+            "streams": streams_equal(got_out, cpu_streams, (check_bytes + 31) // 32)}
+        del cpu_streams
         res["cpu_baseline"] = cb
     prog.close()
     del out, data
@@ -334,7 +341,7 @@ def run_reference(args):
     ps, groups, base, reps = workload(args)
     vals = []
     for i in range(args.warmup + args.steps):
-        cb, _ = cpu_baseline(groups, base, args.cpu_sample or args.bytes)
+        cb, _, _ = cpu_baseline(groups, base, args.cpu_sample or args.bytes)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)
@@ -400,14 +407,15 @@ def main():
     check = None
     if rank == 0 and not args.no_cpu:
         sample = min(args.cpu_sample or n, n)
-        cb, cpu_counts = cpu_baseline(groups, base, sample)
-        if sample == n:                     # the counts of the warm-up launches themselves
-            gpu_counts = [int(x) for x in counts[:, 0].tolist()]
+        cb, cpu_streams, cpu_counts = cpu_baseline(groups, base, sample)
+        if sample == n:                     # the streams and counts of the warm-up launches
+            gpu_counts, gpu_out = [int(x) for x in counts[:, 0].tolist()], out
         else:
-            sub = bytes_input(data[:sample].contiguous())
-            r = prog.scan(sub, streams=False, counts=True)
-            gpu_counts = [int(x) for x in r.counts[:, 0].tolist()]
-        check = gpu_counts == list(cpu_counts)
+            r = prog.scan(bytes_input(data[:sample].contiguous()))
+            gpu_counts, gpu_out = [int(x) for x in r.counts[:, 0].tolist()], r.streams
+        check = {"bytes": sample, "counts": gpu_counts == list(cpu_counts),
+                 "streams": streams_equal(gpu_out, cpu_streams, (sample + 31) // 32)}
+        del cpu_streams
     else:
         cb = None
 
@@ -485,18 +493,6 @@ def main():
     b_alg = n + prog.n_outputs * ((n + 31) // 32) * 4   # input once + each output stream once
     achieved = b_alg / (kernel_ms / 1e3) / 1e9
     info = prog.info()
-    # integer work: Pablo IR operations of the compiled groups per 32-bit word (before any
-    # tile skipping) x input words, against the dense ALU rate of 64 32-bit logical results per
-    # clock per SM at the maximum SM clock
-    from bitgen_gb300.pablo import Op, walk
-    ir_ops = sum(1 for g in gs for s in walk(g.stmts) if isinstance(s, Op) and s.op != "assign")
-    ops_launch = ir_ops * ((n + 31) // 32)
-    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
-    alu_peak = sm_count * 64 * float((clk or {}).get("sm_max_mhz") or 2070.0) * 1e6
-    int_ops = {"ir_ops_per_word": ir_ops, "ops_per_launch": ops_launch,
-               "achieved_Tops": round(ops_launch / (kernel_ms / 1e3) / 1e12, 2),
-               "dense_alu_peak_Tops": round(alu_peak / 1e12, 2),
-               "frac_of_dense_alu": round(ops_launch / (kernel_ms / 1e3) / alu_peak, 3)}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
@@ -510,13 +506,13 @@ def main():
                               "block": tuning.block, "skip_interval": tuning.skip_interval},
                    "registers": info.get("registers"), "adds": info.get("adds"),
                    "pre_pass_adds": info.get("pre_adds"),
-                   "compile_s": round(compile_s, 2), "bit_exact_vs_cpu_sample": check,
+                   "compile_s": round(compile_s, 2), "bit_exact_vs_cpu": check,
                    "work": work},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": recorded_traffic(),
+                     "frac": round(achieved / peak, 5), "traffic": None,
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg,
                      "kernel_ms": round(kernel_ms, 4), "kernel_ms_of": "median of 10 launches",
-                     "avg_ms_sync": round(avg_ms_sync, 4), "int_ops": int_ops},
+                     "avg_ms_sync": round(avg_ms_sync, 4)},
         "e2e": {"value": round(total_bytes / (e2e_ms / 1e3) / 1e9, 3), "unit": UNIT,
                 "h2d_bytes_per_step": n, "d2h_bytes_per_step": prog.n_outputs * 8,
                 "mode": "streamed (StreamScanner: copy of step i+1 beside the scan of step i, "

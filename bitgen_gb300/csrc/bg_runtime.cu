@@ -951,8 +951,10 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   prm.positions = plan->positions;
   prm.pos_capacity = plan->pos_capacity;
   prm.runs = plan->d_runs;
+  /* the pre-pass bitmaps start after the records of the reserved tile count, so that a layout
+   * with more tiles than the last one never finds bitmap words where it looks for records */
   prm.pre_bits = reinterpret_cast<uint32_t *>(plan->d_records +
-                                              (int64_t)std::max(1, plan->prog->desc.n_adds) * plan->n_tiles);
+                                              (int64_t)std::max(1, plan->prog->desc.n_adds) * plan->cap_tiles);
   prm.work = plan->d_work;
   if (plan->spin_limit > 0) prm.spin_limit = plan->spin_limit;
   prm.n_inputs = (int32_t)n;
@@ -1016,10 +1018,12 @@ int bg_plan_destroy(bg_plan *plan) {
  *   [32, end) look-back records, [n_adds][n_tiles], the pre-pass bitmaps (3 words of 32
  *             tiles per pre-pass addition), then (split form) the run masks,
  *             [n_run][n_tiles] 32-bit words, and the work list.
- * The array starts zeroed when the module loads.  Every call then clears the counters and
- * the status, and bumps the epoch.  Records left by an earlier call carry an older epoch, so
- * the look-back reads them as not yet published and they need no clearing.  Calls share the
- * array, so calls that overlap on the GPU race on it. */
+ * The array starts zeroed when the module loads.  Every call clears the counters and the
+ * status, bumps the epoch and zeroes its own record range [32, 32 + additions * tiles): that
+ * range moves with the program and the input size, so it can cover words an earlier call used
+ * as pre-pass bitmaps, run masks or work list, untagged values the look-back could take for a
+ * record of this call's epoch.  Calls share the array, so calls that overlap on the GPU race
+ * on it. */
 namespace {
 
 constexpr int64_t kNoallocWords = BG_NOALLOC_SCRATCH_BYTES / 8;
@@ -1162,6 +1166,8 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
   bg_noalloc_prologue_kernel<<<1, 256, 0, s>>>(scratch, n_bytes, tiles, counts,
                                                prog->desc.n_outputs);
   BG_CUDA(cudaGetLastError());
+  /* a zero word is an unpublished record of every epoch (a memset allocates nothing) */
+  BG_CUDA(cudaMemsetAsync(prm.records, 0, sizeof(unsigned long long) * (size_t)(adds * tiles), s));
   const int lrc = launch_passes(prog, prm, grid, s);
   if (lrc != BG_OK) return lrc;
   bg_noalloc_epilogue_kernel<<<1, 1, 0, s>>>(scratch, status);

@@ -183,9 +183,10 @@ int bg_plan_destroy(bg_plan *plan);
  * anything is enqueued, and bg_last_error() gives the sizes and the largest input that fits.
  * The first call on each device looks up the array's device address once
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream
- * capture begins.
- * Every call on a device shares the one array.  The call clears what must start at zero and
- * retags the look-back records.  Two calls whose work overlaps on the GPU (on different
+ * capture begins.  The address is kept for the life of the process: a device reset
+ * (cudaDeviceReset) after that first call is not supported.
+ * Every call on a device shares the one array.  The call clears what must start at zero,
+ * including its own look-back records, and bumps the records' epoch.  Two calls whose work overlaps on the GPU (on different
  * streams, or from different host threads) race on the array and give wrong results.
  * Serialise them, for example on one stream.
  * ------------------------------------------------------------------------------------- */

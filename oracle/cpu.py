@@ -68,13 +68,67 @@ def run_code(code, n_slots: int, outs: Sequence[int], data: np.ndarray, max_iter
     return out[:, :W32], cnt
 
 
+def reach(code) -> "tuple[int, int] | None":
+    """(back, ahead): how many characters before and after a position the outputs of a flat
+    program can depend on, or None when the program has additions or loops (MatchStar,
+    ScanThru, while, if), whose reach is unbounded."""
+    back: dict = {}
+    ahead: dict = {}
+    for op, dst, a, b, c, shift in code:
+        if op in (6, 7, 9, 10):
+            return None
+        srcs = [x for x in (a, b, c) if x >= 0]
+        bk = max([back.get(x, 0) for x in srcs] + [0])
+        ah = max([ahead.get(x, 0) for x in srcs] + [0])
+        if op == 5:
+            bk += shift
+        elif op == 11:
+            ah += shift
+        back[dst], ahead[dst] = bk, ah
+    return max(list(back.values()) + [0]), max(list(ahead.values()) + [0])
+
+
 def run_groups(groups, data: np.ndarray, per_regex: bool = False, threads: int = 0,
-               max_iter: int = 0):
-    """Evaluate each group on its own thread.  Returns (list of uint32 streams, counts)."""
+               max_iter: int = 0, split: bool = False):
+    """Evaluate Pablo groups over one input on the host.  Returns (list of uint32 streams,
+    counts).  By default each group runs on its own thread.  With ``split`` and programs of
+    bounded reach (no additions or loops, see `reach`), the input is instead cut into one
+    byte range per thread, each range evaluated with enough bytes before and after it to
+    cover that reach, so that every thread works whatever the number of groups; the stitched
+    streams equal the unsplit ones."""
     from bitgen_gb300.engine import lower_interp
 
     progs = [lower_interp([g], per_regex) for g in groups]
     threads = threads or os.cpu_count() or 1
+    reaches = [reach(p[0]) for p in progs]
+    n = int(data.size)
+    if split and threads > 1 and all(r is not None for r in reaches) and n >= 64 * threads:
+        back = max(r[0] for r in reaches)
+        ahead = max(r[1] for r in reaches)
+        hb = -(-back // 64) * 64           # whole 64-byte words before a range
+        cuts = [min(n, (n * i // threads) // 64 * 64) for i in range(threads)] + [n]
+        W = (n + 31) // 32
+
+        def one(i):
+            lo, hi = cuts[i], cuts[i + 1]
+            a, b = max(0, lo - hb), min(n, hi + ahead)
+            outs = [run_code(p[0], p[1], p[2], data[a:b], max_iter)[0] for p in progs]
+            return lo, hi, a, outs
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            parts = list(ex.map(one, range(threads)))
+        streams = [np.zeros(W, dtype=np.uint32) for p in progs for _ in p[2]]
+        for lo, hi, a, outs in parts:
+            if hi <= lo:
+                continue
+            w0, w1, skip = lo // 32, (hi + 31) // 32, (lo - a) // 32
+            k = 0
+            for o in outs:
+                for row in o:
+                    streams[k][w0:w1] = row[skip:skip + w1 - w0]
+                    k += 1
+        counts = [int(np.bitwise_count(s).sum(dtype=np.int64)) for s in streams]
+        return streams, counts
     with ThreadPoolExecutor(max_workers=max(1, min(threads, len(progs)))) as ex:
         res = list(ex.map(lambda p: run_code(p[0], p[1], p[2], data, max_iter), progs))
     streams: List[np.ndarray] = []

@@ -130,6 +130,54 @@ def test_limit_is_exact_and_enforced(program, cuda):
     assert _noalloc(prog, data, n_max, out[:, :8], cnt, st) == N.BG_ERR_INVALID
 
 
+def _max_bytes(prog: Program) -> int:
+    """Largest input (whole tiles) the fixed scratch admits for this program."""
+    s = prog.spec
+
+    def words(tiles):   # the scratch rule stated in include/bitgen_gb300.h
+        rows = -(-tiles // 32)
+        w = s.n_parts * (rows + 1) + 16 + s.n_run * rows if s.n_run else 0
+        return (max(1, s.n_adds) * tiles + (3 * s.n_pre * rows + 1) // 2
+                + (s.n_run * tiles + 1) // 2 + (w + 1) // 2)
+    lo, hi = 1, RECORDS
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        lo, hi = (mid, hi) if words(mid) <= RECORDS else (lo, mid)
+    return lo * s.tile_words * 32
+
+
+@pytest.mark.gpu
+def test_record_range_moves_over_an_earlier_calls_masks(program, cuda):
+    """A call whose look-back records reach past the previous call's records lands on words
+    that call used as run masks and work list (untagged values).  Programs and sizes alternate
+    so that the record range grows and shrinks; every call must equal the plan path."""
+    prog_a, ps_a = program
+    ps_b = workloads.pattern_set(40, seed=12, min_len=8, max_len=40, unbounded_frac=0.9)
+    prog_b = Program.from_regex_groups(ps_b.groups(4))
+    assert prog_a.spec.n_run > 0 and prog_b.spec.n_run > 0
+    assert prog_b.spec.n_adds > prog_a.spec.n_adds
+    cases = []
+    for prog, ps, frac, seed in ((prog_a, ps_a, 1.0, 50), (prog_b, ps_b, 1.0, 51),
+                                 (prog_a, ps_a, 0.5, 52), (prog_b, ps_b, 0.9, 53),
+                                 (prog_a, ps_a, 1.0, 54)):
+        n = max(32, int(_max_bytes(prog) * frac) // 32 * 32 - 32)
+        data = torch.from_numpy(_text(n, ps, seed)).to(cuda)
+        cases.append((prog, data, n, _plan_path(prog, data, n)))
+    outs = [torch.empty((p.n_outputs, -(-n // 32)), dtype=torch.int32, device=cuda)
+            for p, _, n, _ in cases]
+    cnts = [torch.empty((p.n_outputs,), dtype=torch.int64, device=cuda) for p, _, _, _ in cases]
+    stats = [torch.full((1,), -1, dtype=torch.int32, device=cuda) for _ in cases]
+    torch.cuda.synchronize()
+    for i, (prog, data, n, _) in enumerate(cases):   # back to back, one stream
+        assert _noalloc(prog, data, n, outs[i], cnts[i], stats[i]) == N.BG_OK, N.lib().bg_last_error()
+    torch.cuda.synchronize()
+    for i, (prog, data, n, (ws, wc)) in enumerate(cases):
+        assert int(stats[i].item()) == 0, i
+        assert np.array_equal(outs[i].cpu().numpy().view(np.uint32), ws), i
+        assert np.array_equal(cnts[i].cpu().numpy(), wc), i
+    prog_b.close()
+
+
 @pytest.mark.gpu
 def test_empty_input(program, cuda):
     prog, _ = program
