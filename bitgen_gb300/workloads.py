@@ -26,9 +26,10 @@ from typing import List, Sequence, Tuple
 import numpy as np
 
 LITERALS = "abcdefghijklmnopqrstuvwxyz0123456789"
-CLASSES = [("[a-z0-9]", "abcdefghijklmnopqrstuvwxyz0123456789"), ("[0-9]", "0123456789"),
-           ("[a-f]", "abcdef"), ("[aeiou]", "aeiou"), ("[a-z]", "abcdefghijklmnopqrstuvwxyz")]
+CLASS = "[a-z0-9]"                  # the grammar's bracket class; its members are LITERALS
 PRINTABLE = bytes(range(0x20, 0x7F))
+LIT_MIN, LIT_MAX = 4, 12            # literal length
+REP_LO, REP_HI = 2, 5               # the bounded repeat {2,5}
 
 
 @dataclass
@@ -45,58 +46,64 @@ def _lit(rng, k) -> str:
     return "".join(LITERALS[i] for i in rng.integers(0, len(LITERALS), size=k))
 
 
+def _members(rng, k) -> bytes:
+    return _lit(rng, k).encode()
+
+
 def synth_regex(rng, min_len: int, max_len: int, unbounded: str = "", alternation: bool = False) -> Tuple[str, bytes]:
     """One regex of the benchmark grammar and a string it matches.
 
-    ``unbounded`` is "" (none), "star" (a class with ``*`` / ``+``) or "gap" (a ``.*`` gap)."""
+    A regex is literals of 4-12 bytes over [a-z0-9] separated by class pieces, starting and
+    ending with a literal; a class piece is ``[a-z0-9]`` or the bounded repeat
+    ``[a-z0-9]{2,5}``.  The regex text is min_len..max_len characters long (a single literal
+    when the length leaves no room for a class piece).  ``unbounded`` turns one class piece
+    into an unbounded repetition: "star" gives ``[a-z0-9]*`` or ``[a-z0-9]+`` (MatchStar),
+    "gap" a ``.*`` gap.  ``alternation`` turns one literal after the first into a two-way
+    alternation of 4-6-byte literals."""
     target = int(rng.integers(min_len, max_len + 1))
     parts: List[Tuple[str, bytes]] = []
-    # a literal prefix keeps matches selective, as in real signature sets
-    k = int(rng.integers(3, 6))
-    s = _lit(rng, k)
-    parts.append((s, s.encode()))
+
+    def literal(room: int) -> Tuple[str, bytes]:
+        k = int(rng.integers(LIT_MIN, LIT_MAX + 1))
+        k = max(LIT_MIN, min(k, room))
+        s = _lit(rng, k)
+        return s, s.encode()
+
     special = []
     if unbounded:
         special.append(unbounded)
     if alternation:
         special.append("alt")
-    cur = sum(len(p[0]) for p in parts)
+    cur = 0
+    parts.append(literal(min(LIT_MAX, target if (special or target < 16) else target - 12)))
+    cur = len(parts[0][0])
     while cur < target or special:
-        choice = special.pop(0) if special and (cur + 8 >= target or rng.random() < 0.3) else None
-        if choice is None:
-            r = rng.random()
-            if r < 0.55:
-                s = _lit(rng, int(rng.integers(1, 4)))
-                parts.append((s, s.encode()))
-            elif r < 0.8:
-                cls, members = CLASSES[int(rng.integers(0, len(CLASSES)))]
-                parts.append((cls, members[int(rng.integers(0, len(members)))].encode()))
+        # the class piece: a pending unbounded repetition, else [a-z0-9] or [a-z0-9]{2,5}
+        if special and special[0] in ("star", "gap") and (target - cur < 30 or rng.random() < 0.6):
+            kind = special.pop(0)
+            if kind == "star":
+                op = "*" if rng.random() < 0.5 else "+"
+                n = int(rng.integers(1 if op == "+" else 0, 5))
+                sep = (CLASS + op, _members(rng, n))
             else:
-                cls, members = CLASSES[int(rng.integers(0, len(CLASSES)))]
-                lo = int(rng.integers(0, 3))
-                hi = lo + int(rng.integers(1, 4))
-                n = int(rng.integers(lo, hi + 1))
-                w = "".join(members[int(rng.integers(0, len(members)))] for _ in range(n))
-                parts.append((f"{cls}{{{lo},{hi}}}" if lo != hi else f"{cls}{{{lo}}}", w.encode()))
-        elif choice == "star":
-            cls, members = CLASSES[int(rng.integers(0, len(CLASSES)))]
-            op = "*" if rng.random() < 0.5 else "+"
-            n = int(rng.integers(1 if op == "+" else 0, 5))
-            w = "".join(members[int(rng.integers(0, len(members)))] for _ in range(n))
-            parts.append((cls + op, w.encode()))
-        elif choice == "gap":
-            n = int(rng.integers(0, 12))
-            w = bytes(PRINTABLE[i] for i in rng.integers(0, len(PRINTABLE), size=n))
-            parts.append((".*", w))
-        elif choice == "alt":
-            a, b = _lit(rng, int(rng.integers(2, 5))), _lit(rng, int(rng.integers(2, 5)))
-            parts.append((f"({a}|{b})", (a if rng.random() < 0.5 else b).encode()))
-        cur = sum(len(p[0]) for p in parts)
-        if cur > max_len + 16:
+                n = int(rng.integers(0, 12))
+                sep = (".*", bytes(PRINTABLE[i] for i in rng.integers(0, len(PRINTABLE), size=n)))
+        elif rng.random() < 0.5:
+            sep = (CLASS, _members(rng, 1))
+        else:
+            sep = (f"{CLASS}{{{REP_LO},{REP_HI}}}", _members(rng, int(rng.integers(REP_LO, REP_HI + 1))))
+        if not special and cur + len(sep[0]) + LIT_MIN > max_len:
             break
-    # end on a literal so matches stay rare
-    s = _lit(rng, 2)
-    parts.append((s, s.encode()))
+        parts.append(sep)
+        cur += len(sep[0])
+        if special and special[0] == "alt" and (target - cur < 16 or rng.random() < 0.5):
+            special.pop(0)
+            a = _lit(rng, int(rng.integers(LIT_MIN, 7)))
+            b = _lit(rng, int(rng.integers(LIT_MIN, 7)))
+            parts.append((f"({a}|{b})", (a if rng.random() < 0.5 else b).encode()))
+        else:
+            parts.append(literal(max(LIT_MIN, min(target, max_len) - cur)))
+        cur += len(parts[-1][0])
     return "".join(p[0] for p in parts), b"".join(p[1] for p in parts)
 
 
@@ -125,7 +132,7 @@ def small_patterns(seed: int = 1) -> PatternSet:
     rng = np.random.default_rng(seed)
     regexes, wits = [], []
     for i in range(8):
-        r, w = synth_regex(rng, 6, 16, "gap" if i == 0 else "", alternation=(i == 1))
+        r, w = synth_regex(rng, 8, 24, "gap" if i == 0 else "", alternation=(i == 1))
         regexes.append(r)
         wits.append(w)
     return PatternSet(regexes, wits)

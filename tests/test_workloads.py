@@ -16,14 +16,48 @@ def test_small_workload():
     assert len(ps.regexes) == 8 and text.size == 10240
     assert text.min() >= 0x20 and text.max() <= 0x7E
     assert any(".*" in r for r in ps.regexes) and any("|" in r for r in ps.regexes)
+    assert check_grammar(ps, 8, 40) == 1.0 and any("{2,5}" in r for r in ps.regexes)
     data = text.tobytes()
     ends = sum(bin(match_ends(r, data)).count("1") for r in ps.regexes)
     assert ends >= 10                                     # the planted witnesses match
 
 
+PIECE = re.compile(r"\[a-z0-9\](\{2,5\}|\*|\+)?|\.\*|\(([a-z0-9]+)\|([a-z0-9]+)\)|([a-z0-9]+)")
+
+
+def grammar_pieces(rx: str):
+    """The pieces of a regex of the benchmark grammar; fails on anything else."""
+    out, at = [], 0
+    while at < len(rx):
+        m = PIECE.match(rx, at)
+        assert m, f"{rx!r}: no grammar piece at {at}"
+        out.append(m)
+        at = m.end()
+    return out
+
+
+def check_grammar(ps, lo: int, hi: int):
+    """4-12-byte literals over [a-z0-9], [a-z0-9] classes with the bounded repeat {2,5} or an
+    unbounded repetition, .* gaps, two-way alternations; regex text lo..hi characters."""
+    within = 0
+    for rx in ps.regexes:
+        pieces = grammar_pieces(rx)
+        assert pieces[0].group(4), f"{rx!r} starts with a literal"
+        for m in pieces:
+            if m.group(4):
+                assert 4 <= len(m.group(4)) <= 12, rx
+            if m.group(2):
+                assert 4 <= len(m.group(2)) <= 6 and 4 <= len(m.group(3)) <= 6, rx
+        within += lo <= len(rx) <= hi
+    return within / len(ps.regexes)
+
+
 def test_throughput_pattern_set():
     ps = workloads.throughput_patterns(seed=3, n=256)
     assert len(ps.regexes) == len(ps.witnesses) == 256
+    assert check_grammar(ps, 8, 40) >= 0.95
+    assert any("{2,5}" in r for r in ps.regexes) and any(".*" in r for r in ps.regexes)
+    assert any("|" in r for r in ps.regexes)
     unbounded = [r for r in ps.regexes if re.search(r"\*|\+", r)]
     assert 0.2 <= len(unbounded) / 256 <= 0.4            # about 30%
     for r, w in zip(ps.regexes[:64], ps.witnesses[:64]):
