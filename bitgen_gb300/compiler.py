@@ -333,8 +333,9 @@ class Tuning:
     cls_block: int = 1024    # split form: threads per classify block (one block per SM holds
                              # the Bloom bitmap, the exact keys and the warps' run masks)
     prefilter_limit: float = 0.25  # prefilter only while a tile is expected to run fewer than
-                                   # this fraction of the terms (text taken as uniform over
-                                   # the bytes the filters name)
+                                   # this fraction of the terms and to take fewer than 32 times
+                                   # this many slow-path filter hits per 1024 bytes (text taken
+                                   # as uniform over the bytes the filters name); >= 1: always
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
     inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
@@ -342,7 +343,9 @@ class Tuning:
     single_min_blocks: int = 3   # back to the single-kernel form because the filters are
                                  # unselective (0: keep wpt / min_blocks)
     basis_filter: bool = False   # split form: rebuild the bytes of basis-plane inputs and run
-                                 # the trigram filter on them (else every term runs there)
+                                 # the q-gram filter on them (else every term runs there)
+    filter_config: Optional[Tuple[int, int]] = None  # prefilter (q-gram length, stride); None:
+                                                     # the cheapest by the filter's cost model
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
@@ -350,7 +353,7 @@ class Tuning:
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
-                self.basis_filter)
+                self.basis_filter, self.filter_config)
 
 
 @dataclass
@@ -1124,10 +1127,13 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     filt = None
     if tuning.prefilter and not tuning.lockstep and not tuning.edge_variants:
         pre_nodes = [v for v, _ in sorted(gen.pre.items(), key=lambda x: x[1])]
-        filt = prefilter.build(gen, [v for v, _ in terms], pre_nodes)
+        filt = prefilter.build(gen, [v for v, _ in terms], pre_nodes,
+                               config=tuning.filter_config, bloom_bits=tuning.bloom_bits)
         positions = 32 * 32 * tuning.wpt
-        if not filt.enabled or (filt.expected_per_tile(positions) >
-                                tuning.prefilter_limit * len(terms)):
+        lim = tuning.prefilter_limit
+        if not filt.enabled or (lim < 1.0 and (
+                filt.expected_per_tile(positions) > lim * len(terms)
+                or filt.hits * 1024 / positions > lim * 32)):
             # the filter would pass most terms: single-kernel form, with its own tile shape
             # (programs whose terms have no filter at all keep the requested shape)
             # (the terms run on every tile and mostly stay non-zero for several steps, so
@@ -1416,14 +1422,20 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     else:
         dispatch = f"      bg_part_tab[k]({part_args});\n"
     # classify kernel ------------------------------------------------------------------------
+    # The tile's bytes are at hand (raw); its basis planes are made only where a class test
+    # needs them (basis_of): a class whose complement is at most three bytes (such as '.',
+    # everything but a line feed) is tested on the bytes themselves, and the branches that
+    # compute classes from the basis run on few tiles.
     gen.lines = []
     gen.indent = 4
     gen.scopes = [{}]
+    basis_decl = ", ".join(f"b{i}_{j} = bb[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+    basis_block = f"S bb[8]; basis_of(raw, bb); const uint32_t {basis_decl};"
     for w in range(nw):
         m = (always >> (32 * w)) & 0xFFFFFFFF
         if m:
             gen.emit(f"t.run[{w}] |= 0x{m:08x}u;")
-    # pre-pass aggregates: with a zero marker (no trigram of it in the tile) the aggregate
+    # pre-pass aggregates: with a zero marker (no q-gram of it in the tile) the aggregate
     # depends on the class alone
     # additions sharing a class and carry lane have the same zero-marker aggregate: one test
     # per group; an addition whose marker filter fired (rare) replaces its bits
@@ -1431,9 +1443,24 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     for v, k in gen.pre.items():
         key = (d.nodes[v].args[1], gen.dl[v])
         groups_[key] = groups_.get(key, 0) | (1 << k)
+    full256 = (1 << 256) - 1
+
+    def excluded(cnode):
+        """The bytes outside class `cnode` when there are one to three of them, else None."""
+        comp = ~gen.byteset(cnode) & full256
+        xs = [b for b in range(256) if (comp >> b) & 1]
+        return xs if 1 <= len(xs) <= 3 else None
+    basis_always = any(excluded(c) is None for (c, _) in groups_)
+    if basis_always:
+        gen.emit(basis_block)
     for (cnode, dl), kmask in sorted(groups_.items()):
-        c = gen.mat(cnode)
-        gen.emit(f"{{ const uint32_t pz = pre_propagates<{dl}>(ones_lanes(t, {gen.pack(c)})) ? 0xffffffffu : 0u;")
+        xs = excluded(cnode)
+        if xs is not None:
+            args = ", ".join(f"{x}u" for x in xs)
+            gen.emit(f"{{ const uint32_t pz = pre_propagates<{dl}>(excl_lanes<{len(xs)}, {args}>(t, raw)) ? 0xffffffffu : 0u;")
+        else:
+            c = gen.mat(cnode)
+            gen.emit(f"{{ const uint32_t pz = pre_propagates<{dl}>(ones_lanes(t, {gen.pack(c)})) ? 0xffffffffu : 0u;")
         for j in range(-(-len(gen.pre) // 32)):
             m = (kmask >> (32 * j)) & 0xFFFFFFFF
             if m:
@@ -1468,11 +1495,34 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(run_bits.items()))
         basis_names = ", ".join(f"b{i}_{jj}" for i in range(8) for jj in range(wpt))
         saved[0].append(" " * saved[1] +
-                        f"if ({cond}) {{ const uint3 cr = bg_cand_{j}(t, {basis_names}); "
+                        f"if ({cond}) {{ {'' if basis_always else basis_block + ' '}"
+                        f"const uint3 cr = bg_cand_{j}(t, {basis_names}); "
                         f"pg[{j}] |= cr.x; pp[{j}] = (pp[{j}] & ~cr.y) | cr.z; }}")
     gen.lines, gen.indent, gen.scopes = saved
     live_needs = [(c, dl, mask & ~always) for (c, dl), mask in sorted(need_masks.items())
                   if mask & ~always]
+    # a lane can be all ones in an obligation class only if its first four bytes are in it:
+    # one table lookup per byte (bit i of obl_tab[b]: byte b is in the i-th class) decides
+    # for most tiles that no obligation holds, before any class is computed from the basis
+    obl_classes = sorted({c for c, _, _ in live_needs})
+    obl_tab = [0] * 256
+    if 0 < len(obl_classes) <= 32:
+        for i, c in enumerate(obl_classes):
+            bs = gen.byteset(c)
+            for b in range(256):
+                if (bs >> b) & 1:
+                    obl_tab[b] |= 1 << i
+    else:
+        obl_tab = [0xFFFFFFFF] * 256
+    obl_lanes = 0
+    for _, dl, _ in live_needs:
+        obl_lanes |= 1 << dl
+        if sl + dl < 32:
+            obl_lanes |= 1 << (sl + dl)
+    if live_needs:
+        gen.open(f"__ballot_sync(FULL, first4_classes(raw, bg_obl_s) != 0u) & 0x{obl_lanes:08x}u")
+        if not basis_always:
+            gen.emit(basis_block)
     # when one class contains all the others, a lane that is not all ones in it is not all ones
     # in any: test that class at the carry lanes first and skip the rest (the common case)
     guard = None
@@ -1489,7 +1539,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             gen.emit(f"const uint32_t {pm_classes[sup]} = ones_lanes(t, {gen.pack(ref)});")
             gen.open(f"{pm_classes[sup]} & 0x{lanes:08x}u")
     for c, pm in sorted(pm_classes.items()):
-        if c == guard:
+        if c == guard or c not in obl_classes:
             continue
         ref = gen.mat(c)
         gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
@@ -1499,6 +1549,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
                        for w in range(nw) if (mask >> (32 * w)) & 0xFFFFFFFF)
         gen.emit(f"if ((({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u) {{ {ors} }}")
     if guard is not None:
+        gen.close()
+    if live_needs:
         gen.close()
     # run masks: kept in the warp's shared words, stored per chunk (flush_runs)
     gen.emit("if (t.lane == 0) {" + " ".join(f"runs_s[{w * 32} + l] = t.run[{w}];" for w in range(nw)) + " }")
@@ -1516,7 +1568,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
 
     def cls_words(bits, block):     # up to the warps' byte buffers (16-byte aligned)
-        w = (1 << bits) // 32 + len(keys) + len(info_tab) + len(rec_tab) + (block // 32) * nw * 32
+        w = ((1 << bits) // 32 + len(keys) + len(info_tab) + 256 + len(rec_tab)
+             + (block // 32) * nw * 32)
         return -(-w // 4) * 4
 
     def cls_bytes(bits, block):
@@ -1534,8 +1587,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
               f"static __device__ const __align__(16) uint32_t bg_bloom_g[{len(bloom)}] = {{\n{_hex_array(bloom)}\n}};\n"
               f"static __device__ const __align__(16) uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
               f"static __device__ const __align__(16) uint32_t bg_exinfo[{len(info_tab)}] = {{\n{_hex_array(info_tab)}\n}};\n"
-              f"static __device__ const uint32_t bg_exrecs[{len(rec_tab)}] = {{\n{_hex_array(rec_tab)}\n}};\n")
-    basis_decl = ", ".join(f"b{i}_{j} = b[{i}].w[{j}]" for i in range(8) for j in range(wpt))
+              f"static __device__ const uint32_t bg_exrecs[{len(rec_tab)}] = {{\n{_hex_array(rec_tab)}\n}};\n"
+              f"static __device__ const __align__(16) uint32_t bg_obl[256] = {{\n{_hex_array(obl_tab)}\n}};\n")
     cls_warps = cls_block // 32
     cls_smem = cls_bytes(bloom_bits, cls_block)
     cls_maxreg = max(32, min(255, 65536 // cls_block // 8 * 8))
@@ -1552,7 +1605,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *bg_bloom_s = bg_dyn_s;                            /* {len(bloom)} words */\n"
         f"  uint32_t *bg_exkeys_s = bg_dyn_s + {len(bloom)};            /* {len(keys)} words */\n"
         f"  uint32_t *bg_exinfo_s = bg_exkeys_s + {len(keys)};         /* {len(info_tab)} words */\n"
-        f"  uint32_t *bg_exrecs_s = bg_exinfo_s + {len(info_tab)};     /* {len(rec_tab)} words */\n"
+        f"  uint32_t *bg_obl_s = bg_exinfo_s + {len(info_tab)};        /* 256 words */\n"
+        f"  uint32_t *bg_exrecs_s = bg_obl_s + 256;                     /* {len(rec_tab)} words */\n"
         f"  uint32_t *bg_runs_s = bg_exrecs_s + {len(rec_tab)};        /* {cls_warps * nw * 32} words */\n"
         f"  /* the tables, 16 bytes per load with several loads in flight (sizes are multiples of 4 words) */\n"
         f"#pragma unroll 4\n"
@@ -1561,6 +1615,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  for (int i = threadIdx.x; i < {len(info_tab) // 4}; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_exinfo_s)[i] = reinterpret_cast<const uint4 *>(bg_exinfo)[i];\n"
         f"  for (int i = threadIdx.x; i < {len(rec_tab)}; i += blockDim.x) bg_exrecs_s[i] = bg_exrecs[i];\n"
+        f"  for (int i = threadIdx.x; i < 64; i += blockDim.x)\n"
+        f"    reinterpret_cast<uint4 *>(bg_obl_s)[i] = reinterpret_cast<const uint4 *>(bg_obl)[i];\n"
         f"  for (int i = threadIdx.x; i < {len(keys) // 4}; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_exkeys_s)[i] = reinterpret_cast<const uint4 *>(bg_exkeys)[i];\n"
         f"  __syncthreads();\n"
@@ -1570,9 +1626,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  init(p, t);\n"
         + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);" if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
-        f"    S b[8];\n"
-        f"    load_scan(p, t, b, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l, bytes_s);\n"
-        f"    const uint32_t {basis_decl};\n"
+        f"    uint32_t raw[BG_WPT][8];\n"
+        f"    load_scan(p, t, raw, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l, bytes_s);\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
         + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + BG_WORK_HEAD + {len(parts)}LL * (1 + rows)") +
@@ -1592,6 +1647,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_NPRE {len(gen.pre)}\n"
         f"#define BG_NRUN {nw}\n"
         f"#define BG_BLOOM_BITS {bloom_bits}\n"
+        f"#define BG_QGRAM {filt.q}\n"
+        f"#define BG_STRIDE {filt.stride}\n"
         f"#define BG_PREFILTER 1\n"
         f"#define BG_BASIS_FILTER {int(tuning.basis_filter)}\n"
         f'#include "bg_device.cuh"\n'

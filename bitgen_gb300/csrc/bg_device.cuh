@@ -806,30 +806,38 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
 }
 
 #if BG_PREFILTER
-/* Trigram prefilter (tables generated by bitgen_gb300/prefilter.py).  Every trigram lying in
- * the bytes this warp computes is hashed into the Bloom bitmap `bloom` (2^BG_BLOOM_BITS bits,
- * shared memory); a hit is resolved in the exact open-addressed table (also in shared memory),
- * whose records set bits of the tile's run mask.  The
- * trigram ending at byte q is byte(q-2) | byte(q-1) << 8 | byte(q) << 16; bytes before the
- * warp's first byte read as zero. */
+/* Q-gram prefilter (tables generated by bitgen_gb300/prefilter.py).  The q-grams (BG_QGRAM = 3
+ * or 4 bytes) ending at every BG_STRIDE-th byte of the bytes this warp computes (byte e of a
+ * 32-byte lane word with e % BG_STRIDE == BG_STRIDE - 1) are probed in the Bloom bitmap `bloom`
+ * (2^BG_BLOOM_BITS bits, shared memory); a hit is resolved in the exact open-addressed table
+ * (also in shared memory), whose records set bits of the tile's run mask.  A q-gram key holds
+ * its oldest byte in bits 0-7; bytes before the warp's first byte read as zero. */
+#ifndef BG_QGRAM
+#define BG_QGRAM 3
+#endif
+#ifndef BG_STRIDE
+#define BG_STRIDE 1
+#endif
+constexpr int QG = BG_QGRAM, QS = BG_STRIDE;
+constexpr int NPROBE = 32 / QS;              /* probes per 32-byte lane word */
+static_assert((QG == 3 || QG == 4) && (QS == 1 || QS == 2), "q-gram configuration");
 constexpr uint32_t BLOOM_HASH = 0x9E3779B1u, EXACT_HASH = 0x85EBCA6Bu;
 
-/* Exact lookup of a trigram whose Bloom bit is set (all tables in shared memory).  `pre3`
- * holds the three bytes before the trigram (3 back in bits 0-7, 4 back in 8-15, 5 back in
- * 16-23).  Slot s holds the key trigram | 1 << 31 (0 = empty) and info[s] = start << 8 | count
- * of its records; record i is recs[2i] = bytes | n << 24 and recs[2i + 1] = the bit it sets when
- * the first n bytes of pre3 equal `bytes` (n = 0: always).  Bit b goes to run[(b / 32) * 32]
- * (the tile's run words in the warp's shared memory, 32 words apart). */
-static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
-                                                  const uint32_t *keys, const uint32_t *info,
-                                                  const uint32_t *recs, int log2, uint32_t *run) {
+/* Exact lookup of a q-gram whose Bloom bit is set (all tables in shared memory).  `pre3` holds
+ * the three bytes before the q-gram (the nearest in bits 0-7).  Slot s holds the key in keys[s]
+ * and info[s] = start << 8 | count of its records (0 = empty slot); record i is
+ * recs[2i] = bytes | n << 24 and recs[2i + 1] = the bit it sets when the n nearest bytes of
+ * pre3 equal `bytes` (n = 0: always).  Bit b goes to run[(b / 32) * 32] (the tile's run words
+ * in the warp's shared memory, 32 words apart). */
+static __device__ __noinline__ void qgram_exact(uint32_t key, uint32_t pre3, const uint32_t *keys,
+                                                const uint32_t *info, const uint32_t *recs,
+                                                int log2, uint32_t *run) {
   const uint32_t slots = 1u << log2;
   uint32_t s = (key * EXACT_HASH) >> (32 - log2);
   for (uint32_t it = 0; it < slots; ++it) {
-    const uint32_t k = keys[s];
-    if (k == 0u) return;
-    if (k == (key | 0x80000000u)) {
-      const uint32_t e = info[s];
+    const uint32_t e = info[s];
+    if (e == 0u) return;
+    if (keys[s] == key) {
       for (uint32_t i = e >> 8, n = e & 255u; n > 0u; --n, ++i) {
         const uint32_t r = recs[2 * i], bit = recs[2 * i + 1];
         const uint32_t cmp = (1u << (8u * (r >> 24))) - 1u; /* n <= 3 */
@@ -841,46 +849,68 @@ static __device__ __noinline__ void trigram_exact(uint32_t key, uint32_t pre3,
   }
 }
 
-/* The Bloom bit of trigram t (bits 0-23 of x; the top byte of x is ignored), moved to bit q (a
- * rotation, so that the probes of several keys OR into one word of hits).  The bit index is
- * the top BG_BLOOM_BITS bits of the 24-bit product t * BLOOM_HASH mod 2^24 (word = index / 32,
- * bit = index % 32).  Multiplying x by the constant shifted left by 8 gives that product in the
- * top 24 bits whatever the top byte of x; subtracting q before the bit field is shifted down
- * makes the rotation put the bit at position q. */
-__device__ __forceinline__ uint32_t bloom_probe(uint32_t x, const uint32_t *bloom, int q) {
-  constexpr uint32_t M = BLOOM_HASH << 8;
-  constexpr int S = 32 - BG_BLOOM_BITS;
-  const uint32_t w = bloom[(x * M) >> (S + 5)];
-  const uint32_t a = (x * M - ((uint32_t)q << S)) >> S;
-  return __funnelshift_r(w, w, a) & (1u << q);
+/* Bloom bit of q-gram x at bit 0 of the result (the other bits are arbitrary).  The word is the
+ * top BG_BLOOM_BITS - 5 bits of the product x * BLOOM_HASH (for a trigram the constant is
+ * shifted up by 8, which makes the product ignore the byte above the trigram); the bit within
+ * the word is x's low 5 bits, the low bits of the oldest byte: a funnel shift in wrap mode
+ * rotates the word right by exactly that. */
+__device__ __forceinline__ uint32_t bloom_bit(uint32_t x, const uint32_t *bloom) {
+  constexpr uint32_t M = QG == 3 ? (BLOOM_HASH << 8) : BLOOM_HASH;
+  const uint32_t w = bloom[(x * M) >> (32 - BG_BLOOM_BITS + 5)];
+  return __funnelshift_r(w, w, x);
 }
+
+/* The q-gram ending at byte e (0..31) of a lane word u[0..7] (little-endian 32-bit words),
+ * with `pw` the previous lane word's last 32-bit word; bytes of a trigram key above bit 23 are
+ * arbitrary. */
+template <int E>
+__device__ __forceinline__ uint32_t qgram_at(const uint32_t *u, uint32_t pw) {
+  constexpr int I = E >> 2, R = E & 3;
+  const uint32_t lo = I == 0 ? pw : u[I > 0 ? I - 1 : 0], hi = u[I];
+  if (QG == 4) {
+    if (R == 3) return hi;
+    return __byte_perm(lo, hi, R == 0 ? 0x4321 : (R == 1 ? 0x5432 : 0x6543));
+  }
+  if (R == 2) return hi;
+  if (R == 3) return hi >> 8;
+  return __byte_perm(lo, hi, R == 0 ? 0x0432 : 0x0543);
+}
+
+/* Probes of one lane word: bit 32 - NPROBE + k of the result = the Bloom bit of probe k
+ * (the q-gram ending at byte QS * k + QS - 1).  Each probe's bit enters at bit 31 while the
+ * earlier ones move down one place. */
+template <int K>
+struct Probes {
+  static __device__ __forceinline__ uint32_t run(const uint32_t *u, uint32_t pw,
+                                                 const uint32_t *bloom, uint32_t acc) {
+    acc = __funnelshift_r(acc, bloom_bit(qgram_at<QS * K + QS - 1>(u, pw), bloom), 1);
+    return Probes<K + 1>::run(u, pw, bloom, acc);
+  }
+};
+template <>
+struct Probes<NPROBE> {
+  static __device__ __forceinline__ uint32_t run(const uint32_t *, uint32_t, const uint32_t *,
+                                                 uint32_t acc) {
+    return acc;
+  }
+};
 
 #ifndef BG_BASIS_FILTER
 #define BG_BASIS_FILTER 0
 #endif
-/* Load the tile's bytes, fill t.run from the trigram scan (warp-uniform) and transpose the bytes
- * into the basis.  Inputs given as basis planes: every term runs, or, with BG_BASIS_FILTER, the
- * bytes are rebuilt from the planes and scanned the same way (bytes at or beyond the input's
- * length are the planes' padding there, which can only add hits). */
-__device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
+/* Load the tile's bytes into raw (lane word j = raw[j][0..7], little-endian) and fill t.run
+ * from the q-gram scan (warp-uniform).  Inputs given as basis planes: the bytes are rebuilt
+ * from the planes (bytes at or beyond the input's length are the planes' padding there), and
+ * every term runs, or, with BG_BASIS_FILTER, the rebuilt bytes are scanned the same way (the
+ * padding can only add hits).  The basis planes of the bytes, where a caller needs them, come
+ * from basis_of. */
+__device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t raw[WPT][8],
                                           const uint32_t *bloom, const uint32_t *keys,
                                           const uint32_t *info, const uint32_t *recs, int log2,
                                           uint32_t *run, uint8_t *bytes_s) {
   /* run: the tile's run words in shared memory (word w at run[32 w]); hits OR into them */
-  if (!BG_BASIS_FILTER && p.input_kind == BG_INPUT_BASIS) {
-    load_basis(p, t, b);
-#pragma unroll
-    for (int w = 0; w < BG_NRUN; ++w) t.run[w] = FULL;
-    return;
-  }
-  const bool from_basis = BG_BASIS_FILTER && p.input_kind == BG_INPUT_BASIS;
-  if (t.lane == 0) {
-#pragma unroll
-    for (int w = 0; w < BG_NRUN; ++w) run[32 * w] = 0u;
-  }
-  __syncwarp();
-  uint32_t raw[WPT][8];
-  if (from_basis) {
+  if (p.input_kind == BG_INPUT_BASIS) {
+    S b[8];
     load_basis(p, t, b);
 #pragma unroll
     for (int j = 0; j < WPT; ++j) {
@@ -889,79 +919,107 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, S b[8],
       for (int i = 0; i < 8; ++i) o[i] = b[i].w[j];
       untranspose32(o, raw[j]);
     }
+    if (!BG_BASIS_FILTER) {
+#pragma unroll
+      for (int w = 0; w < BG_NRUN; ++w) t.run[w] = FULL;
+      return;
+    }
   } else {
 #pragma unroll
     for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
   }
-  uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
-  uint32_t pprev = __shfl_up_sync(FULL, raw[WPT - 1][6], 1);
-  if (t.lane == 0) prev = pprev = 0u;
-  /* eight trigrams (two words) per step, all Bloom probes; bit 8 g + q of hits[j] = trigram q
-   * of step g (ending at byte 32 j + 8 g + q of the lane's bytes) may be a key */
-  uint32_t hits[WPT];
+  if (t.lane == 0) {
 #pragma unroll
-  for (int j = 0; j < WPT; ++j) {
-    hits[j] = 0u;
-#pragma unroll
-    for (int i = 0; i < 8; i += 2) {
-      const uint32_t c0 = raw[j][i], c1 = raw[j][i + 1];
-      uint32_t k[8]; /* trigram q in bits 0-23, any top byte */
-      k[0] = __byte_perm(prev, c0, 0x0432);
-      k[1] = __byte_perm(prev, c0, 0x0543);
-      k[2] = c0;
-      k[3] = c0 >> 8;
-      k[4] = __byte_perm(c0, c1, 0x0432);
-      k[5] = __byte_perm(c0, c1, 0x0543);
-      k[6] = c1;
-      k[7] = c1 >> 8;
-      uint32_t hb = 0u;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) hb |= bloom_probe(k[q], bloom, q);
-      hits[j] |= hb << (4 * i);
-      pprev = c0;
-      prev = c1;
-    }
+    for (int w = 0; w < BG_NRUN; ++w) run[32 * w] = 0u;
   }
+  uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
+  if (t.lane == 0) prev = 0u;
+  constexpr uint32_t KEEP = NPROBE == 32 ? FULL : ~((1u << (32 - NPROBE)) - 1u);
+  uint32_t hits[WPT];
   uint32_t any = 0u;
 #pragma unroll
-  for (int j = 0; j < WPT; ++j) any |= hits[j];
-  const bool look = __any_sync(FULL, any != 0u);
-  if (look) { /* the warp's bytes in shared memory, for the lookups below */
+  for (int j = 0; j < WPT; ++j) {
+    hits[j] = Probes<0>::run(raw[j], prev, bloom, 0u) & KEEP;
+    any |= hits[j];
+    prev = raw[j][7];
+  }
+  if (__any_sync(FULL, any != 0u)) {
+    /* the rare Bloom hits: the warp's bytes go to shared memory; then the q-gram ending at
+     * byte e of the warp's bytes and the three bytes before it (bytes before the warp's first
+     * byte read as zero) are looked up, from one call site */
 #pragma unroll
     for (int j = 0; j < WPT; ++j) {
       uint4 *d = reinterpret_cast<uint4 *>(bytes_s + 32 * (t.lane * WPT + j));
       d[0] = make_uint4(raw[j][0], raw[j][1], raw[j][2], raw[j][3]);
       d[1] = make_uint4(raw[j][4], raw[j][5], raw[j][6], raw[j][7]);
     }
-  }
-  if (!from_basis) {
-#pragma unroll
-    for (int j = 0; j < WPT; ++j) {
-      uint32_t o[8];
-      transpose32(raw[j], o);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
-    }
-  }
-  if (look) {
-    /* the rare Bloom hits: the trigram ending at byte e of the warp's bytes and the three bytes
-     * before it (bytes before the warp's first byte read as zero); one lookup call site */
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < WPT; ++j) {
       for (uint32_t m = hits[j]; m; m &= m - 1u) {
-        const int e = 32 * (t.lane * WPT + j) + __ffs(m) - 1;
-        uint32_t v[6];
+        const int k = __ffs(m) - 1 - (32 - NPROBE);
+        const int e = 32 * (t.lane * WPT + j) + QS * k + QS - 1;
+        uint32_t v[7];
 #pragma unroll
-        for (int d = 0; d < 6; ++d) v[d] = e - d >= 0 ? bytes_s[e - d] : 0u;
-        trigram_exact(v[2] | v[1] << 8 | v[0] << 16, v[3] | v[4] << 8 | v[5] << 16, keys, info,
-                      recs, log2, run);
+        for (int d = 0; d < 7; ++d) v[d] = e - d >= 0 ? bytes_s[e - d] : 0u;
+        const uint32_t key = QG == 4 ? (v[3] | v[2] << 8 | v[1] << 16 | v[0] << 24)
+                                     : (v[2] | v[1] << 8 | v[0] << 16);
+        const uint32_t pre3 = QG == 4 ? (v[4] | v[5] << 8 | v[6] << 16)
+                                      : (v[3] | v[4] << 8 | v[5] << 16);
+        qgram_exact(key, pre3, keys, info, recs, log2, run);
       }
     }
   }
   __syncwarp();
 #pragma unroll
   for (int w = 0; w < BG_NRUN; ++w) t.run[w] = run[32 * w];
+}
+
+/* The basis planes of the tile's bytes (as load_basis gives them). */
+__device__ __forceinline__ void basis_of(const uint32_t raw[WPT][8], S b[8]) {
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    uint32_t o[8];
+    transpose32(raw[j], o);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i].w[j] = o[i];
+  }
+}
+
+/* Lanes whose bytes are all outside {X0, X1, X2} (the first K of them) and whose words lie
+ * inside the input: ones_lanes of the class of the other bytes, from the bytes themselves.
+ * A byte equals x exactly when the byte of v = w ^ (x * 0x01010101) is zero, and
+ * (v - 0x01010101) & ~v & 0x80808080 is non-zero exactly when some byte of v is zero. */
+template <int K, uint32_t X0, uint32_t X1 = 0u, uint32_t X2 = 0u>
+__device__ __forceinline__ uint32_t excl_lanes(const Tile &t, const uint32_t raw[WPT][8]) {
+  uint32_t h = 0u, in = 1u;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t w = raw[j][i];
+      const uint32_t v0 = w ^ (X0 * 0x01010101u);
+      h |= (v0 - 0x01010101u) & ~v0 & 0x80808080u;
+      if (K > 1) {
+        const uint32_t v1 = w ^ (X1 * 0x01010101u);
+        h |= (v1 - 0x01010101u) & ~v1 & 0x80808080u;
+      }
+      if (K > 2) {
+        const uint32_t v2 = w ^ (X2 * 0x01010101u);
+        h |= (v2 - 0x01010101u) & ~v2 & 0x80808080u;
+      }
+    }
+    in &= t.vm.w[j] == FULL ? 1u : 0u;
+  }
+  return __ballot_sync(FULL, h == 0u && in);
+}
+
+/* Classes of the look-back carry obligations, for a cheap test before the exact one: bit c of
+ * the result is set when the lane's first four bytes all lie in class c (tab[b] holds the
+ * classes of byte b).  A lane whose words are all ones in class c has this bit set. */
+__device__ __forceinline__ uint32_t first4_classes(const uint32_t raw[WPT][8], const uint32_t *tab) {
+  const uint32_t w = raw[0][0];
+  return tab[w & 255u] & tab[(w >> 8) & 255u] & tab[(w >> 16) & 255u] & tab[w >> 24];
 }
 
 /* Lanes whose words of class stream C are all ones (inside the input): an addition over C
@@ -1005,6 +1063,45 @@ __device__ __forceinline__ void zero_store(const BgParams &p, const Tile &t, int
   }
 }
 
+/* Launches without output streams (pos_set): insert position key `key` into the set; true when
+ * it was not there yet.  Linear probing from a multiplicative hash; a full set (which the
+ * runtime sizes at twice the position capacity) reports BG_DEV_ERR_SETFULL. */
+__device__ __forceinline__ bool set_insert(const BgParams &p, unsigned long long key) {
+  unsigned long long h = (key * 0x9E3779B97F4A7C15ull) >> 20;
+  for (long long i = 0; i <= p.pos_set_mask; ++i) {
+    const unsigned long long at = (h + (unsigned long long)i) & (unsigned long long)p.pos_set_mask;
+    const unsigned long long prev = atomicCAS(p.pos_set + at, ~0ull, key);
+    if (prev == ~0ull) return true;
+    if (prev == key) return false;
+  }
+  atomicOr(p.state + 1, BG_DEV_ERR_SETFULL);
+  return false;
+}
+
+/* merge_store for launches without output streams: the bits of this part's value of output o
+ * that no part set before are those whose positions enter the set first; only they are
+ * counted and listed. */
+static __device__ __noinline__ void set_store(const BgParams &p, const Tile &t, int o, const S v) {
+  S nb;
+  const unsigned long long key = ((unsigned long long)o << 52) | ((unsigned long long)t.input << 32);
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    nb.w[j] = 0u;
+    if (t.lane >= HL && t.lane < 32 - TL && w >= 0 && w < t.W) {
+      uint32_t val = v.w[j];
+      const long long rem = t.n - 32 * w;
+      if (rem < 32) val &= FULL << (32 - rem);
+      while (val) {
+        const int b = 31 - __clz(val); /* highest set bit = lowest position */
+        val &= ~(1u << b);
+        if (set_insert(p, key | (unsigned long long)(32 * w + (31 - b)))) nb.w[j] |= 1u << b;
+      }
+    }
+  }
+  store_new_bits(p, t, o, nb);
+}
+
 /* Split form with outputs shared by several parts: OR this part's value of output o into the
  * tile's words (which the classify pass zeroed) and count, and list as positions, only the
  * bits it newly sets, so that counts stay exact whichever parts set a bit first.  Needs the
@@ -1014,6 +1111,10 @@ static __device__ __noinline__ void merge_store(const BgParams &p, const Tile &t
 #pragma unroll
   for (int j = 0; j < WPT; ++j) x |= v.w[j];
   if (!__any_sync(FULL, x != 0u)) return;
+  if (!p.out) {
+    set_store(p, t, o, v);
+    return;
+  }
   uint32_t *dst = p.out + (long long)o * p.out_stride + p.out_off[t.input];
   S nb;
 #pragma unroll
@@ -1065,6 +1166,13 @@ __device__ __forceinline__ void cls_prologue(const BgParams &p, int n_out) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc;
          i += (long long)gridDim.x * blockDim.x)
       p.counts[i] = 0ull;
+  }
+  if (p.pos_set) { /* an empty position set for the execute pass (slots: a multiple of 2) */
+    ulonglong2 *s2 = reinterpret_cast<ulonglong2 *>(p.pos_set);
+    const long long n2 = (p.pos_set_mask + 1) >> 1;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n2;
+         i += (long long)gridDim.x * blockDim.x)
+      s2[i] = make_ulonglong2(~0ull, ~0ull);
   }
 }
 

@@ -26,6 +26,7 @@ typedef unsigned long long uint64_t;
 #define BG_DEV_ERR_TIMEOUT 1u /* a look-back wait ran out of time                    */
 #define BG_DEV_ERR_CHAIN 2u   /* a look-back walked past the first tile of its input */
 #define BG_DEV_ERR_CAPACITY 4u /* the match-position buffer was too small             */
+#define BG_DEV_ERR_SETFULL 8u  /* the position set ran out of slots (counts incomplete) */
 
 typedef struct BgParams {
   const uint8_t *in_bytes;   /* BG_INPUT_BYTES: base of all inputs                        */
@@ -42,6 +43,11 @@ typedef struct BgParams {
                                 [6..7] match positions written (u64)                         */
   unsigned long long *positions; /* sparse output or NULL: (output << 52 | input << 32 | pos) */
   int64_t pos_capacity;
+  unsigned long long *pos_set; /* launches without output streams of a program whose parts
+                                  share outputs: open-addressed set of the positions set so far
+                                  (all ones = empty slot, cleared by the classify pass), so that
+                                  a bit two parts set is counted once; NULL otherwise          */
+  int64_t pos_set_mask;      /* slots - 1 (slots a power of two)                           */
   int64_t basis_stride;      /* words between the basis planes of one input               */
   int64_t out_stride;        /* words between two output streams                          */
   int64_t n_tiles;

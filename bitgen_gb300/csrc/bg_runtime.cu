@@ -309,6 +309,9 @@ struct bg_plan {
   int64_t cap_inputs = 0, cap_tiles = 0;
   unsigned long long *positions = nullptr;
   int64_t pos_capacity = 0;
+  unsigned long long *d_set = nullptr; /* position set of launches without output streams */
+  int64_t set_slots = 0;
+  bool count_only = false;             /* a set sized for counting, no positions written  */
   int64_t *h_stage = nullptr; /* pinned staging of the tables */
   cudaEvent_t staged = nullptr;
   bool staged_pending = false;
@@ -764,12 +767,30 @@ int bg_plan_create(bg_program *prog, const bg_layout *L, bg_plan **out) {
 int64_t bg_plan_tiles(const bg_plan *plan) { return plan ? plan->n_tiles : -1; }
 
 int bg_plan_set_positions(bg_plan *plan, unsigned long long *positions, int64_t capacity) {
-  if (!plan || capacity < 0 || (capacity > 0 && !positions))
+  if (!plan || capacity < 0 || capacity > ((int64_t)1 << 40))
     return fail(BG_ERR_INVALID, "bg_plan_set_positions: bad arguments");
-  if (plan->prog->desc.n_outputs >= 4096 || plan->cap_inputs >= (1 << 20))
-    return fail(BG_ERR_INVALID, "bg_plan_set_positions: more than 4095 outputs or 2^20 inputs");
+  if (plan->prog->desc.n_outputs >= 4095 || plan->cap_inputs >= (1 << 20))
+    return fail(BG_ERR_INVALID, "bg_plan_set_positions: more than 4094 outputs or 2^20 inputs");
+  /* a program whose parts share outputs counts the bits it adds against the output streams;
+   * for launches without them it keeps a set of the positions found so far, sized here at
+   * twice the capacity (a power of two), allocated once and reused while it is big enough */
+  if ((plan->prog->desc.flags & BG_PROGRAM_MERGES) && capacity > 0) {
+    int64_t slots = 1024;
+    while (slots < 2 * capacity) slots <<= 1;
+    if (slots > plan->set_slots) {
+      if (plan->d_set) cudaFree(plan->d_set);
+      plan->d_set = nullptr;
+      plan->set_slots = 0;
+      if (cudaMalloc(&plan->d_set, (size_t)slots * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(BG_ERR_NOMEM, "bg_plan_set_positions: position set");
+      }
+      plan->set_slots = slots;
+    }
+  }
   plan->positions = capacity ? positions : nullptr;
-  plan->pos_capacity = capacity;
+  plan->pos_capacity = positions ? capacity : 0;
+  plan->count_only = capacity > 0 && !positions;
   return BG_OK;
 }
 
@@ -924,9 +945,11 @@ extern "C" {
 int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
                    unsigned long long *counts, void *stream) {
   if (!plan || !input) return fail(BG_ERR_INVALID, "bg_plan_launch: null plan or input");
-  if (!out_streams && (plan->prog->desc.flags & BG_PROGRAM_MERGES))
+  const bool use_set = !out_streams && (plan->prog->desc.flags & BG_PROGRAM_MERGES);
+  if (use_set && (!plan->d_set || (!plan->positions && !plan->count_only)))
     return fail(BG_ERR_INVALID,
-                "bg_plan_launch: this program merges outputs across parts and needs out_streams");
+                "bg_plan_launch: this program merges outputs across parts: without out_streams "
+                "it needs a position capacity (bg_plan_set_positions)");
   const bg_layout &L = plan->layout;
   if (L.input_kind == BG_INPUT_BYTES && !aligned16(input))
     return fail(BG_ERR_ALIGN, "bg_plan_launch: input not 16-byte aligned");
@@ -950,6 +973,8 @@ int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
   prm.debug_wait_tile = plan->debug_wait_tile;
   prm.positions = plan->positions;
   prm.pos_capacity = plan->pos_capacity;
+  prm.pos_set = use_set ? plan->d_set : nullptr;
+  prm.pos_set_mask = use_set ? plan->set_slots - 1 : 0;
   prm.runs = plan->d_runs;
   /* the pre-pass bitmaps start after the records of the reserved tile count, so that a layout
    * with more tiles than the last one never finds bitmap words where it looks for records */
@@ -977,6 +1002,9 @@ int bg_plan_sync(bg_plan *plan, void *stream) {
   if (st) {
     BG_CUDA(cudaMemset(plan->d_state + 1, 0, sizeof st));
     if (st & BG_DEV_ERR_TIMEOUT) return fail(BG_ERR_TIMEOUT, "carry look-back wait timed out");
+    if (st & BG_DEV_ERR_SETFULL)
+      return fail(BG_ERR_CAPACITY, "match positions exceeded twice the position capacity of a "
+                                   "launch without output streams; counts are incomplete");
     if (st & BG_DEV_ERR_CAPACITY)
       return fail(BG_ERR_CAPACITY, "match positions exceeded the buffer; counts are complete");
     return fail(BG_ERR_DEVICE, "carry look-back walked past the start of its input");
@@ -995,6 +1023,7 @@ int bg_plan_destroy(bg_plan *plan) {
   if (plan->d_state) cudaFree(plan->d_state);
   if (plan->d_runs) cudaFree(plan->d_runs);
   if (plan->d_work) cudaFree(plan->d_work);
+  if (plan->d_set) cudaFree(plan->d_set);
   if (plan->h_stage) cudaFreeHost(plan->h_stage);
   delete plan;
   return BG_OK;
@@ -1151,6 +1180,8 @@ extern "C" int bg_scan_noalloc(const bg_program *prog, const uint8_t *input, int
                  : nullptr;
   prm.positions = nullptr;
   prm.pos_capacity = 0;
+  prm.pos_set = nullptr;
+  prm.pos_set_mask = 0;
   prm.basis_stride = 0;
   prm.out_stride = out_stride;
   prm.n_tiles = tiles;

@@ -291,10 +291,14 @@ class Plan:
     def tiles(self) -> int:
         return int(N.lib().bg_plan_tiles(self._h))
 
-    def set_positions(self, buf: Optional[torch.Tensor]):
-        """Sparse output buffer (int64 view of u64 entries) for later launches, or None."""
-        ptr, cap = (buf.data_ptr(), buf.numel()) if buf is not None else (None, 0)
+    def set_positions(self, buf: Optional[torch.Tensor], count_capacity: int = 0):
+        """Sparse output buffer (int64 view of u64 entries) for later launches, or None.  A
+        program whose parts share outputs can then also be launched without output streams
+        (positions only): its position set holds twice the buffer's entries.  With no buffer,
+        ``count_capacity`` > 0 sizes that set for counts-only launches."""
+        ptr, cap = (buf.data_ptr(), buf.numel()) if buf is not None else (None, int(count_capacity))
         N.check(N.lib().bg_plan_set_positions(self._h, ptr, cap), "bg_plan_set_positions")
+        self._set_capacity = cap
 
     def positions_written(self, stream: int) -> int:
         v = C.c_int64()
@@ -321,7 +325,7 @@ class Plan:
         N.check(N.lib().bg_plan_set_wait_limit(self._h, cycles, debug_wait_tile), "bg_plan_set_wait_limit")
 
     def launch(self, data_ptr: int, out_ptr: int, counts_ptr: int, stream: int):
-        if not out_ptr and self.program.merges:
+        if not out_ptr and self.program.merges and not getattr(self, "_set_capacity", 0):
             self._ensure_scratch()
             out_ptr = self._scratch.data_ptr()
         N.check(N.lib().bg_plan_launch(self._h, data_ptr, out_ptr or None, counts_ptr or None,
@@ -452,6 +456,8 @@ class Program:
         if self.fused:
             plan = self.plan(inp, offs, stride)
             pbuf = torch.empty(pos_capacity, dtype=torch.int64, device=dev) if positions else None
+            # positions without streams: a program whose parts share outputs counts each bit
+            # once through the plan's position set instead of the output streams
             plan.set_positions(pbuf)
             plan.launch(inp.data.data_ptr(), out_ptr, cnt_ptr, sp)
             if sync or positions:

@@ -135,8 +135,17 @@ class Group:
                         lines.append(" " * ind + "else:")
                         emit(s.orelse, ind + 2)
 
-        emit(self.stmts, 0)
-        lines.append(f"output.matches = {self.result}")
+        # a program ending in "result = x" stores x directly: the reference's alias removal
+        # (bitgen/passes/remove_alias.py:10-52) drops such an assignment but leaves the store
+        # "output.matches = result" reading the removed name
+        stmts, res = list(self.stmts), self.result
+        last = stmts[-1] if stmts else None
+        if (isinstance(last, Op) and last.op == "assign" and last.dst == res
+                and not any(res in (s.args if isinstance(s, Op) else (s.cond,))
+                            for s in walk(stmts[:-1]))):
+            stmts, res = stmts[:-1], last.args[0]
+        emit(stmts, 0)
+        lines.append(f"output.matches = {res}")
         return "\n".join(lines) + "\n"
 
 

@@ -1,54 +1,73 @@
-"""Trigram prefilter: which terms of a program can be non-zero in a tile, decided from the
+"""Q-gram prefilter: which terms of a program can be non-zero in a tile, decided from the
 tile's bytes before any bitstream is computed.
 
-A *trigram node* is a node z whose set bits constrain the bytes at and just before them: if z
-is set at position p, then bytes p-2, p-1 and p lie in sets S0, S1 and S2 (position bounds,
-derived through AND, OR and Advance; see ``position_bounds``).  So when no trigram of
-S0 x S1 x S2 occurs among the bytes a warp computes, z is zero in all of the warp's exact
-lanes.  A node that bounds only its last two bytes is a bigram node: S0 is then every byte.
+Position bounds.  PB[v][k] is the set of byte values that can stand k positions before a set
+bit of node v (``position_bounds``: AND intersects, OR / XOR / SEL unite, Advance shifts, a
+class bounds its own position).  A *window* of node z is a run of W = q + s - 1 consecutive
+positions k = o .. o + W - 1 whose bounds are all constrained: when z is set at p, the bytes
+p - o - W + 1 .. p - o lie in those sets, so one of the s q-grams of the window (ending at
+p - o - j, j < s) ends at a position that is a multiple of s plus s - 1.  The kernel probes
+exactly those q-grams: with stride s it looks at one q-gram in s positions.  When none of
+the window's q-grams occurs among the warp's bytes, z is zero in all of the warp's exact
+lanes (the window lies inside the bytes the warp computes, since it is no deeper than the
+program's halo).
 
-Zero implication.  Z(v) is the set of trigram nodes whose being zero makes v zero: AND and
+Configurations (q, s): (4, 2) probes 16 four-byte q-grams per 32 bytes and needs windows of
+five positions (a literal of five bytes, or four bytes and a small class); (4, 1) and (3, 1)
+need four and three.  ``build`` picks, per program, the configuration with the lowest
+estimated cost per tile: probes, expected Bloom hits (each resolved on the slow path) and
+terms run.
+
+Zero implication.  Z(v) is the set of window nodes whose being zero makes v zero: AND and
 Advance / Lookahead inherit the union of their operands' sets, OR / XOR / SEL the intersection,
 and an addition its marker's set.  The last rule holds only while no carry enters the tile, so
 the kernel also runs a term whenever one of its additions could take or owe a carry: a
 look-back addition whose class is all ones at its carry lane or at its successor's, or a
 pre-pass addition with a carry-in when the term's filter holds only through it.
 
-Each term (an OR-ed leaf of an output) gets the most selective trigram node of Z(term) as its
+Each term (an OR-ed leaf of an output) gets the most selective window of Z(term) as its
 filter, preferring one that does not pass through a pre-pass addition; a term without one
-always runs.  Each pre-pass addition gets the filter of its marker,
-so the pre-pass can skip the marker's computation too.
+always runs.  Each pre-pass addition gets the filter of its marker, so the pre-pass can skip
+the marker's computation too.
 
-Extensions.  Where the filter node's bounds also fix single bytes 3, 4 and 5 positions back,
-the trigram alone would pass the term on every chance occurrence of its last three bytes; the
-table then holds, under the trigram, an extension record (those bytes and the term's bit), and
-the kernel sets the bit only when the bytes before the trigram match.  On printable text this
-makes the chance hits of literal filters about a hundred times rarer per byte of extension.
+Extensions.  Where the bounds also fix single bytes 1, 2 and 3 positions before a q-gram, the
+table holds, under the q-gram, an extension record (those bytes and the term's bit), and the
+kernel sets the bit only when the bytes before the q-gram match.
 
-The kernel tests every trigram of the tile against a Bloom bitmap (2^20 bits by default, in
-shared memory: a warp takes the slow path whenever any of its 32 lanes hits, so the bitmap is
-sized for a per-lane false-hit rate well below 1/32) and resolves the rare hits in an exact open-addressed table that maps a trigram to the bit mask
-of the filters containing it.  Both tables are generated here and compiled into the kernel.
+The kernel probes the q-grams in a Bloom bitmap (2^20 bits by default, in shared memory) and
+resolves the rare hits in an exact open-addressed table that maps a q-gram to the records of
+the filters containing it.  Both tables are generated here and compiled into the kernel.
 """
 
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 from typing import Dict, FrozenSet, List, Optional, Sequence, Tuple
 
 ALL = (1 << 256) - 1
-MAX_SET = 4096          # largest trigram set one filter may carry
-MAX_EXT = 3             # bytes before the trigram an extension record may fix
-EXT_DEPTH = 3 + MAX_EXT
+MAX_KEYS = 4096         # most q-grams one filter may register
+MAX_EXT = 3             # bytes before a q-gram an extension record may fix
+DEPTH = 12              # positions before a set bit the bounds are followed for
 BLOOM_BITS = 20         # log2 of the Bloom bitmap size (128 KB of shared memory)
 HASH_BLOOM = 0x9E3779B1
 HASH_EXACT = 0x85EBCA6B
+CONFIGS = ((4, 2), (4, 1), (3, 1))   # (q, stride), cheapest probes first
+# estimated warp instructions per tile, for choosing the configuration: a probe per lane, a
+# Bloom hit (the slow path: bytes to shared memory, lookup), a term run by the execute pass
+COST_PROBE, COST_HIT, COST_RUN = 5.0, 150.0, 600.0
 
 
-def bloom_hash(key: int, bits: int = BLOOM_BITS) -> int:
-    """Bit index of trigram `key` in a 2^bits-bit Bloom bitmap: the top `bits` bits of the 24-bit
-    product key * HASH_BLOOM mod 2^24 (the kernel's bg_device.cuh bloom_probe)."""
-    return ((key * HASH_BLOOM) & 0xFFFFFF) >> (24 - bits)
+def bloom_hash(key: int, bits: int = BLOOM_BITS, q: int = 3) -> int:
+    """Bit index of q-gram `key` (oldest byte in bits 0-7) in a 2^bits-bit Bloom bitmap, as the
+    kernel computes it (bg_device.cuh bloom_probe): the word is the top bits - 5 bits of the
+    32-bit product key * HASH_BLOOM (of the 24-bit product shifted up by 8 for a trigram, so
+    that the byte above it does not matter), the bit within the word is the key's low 5 bits."""
+    if q == 3:
+        h = ((key & 0xFFFFFF) * HASH_BLOOM << 8) & 0xFFFFFFFF
+    else:
+        h = (key * HASH_BLOOM) & 0xFFFFFFFF
+    return ((h >> (32 - bits + 5)) << 5) | (key & 31)
 
 
 def exact_hash(key: int, log2_slots: int) -> int:
@@ -59,7 +78,11 @@ def _bytes(s: int) -> List[int]:
     return [b for b in range(256) if (s >> b) & 1]
 
 
-def position_bounds(gen, depth: int = 3) -> Dict[int, Tuple[int, ...]]:
+def _n(s: int) -> int:
+    return bin(s).count("1")
+
+
+def position_bounds(gen, depth: int = DEPTH) -> Dict[int, Tuple[int, ...]]:
     """PB[v][k]: set of byte values that can stand k positions before a set bit of node v
     (k < depth; ALL when unconstrained).  AND intersects its operands' bounds, OR / XOR / SEL
     unite them, Advance(a, s) moves a's bounds s positions back, a class bounds its own position
@@ -90,28 +113,63 @@ def position_bounds(gen, depth: int = 3) -> Dict[int, Tuple[int, ...]]:
     return PB
 
 
-def trigram_nodes(gen, PB: Dict[int, Tuple[int, ...]]) -> Dict[int, Tuple[int, int, int]]:
-    """Trigram nodes of the live program and their byte sets (S0, S1, S2): every heavy node
-    whose bounds at the last three positions are all constrained, with a small product."""
+@dataclass(frozen=True)
+class Window:
+    """q-grams of one filter: grams[j] = byte sets of the q-gram ending j positions before the
+    window's end (oldest byte first), ext[j] = single bytes fixed before it (nearest first)."""
+    grams: Tuple[Tuple[int, ...], ...]
+    ext: Tuple[Tuple[int, ...], ...]
+
+    def keys(self) -> int:
+        return sum(math.prod(_n(x) for x in g) for g in self.grams)
+
+    def chance(self, alpha: int) -> float:
+        """Expected table hits per probe on text uniform over `alpha` (before extensions)."""
+        na = max(1, _n(alpha))
+        return sum(math.prod(_n(x & alpha) / na for x in g) for g in self.grams)
+
+    def exact_chance(self, alpha: int) -> float:
+        na = max(1, _n(alpha))
+        return sum(math.prod(_n(x & alpha) / na for x in g) * (1.0 / na) ** len(e)
+                   for g, e in zip(self.grams, self.ext))
+
+
+def windows(gen, PB, q: int, stride: int) -> Dict[int, List[Window]]:
+    """Every window of every heavy live node for q-grams probed at `stride`."""
     d = gen.d
-    out: Dict[int, Tuple[int, int, int]] = {}
+    W = q + stride - 1
+    out: Dict[int, List[Window]] = {}
     for z in sorted(gen.live):
         if d.is_cc(z):
             continue
-        s2, s1, s0 = PB[z][0], PB[z][1], PB[z][2]
-        if ALL in (s1, s2):
-            continue
-        # a bigram node (only its last two bytes bounded) is the trigram set ALL x S1 x S2
-        size = bin(s0).count("1") * bin(s1).count("1") * bin(s2).count("1")
-        if 0 < size <= MAX_SET:
-            out[z] = (s0, s1, s2)
+        b = PB[z]
+        ws = []
+        for o in range(0, len(b) - W + 1):
+            seg = b[o:o + W]
+            if any(x == ALL or x == 0 for x in seg):
+                continue
+            grams, exts = [], []
+            for j in range(stride):
+                # the q-gram ending at distance o + j covers distances o + j .. o + j + q - 1
+                g = tuple(b[o + j + q - 1 - i] for i in range(q))      # oldest first
+                e = []
+                for k in range(o + j + q, min(len(b), o + j + q + MAX_EXT)):
+                    if _n(b[k]) != 1:
+                        break
+                    e.append(b[k].bit_length() - 1)
+                grams.append(g)
+                exts.append(tuple(e))
+            w = Window(tuple(grams), tuple(exts))
+            if w.keys() <= MAX_KEYS:
+                ws.append(w)
+        if ws:
+            out[z] = ws
     return out
 
 
-def zero_sets(gen, tri: Dict[int, Tuple[int, int, int]],
-              blocked=frozenset()) -> Dict[int, FrozenSet[int]]:
-    """Z(v) for every live node.  The result of an addition in `blocked` implies nothing (its
-    carry may be non-zero whatever its marker)."""
+def zero_sets(gen, tri, blocked=frozenset()) -> Dict[int, FrozenSet[int]]:
+    """Z(v) for every live node (`tri`: the nodes that have a window).  The result of an
+    addition in `blocked` implies nothing (its carry may be non-zero whatever its marker)."""
     d = gen.d
     Z: Dict[int, FrozenSet[int]] = {}
     empty: FrozenSet[int] = frozenset()
@@ -137,31 +195,35 @@ def zero_sets(gen, tri: Dict[int, Tuple[int, int, int]],
     return Z
 
 
-def _set_size(sets: Tuple[int, int, int]) -> int:
-    n = 1
-    for x in sets:
-        n *= bin(x).count("1")
-    return n
-
-
-def trigram_set(sets: Tuple[int, int, int]) -> List[int]:
-    s0, s1, s2 = (_bytes(s) for s in sets)
-    return [a | (b << 8) | (c << 16) for a in s0 for b in s1 for c in s2]
+def qgram_set(sets: Tuple[int, ...]) -> List[int]:
+    """Keys of a q-gram with these byte sets (oldest first): oldest byte in bits 0-7."""
+    keys = [0]
+    for i, s in enumerate(sets):
+        keys = [k | (b << (8 * i)) for k in keys for b in _bytes(s)]
+    return keys
 
 
 @dataclass
 class TermFilter:
     """Per-program prefilter: bit r (r < n_terms) = term r may be non-zero, bit n_terms + k =
-    pre-pass addition k's marker may be non-zero.  ``always`` holds the terms without a filter."""
+    pre-pass addition k's marker may be non-zero.  ``always`` holds the terms without a filter.
+    q-grams of q bytes are probed at the positions that are a multiple of ``stride`` plus
+    stride - 1 (of a 32-byte aligned lane)."""
     n_terms: int
     n_pre: int
     term_node: List[Optional[int]]
     pre_node: List[Optional[int]]
     term_cond: List[bool] = field(default_factory=list)  # filter implies zero only if no carry
-    table: Dict[int, int] = field(default_factory=dict)   # trigram -> bits it sets by itself
-    # trigram -> extension records (bytes 3, 4, 5 positions back packed low byte first, their
-    # number, bit): the bit is set when those bytes precede the trigram
+    table: Dict[int, int] = field(default_factory=dict)   # q-gram -> bits it sets by itself
+    # q-gram -> extension records (bytes 1, 2, 3 positions before it packed nearest first in
+    # bits 0-7, 8-15, 16-23, their number, bit): the bit is set when those bytes precede it
     ext: Dict[int, List[Tuple[int, int, int]]] = field(default_factory=dict)
+    q: int = 3
+    stride: int = 1
+    alphabet: int = 0                                     # estimated text alphabet (bit set)
+    windows: List[Optional[Window]] = field(default_factory=list)
+    cost: float = 0.0                                     # estimated instructions per tile
+    hits: float = 0.0                                     # estimated slow-path hits per tile
 
     @property
     def n_bits(self) -> int:
@@ -175,32 +237,28 @@ class TermFilter:
     def enabled(self) -> bool:
         return bool(self.table)
 
-    alphabet: int = 0                                     # estimated text alphabet (bit set)
-    sets: List[Optional[Tuple[int, int, int]]] = field(default_factory=list)
-
     def expected_per_tile(self, positions: int) -> float:
         """Terms a tile of `positions` bytes is expected to run, taking the text to be uniform
         over the estimated alphabet (the bytes of the program's narrow classes)."""
-        a = self.alphabet
-        na = bin(a).count("1")
-        if na == 0:
+        if _n(self.alphabet) == 0:
             return 0.0
         e = 0.0
-        for r, z in enumerate(self.term_node):
-            if z is None or self.sets[r] is None:
+        for r, w in enumerate(self.windows[:self.n_terms]):
+            if w is None:
                 e += 1.0
-                continue
-            p = 1.0
-            for s in self.sets[r]:
-                p *= bin(s & a).count("1") / na
-            e += min(1.0, p * positions)
+            else:
+                e += min(1.0, w.exact_chance(self.alphabet) * positions / self.stride)
         return e
 
-    def match(self, trigram: int, pre3: int) -> int:
-        """Bits set by `trigram` when the three bytes before it, packed like the records
-        (byte 3 back in bits 0-7), are `pre3`."""
-        m = self.table.get(trigram, 0)
-        for b, n, bit in self.ext.get(trigram, ()):
+    def mask_key(self, key: int) -> int:
+        return key & ((1 << (8 * self.q)) - 1)
+
+    def match(self, key: int, pre3: int) -> int:
+        """Bits set by q-gram `key` when the three bytes before it, packed like the records
+        (the nearest in bits 0-7), are `pre3`."""
+        key = self.mask_key(key)
+        m = self.table.get(key, 0)
+        for b, n, bit in self.ext.get(key, ()):
             mask = (1 << (8 * n)) - 1
             if (pre3 ^ b) & mask == 0:
                 m |= 1 << bit
@@ -217,25 +275,25 @@ class TermFilter:
         return m
 
     def bloom(self, bits: int = BLOOM_BITS) -> List[int]:
-        assert 5 < bits <= 24, "the Bloom index comes from a 24-bit product"
+        assert 10 <= bits <= 24
         words = [0] * ((1 << bits) // 32)
         for key in self.table:
-            h = bloom_hash(key, bits)
+            h = bloom_hash(key, bits, self.q)
             words[h >> 5] |= 1 << (h & 31)
         return words
 
     def records(self, key: int) -> List[Tuple[int, int, int]]:
-        """The records of trigram `key`: (bytes, count, bit), the bit set when the first
-        `count` bytes before the trigram equal `bytes` (count 0: always)."""
+        """The records of q-gram `key`: (bytes, count, bit), the bit set when the first
+        `count` bytes before the q-gram equal `bytes` (count 0: always)."""
         m = self.table.get(key, 0)
         base = [(0, 0, b) for b in range(self.n_bits) if (m >> b) & 1]
         return base + list(self.ext.get(key, []))
 
     def exact(self) -> Tuple[int, List[int], List[int], List[int]]:
-        """(log2 slots, keys, slot info, records): open addressing with linear probing; a key
-        slot holds trigram | 1 << 31 (0 = empty) and its info word record_start << 8 |
-        record_count; a record is two words, bytes | count << 24 and the bit it sets (see
-        `records`).  All of it fits the kernel's shared memory."""
+        """(log2 slots, keys, slot info, records): open addressing with linear probing; a slot
+        holds the key and its info word record_start << 8 | record_count (0 = empty slot, a
+        key has at least one record); a record is two words, bytes | count << 24 and the bit it
+        sets (see `records`).  All of it fits the kernel's shared memory."""
         n = len(self.table)
         log2 = 4
         while (1 << log2) < 2 * max(1, n):
@@ -246,77 +304,107 @@ class TermFilter:
         recs: List[int] = []
         for key in sorted(self.table):
             s = exact_hash(key, log2)
-            while keys[s]:
+            while info[s]:
                 s = (s + 1) & (slots - 1)
-            keys[s] = key | (1 << 31)
+            keys[s] = key
             rs = self.records(key)
-            assert len(rs) < 256 and len(recs) // 2 < (1 << 23)
+            assert 0 < len(rs) < 256 and len(recs) // 2 < (1 << 23)
             info[s] = ((len(recs) // 2) << 8) | len(rs)
             for b, cnt, bit in rs:
                 recs += [b | (cnt << 24), bit]
         return log2, keys, info, recs or [0, 0]
 
-def build(gen, terms: Sequence[int], pre: Sequence[int], tri_limit: int = 1 << 16) -> TermFilter:
-    """Filters for `terms` (node ids, in bit order) and pre-pass additions `pre` (node ids, in
-    index order)."""
-    tri = trigram_nodes(gen, position_bounds(gen))
-    Z = zero_sets(gen, tri)
+
+def _choose(gen, terms, pre, q, stride, PB, bloom_bits):
+    """Filters of one configuration: (term windows/nodes, pre nodes, conditions, alphabet)."""
+    d = gen.d
+    wins = windows(gen, PB, q, stride)
+    Z = zero_sets(gen, wins)
     # through a pre-pass addition a filter holds only while that addition's carry-in is zero,
     # which a '.*' after its first match almost never is; other additions are checked anyway
-    Zp = zero_sets(gen, tri, blocked=frozenset(pre))
-    d = gen.d
-    deep = position_bounds(gen, depth=EXT_DEPTH)
+    Zp = zero_sets(gen, wins, blocked=frozenset(pre))
+    # the text's alphabet, as the program sees it: the bytes its windows' narrow sets name
+    # (a wide set such as '.' says nothing about the text)
+    alpha = 0
+    for ws in wins.values():
+        for w in ws:
+            for g in w.grams:
+                for x in g:
+                    if _n(x) <= 64:
+                        alpha |= x
+    bloom_p = 1.0 / (1 << bloom_bits)
 
-    def fixed_before(z) -> List[int]:
-        """Single bytes that the bounds of z fix 3, 4, 5 positions back (stopping at the
-        first position that is not a single byte)."""
-        out = []
-        for k in range(3, EXT_DEPTH):
-            s = deep[z][k]
-            if s == ALL or bin(s).count("1") != 1:
-                break
-            out.append(s.bit_length() - 1)
-        return out
+    def score(w: Window) -> float:
+        # chance hits of the exact records plus the Bloom false hits the keys add (per probe)
+        return w.exact_chance(alpha) + (w.chance(alpha) + w.keys() * bloom_p) * COST_HIT / COST_RUN
 
-    def best(zs) -> Optional[int]:
-        # smallest trigram set, then the longest extension (fewest chance hits)
-        cands = sorted(zs, key=lambda z: (_set_size(tri[z]), -len(fixed_before(z)), z))
-        return cands[0] if cands else None
+    def best(zs):
+        cands = [(score(w), z, w) for z in zs for w in wins[z]]
+        if not cands:
+            return None, None
+        sc, z, w = min(cands, key=lambda c: (c[0], c[1]))
+        return z, w
 
-    term_node, term_cond = [], []
+    term_node, term_win, term_cond = [], [], []
     for v in terms:
-        z = best(Zp.get(v, ()))
+        z, w = best(Zp.get(v, ()))
         cond = z is None
         if z is None:
-            z = best(Z.get(v, ()))
+            z, w = best(Z.get(v, ()))
         term_node.append(z)
+        term_win.append(w)
         term_cond.append(cond and z is not None)
-    pre_node = [best(Z.get(d.nodes[a].args[0], ())) for a in pre]
-    f = TermFilter(len(terms), len(pre), term_node, pre_node, term_cond)
-    f.sets = [tri[z] if z is not None else None for z in term_node]
-    # the text's alphabet, as the program sees it: the bytes its filters name
-    alpha = 0
-    for s in f.sets:
-        for x in s or ():
-            if x != ALL:
-                alpha |= x
-    f.alphabet = alpha
-    table: Dict[int, int] = {}
-    ext: Dict[int, List[Tuple[int, int, int]]] = {}
-    for bit, z in list(enumerate(term_node)) + [(len(terms) + k, z) for k, z in enumerate(pre_node)]:
-        if z is None:
+    pre_node, pre_win = [], []
+    for a in pre:
+        z, w = best(Z.get(d.nodes[a].args[0], ()))
+        pre_node.append(z)
+        pre_win.append(w)
+    return term_node, term_win, term_cond, pre_node, pre_win, alpha
+
+
+def build(gen, terms: Sequence[int], pre: Sequence[int], key_limit: int = 1 << 16,
+          config: Optional[Tuple[int, int]] = None, bloom_bits: int = BLOOM_BITS) -> TermFilter:
+    """Filters for `terms` (node ids, in bit order) and pre-pass additions `pre` (node ids, in
+    index order), in the configuration (q, stride) of lowest estimated cost per tile (or the
+    one given)."""
+    PB = position_bounds(gen)
+    best_f, best_cost = None, None
+    positions = 1024
+    for q, stride in ([config] if config else CONFIGS):
+        tn, tw, tc, pn, pw, alpha = _choose(gen, terms, pre, q, stride, PB, bloom_bits)
+        f = TermFilter(len(terms), len(pre), tn, pn, tc, q=q, stride=stride, alphabet=alpha,
+                       windows=tw + pw)
+        table: Dict[int, int] = {}
+        ext: Dict[int, List[Tuple[int, int, int]]] = {}
+        for bit, w in enumerate(tw + pw):
+            if w is None:
+                continue
+            for g, e in zip(w.grams, w.ext):
+                packed = sum(b << (8 * i) for i, b in enumerate(e))
+                for key in qgram_set(g):
+                    if e:
+                        table.setdefault(key, 0)
+                        ext.setdefault(key, []).append((packed, len(e), bit))
+                    else:
+                        table[key] = table.get(key, 0) | (1 << bit)
+        if len(table) > key_limit or any(
+                bin(table.get(k, 0)).count("1") + len(ext.get(k, [])) > 255 for k in table):
+            table, ext = {}, {}
+        f.table, f.ext = table, ext
+        if not f.enabled:
             continue
-        fixed = fixed_before(z)
-        packed = sum(b << (8 * i) for i, b in enumerate(fixed))
-        for key in trigram_set(tri[z]):
-            if fixed:
-                table.setdefault(key, 0)
-                ext.setdefault(key, []).append((packed, len(fixed), bit))
-            else:
-                table[key] = table.get(key, 0) | (1 << bit)
-    if len(table) > tri_limit or any(
-            bin(table.get(k, 0)).count("1") + len(ext.get(k, [])) > 255 for k in table):
-        table, ext = {}, {}
-    f.table = table
-    f.ext = ext
-    return f
+        # per tile of `positions` bytes (a warp of 32 lanes): probes per lane, slow-path hits
+        # (Bloom false hits and chance q-grams), terms run
+        hits = positions / stride * (len(table) / (1 << bloom_bits)
+                                     + sum(w.chance(alpha) for w in tw + pw if w is not None))
+        cost = (positions / 32 / stride * COST_PROBE + hits * COST_HIT
+                + f.expected_per_tile(positions) * COST_RUN)
+        f.cost, f.hits = cost, hits
+        if best_cost is None or cost < best_cost:
+            best_f, best_cost = f, cost
+    if best_f is None:
+        q, stride = config or CONFIGS[-1]
+        tn = [None] * len(terms)
+        best_f = TermFilter(len(terms), len(pre), tn, [None] * len(pre), [False] * len(terms),
+                            q=q, stride=stride, windows=[None] * (len(terms) + len(pre)))
+    return best_f

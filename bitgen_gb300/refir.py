@@ -1,22 +1,40 @@
 """Adapter from BitGen's bitstream IR (``bitgen/inst``) to this engine's Pablo IR.
 
 BitGen's front end parses Pablo into ``BsInst`` lists (``bitgen/bitparser/bitstream_parser.py:
-249-279``): eight ``STREAMLOAD`` of the basis planes, the program, and a final ``STREAMSTORE``
-(``bs_result_stream |= <last result>``).  For the CUDA backend a ``SEL`` is already split into
-NOT / AND / AND / OR (``bitstream_parser.py:214-227``).  These functions turn such a list, given
-either as live objects with the parser's ``var_name_map`` or as the JSON form written by
-``tests/golden/make_golden.py``, into a :class:`bitgen_gb300.pablo.Group`.  Only the IR's
-meaning is used; performance passes that inject raw CUDA text (``BsStr`` from ``cc_advance`` /
-``graph_break``) have no meaning here and are rejected.
+249-279``): eight ``STREAMLOAD`` of the basis planes from ``basic_stream``, the program, and a
+final ``STREAMSTORE`` into ``bs_result_stream``.  For the CUDA backend a ``SEL`` is already split
+into NOT / AND / AND / OR (``bitstream_parser.py:214-227``).  ``run_passes``
+(``bitgen/from_icgrep.py:124-166``) then rewrites the list for the reference's code generator;
+these functions turn the result, given either as live objects with the parser's
+``var_name_map`` or as the JSON form written by ``tests/golden/make_golden.py``, into a
+:class:`bitgen_gb300.pablo.Group`.  Only the IR's meaning is kept:
+
+* ``graph_break`` (``bitgen/passes/graph_break.py``) cuts the program into kernels: a value used
+  past a cut is stored to a temporary stream (``STREAMSTORE`` into ``<var>_stream``, line 36)
+  and loaded back (``STREAMLOAD``, line 117) - an assignment through that stream; inside a
+  loop a carried value goes to ``<var>_stream_next``, swapped with ``<var>_stream`` after
+  every iteration (lines 308-319);
+  ``STREAMDEFINE`` (the stream's pointer, line 83) and ``GRAPHBREAK`` (the cut) carry no
+  value.  Stores are wrapped in ``if (idx < n_unit_basic)`` (lines 179, 405), the kernel's
+  bounds check on its thread index, which holds for every position of the stream.
+* ``short_circuit`` (``bitgen/passes/short_circuit.py:263-361``) adds raw CUDA text: a jump
+  ``if (block_all_zeros(x, &zero_flag)) { goto LABELn; }`` over an AND chain that is zero
+  when ``x`` is zero, and the label ``LABELn:``.  It skips work whose result is zero anyway,
+  so both are dropped.
+* Other raw CUDA text (``cc_advance`` shifts) has no meaning here and is rejected.
 """
 
 from __future__ import annotations
 
+import re
 from typing import Dict, List
 
 from .pablo import Group, If, Op, While
 
 _BIN = {"AND": "and", "OR": "or", "XOR": "xor"}
+_THREAD_GUARD = "idx < n_unit_basic"
+_SHORT_JUMP = re.compile(r"^\s*if \(block_all_zeros\(\w+, &zero_flag\)\) \{ goto LABEL\d+; \}\s*$")
+_SHORT_LABEL = re.compile(r"^\s*LABEL\d+:\s*$")
 
 
 def _convert(items, name, result_box) -> List:
@@ -25,11 +43,23 @@ def _convert(items, name, result_box) -> List:
         t = it["type"]
         ops = it.get("operands", [])
         ret = it.get("ret")
+        if t in ("STREAMDEFINE", "GRAPHBREAK"):
+            continue
         if t == "STREAMLOAD":
+            if ops and ops[0] != "basic_stream":     # a value reloaded after a graph break
+                out.append(Op(name(ret), "assign", (name(ops[0]),)))
             continue
         if t == "STREAMSTORE":
-            result_box[0] = name(ops[0])
+            if ret in (None, "bs_result_stream"):
+                result_box[0] = name(ops[0])
+            else:                                    # spilled for a reload
+                out.append(Op(name(ret), "assign", (name(ops[0]),)))
             continue
+        if t == "STR":
+            text = it.get("text", "")
+            if _SHORT_JUMP.match(text) or _SHORT_LABEL.match(text):
+                continue
+            raise ValueError(f"raw CUDA text {text!r} has no meaning for this engine")
         if t in _BIN:
             out.append(Op(name(ret), _BIN[t], (name(ops[0]), name(ops[1]))))
         elif t == "NOT":
@@ -45,7 +75,16 @@ def _convert(items, name, result_box) -> List:
         elif t == "SEL":
             out.append(Op(name(ret), "sel", (name(it["cond"]), name(ops[0]), name(ops[1]))))
         elif t == "WHILE":
-            out.append(While(name(it["cond"]), _convert(it["body"], name, result_box)))
+            body = _convert(it["body"], name, result_box)
+            # the loop swaps each double-buffered stream with its "_next" store after every
+            # iteration (graph_break.py:308-319, inst_block_while.py:126)
+            for cur, nxt in it.get("swap", []):
+                body.append(Op(name(cur), "assign", (name(nxt),)))
+            out.append(While(name(it["cond"]), body))
+        elif t == "IF" and it["cond"] == _THREAD_GUARD:
+            out.extend(_convert(it["then"], name, result_box))
+            if it.get("else"):
+                raise ValueError("a thread-bounds guard with an else branch")
         elif t == "IF":
             out.append(If(name(it["cond"]), _convert(it["then"], name, result_box),
                           _convert(it["else"], name, result_box) if it.get("else") is not None else None))
@@ -58,6 +97,28 @@ def _name(v: str) -> str:
     return v if v != "output.matches" else "output_matches"
 
 
+def _check_defined(stmts, defined: set):
+    """Every variable is defined before it is read (loop bodies may read what a later
+    iteration defines, as long as it is defined before the loop too)."""
+    for s in stmts:
+        if isinstance(s, Op):
+            for a in s.args:
+                if a not in defined and a not in ("0", "1") and not a.startswith("basis"):
+                    raise ValueError(f"the IR reads {a!r}, which no earlier instruction defines "
+                                     f"(an assignment the reference's alias removal dropped?)")
+            defined.add(s.dst)
+        elif isinstance(s, While):
+            if s.cond not in defined:
+                raise ValueError(f"the IR's loop tests {s.cond!r} before it is defined")
+            _check_defined(s.body, defined)
+        else:
+            if s.cond not in defined:
+                raise ValueError(f"the IR's branch tests {s.cond!r} before it is defined")
+            _check_defined(s.then, defined)
+            if s.orelse:
+                _check_defined(s.orelse, defined)
+
+
 def group_from_ir(items: List[dict]) -> Group:
     """Group from the JSON dump of a reference instruction list."""
     box = [None]
@@ -65,6 +126,7 @@ def group_from_ir(items: List[dict]) -> Group:
     if box[0] is None:
         last = [s for s in stmts if isinstance(s, Op)]
         box[0] = last[-1].dst
+    _check_defined(stmts, set())
     return Group(stmts, box[0])
 
 
@@ -77,6 +139,9 @@ def _dump(inst, names: Dict[int, str]) -> dict:
     if t == "WHILE":
         d["cond"] = nm(inst.condition)
         d["body"] = [_dump(x, names) for x in inst.body.body]
+        swaps = [re.findall(r"&(\w+)", c) for c in getattr(inst, "cuda_swap_pointer", [])]
+        if swaps:
+            d["swap"] = swaps
     elif t == "IF":
         d["cond"] = nm(inst.condition)
         d["then"] = [_dump(x, names) for x in inst.body_1.body]
@@ -85,9 +150,9 @@ def _dump(inst, names: Dict[int, str]) -> dict:
         d["cond"] = nm(inst.condition)
         d["operands"] = [nm(o) for o in inst.operands]
     elif t == "STR":
-        raise ValueError("raw CUDA text (cc_advance / graph_break passes) cannot be executed")
+        d["text"] = inst.str
     else:
-        d["operands"] = [nm(o) for o in inst.operands]
+        d["operands"] = [nm(o) for o in (inst.operands or [])]
     return d
 
 

@@ -8,6 +8,11 @@ launches one fused scan.  Batches on different slots overlap on the GPU, and req
 arrive while others run are admitted as soon as a slot and the budget allow.  Each request's
 latency runs from its arrival to the moment its counts are back on the host.
 
+Request payloads may live in pinned host arenas (``RequestArena``): each pattern set's requests
+laid out in arrival order, 32-byte aligned, so that the oldest requests of one set, which form
+a batch, are one contiguous run of the arena (two where it wraps) and reach the device with one
+copy each.  Payloads elsewhere are gathered into the slot's pinned staging buffer first.
+
 ``serve_plain`` is the comparison form: one launch per request, one at a time, in arrival order.
 """
 
@@ -35,6 +40,38 @@ class Request:
     arrival: float          # seconds from the start of the run
     pset: str
     data: np.ndarray        # uint8
+
+
+class RequestArena:
+    """Pinned host memory holding request payloads back to back (32-byte aligned).  ``take(n)``
+    returns the next n bytes as a numpy view, wrapping to the start when the arena is full, so
+    consecutive takes are contiguous except at a wrap."""
+
+    def __init__(self, nbytes: int, fill: Optional[np.ndarray] = None):
+        self.tensor = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+        self.view = self.tensor.numpy()
+        if fill is not None:
+            reps = -(-nbytes // fill.size)
+            for i in range(reps):
+                a = i * fill.size
+                self.view[a:a + fill.size] = fill[:max(0, min(fill.size, nbytes - a))]
+        self.at = 0
+        self.base = self.view.ctypes.data
+
+    def take(self, n: int) -> np.ndarray:
+        span = -(-n // ALIGN) * ALIGN
+        if span > self.view.size:
+            raise ValueError("request larger than its arena")
+        if self.at + span > self.view.size:
+            self.at = 0
+        v = self.view[self.at:self.at + n]
+        self.at += span
+        return v
+
+    def offset(self, a: np.ndarray) -> int:
+        """Byte offset of view `a` in the arena, or -1 when it lies elsewhere."""
+        off = a.ctypes.data - self.base if a.size else -1
+        return off if 0 <= off and off + a.size <= self.view.size else -1
 
 
 @dataclass
@@ -67,8 +104,9 @@ class _Slot:
 class Server:
     def __init__(self, programs: Dict[str, Program], hbm_budget: int = 120 << 30, slots: int = 4,
                  max_batch_bytes: int = 64 << 20, max_batch_inputs: int = 1024, device="cuda",
-                 return_streams: bool = False):
+                 return_streams: bool = False, arenas: Sequence[RequestArena] = ()):
         self.programs = programs
+        self.arenas = list(arenas)
         self.budget = hbm_budget
         self.max_bytes = max_batch_bytes
         self.max_inputs = max_batch_inputs
@@ -99,31 +137,61 @@ class Server:
         self.pool = ThreadPoolExecutor(max_workers=self.copy_threads)
 
     # --------------------------------------------------------------------------------------
+    def _runs(self, batch: List[Request]):
+        """The batch as contiguous runs of one arena: [(arena, first byte, bytes, first request,
+        requests)], or None when a payload lies outside every arena."""
+        runs = []
+        for i, r in enumerate(batch):
+            where = None
+            for a in self.arenas:
+                off = a.offset(r.data)
+                if off >= 0:
+                    where = (a, off)
+                    break
+            if where is None:
+                return None
+            a, off = where
+            if runs and runs[-1][0] is a and runs[-1][1] + runs[-1][2] == off:
+                run = runs[-1]
+                runs[-1] = (a, run[1], run[2] + -(-r.data.size // ALIGN) * ALIGN, run[3], run[4] + 1)
+            else:
+                runs.append((a, off, -(-r.data.size // ALIGN) * ALIGN, i, 1))
+        return runs
+
     def _launch(self, slot: _Slot, pset: str, batch: List[Request], footprint: int):
         prog = self.programs[pset]
         offs, pos = [], 0
-        host = slot.host_in.numpy()
         for r in batch:
             offs.append(pos)
             pos += -(-r.data.size // ALIGN) * ALIGN
-        # gather the requests into the pinned staging buffer, on several host threads for
-        # large batches (numpy copies release the GIL)
-        def gather(lo: int, hi: int):
-            for i in range(lo, hi):
-                d = batch[i].data
-                host[offs[i]:offs[i] + d.size] = d
-        if pos >= (8 << 20) and len(batch) > 1:
-            k = min(self.copy_threads, len(batch))
-            step = -(-len(batch) // k)
-            list(self.pool.map(lambda a: gather(a, min(len(batch), a + step)), range(0, len(batch), step)))
-        else:
-            gather(0, len(batch))
         lens = [int(r.data.size) for r in batch]
         out_offs, words, total = out_layout(lens)
         s = slot.stream
         sp = int(s.cuda_stream)
-        with torch.cuda.stream(s):
-            slot.dev_in[:pos].copy_(slot.host_in[:pos], non_blocking=True)
+        runs = self._runs(batch)
+        if runs is not None:
+            # payloads in arenas: one host-to-device copy per contiguous run
+            with torch.cuda.stream(s):
+                for a, off, span, first, _ in runs:
+                    at = offs[first]
+                    slot.dev_in[at:at + span].copy_(a.tensor[off:off + span], non_blocking=True)
+        else:
+            # gather the requests into the pinned staging buffer, on several host threads for
+            # large batches (numpy copies release the GIL), then one copy
+            host = slot.host_in.numpy()
+
+            def gather(lo: int, hi: int):
+                for i in range(lo, hi):
+                    d = batch[i].data
+                    host[offs[i]:offs[i] + d.size] = d
+            if pos >= (8 << 20) and len(batch) > 1:
+                k = min(self.copy_threads, len(batch))
+                step = -(-len(batch) // k)
+                list(self.pool.map(lambda a: gather(a, min(len(batch), a + step)), range(0, len(batch), step)))
+            else:
+                gather(0, len(batch))
+            with torch.cuda.stream(s):
+                slot.dev_in[:pos].copy_(slot.host_in[:pos], non_blocking=True)
         plan = slot.plans[pset]
         plan.set_layout(Inputs(slot.dev_in, N.BG_INPUT_BYTES, offs, lens), out_offs, total, sp)
         out_ptr = slot.dev_out.data_ptr() if slot.dev_out is not None else 0
@@ -217,8 +285,9 @@ class Server:
 
 
 def serve_plain(programs: Dict[str, Program], requests: Sequence[Request], device="cuda",
-                realtime: bool = True) -> Dict[int, Result]:
-    """One launch per request, one request at a time, in arrival order."""
+                realtime: bool = True, arenas: Sequence[RequestArena] = ()) -> Dict[int, Result]:
+    """One launch per request, one request at a time, in arrival order (payloads in `arenas`
+    are copied from there, others through a pinned staging buffer)."""
     reqs = sorted(requests, key=lambda r: r.arrival)
     results: Dict[int, Result] = {}
     stream = torch.cuda.Stream(device=device)
@@ -238,9 +307,17 @@ def serve_plain(programs: Dict[str, Program], requests: Sequence[Request], devic
             if wait > 0:
                 time.sleep(wait)
         prog = programs[r.pset]
-        host_in.numpy()[:r.data.size] = r.data
+        src = None
+        for a in arenas:
+            off = a.offset(r.data)
+            if off >= 0:
+                src = a.tensor[off:off + r.data.size]
+                break
+        if src is None:
+            host_in.numpy()[:r.data.size] = r.data
+            src = host_in[:r.data.size]
         with torch.cuda.stream(stream):
-            dev_in[:r.data.size].copy_(host_in[:r.data.size], non_blocking=True)
+            dev_in[:r.data.size].copy_(src, non_blocking=True)
         offs, words, total = out_layout([r.data.size])
         plans[r.pset].set_layout(Inputs(dev_in, N.BG_INPUT_BYTES, [0], [int(r.data.size)]), offs, total, sp)
         plans[r.pset].launch(dev_in.data_ptr(), 0, dev_counts.data_ptr(), sp)

@@ -129,9 +129,16 @@ int64_t bg_plan_tiles(const bg_plan *plan);
  * bound and the BG_ERR_TIMEOUT report can be exercised without faulting or hanging the GPU. */
 int bg_plan_set_wait_limit(bg_plan *plan, int64_t spin_limit_cycles, int64_t debug_wait_tile);
 /* Sparse output for later launches: every set bit of every output stream is also appended to
- * `positions` as (output << 52) | (input << 32) | position (unordered; limits: < 4096 outputs,
+ * `positions` as (output << 52) | (input << 32) | position (unordered; limits: < 4095 outputs,
  * < 2^20 inputs, positions < 2^32).  capacity 0 turns it off.  Entries beyond the capacity are
- * dropped and bg_plan_sync reports BG_ERR_CAPACITY (the counts stay exact). */
+ * dropped and bg_plan_sync reports BG_ERR_CAPACITY (the counts stay exact).
+ * Positions-only launches (bg_plan_launch with out_streams NULL) of a program whose parts share
+ * outputs (BG_PROGRAM_MERGES) need this call first: they count each set bit once through a
+ * set of the positions found so far, which this call allocates in the plan (twice `capacity`
+ * slots, rounded up to a power of two) and the launch clears.  `positions` may then be NULL:
+ * counts only.  Beyond twice the capacity of distinct positions, bg_plan_sync reports
+ * BG_ERR_CAPACITY and the counts are incomplete.  Such launches write no output streams: the
+ * device traffic is the input, the positions and the counts. */
 int bg_plan_set_positions(bg_plan *plan, unsigned long long *positions, int64_t capacity);
 /* Number of positions the last launch on `stream` produced (waits for the stream). */
 int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written);
@@ -144,10 +151,11 @@ int bg_plan_positions_written(bg_plan *plan, void *stream, int64_t *written);
  * timed loops.  BG_ERR_INVALID for a single-kernel program, where every tile runs every term. */
 int bg_plan_stats(bg_plan *plan, void *stream, int32_t n_parts, int64_t *tiles_run, int64_t *rows);
 /* Enqueue one scan on `stream`: input is the device base of the bytes / basis planes;
- * out_streams (may be NULL) receives n_outputs streams in the reference bit layout, positions at
- * or beyond an input's length cleared; counts (may be NULL) receives uint64 popcounts
- * [n_outputs][n_inputs] (zeroed by the call).  Only asynchronous work is enqueued, so the call
- * can be captured into a CUDA graph. */
+ * out_streams (may be NULL; see bg_plan_set_positions for programs with BG_PROGRAM_MERGES)
+ * receives n_outputs streams in the reference bit layout, positions at or beyond an input's
+ * length cleared; counts (may be NULL) receives uint64 popcounts [n_outputs][n_inputs] (zeroed
+ * by the call).  Only asynchronous work is enqueued, so the call can be captured into a CUDA
+ * graph. */
 int bg_plan_launch(bg_plan *plan, const void *input, uint32_t *out_streams,
                    unsigned long long *counts, void *stream);
 /* Wait for `stream`, then report (and clear) device-side errors of earlier launches. */

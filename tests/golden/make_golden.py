@@ -24,7 +24,11 @@ parts of the reference are what pin the oracle:
   imports the GPU runner, so only those three function definitions are taken from its source
   and executed.
 
-Usage:  python tests/golden/make_golden.py [grouping]   (``grouping``: only grouping.json)
+* ``passes.json``    - the reference's pass pipeline (``run_passes``) applied to parsed Pablo
+  under several pass flags, dumped from the live objects by ``bitgen_gb300.refir``: the IR
+  the drop-in boundary must accept (see ``passes`` below).
+
+Usage:  python tests/golden/make_golden.py [grouping|passes]   (only grouping.json / passes.json)
 """
 
 from __future__ import annotations
@@ -42,13 +46,19 @@ REF = os.environ.get("BITGEN_REF", "/root/reference")
 
 
 def import_reference():
+    import logging
+
+    class _Formatter(logging.Formatter):   # colorlog.ColoredFormatter's stand-in
+        def __init__(self, *a, **k):
+            super().__init__()
+
     os.environ.setdefault("PYTHONDONTWRITEBYTECODE", "1")
     sys.dont_write_bytecode = True
     for name in ("pandas", "colorlog", "colorama", "matplotlib", "matplotlib.pyplot"):
         m = types.ModuleType(name)
         m.Fore = types.SimpleNamespace(RED="", GREEN="", YELLOW="", BLUE="", RESET="", CYAN="")
         m.Style = types.SimpleNamespace(RESET_ALL="", BRIGHT="")
-        m.ColoredFormatter = object
+        m.ColoredFormatter = _Formatter
         sys.modules.setdefault(name, m)
     cuda = types.ModuleType("bitgen.cuda")
     cuda.byte_stream_transpose = lambda *a, **k: None
@@ -123,6 +133,13 @@ def main():
     if sys.argv[1:] == ["grouping"]:
         write_grouping()
         print("grouping.json written to", HERE)
+        return
+    if sys.argv[1:] == ["passes"]:
+        import tempfile
+        cfg = import_reference()
+        sys.path.insert(0, REPO)
+        passes(cfg, tempfile.mkdtemp(prefix="bg_golden_"))
+        print("passes.json written to", HERE)
         return
     write_grouping()
     cfg = import_reference()
@@ -228,7 +245,67 @@ def main():
     res = {k: dump(v) for k, v in parser_cases.items()}
     with open(os.path.join(HERE, "parser.json"), "w") as f:
         json.dump({"reference_ir": res, "emitted_pablo": emitted}, f, indent=1, sort_keys=True)
+    passes(cfg, tmpdir)
     print("golden vectors written to", HERE)
+
+
+def passes(cfg, tmpdir):
+    """passes.json: the instruction lists the reference's run_passes (bitgen/from_icgrep.py:
+    124-166) makes of parsed Pablo, dumped from the live objects by this project's adapter
+    (bitgen_gb300.refir._dump), under the runner's pass flags (scripts/run_bitgen.py:415-480
+    defaults) with pass_cc_advanced = 0 and short_circuit / graph_break varied.
+
+    The short-circuit pass finds no AND chain it rewrites in Pablo from this project's emitter
+    (its chain search, short_circuit.py:91-130, expects icgrep's program shape), so the case
+    "short_circuit_text" adds, in the pass's own form (BsStr, short_circuit.py:280-282 and
+    352-353), a jump over an AND chain and its label: the adapter must drop both."""
+    from bitgen import from_icgrep
+    from bitgen.bitparser.bitstream_parser import BitstreamParser
+    from bitgen.inst.inst import BsInstType
+    from bitgen.inst.inst_str import BsStr
+    from bitgen_gb300 import refir, workloads
+    from bitgen_gb300.regex import compile_group
+
+    defaults = {"pass_cc_advanced": 0, "pass_cc_advanced_max": 1, "pass_cc_advanced_merge_cc": 1,
+                "pass_short_circuit_start": 2, "pass_short_circuit_interval": 2,
+                "pass_short_circuit_interval_disable": 0, "pass_short_circuit_syncpoint": 1,
+                "pass_print_graph": 0, "pass_inst_stats": 0, "pass_inst_stats_dyn": 0}
+    for k, v in defaults.items():
+        cfg.set_config(k, v)
+    regexes = workloads.throughput_patterns(seed=3, n=8).regexes
+    programs = {}
+    for gi, g in enumerate(workloads.PatternSet(regexes, []).groups(2)):
+        path = os.path.join(tmpdir, f"passes_{gi}.pablo")
+        with open(path, "w") as f:
+            f.write(compile_group(g, matchstar=False).to_pablo())
+        programs[f"group{gi}"] = (path, g)
+    programs["xml_lexical_parsing"] = (os.path.join(REF, "bitgen/bitparser/xml_lexical_parsing.pablo"), None)
+    cases = {}
+    for pname, (path, rx) in programs.items():
+        for sc, gb in ((0, -1), (1, -1), (0, 0), (1, 0), (1, 1)):
+            cfg.set_config("pass_short_circuit", sc)
+            cfg.set_config("pass_graph_break", gb)
+            p = BitstreamParser()
+            insts = from_icgrep.run_passes(p.parse_file(path), p.var_name_map)
+            cases[f"{pname}/short_circuit={sc}/graph_break={gb}"] = {
+                "regexes": rx, "ir": [refir._dump(i, p.var_name_map) for i in insts]}
+    # the pass's jump and label around the first AND chain after the first Advance
+    cfg.set_config("pass_short_circuit", 1)
+    cfg.set_config("pass_graph_break", -1)
+    path, rx = programs["group0"]
+    p = BitstreamParser()
+    insts = from_icgrep.run_passes(p.parse_file(path), p.var_name_map)
+    first_adv = next(i for i, x in enumerate(insts) if x.type == BsInstType.ADVANCE)
+    at = next(i for i in range(first_adv, len(insts)) if insts[i].type == BsInstType.AND)
+    end = next(i for i in range(at + 1, len(insts)) if insts[i].type != BsInstType.AND)
+    var = p.var_name_map[insts[at].ret]
+    insts = (insts[:at + 1]
+             + [BsStr([f"if (block_all_zeros({var}, &zero_flag)) {{ goto LABEL0; }}"])]
+             + insts[at + 1:end] + [BsStr(["LABEL0:"])] + insts[end:])
+    cases["group0/short_circuit_text"] = {"regexes": rx,
+                                          "ir": [refir._dump(i, p.var_name_map) for i in insts]}
+    with open(os.path.join(HERE, "passes.json"), "w") as f:
+        json.dump(cases, f, separators=(",", ":"), sort_keys=True)
 
 
 if __name__ == "__main__":

@@ -1,11 +1,12 @@
-"""CPU checks of the trigram prefilter (bitgen_gb300/prefilter.py).
+"""CPU checks of the q-gram prefilter (bitgen_gb300/prefilter.py).
 
 Soundness: a term that is non-zero in a tile's exact lanes must have its bit set by the tile's
-trigram scan.  The scan is simulated here exactly as the kernel does it (every trigram lying
-wholly inside the bytes the warp computes, looked up in the exact table), and the per-regex
-streams come from the C oracle.  Terms behind an addition are excluded, since the kernel runs
-those on its own carry checks.  The Bloom bitmap must contain every key of the exact table
-(the table only removes Bloom false positives), and the table's probes must find every key.
+q-gram scan.  The scan is simulated here exactly as the kernel does it (every q-gram lying
+wholly inside the bytes the warp computes and ending at a probed position, looked up in the
+exact table), and the per-regex streams come from the C oracle.  Terms behind an addition are
+excluded, since the kernel runs those on its own carry checks.  The Bloom bitmap must contain
+every key of the exact table (the table only removes Bloom false positives), and the table's
+probes must find every key.  Every configuration (q-gram length, stride) is checked.
 """
 
 import numpy as np
@@ -17,24 +18,25 @@ from bitgen_gb300.regex import compile_group
 from oracle import cpu
 
 
-def _setup(patterns, n_groups, per_regex=True, wpt=2):
+def _setup(patterns, n_groups, per_regex=True, wpt=2, config=None):
     groups = [compile_group(g) for g in patterns.groups(n_groups)]
     dag, outs, names = build_dag(groups, per_regex)
     gen = _Gen(dag, Tuning(wpt=wpt))
     gen.analyse(outs)
     terms = [(leaf, o) for o, v in enumerate(outs) for leaf in gen.or_leaves(v)]
     pre = [v for v, _ in sorted(gen.pre.items(), key=lambda x: x[1])]
-    f = prefilter.build(gen, [v for v, _ in terms], pre)
+    f = prefilter.build(gen, [v for v, _ in terms], pre, config=config)
     return groups, gen, terms, f
 
 
 def _lookup(f, key, pre3, log2, keys, info, recs):
-    """The kernel's exact lookup (bg_device.cuh trigram_exact), over the generated tables."""
+    """The kernel's exact lookup (bg_device.cuh qgram_exact), over the generated tables."""
+    key = f.mask_key(key)
     s = prefilter.exact_hash(key, log2)
     for _ in range(len(keys)):
-        if keys[s] == 0:
+        if info[s] == 0:
             return 0
-        if keys[s] == key | (1 << 31):
+        if keys[s] == key:
             m = 0
             e = info[s]
             for i in range(e >> 8, (e >> 8) + (e & 255)):
@@ -47,25 +49,51 @@ def _lookup(f, key, pre3, log2, keys, info, recs):
     return 0
 
 
-def test_tables_are_consistent():
-    _, _, _, f = _setup(workloads.throughput_patterns(seed=3, n=64), 4)
-    assert f.enabled and f.ext
+@pytest.mark.parametrize("config", prefilter.CONFIGS)
+def test_tables_are_consistent(config):
+    _, _, _, f = _setup(workloads.throughput_patterns(seed=3, n=64), 4, config=config)
+    assert f.enabled and f.ext and (f.q, f.stride) == config
     bloom = f.bloom()
     tabs = f.exact()
     rng = np.random.default_rng(5)
     for key, m in f.table.items():
-        h = prefilter.bloom_hash(key)
+        h = prefilter.bloom_hash(key, q=f.q)
         assert (bloom[h >> 5] >> (h & 31)) & 1
+        if f.q == 3:   # the byte above a trigram does not move its Bloom bit
+            assert prefilter.bloom_hash(key | 0xAB000000, q=3) == h
         recs = f.ext.get(key, [])
         pres = [int(x) for x in rng.integers(0, 1 << 24, size=4)] + [b for b, _, _ in recs]
         for pre3 in pres:
             assert _lookup(f, key, pre3, *tabs) == f.match(key, pre3)
         assert _lookup(f, key, 0, *tabs) & m == m
-    assert _lookup(f, 0x7f7f7f, 0, *tabs) == 0 or 0x7f7f7f in f.table
+    absent = 0x7f7f7f7f & ((1 << (8 * f.q)) - 1)
+    assert _lookup(f, absent, 0, *tabs) == 0 or absent in f.table
 
 
-@pytest.mark.parametrize("wpt,kind", [(1, "throughput"), (2, "throughput"), (2, "dna")])
-def test_prefilter_is_sound(wpt, kind):
+def _probe_hits(f, text):
+    """Per position p: the bits the kernel's probe of the q-gram ending at p sets (0 where p is
+    not probed), given that the warp's bytes start at or before p - q - 2."""
+    n = text.size
+    b = text.astype(np.int64)
+    key = np.zeros(n, dtype=np.int64)
+    for i in range(f.q):
+        key[f.q - 1:] |= b[i:n - f.q + 1 + i] << (8 * i)
+    pre3 = np.zeros(n, dtype=np.int64)          # the three bytes before it, nearest first
+    for d in range(3):
+        pre3[f.q + d:] |= b[:n - f.q - d] << (8 * d)
+    probed = (np.arange(n) % f.stride) == f.stride - 1
+    probed[:f.q - 1] = False
+    hit = np.zeros(n, dtype=object)
+    cand = probed & np.isin(key, np.array(sorted(f.table), dtype=np.int64))
+    for p in np.nonzero(cand)[0]:
+        hit[p] = f.match(int(key[p]), int(pre3[p]))
+    return key, pre3, probed, hit
+
+
+@pytest.mark.parametrize("wpt,kind,config", [(1, "throughput", None), (2, "throughput", (4, 2)),
+                                             (1, "throughput", (4, 1)), (2, "throughput", (3, 1)),
+                                             (2, "dna", None)])
+def test_prefilter_is_sound(wpt, kind, config):
     """Also on IUPAC motifs over DNA text (the filter the split form would use there if forced;
     the compiler picks the single-kernel form for it)."""
     n = 300_000
@@ -75,22 +103,15 @@ def test_prefilter_is_sound(wpt, kind):
     else:
         ps = workloads.throughput_patterns(seed=3, n=64)
         text = workloads.plant(workloads.printable_text(n, 41), ps.witnesses, 700, 42)
-    groups, gen, terms, f = _setup(ps, 4, wpt=wpt)
+    groups, gen, terms, f = _setup(ps, 4, wpt=wpt, config=config)
+    if config:
+        assert (f.q, f.stride) == config
     streams, _ = cpu.run_groups(groups, text, per_regex=True)
     hl, tl = gen.hl, gen.tl
     tile_words = (32 - hl - tl) * wpt
     W = (n + 31) // 32
-    b = text.astype(np.int64)
-    tri = np.zeros(n, dtype=np.int64)
-    tri[2:] = b[:-2] | (b[1:-1] << 8) | (b[2:] << 16)   # trigram ending at each position
-    pre3 = np.zeros(n, dtype=np.int64)                 # the three bytes before it
-    pre3[3:] = b[:-3]
-    pre3[4:] |= b[:-4] << 8
-    pre3[5:] |= b[:-5] << 16
-    hit_bits = np.zeros(n, dtype=object)
-    for p in np.nonzero(np.isin(tri, np.array(sorted(f.table), dtype=np.int64)))[0]:
-        if p >= 2:
-            hit_bits[p] = f.match(int(tri[p]), int(pre3[p]))
+    key, pre3, probed, hit_bits = _probe_hits(f, text)
+    q = f.q
     has_add = [any(gen.d.nodes[a].op in ADD_OPS for a in gen.heavy_ancestors(v)) for v, _ in terms]
     by_out = {}
     for r, (v, o) in enumerate(terms):
@@ -102,11 +123,13 @@ def test_prefilter_is_sound(wpt, kind):
         lo_b = max(0, base * 32)
         hi_b = min(n, (base + 32 * wpt) * 32)
         cand = 0
-        for p in range(lo_b + 2, hi_b):
-            if p < lo_b + 5 and int(tri[p]) in f.table:
+        for p in range(lo_b + q - 1, hi_b):
+            if not probed[p]:
+                continue
+            if p < lo_b + q + 2 and f.mask_key(int(key[p])) in f.table:
                 # bytes before the warp's first byte read as zero in the kernel
-                keep = (1 << (8 * (p - 2 - lo_b))) - 1
-                cand |= f.match(int(tri[p]), int(pre3[p]) & keep)
+                keep = (1 << (8 * max(0, p - q + 1 - lo_b))) - 1
+                cand |= f.match(int(key[p]), int(pre3[p]) & keep)
             elif hit_bits[p]:
                 cand |= hit_bits[p]
         cand |= f.always_mask()
@@ -120,6 +143,17 @@ def test_prefilter_is_sound(wpt, kind):
     assert checked > 10
     # selective: on this text most tiles flag few terms
     assert sum(1 for r, z in enumerate(f.term_node) if z is None) < len(terms) // 4
+
+
+def test_cost_model_prefers_four_byte_grams_on_the_benchmark_grammar():
+    """The 256-regex workload's literals are 4-12 bytes: 4-grams, which are far rarer by chance
+    than trigrams, cover every term."""
+    _, _, terms, f = _setup(workloads.throughput_patterns(seed=3, n=256), 16, per_regex=False,
+                            wpt=1)
+    assert f.q == 4 and f.always_mask() == 0
+    tri = _setup(workloads.throughput_patterns(seed=3, n=256), 16, per_regex=False, wpt=1,
+                 config=(3, 1))[3]
+    assert f.cost < tri.cost
 
 
 def test_form_follows_expected_selectivity():
