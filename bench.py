@@ -157,17 +157,32 @@ def streams_equal(out, cpu_streams, words: int) -> bool:
         for k in range(got.shape[0]))
 
 
-def batched_leg(prog, ps, dev):
+def batched_leg(prog, gs, ps, dev):
     """4096 inputs, log-normal lengths (median 8 KiB, sigma 1, 200 B - 64 KiB): one persistent
-    CUDA-graph launch vs one launch per input, same GPU, outputs compared bit for bit."""
+    CUDA-graph launch vs one launch per input, same GPU, outputs compared bit for bit.  The
+    program's tuning is chosen by the autotuner on a sample of 512 of the inputs."""
     import numpy as np
     import torch
+    from dataclasses import asdict
     from bitgen_gb300 import workloads
+    from bitgen_gb300.autotune import autotune
     from bitgen_gb300.batched import BatchScanner, PerInputScanner
+    from bitgen_gb300.compiler import Tuning
+    from bitgen_gb300.engine import Program, pack_bytes
 
     lens = workloads.batched_lengths(4096, seed=7)
     items = workloads.batched_inputs(lens, 7, ps.witnesses)
     total = int(sum(lens))
+    space = [Tuning(), Tuning(part_cap=1), Tuning(part_cap=4, exec_groups=8)]
+    t0 = time.perf_counter()
+    best, report = autotune(gs, pack_bytes(items[:512], device=dev), space=space, use_cache=False)
+    tune_s = time.perf_counter() - t0
+    default = asdict(Tuning())
+
+    def diff(t):
+        return {k: v for k, v in t.items() if default.get(k) != v}
+    if asdict(best) != default:
+        prog = Program(gs, tuning=best)
     b = BatchScanner(prog, items, device=dev, graph=True)
     p = PerInputScanner(prog, items, device=dev)
     for _ in range(2):
@@ -189,7 +204,12 @@ def batched_leg(prog, ps, dev):
     return {"inputs": len(items), "bytes": total, "graph": True,
             "batched_GBps": round(total / tb / 1e6, 3), "plain_GBps": round(total / tp / 1e6, 3),
             "batched_ms": round(tb, 4), "plain_ms": round(tp, 4), "speedup": round(tp / tb, 2),
-            "bit_exact": exact, "median_len": int(np.median(lens))}
+            "plain_us_per_input": round(tp * 1e3 / len(items), 2),
+            "bit_exact": exact, "median_len": int(np.median(lens)),
+            "autotune": {"sample_inputs": 512, "seconds": round(tune_s, 1),
+                         "chosen": diff(asdict(best)) or "default",
+                         "candidates": [{"tuning": diff(t) or "default", "ms": ms, "error": err}
+                                        for t, ms, err in report]}}
 
 
 def positions_leg(prog, data, n, dense_out, dev, steps=10, capacity=1 << 20):
@@ -616,7 +636,7 @@ def main():
             line["positions_only"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and not args.no_modes:
         try:
-            line["batched"] = batched_leg(prog, ps, dev)
+            line["batched"] = batched_leg(prog, gs, ps, dev)
         except Exception as e:  # a failed leg is reported, it does not void the main line
             line["batched"] = {"error": f"{type(e).__name__}: {e}"[:300]}
         try:

@@ -224,19 +224,48 @@ __device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
   if (threadIdx.x == 0) work[BG_WORK_HEAD + p] = total;
 }
 
+/* work_list_block for launches of at most WARP_LIST_ROWS rows: one warp lists part p, walking
+ * the rows 32 at a time (no block-wide scan), so one block serves 32 parts. */
+constexpr int64_t WARP_LIST_ROWS = 256;
+__device__ __forceinline__ void work_list_warp(int p, const uint32_t *rowrun, const uint32_t *pmask,
+                                               int pmw, uint32_t *work, int n_parts, int64_t rows) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
+  uint32_t *out = work + BG_WORK_HEAD + n_parts + (int64_t)p * rows;
+  if (p == 0 && lane < BG_WORK_HEAD) work[lane] = 0u;
+  uint32_t pos = 0;
+  for (int64_t st = 0; st * 32 < rows; ++st) {
+    const int64_t r = st * 32 + lane;
+    uint32_t any = 0u;
+    if (r < rows)
+      for (int e = 0; e < pmw; ++e) {
+        const uint32_t m = pm[2 * e + 1];
+        if (m) any |= rowrun[(int64_t)pm[2 * e] * rows + r] & m;
+      }
+    const uint32_t b = __ballot_sync(0xffffffffu, any != 0u);
+    if ((b >> lane) & 1u) out[pos + __popc(b & ((1u << lane) - 1u))] = (uint32_t)r;
+    pos += __popc(b);
+  }
+  if (lane == 0) work[BG_WORK_HEAD + p] = pos;
+}
+
 /* The split form's row-level work between classify and execute in one launch: blocks
- * [0, n_pre) scan the pre-pass carries (one addition each), blocks [n_pre, n_pre + n_parts)
- * list the parts' rows. */
+ * [0, n_pre) scan the pre-pass carries (one addition each), the other blocks list the parts'
+ * rows: one part per block, or, for launches of few rows, one part per warp. */
 __global__ void __launch_bounds__(1024) bg_rows_kernel(uint32_t *pre_bits, int64_t n_tiles,
                                                        const int64_t *tile_prefix, int n_inputs,
                                                        int n_pre, const uint32_t *rowrun,
                                                        const uint32_t *pmask, int pmw,
                                                        uint32_t *work, int n_parts, int64_t rows) {
   asm volatile("griddepcontrol.wait;" ::: "memory"); /* classify's results */
-  if ((int)blockIdx.x < n_pre)
+  if ((int)blockIdx.x < n_pre) {
     carry_scan_block(blockIdx.x, pre_bits, n_tiles, tile_prefix, n_inputs);
-  else
+  } else if (rows <= WARP_LIST_ROWS) {
+    const int p = ((int)blockIdx.x - n_pre) * 32 + (int)(threadIdx.x >> 5);
+    if (p < n_parts) work_list_warp(p, rowrun, pmask, pmw, work, n_parts, rows);
+  } else {
     work_list_block(blockIdx.x - n_pre, rowrun, pmask, pmw, work, n_parts, rows);
+  }
 }
 
 /* 32-bit words of the split form's work list (claim counters, counts, rows per part, row
@@ -910,7 +939,8 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     cfg.stream = s;
     cfg.attrs = &pdl;
     cfg.numAttrs = 1;
-    cfg.gridDim = dim3(prog->desc.n_pre + std::max(1, prog->desc.n_parts));
+    const int n_parts = std::max(1, prog->desc.n_parts);
+    cfg.gridDim = dim3(prog->desc.n_pre + (rows <= WARP_LIST_ROWS ? (n_parts + 31) / 32 : n_parts));
     cfg.blockDim = dim3(1024);
     BG_CUDA(cudaLaunchKernelEx(&cfg, bg_rows_kernel, prm.pre_bits, prm.n_tiles,
                                (const int64_t *)prm.tile_prefix, (int)prm.n_inputs,
@@ -919,7 +949,12 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
                                                   (int64_t)prog->desc.n_parts * (1 + rows)),
                                prog->pmask, prog->pmw, prm.work,
                                (int)std::max(1, prog->desc.n_parts), (int64_t)rows));
-    cfg.gridDim = dim3((unsigned)std::max<int64_t>(1, (int64_t)sm_count() * prog->blocks_per_sm));
+    /* persistent execute blocks: every resident slot for a large launch, no more warps than
+     * tiles for a small one (its work items, (part, row) pairs, are fewer still) */
+    const int64_t warps = prog->desc.block / 32;
+    cfg.gridDim = dim3((unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((int64_t)sm_count() * prog->blocks_per_sm,
+                             (prm.n_tiles + warps - 1) / warps)));
     cfg.blockDim = dim3(prog->desc.block);
     BG_CUDA(cudaLaunchKernelExC(&cfg, (const void *)prog->kernel, args));
     return BG_OK;

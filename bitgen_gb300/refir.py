@@ -33,6 +33,7 @@ from .pablo import Group, If, Op, While
 
 _BIN = {"AND": "and", "OR": "or", "XOR": "xor"}
 _THREAD_GUARD = "idx < n_unit_basic"
+_BASIS = re.compile(r"^basis[0-7]$")
 _SHORT_JUMP = re.compile(r"^\s*if \(block_all_zeros\(\w+, &zero_flag\)\) \{ goto LABEL\d+; \}\s*$")
 _SHORT_LABEL = re.compile(r"^\s*LABEL\d+:\s*$")
 
@@ -46,7 +47,9 @@ def _convert(items, name, result_box) -> List:
         if t in ("STREAMDEFINE", "GRAPHBREAK"):
             continue
         if t == "STREAMLOAD":
-            if ops and ops[0] != "basic_stream":     # a value reloaded after a graph break
+            # a value reloaded after a graph break; the basis planes never change, so their
+            # reloads (from basic_stream or from a spill of their own) are identities
+            if ops and ops[0] != "basic_stream" and not _BASIS.match(ret or ""):
                 out.append(Op(name(ret), "assign", (name(ops[0]),)))
             continue
         if t == "STREAMSTORE":

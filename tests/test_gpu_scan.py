@@ -273,9 +273,9 @@ def test_sparse_positions_match_streams(cuda):
 
 def test_counts_only_launches_of_merging_programs(cuda):
     """A program whose parts OR into shared outputs takes its counts from the bits each part
-    adds, so a launch needs the output streams: the C ABI rejects a counts-only launch with
-    BG_ERR_INVALID, and the Python plan supplies its own streams.  Counts equal those of a
-    launch with streams and those of the oracle."""
+    adds, so a launch without output streams needs a position set: the C ABI rejects it with
+    BG_ERR_INVALID until bg_plan_set_positions sized one, and the Python plan supplies its own
+    streams.  Counts equal those of a launch with streams and those of the oracle."""
     import ctypes as C
     from bitgen_gb300 import _native as N
     ps, text, groups = small()
@@ -291,7 +291,7 @@ def test_counts_only_launches_of_merging_programs(cuda):
     plan = prog.plan(inp, b.word_offsets, b.streams.shape[1])
     rc = N.lib().bg_plan_launch(plan._h, inp.data.data_ptr(), None, b.counts.data_ptr(), None)
     assert rc == N.BG_ERR_INVALID
-    assert b"needs out_streams" in N.lib().bg_last_error()
+    assert b"merges outputs across parts" in N.lib().bg_last_error()
 
 
 def test_large_pattern_set_matches_c_oracle(cuda):
