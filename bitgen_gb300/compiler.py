@@ -346,6 +346,8 @@ class Tuning:
                                  # the q-gram filter on them (else every term runs there)
     filter_config: Optional[Tuple[int, int]] = None  # prefilter (q-gram length, stride); None:
                                                      # the cheapest by the filter's cost model
+    bulk_zero: bool = True   # split form: classify zeroes the outputs with bulk copies from
+                             # shared memory (else with vector stores of its lanes)
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
@@ -353,7 +355,7 @@ class Tuning:
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
-                self.basis_filter, self.filter_config)
+                self.basis_filter, self.filter_config, self.bulk_zero)
 
 
 @dataclass
@@ -1051,10 +1053,12 @@ PRE_CHUNK_OPEN = _CHUNK_HEAD + _TILE_LOOP
 CLS_CHUNK_OPEN = (                   # classify: PRE_CHUNK_OPEN plus the chunk's output zeroing
     _CHUNK_HEAD +
     "   const int zin = chunk_input(p, g0, g1);\n"
-    "   if (zin >= 0) { @ZERO@ }\n" + _TILE_LOOP)
+    "   if (zin >= 0) { @ZERO@ }\n"
+    "   cx.row = row;\n" + _TILE_LOOP)
 CLS_CHUNK_CLOSE = (
     "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
     "   }\n"
+    "@CHUNKEND@"
     "   if (NPRE > 0) pre_flush(p, row, gw, pw, t.lane, CT < 32);\n"
     "   flush_runs(p, row, l0, CT, runs_s, @ROWRUN@, t.lane);\n"
     "  }\n")
@@ -1431,10 +1435,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     gen.scopes = [{}]
     basis_decl = ", ".join(f"b{i}_{j} = bb[{i}].w[{j}]" for i in range(8) for j in range(wpt))
     basis_block = f"S bb[8]; basis_of(raw, bb); const uint32_t {basis_decl};"
-    for w in range(nw):
-        m = (always >> (32 * w)) & 0xFFFFFFFF
-        if m:
-            gen.emit(f"t.run[{w}] |= 0x{m:08x}u;")
+    # the terms that always run start every tile's run words (bg_always, preset by load_scan)
+    always_words = [(always >> (32 * w)) & 0xFFFFFFFF for w in range(nw)]
     # pre-pass aggregates: with a zero marker (no q-gram of it in the tile) the aggregate
     # depends on the class alone
     # additions sharing a class and carry lane have the same zero-marker aggregate: one test
@@ -1469,6 +1471,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     # additions whose marker filter fired (a few percent of tiles): out of line, one function per
     # word of 32 additions, so that the common path stays short in the instruction caches
     cand_funcs = []
+    cand_calls = []
     saved = (gen.lines, gen.indent, gen.scopes)
     pre_sorted = sorted(gen.pre.items(), key=lambda x: x[1])
     for j in range(-(-len(gen.pre) // 32)):
@@ -1481,23 +1484,33 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
             bit = nt + k
             run_bits[bit >> 5] = run_bits.get(bit >> 5, 0) | (1 << (bit & 31))
             mode = 0 if n.op == "matchstar" else 1
-            gen.open(f"(t.run[{bit >> 5}] >> {bit & 31}) & 1u")
+            gen.open(f"(run[{32 * (bit >> 5)}] >> {bit & 31}) & 1u")
             m = gen.mat(n.args[0])
             c = gen.mat(n.args[1])
             gen.emit(f"uint32_t G, P; pre_aggregate<{gen.dl[v]}, E>(t, {mode}, {gen.pack(m)}, {gen.pack(c)}, G, P); "
                      f"pg |= G << {k & 31}; pm |= 1u << {k & 31}; pv |= P << {k & 31};")
             gen.close()
         cand_funcs.append(
-            f"static __device__ __noinline__ uint3 bg_cand_{j}(const Tile &t, {_basis_params(wpt)}) {{\n"
+            f"static __device__ __noinline__ uint3 bg_cand_{j}(const Tile &t, const uint32_t *run, {_basis_params(wpt)}) {{\n"
             f"  constexpr bool E = true;\n"
             f"  uint32_t pg = 0u, pm = 0u, pv = 0u;\n" + "\n".join(gen.lines) + "\n"
             f"  return make_uint3(pg, pm, pv);\n}}\n")
-        cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(run_bits.items()))
+        # at the chunk's end, once its Bloom hits are resolved: lane i looks at tile l0 + i,
+        # and every tile where the marker filter of one of these additions fired gets their
+        # aggregates from its basis, replacing the zero-marker bits pre_collect gathered
+        cond = " | ".join(f"(runs_s[{32 * w} + l0 + t.lane] & 0x{m:08x}u)" for w, m in sorted(run_bits.items()))
         basis_names = ", ".join(f"b{i}_{jj}" for i in range(8) for jj in range(wpt))
-        saved[0].append(" " * saved[1] +
-                        f"if ({cond}) {{ {'' if basis_always else basis_block + ' '}"
-                        f"const uint3 cr = bg_cand_{j}(t, {basis_names}); "
-                        f"pg[{j}] |= cr.x; pp[{j}] = (pp[{j}] & ~cr.y) | cr.z; }}")
+        cand_calls.append(
+            f"   {{ const uint32_t cw = (t.lane < CT && row * 32 + l0 + t.lane < p.n_tiles) ? ({cond}) : 0u;\n"
+            f"     for (uint32_t todo = __ballot_sync(FULL, cw != 0u); todo; todo &= todo - 1u) {{\n"
+            f"       const int l = l0 + __ffs(todo) - 1;\n"
+            f"       setup_tile(p, t, (unsigned int)(row * 32 + l), false, false);\n"
+            f"       S bb[8]; load_basis(p, t, bb); const uint32_t {basis_decl};\n"
+            f"       const uint3 cr = bg_cand_{j}(t, runs_s + l, {basis_names});\n"
+            f"       gw[{j}] |= ((cr.x >> t.lane) & 1u) << l;\n"
+            f"       pw[{j}] = (pw[{j}] & ~(((cr.y >> t.lane) & 1u) << l)) | (((cr.z >> t.lane) & 1u) << l);\n"
+            f"     }}\n"
+            f"   }}\n")
     gen.lines, gen.indent, gen.scopes = saved
     live_needs = [(c, dl, mask & ~always) for (c, dl), mask in sorted(need_masks.items())
                   if mask & ~always]
@@ -1545,21 +1558,27 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         gen.emit(f"const uint32_t {pm} = ones_lanes(t, {gen.pack(ref)});")
     for c, dl, mask in live_needs:
         pm = pm_classes[c]
-        ors = " ".join(f"t.run[{w}] |= 0x{(mask >> (32 * w)) & 0xFFFFFFFF:08x}u;"
+        ors = " ".join(f"runs_s[{32 * w} + l] |= 0x{(mask >> (32 * w)) & 0xFFFFFFFF:08x}u;"
                        for w in range(nw) if (mask >> (32 * w)) & 0xFFFFFFFF)
-        gen.emit(f"if ((({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u) {{ {ors} }}")
+        gen.emit(f"if (t.lane == 0 && ((({pm} >> {dl}) | ({pm} >> {sl + dl})) & 1u)) {{ {ors} }}")
     if guard is not None:
         gen.close()
     if live_needs:
         gen.close()
     # run masks: kept in the warp's shared words, stored per chunk (flush_runs)
-    gen.emit("if (t.lane == 0) {" + " ".join(f"runs_s[{w * 32} + l] = t.run[{w}];" for w in range(nw)) + " }")
+    nonmerged_zero = ""
     if merge:                            # parts OR into the outputs: start every word at zero
         gen.emit(f"if (zin < 0) zero_outputs(p, t, {len(names)});   /* else zeroed per chunk */")
     else:
+        # outputs of parts that do not run on a tile are written as zeros, once the chunk's run
+        # words are complete
+        zs = []
         for ci, outs_k in enumerate(parts):
-            cond = " | ".join(f"(t.run[{w}] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
-            gen.emit(f"if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
+            cond = " | ".join(f"(runs_s[{32 * w} + l] & 0x{m:08x}u)" for w, m in sorted(part_masks[ci].items())) or "0u"
+            zs.append(f"     if (!({cond})) {{ " + " ".join(f"zero_store(p, t, {o});" for o in outs_k) + " }")
+        nonmerged_zero = ("   for (int l = l0; l < l0 + CT && row * 32 + l < p.n_tiles; ++l) {\n"
+                          "     setup_tile(p, t, (unsigned int)(row * 32 + l), false, false);\n"
+                          + "\n".join(zs) + "\n   }\n")
     cls_code = "\n".join(gen.lines)
     log2, keys, info_tab, rec_tab = filt.exact()
     # classify's shared memory: Bloom bitmap, exact table, the warps' run masks.  Programs with
@@ -1567,13 +1586,16 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     bloom_bits = tuning.bloom_bits
     cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
 
-    def cls_words(bits, block):     # up to the warps' byte buffers (16-byte aligned)
+    hit_cap = 64 * wpt                 # Bloom-hit records per warp (BG_HIT_CAP)
+    zero_bytes = 4096                  # zeros in shared memory, the bulk zeroing's source
+
+    def cls_words(bits, block):     # up to the warps' hit records (16-byte aligned)
         w = ((1 << bits) // 32 + len(keys) + len(info_tab) + 256 + len(rec_tab)
-             + (block // 32) * nw * 32)
+             + (block // 32) * nw * 32 + -(-nw // 4) * 4)
         return -(-w // 4) * 4
 
     def cls_bytes(bits, block):
-        return 4 * cls_words(bits, block) + (block // 32) * 1024 * wpt
+        return 4 * cls_words(bits, block) + (block // 32) * 8 * hit_cap + zero_bytes
 
     while cls_bytes(bloom_bits, cls_block) > 227 * 1024:
         if cls_block > 256:
@@ -1588,7 +1610,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
               f"static __device__ const __align__(16) uint32_t bg_exkeys[{len(keys)}] = {{\n{_hex_array(keys)}\n}};\n"
               f"static __device__ const __align__(16) uint32_t bg_exinfo[{len(info_tab)}] = {{\n{_hex_array(info_tab)}\n}};\n"
               f"static __device__ const uint32_t bg_exrecs[{len(rec_tab)}] = {{\n{_hex_array(rec_tab)}\n}};\n"
-              f"static __device__ const __align__(16) uint32_t bg_obl[256] = {{\n{_hex_array(obl_tab)}\n}};\n")
+              f"static __device__ const __align__(16) uint32_t bg_obl[256] = {{\n{_hex_array(obl_tab)}\n}};\n"
+              f"static __device__ const uint32_t bg_always[{nw}] = {{\n{_hex_array(always_words)}\n}};\n")
     cls_warps = cls_block // 32
     cls_smem = cls_bytes(bloom_bits, cls_block)
     cls_maxreg = max(32, min(255, 65536 // cls_block // 8 * 8))
@@ -1608,6 +1631,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *bg_obl_s = bg_exinfo_s + {len(info_tab)};        /* 256 words */\n"
         f"  uint32_t *bg_exrecs_s = bg_obl_s + 256;                     /* {len(rec_tab)} words */\n"
         f"  uint32_t *bg_runs_s = bg_exrecs_s + {len(rec_tab)};        /* {cls_warps * nw * 32} words */\n"
+        f"  uint32_t *bg_always_s = bg_runs_s + {cls_warps * nw * 32};  /* {nw} words */\n"
         f"  /* the tables, 16 bytes per load with several loads in flight (sizes are multiples of 4 words) */\n"
         f"#pragma unroll 4\n"
         f"  for (int i = threadIdx.x; i < {len(bloom) // 4}; i += blockDim.x)\n"
@@ -1617,20 +1641,36 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  for (int i = threadIdx.x; i < {len(rec_tab)}; i += blockDim.x) bg_exrecs_s[i] = bg_exrecs[i];\n"
         f"  for (int i = threadIdx.x; i < 64; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_obl_s)[i] = reinterpret_cast<const uint4 *>(bg_obl)[i];\n"
+        f"  for (int i = threadIdx.x; i < {nw}; i += blockDim.x) bg_always_s[i] = bg_always[i];\n"
         f"  for (int i = threadIdx.x; i < {len(keys) // 4}; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_exkeys_s)[i] = reinterpret_cast<const uint4 *>(bg_exkeys)[i];\n"
         f"  __syncthreads();\n"
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
-        f"  uint8_t *bytes_s = reinterpret_cast<uint8_t *>(bg_dyn_s + {cls_words(bloom_bits, cls_block)}) + (threadIdx.x >> 5) * {1024 * wpt};\n"
+        f"  ClsCtx cx;\n"
+        f"  cx.bloom = bg_bloom_s; cx.keys = bg_exkeys_s; cx.info = bg_exinfo_s; cx.recs = bg_exrecs_s;\n"
+        f"  cx.always = bg_always_s; cx.log2 = BG_EXLOG2; cx.runs_s = runs_s; cx.n_hits = 0; cx.row = 0;\n"
+        f"  cx.hits_s = reinterpret_cast<uint2 *>(bg_dyn_s + {cls_words(bloom_bits, cls_block)}) + (threadIdx.x >> 5) * BG_HIT_CAP;\n"
+        f"  /* {zero_bytes} bytes of zeros, read by the bulk copies that zero the outputs (16-byte aligned) */\n"
+        f"  uint32_t *bg_zero_s = bg_dyn_s + {cls_words(bloom_bits, cls_block) + cls_warps * 2 * hit_cap};\n"
+        f"  for (int i = threadIdx.x; i < {zero_bytes // 16}; i += blockDim.x)\n"
+        f"    reinterpret_cast<uint4 *>(bg_zero_s)[i] = make_uint4(0u, 0u, 0u, 0u);\n"
+        f"  asm volatile(\"fence.proxy.async.shared::cta;\" ::: \"memory\"); /* visible to the copy engine */\n"
+        f"  __syncthreads();\n"
+        f"  const uint32_t zsm = (uint32_t)__cvta_generic_to_shared(bg_zero_s);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
-        + CLS_CHUNK_OPEN.replace("@ZERO@", f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);" if merge else "") +
+        + CLS_CHUNK_OPEN.replace("@ZERO@", (f"zero_chunk_bulk(p, zin, g0, g1, {len(names)}, t.lane, zsm, {zero_bytes}u);"
+                                             if tuning.bulk_zero else
+                                             f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);") if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    uint32_t raw[BG_WPT][8];\n"
-        f"    load_scan(p, t, raw, bg_bloom_s, bg_exkeys_s, bg_exinfo_s, bg_exrecs_s, BG_EXLOG2, runs_s + l, bytes_s);\n"
+        f"    load_scan(p, t, raw, cx, l);\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
-        + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + BG_WORK_HEAD + {len(parts)}LL * (1 + rows)") +
+        + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + BG_WORK_HEAD + {len(parts)}LL * (1 + rows)")
+                         .replace("@CHUNKEND@", "   if (cx.n_hits) resolve_hits(p, cx, t.lane);\n"
+                                  + "".join(cand_calls) + nonmerged_zero) +
+        f"  if (t.lane == 0) bulk_wait();   /* this warp's zeroing copies are complete */\n"
         f"}}\n")
     warps_per_smsp = -(-(tuning.block // 32) * max(1, tuning.min_blocks) // 4)
     maxreg = max(32, min(255, (16384 // (warps_per_smsp * 32)) // 8 * 8))
@@ -1648,6 +1688,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_NRUN {nw}\n"
         f"#define BG_BLOOM_BITS {bloom_bits}\n"
         f"#define BG_QGRAM {filt.q}\n"
+        f"#define BG_HIT_CAP {hit_cap}\n"
         f"#define BG_STRIDE {filt.stride}\n"
         f"#define BG_PREFILTER 1\n"
         f"#define BG_BASIS_FILTER {int(tuning.basis_filter)}\n"

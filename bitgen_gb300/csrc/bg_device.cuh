@@ -898,17 +898,81 @@ struct Probes<NPROBE> {
 #ifndef BG_BASIS_FILTER
 #define BG_BASIS_FILTER 0
 #endif
-/* Load the tile's bytes into raw (lane word j = raw[j][0..7], little-endian) and fill t.run
- * from the q-gram scan (warp-uniform).  Inputs given as basis planes: the bytes are rebuilt
- * from the planes (bytes at or beyond the input's length are the planes' padding there), and
- * every term runs, or, with BG_BASIS_FILTER, the rebuilt bytes are scanned the same way (the
- * padding can only add hits).  The basis planes of the bytes, where a caller needs them, come
- * from basis_of. */
+#ifndef BG_HIT_CAP
+#define BG_HIT_CAP 64 /* Bloom-hit records a warp holds before resolving them */
+#endif
+
+/* A classify warp's state for one chunk of tiles (row `row`, tiles row * 32 + l): the filter
+ * tables in shared memory, the chunk's run words (runs_s[w * 32 + l]: word w of tile l) and the
+ * Bloom hits not yet looked up (hits_s, n_hits records).  A record is (tile l << 16 | lane word,
+ * probe mask): the probes of that lane word whose Bloom bit was set. */
+struct ClsCtx {
+  const uint32_t *bloom, *keys, *info, *recs, *always;
+  int log2;
+  uint32_t *runs_s;
+  uint2 *hits_s;
+  uint32_t n_hits;
+  long long row;
+};
+
+/* Byte `pos` of input `in` as the classify probes saw it: zero before the input, at or beyond
+ * its end, and before the first byte `lo` of the warp that probed it. */
+__device__ __forceinline__ uint32_t probe_byte(const BgParams &p, int in, long long n, long long lo,
+                                               long long pos) {
+  if (pos < lo || pos < 0 || pos >= n) return 0u;
+  if (p.input_kind == BG_INPUT_BYTES) return __ldg(p.in_bytes + p.in_off[in] + pos);
+  const uint32_t *src = p.in_basis + p.in_off[in] + (pos >> 5);
+  const int sh = 31 - (int)(pos & 31);
+  uint32_t b = 0u;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) b |= ((__ldg(src + i * p.basis_stride) >> sh) & 1u) << (7 - i);
+  return b;
+}
+
+/* Look up every recorded Bloom hit of the chunk, one record per lane (so a warp resolves up to
+ * 32 hits in the time of one): the q-gram ending at the probed byte and the three bytes before
+ * it, read again from the input, go through the exact table, whose records set run bits of the
+ * hit's tile in runs_s.  Clears the records. */
+__device__ __noinline__ void resolve_hits(const BgParams &p, ClsCtx &c, int lane) {
+  __syncwarp();
+  for (uint32_t i = lane; i < c.n_hits; i += 32) {
+    const uint2 rec = c.hits_s[i];
+    const int l = (int)(rec.x >> 16), lw = (int)(rec.x & 0xffffu);
+    const long long g = c.row * 32 + l;
+    int lo = 0, hi = p.n_inputs; /* the tile's input */
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (p.tile_prefix[mid] <= g) lo = mid; else hi = mid;
+    }
+    const long long n = p.in_len[lo];
+    const long long wbase = (g - p.tile_prefix[lo]) * SW - (long long)HL * WPT; /* warp's first word */
+    for (uint32_t m = rec.y; m; m &= m - 1u) {
+      const int k = __ffs(m) - 1 - (32 - NPROBE);
+      const long long e = 32 * (wbase + lw) + QS * k + QS - 1; /* byte position in the input */
+      uint32_t v[7];
+#pragma unroll
+      for (int d = 0; d < 7; ++d) v[d] = probe_byte(p, lo, n, 32 * wbase, e - d);
+      const uint32_t key = QG == 4 ? (v[3] | v[2] << 8 | v[1] << 16 | v[0] << 24)
+                                   : (v[2] | v[1] << 8 | v[0] << 16);
+      const uint32_t pre3 = QG == 4 ? (v[4] | v[5] << 8 | v[6] << 16)
+                                    : (v[3] | v[4] << 8 | v[5] << 16);
+      qgram_exact(key, pre3, c.keys, c.info, c.recs, c.log2, c.runs_s + l);
+    }
+  }
+  __syncwarp();
+  c.n_hits = 0;
+}
+
+/* Load tile l's bytes into raw (lane word j = raw[j][0..7], little-endian), start its run words
+ * in runs_s with the bits of the terms that always run, probe the q-grams and record the Bloom
+ * hits (looked up later, by resolve_hits, for the whole chunk).  Inputs given as basis planes:
+ * the bytes are rebuilt from the planes (bytes at or beyond the input's length are the planes'
+ * padding there), and every term runs, or, with BG_BASIS_FILTER, the rebuilt bytes are
+ * scanned the same way (the padding can only add hits).  The basis planes of the bytes, where
+ * a caller needs them, come from basis_of. */
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t raw[WPT][8],
-                                          const uint32_t *bloom, const uint32_t *keys,
-                                          const uint32_t *info, const uint32_t *recs, int log2,
-                                          uint32_t *run, uint8_t *bytes_s) {
-  /* run: the tile's run words in shared memory (word w at run[32 w]); hits OR into them */
+                                          ClsCtx &c, int l) {
+  uint32_t *run = c.runs_s + l;
   if (p.input_kind == BG_INPUT_BASIS) {
     S b[8];
     load_basis(p, t, b);
@@ -920,18 +984,14 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t r
       untranspose32(o, raw[j]);
     }
     if (!BG_BASIS_FILTER) {
-#pragma unroll
-      for (int w = 0; w < BG_NRUN; ++w) t.run[w] = FULL;
+      if (t.lane < BG_NRUN) run[32 * t.lane] = FULL;
       return;
     }
   } else {
 #pragma unroll
     for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
   }
-  if (t.lane == 0) {
-#pragma unroll
-    for (int w = 0; w < BG_NRUN; ++w) run[32 * w] = 0u;
-  }
+  if (t.lane < BG_NRUN) run[32 * t.lane] = c.always[t.lane];
   uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
   if (t.lane == 0) prev = 0u;
   constexpr uint32_t KEEP = NPROBE == 32 ? FULL : ~((1u << (32 - NPROBE)) - 1u);
@@ -939,40 +999,21 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t r
   uint32_t any = 0u;
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
-    hits[j] = Probes<0>::run(raw[j], prev, bloom, 0u) & KEEP;
+    hits[j] = Probes<0>::run(raw[j], prev, c.bloom, 0u) & KEEP;
     any |= hits[j];
     prev = raw[j][7];
   }
   if (__any_sync(FULL, any != 0u)) {
-    /* the rare Bloom hits: the warp's bytes go to shared memory; then the q-gram ending at
-     * byte e of the warp's bytes and the three bytes before it (bytes before the warp's first
-     * byte read as zero) are looked up, from one call site */
+    if (c.n_hits + 32 * WPT > BG_HIT_CAP) resolve_hits(p, c, t.lane);
 #pragma unroll
     for (int j = 0; j < WPT; ++j) {
-      uint4 *d = reinterpret_cast<uint4 *>(bytes_s + 32 * (t.lane * WPT + j));
-      d[0] = make_uint4(raw[j][0], raw[j][1], raw[j][2], raw[j][3]);
-      d[1] = make_uint4(raw[j][4], raw[j][5], raw[j][6], raw[j][7]);
-    }
-    __syncwarp();
-#pragma unroll
-    for (int j = 0; j < WPT; ++j) {
-      for (uint32_t m = hits[j]; m; m &= m - 1u) {
-        const int k = __ffs(m) - 1 - (32 - NPROBE);
-        const int e = 32 * (t.lane * WPT + j) + QS * k + QS - 1;
-        uint32_t v[7];
-#pragma unroll
-        for (int d = 0; d < 7; ++d) v[d] = e - d >= 0 ? bytes_s[e - d] : 0u;
-        const uint32_t key = QG == 4 ? (v[3] | v[2] << 8 | v[1] << 16 | v[0] << 24)
-                                     : (v[2] | v[1] << 8 | v[0] << 16);
-        const uint32_t pre3 = QG == 4 ? (v[4] | v[5] << 8 | v[6] << 16)
-                                      : (v[3] | v[4] << 8 | v[5] << 16);
-        qgram_exact(key, pre3, keys, info, recs, log2, run);
-      }
+      const uint32_t hb = __ballot_sync(FULL, hits[j] != 0u);
+      if (hits[j])
+        c.hits_s[c.n_hits + __popc(hb & ((1u << t.lane) - 1u))] =
+            make_uint2(((uint32_t)l << 16) | (uint32_t)(t.lane * WPT + j), hits[j]);
+      c.n_hits += __popc(hb);
     }
   }
-  __syncwarp();
-#pragma unroll
-  for (int w = 0; w < BG_NRUN; ++w) t.run[w] = run[32 * w];
 }
 
 /* The basis planes of the tile's bytes (as load_basis gives them). */
@@ -1199,6 +1240,53 @@ __device__ __forceinline__ void zero_span(uint32_t *dst, long long lo, long long
   for (long long i = lane; i < nv; i += 32) v[i] = make_uint4(0u, 0u, 0u, 0u);
   const long long tail = head + 4 * nv;
   if (tail + lane < hi) dst[tail + lane] = 0u;
+}
+
+/* Zero words [lo, hi) of dst with bulk copies from `zbytes` bytes of zeros in shared memory
+ * (shared-memory address zsm): the lanes store the few words up to a 16-byte boundary and after
+ * the last one, lane 0 has the copy engine write the 16-byte aligned middle (cp.async.bulk:
+ * both addresses 16-byte aligned, sizes multiples of 16), without load-store instructions of
+ * its own.  The copies are committed as one bulk group; the kernel waits for its groups
+ * (bulk_wait) before it exits. */
+__device__ __forceinline__ void bulk_zero_span(uint32_t *dst, long long lo, long long hi, int lane,
+                                               uint32_t zsm, uint32_t zbytes) {
+  if (hi <= lo) return;
+  const unsigned mis = (unsigned)(((16u - ((unsigned)(unsigned long long)(dst + lo) & 15u)) & 15u) >> 2);
+  const long long head = lo + mis < hi ? lo + mis : hi;
+  if (lo + lane < head) dst[lo + lane] = 0u;
+  const long long nv = (hi - head) >> 2; /* 16-byte units */
+  const long long tail = head + 4 * nv;
+  if (tail + lane < hi) dst[tail + lane] = 0u;
+  if (lane == 0 && nv > 0) {
+    unsigned long long g = (unsigned long long)(dst + head);
+    long long bytes = nv * 16;
+    while (bytes > 0) {
+      const uint32_t b = bytes < (long long)zbytes ? (uint32_t)bytes : zbytes;
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                   ::"l"(g), "r"(zsm), "r"(b) : "memory");
+      g += b;
+      bytes -= b;
+    }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  }
+}
+
+/* Wait until this thread's bulk copies are complete. */
+__device__ __forceinline__ void bulk_wait() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+/* Split form with merged outputs, classify: zero the words of outputs 0..n-1 that tiles
+ * g0 .. g1-1 of input `in` write, with bulk copies of zeros (bulk_zero_span). */
+__device__ __forceinline__ void zero_chunk_bulk(const BgParams &p, int in, long long g0, long long g1,
+                                                int n, int lane, uint32_t zsm, uint32_t zbytes) {
+  if (!p.out) return;
+  const long long first = p.tile_prefix[in];
+  const long long W = (p.in_len[in] + 31) >> 5;
+  long long lo = (g0 - first) * SW, hi = (g1 - first) * SW;
+  if (hi > W) hi = W;
+  uint32_t *dst = p.out + p.out_off[in];
+  for (int o = 0; o < n; ++o, dst += p.out_stride) bulk_zero_span(dst, lo, hi, lane, zsm, zbytes);
 }
 
 /* Split form with merged outputs, classify: zero the words of outputs 0..n-1 that tiles
