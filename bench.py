@@ -264,6 +264,61 @@ def positions_leg(prog, data, n, dense_out, dev, steps=10, capacity=1 << 20):
                          "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg}}
 
 
+def basis_hook_leg(gs, data, n, dense_out, dev, steps=10):
+    """The reference runner's hook on the headline input: kernels/kernel_0.py written by
+    write_kernel_module, imported the way from_icgrep.init_kernel does (bitgen/from_icgrep.py:
+    169-193), its init_kernel(...)[3] = run_fn called on the basis planes the transpose hook
+    made (bitgen/bitstream.py:166-225), as run_regex_kernel calls it (from_icgrep.py:575-582):
+    one synchronous call per step.  The planes carry no bytes, so the classify pass rebuilds
+    them for the q-gram filter.  Algorithmic bytes per call: the 8 planes (n bytes) plus each
+    group's result stream.  The result must equal the headline launch's output streams."""
+    import importlib
+    import shutil
+    import tempfile
+    import torch
+    from bitgen_gb300.backend import byte_stream_transpose, write_kernel_module
+
+    npad = -(-n // 32) * 32
+    bytestream = torch.zeros((1, 1, npad), dtype=torch.uint8, device=dev)
+    bytestream[0, 0, :n].copy_(data)
+    basis = torch.zeros((1, 1, 8, npad // 32), dtype=torch.uint32, device=dev)
+    byte_stream_transpose(bytestream, basis)
+    tmp = tempfile.mkdtemp(prefix="bg_hook_")
+    try:
+        write_kernel_module(gs, tmp)
+        sys.path.insert(0, tmp)
+        sys.modules.pop("kernels", None)
+        sys.modules.pop("kernels.kernel_0", None)
+        kmod = importlib.import_module("kernels.kernel_0")
+        result, _, handle, run_fn, _ = kmod.init_kernel(len(gs), bytestream, basis, {})
+    finally:
+        if tmp in sys.path:
+            sys.path.remove(tmp)
+        shutil.rmtree(tmp, ignore_errors=True)
+    for _ in range(3):
+        run_fn(basis)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        run_fn(basis)
+    e1.record(s)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    W = npad // 32
+    exact = bool(torch.equal(result[0, 0].view(torch.int32)[:, :W],
+                             dense_out[:, :W].view(torch.int32)))
+    handle.free()
+    peak, peak_kind = peaks()
+    b_alg = n + len(gs) * W * 4
+    return {"GBps": round(n / ms / 1e6, 3), "ms": round(ms, 4), "steps": steps,
+            "call": "kernels/kernel_0.init_kernel(...)[3](basis), synchronous",
+            "bit_exact_vs_byte_launch": exact,
+            "roofline": {"bound": "hbm", "achieved": round(b_alg / ms / 1e6, 2), "peak": peak,
+                         "unit": "GB/s", "frac": round(b_alg / ms / 1e6 / peak, 4),
+                         "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg}}
+
+
 def transpose_leg(dev, n_bytes=1 << 30, reps=20, check_bytes=1 << 20, cpu_bytes=4 << 20):
     """The stand-alone transpose (the reference's byte_stream_transpose, kernel.cu:102-124):
     uint8 [1, 1, n] -> uint32 [1, 1, 8, n/32] on the device, 2n bytes of HBM traffic per call;
@@ -634,6 +689,11 @@ def main():
             line["positions_only"] = positions_leg(prog, data, n, out, dev)
         except Exception as e:
             line["positions_only"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if rank == 0 and n % 32 == 0:
+        try:
+            line["basis_hook"] = basis_hook_leg(gs, data, n, out, dev)
+        except Exception as e:
+            line["basis_hook"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     if rank == 0 and not args.no_modes:
         try:
             line["batched"] = batched_leg(prog, gs, ps, dev)

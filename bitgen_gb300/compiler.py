@@ -333,16 +333,16 @@ class Tuning:
     cls_block: int = 1024    # split form: threads per classify block (one block per SM holds
                              # the Bloom bitmap, the exact keys and the warps' run masks)
     prefilter_limit: float = 0.25  # prefilter only while a tile is expected to run fewer than
-                                   # this fraction of the terms and to take fewer than 32 times
-                                   # this many slow-path filter hits per 1024 bytes (text taken
-                                   # as uniform over the bytes the filters name); >= 1: always
+                                   # this fraction of the terms and to take fewer than 8 times
+                                   # this many Bloom hits per 1024 bytes (text taken as uniform
+                                   # over the bytes the filters name); >= 1: always
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
     inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
     single_wpt: int = 2      # words per lane (and blocks per SM below) when the compiler falls
     single_min_blocks: int = 3   # back to the single-kernel form because the filters are
                                  # unselective (0: keep wpt / min_blocks)
-    basis_filter: bool = False   # split form: rebuild the bytes of basis-plane inputs and run
+    basis_filter: bool = True    # split form: rebuild the bytes of basis-plane inputs and run
                                  # the q-gram filter on them (else every term runs there)
     filter_config: Optional[Tuple[int, int]] = None  # prefilter (q-gram length, stride); None:
                                                      # the cheapest by the filter's cost model
@@ -1137,7 +1137,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         lim = tuning.prefilter_limit
         if not filt.enabled or (lim < 1.0 and (
                 filt.expected_per_tile(positions) > lim * len(terms)
-                or filt.hits * 1024 / positions > lim * 32)):
+                or filt.hits * 1024 / positions > lim * 8)):
             # the filter would pass most terms: single-kernel form, with its own tile shape
             # (programs whose terms have no filter at all keep the requested shape)
             # (the terms run on every tile and mostly stay non-zero for several steps, so
@@ -1586,7 +1586,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     bloom_bits = tuning.bloom_bits
     cls_block = max(32, min(1024, tuning.cls_block // 32 * 32))
 
-    hit_cap = 64 * wpt                 # Bloom-hit records per warp (BG_HIT_CAP)
+    hit_cap = 128 * wpt                # Bloom-hit records per warp (BG_HIT_CAP)
     zero_bytes = 4096                  # zeros in shared memory, the bulk zeroing's source
 
     def cls_words(bits, block):     # up to the warps' hit records (16-byte aligned)

@@ -829,7 +829,7 @@ constexpr uint32_t BLOOM_HASH = 0x9E3779B1u, EXACT_HASH = 0x85EBCA6Bu;
  * recs[2i] = bytes | n << 24 and recs[2i + 1] = the bit it sets when the n nearest bytes of
  * pre3 equal `bytes` (n = 0: always).  Bit b goes to run[(b / 32) * 32] (the tile's run words
  * in the warp's shared memory, 32 words apart). */
-static __device__ __noinline__ void qgram_exact(uint32_t key, uint32_t pre3, const uint32_t *keys,
+static __device__ __forceinline__ void qgram_exact(uint32_t key, uint32_t pre3, const uint32_t *keys,
                                                 const uint32_t *info, const uint32_t *recs,
                                                 int log2, uint32_t *run) {
   const uint32_t slots = 1u << log2;
@@ -899,7 +899,7 @@ struct Probes<NPROBE> {
 #define BG_BASIS_FILTER 0
 #endif
 #ifndef BG_HIT_CAP
-#define BG_HIT_CAP 64 /* Bloom-hit records a warp holds before resolving them */
+#define BG_HIT_CAP 128 /* Bloom-hit records a warp holds per chunk */
 #endif
 
 /* A classify warp's state for one chunk of tiles (row `row`, tiles row * 32 + l): the filter
@@ -933,7 +933,7 @@ __device__ __forceinline__ uint32_t probe_byte(const BgParams &p, int in, long l
  * 32 hits in the time of one): the q-gram ending at the probed byte and the three bytes before
  * it, read again from the input, go through the exact table, whose records set run bits of the
  * hit's tile in runs_s.  Clears the records. */
-__device__ __noinline__ void resolve_hits(const BgParams &p, ClsCtx &c, int lane) {
+__device__ __forceinline__ void resolve_hits(const BgParams &p, ClsCtx &c, int lane) {
   __syncwarp();
   for (uint32_t i = lane; i < c.n_hits; i += 32) {
     const uint2 rec = c.hits_s[i];
@@ -1004,7 +1004,18 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t r
     prev = raw[j][7];
   }
   if (__any_sync(FULL, any != 0u)) {
-    if (c.n_hits + 32 * WPT > BG_HIT_CAP) resolve_hits(p, c, t.lane);
+    uint32_t n = c.n_hits;
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      const uint32_t hb = __ballot_sync(FULL, hits[j] != 0u);
+      n += __popc(hb);
+    }
+    if (n > BG_HIT_CAP) {
+      /* more hits than the chunk's record buffer holds (text dense in filter keys): every
+       * term runs on this tile, which is exact, and its hits need no lookup */
+      if (t.lane < BG_NRUN) run[32 * t.lane] = FULL;
+      return;
+    }
 #pragma unroll
     for (int j = 0; j < WPT; ++j) {
       const uint32_t hb = __ballot_sync(FULL, hits[j] != 0u);

@@ -358,3 +358,22 @@ def test_work_counters(cuda):
     single = Program(groups, tuning=Tuning(prefilter=False))
     assert single.spec.n_parts == 0
     assert single.scan(inp, stats=True).stats == {"form": "single-kernel", "tiles": single.tiles_for([data.size])}
+
+
+@pytest.mark.parametrize("every", [37, 400])
+def test_text_dense_in_filter_keys(cuda, every):
+    """Witnesses planted every `every` bytes put dozens of Bloom hits into each chunk of 32
+    tiles; past the warp's record buffer a tile runs every term instead of looking its hits up.
+    The split form is forced; streams equal the C oracle's."""
+    from oracle import cpu
+    ps = workloads.throughput_patterns(seed=3, n=64)
+    groups = [compile_group(g) for g in ps.groups(4)]
+    text = workloads.plant(workloads.printable_text(600_000, 61), ps.witnesses, every, 62)
+    prog = Program(groups, tuning=Tuning(prefilter_limit=2.0))
+    assert prog.spec.n_parts > 0
+    res = prog.scan(pack_bytes([text]))
+    want, counts = cpu.run_groups(groups, text)
+    W = (text.size + 31) // 32
+    for k, w in enumerate(want):
+        assert first_diff(res.stream(k, 0).cpu().numpy(), w[:W]) is None, k
+    assert res.counts[:, 0].tolist() == counts

@@ -68,27 +68,39 @@ def test_dyn_stats_single_kernel_program(cuda):
     assert init_kernel(len(groups), bytestream, basis, _Config(), groups=groups)[4] is None
 
 
-def test_dyn_stats_split_program(cuda):
+@pytest.mark.parametrize("basis_filter", [True, False])
+def test_dyn_stats_split_program(cuda, basis_filter):
     """64 regexes over printable text compile to the split form: per part the tiles it ran on
-    and the rows of its work list, the same on every run.  The hook scans basis planes, which
-    carry no bytes for the trigram filter, so every part runs on every tile and lists every row
-    (the byte-input path, where the filter skips tiles, is covered by the scan tests)."""
+    and the rows of its work list, the same on every run.  The hook scans basis planes: by
+    default the classify pass rebuilds their bytes and runs the q-gram filter, so parts run on
+    few tiles; with Tuning(basis_filter=False) every part runs on every tile and lists every
+    row.  The streams equal the oracle's either way."""
+    from bitgen_gb300.compiler import Tuning
+    from oracle.pablo_ref import int_to_words, run_group
     ps = workloads.throughput_patterns(seed=91, n=64)
     groups = [compile_group(g) for g in ps.groups(4)]
     data = workloads.plant(workloads.printable_text(200_000, 94), ps.witnesses, 4096, 95)
     bytestream, basis, npad = _basis(data, cuda)
     result, tmp, handle, run_fn, dyn = init_kernel(len(groups), bytestream, basis,
-                                                   {"pass_inst_stats_dyn": True}, groups=groups)
+                                                   {"pass_inst_stats_dyn": True}, groups=groups,
+                                                   tuning=Tuning(basis_filter=basis_filter))
     prog = handle.program
     assert prog.fused and prog.spec.n_parts > 0
     assert tuple(dyn.shape) == (1, 1, prog.spec.n_parts, 2)
     run_fn(basis)
     torch.cuda.synchronize()
-    assert int(np.unpackbits(result.cpu().numpy().view(np.uint8)).sum()) > 0
+    padded = np.concatenate([data, np.zeros(npad - data.size, np.uint8)])
+    for g, grp in enumerate(groups):
+        want = int_to_words(run_group(grp, padded), npad // 32)
+        assert np.array_equal(result[0, 0, g].cpu().numpy().view(np.uint32), want), g
     tiles = prog.tiles_for([npad])
     runs, rows = dyn[0, 0, :, 0].tolist(), dyn[0, 0, :, 1].tolist()
-    assert runs == [tiles] * prog.spec.n_parts
-    assert rows == [-(-tiles // 32)] * prog.spec.n_parts
+    if basis_filter:
+        assert all(0 <= r <= tiles for r in runs) and sum(runs) < prog.spec.n_parts * tiles // 4
+        assert all(0 <= r <= -(-tiles // 32) for r in rows)
+    else:
+        assert runs == [tiles] * prog.spec.n_parts
+        assert rows == [-(-tiles // 32)] * prog.spec.n_parts
     red = _reference_reductions(dyn)
     assert red[0] == sum(runs) and red[1] == sum(rows) and red[2] >= 1.0
     first = dyn.clone()
