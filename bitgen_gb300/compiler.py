@@ -321,7 +321,7 @@ class Tuning:
     part_cap: int = 0       # most OR-ed terms one part function computes (0: 2 in the split
                             # form, 64 in the single-kernel form)
     window: int = 2         # guard blocks kept pending (instruction-level parallelism vs registers)
-    min_blocks: int = 4     # __launch_bounds__ minimum resident blocks per SM (caps registers)
+    min_blocks: int = 3     # __launch_bounds__ minimum resident blocks per SM (caps registers)
     edge_variants: bool = False  # separate unmasked part code for tiles away from input ends
     inline_lookback: bool = False  # look-back code inlined at each addition (else one shared function)
     lockstep: bool = False  # warps of a block run each part together (barrier between parts)
@@ -338,6 +338,7 @@ class Tuning:
                                    # over the bytes the filters name); >= 1: always
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
+    exec_claim: int = 2      # split form: work items an execute warp claims at once
     inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
     single_wpt: int = 2      # words per lane (and blocks per SM below) when the compiler falls
     single_min_blocks: int = 3   # back to the single-kernel form because the filters are
@@ -355,7 +356,7 @@ class Tuning:
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
-                self.basis_filter, self.filter_config, self.bulk_zero)
+                self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim)
 
 
 @dataclass
@@ -1054,7 +1055,9 @@ CLS_CHUNK_OPEN = (                   # classify: PRE_CHUNK_OPEN plus the chunk's
     _CHUNK_HEAD +
     "   const int zin = chunk_input(p, g0, g1);\n"
     "   if (zin >= 0) { @ZERO@ }\n"
-    "   cx.row = row;\n" + _TILE_LOOP)
+    "   cx.row = row;\n"
+    "   bool pf = false;\n"
+    "   uint32_t nraw[BG_WPT][8];\n" + _TILE_LOOP)
 CLS_CHUNK_CLOSE = (
     "    if (NPRE > 0) pre_collect(pg, pp, gw, pw, l, t.lane);\n"
     "   }\n"
@@ -1664,7 +1667,20 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
                                              f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);") if merge else "") +
         f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    uint32_t raw[BG_WPT][8];\n"
-        f"    load_scan(p, t, raw, cx, l);\n"
+        f"    const bool have = pf;\n"
+        f"    if (have) {{\n"
+        f"#pragma unroll\n"
+        f"      for (int j = 0; j < BG_WPT; ++j)\n"
+        f"#pragma unroll\n"
+        f"        for (int q = 0; q < 8; ++q) raw[j][q] = nraw[j][q];\n"
+        f"    }}\n"
+        f"    /* the next tile's bytes, loaded while this one is scanned (same input: consecutive) */\n"
+        f"    pf = zin >= 0 && p.input_kind == BG_INPUT_BYTES && l + 1 < l0 + CT && g + 1 < p.n_tiles;\n"
+        f"    if (pf) {{\n"
+        f"#pragma unroll\n"
+        f"      for (int j = 0; j < BG_WPT; ++j) load_word_bytes_ahead(p, t, SW, j, nraw[j]);\n"
+        f"    }}\n"
+        f"    load_scan(p, t, raw, cx, l, have);\n"
         f"    constexpr bool E = true;\n"
         f"{cls_code}\n"
         + CLS_CHUNK_CLOSE.replace("@ROWRUN@", f"p.work + BG_WORK_HEAD + {len(parts)}LL * (1 + rows)")
@@ -1731,37 +1747,57 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  unsigned int smid;\n"
         f"  asm(\"mov.u32 %0, %%smid;\" : \"=r\"(smid));\n"
         f"  int grp = (int)(smid % {ngroups}u), tried = 0;\n"
+        f"  /* a warp claims {tuning.exec_claim} consecutive items at once and loads their work-list entries and run\n"
+        f"     words together, so that those loads overlap; it then runs them in order (same part:\n"
+        f"     rows increasing) */\n"
         f"  for (;;) {{\n"
         f"    const unsigned int gb = bg_pref[bg_gpos[grp]], ge = bg_pref[bg_gpos[grp + 1]];\n"
-        f"    unsigned int it = 0u;\n"
+        f"    unsigned int it0 = 0u;\n"
         f"    if (t.lane == 0)\n"
-        f"      it = gb < ge && !((*(volatile unsigned int *)&bg_spent >> grp) & 1u) ? gb + atomicAdd(p.work + grp, 1u) : ge;\n"
-        f"    it = __shfl_sync(FULL, it, 0);\n"
-        f"    if (it >= ge) {{\n"
+        f"      it0 = gb < ge && !((*(volatile unsigned int *)&bg_spent >> grp) & 1u) ? gb + atomicAdd(p.work + grp, {tuning.exec_claim}u) : ge;\n"
+        f"    it0 = __shfl_sync(FULL, it0, 0);\n"
+        f"    if (it0 >= ge) {{\n"
         f"      if (t.lane == 0) atomicOr(&bg_spent, 1u << grp);\n"
         f"      if (++tried >= {ngroups}) break;\n"
         f"      grp = grp + 1 < {ngroups} ? grp + 1 : 0;\n"
         f"      continue;\n"
         f"    }}\n"
-        f"    int j = bg_gpos[grp], hi = bg_gpos[grp + 1];\n"
-        f"    while (hi - j > 1) {{ const int m = (j + hi) >> 1; if (bg_pref[m] <= it) j = m; else hi = m; }}\n"
-        f"    const int k = bg_ord[j];\n"
-        f"    const long long g0 = (long long)__ldg(p.work + BG_WORK_HEAD + {len(parts)} + (long long)k * rows + (it - bg_pref[j])) * 32;\n"
-        f"    const long long g = g0 + t.lane;\n"
-        f"    /* each lane loads its tile's run words of the part */\n"
-        f"    uint32_t want = 0u;\n"
-        f"    uint32_t {', '.join(f'rw{i} = 0u' for i in range(pmw))};\n"
-        + "".join(f"    {{ const uint32_t w = bg_pm_s[(k * {pmw} + {i}) * 2], m = bg_pm_s[(k * {pmw} + {i}) * 2 + 1];\n"
-                  f"      if (m && g < p.n_tiles) rw{i} = p.runs[(long long)w * p.n_tiles + g];\n"
-                  f"      want |= rw{i} & m; }}\n" for i in range(pmw)) +
-        f"    uint32_t sel = __ballot_sync(FULL, want != 0u);\n"
-        f"    while (sel) {{\n"
-        f"      const int l = __ffs(sel) - 1;\n"
-        f"      sel &= sel - 1u;\n"
-        f"      setup_tile(p, t, (unsigned int)(g0 + l), true, false);\n"
-        f"      S b[8];\n"
-        f"      load_basis(p, t, b);\n"
+        f"    int kq[{tuning.exec_claim}];\n"
+        f"    long long g0q[{tuning.exec_claim}];\n"
+        f"    uint32_t wantq[{tuning.exec_claim}];\n"
+        + "".join(f"    uint32_t rwq{i}[{tuning.exec_claim}];\n" for i in range(pmw)) +
+        f"#pragma unroll\n"
+        f"    for (int q = 0; q < {tuning.exec_claim}; ++q) {{\n"
+        f"      const unsigned int it = it0 + q;\n"
+        f"      kq[q] = -1; g0q[q] = 0; wantq[q] = 0u;\n"
+        + "".join(f"      rwq{i}[q] = 0u;\n" for i in range(pmw)) +
+        f"      if (it < ge) {{\n"
+        f"        int j = bg_gpos[grp], hi = bg_gpos[grp + 1];\n"
+        f"        while (hi - j > 1) {{ const int m = (j + hi) >> 1; if (bg_pref[m] <= it) j = m; else hi = m; }}\n"
+        f"        const int k = bg_ord[j];\n"
+        f"        kq[q] = k;\n"
+        f"        g0q[q] = (long long)__ldg(p.work + BG_WORK_HEAD + {len(parts)} + (long long)k * rows + (it - bg_pref[j])) * 32;\n"
+        f"        const long long g = g0q[q] + t.lane;\n"
+        f"        /* each lane loads its tile's run words of the part */\n"
+        + "".join(f"        {{ const uint32_t w = bg_pm_s[(k * {pmw} + {i}) * 2], m = bg_pm_s[(k * {pmw} + {i}) * 2 + 1];\n"
+                  f"          if (m && g < p.n_tiles) rwq{i}[q] = p.runs[(long long)w * p.n_tiles + g];\n"
+                  f"          wantq[q] |= rwq{i}[q] & m; }}\n" for i in range(pmw)) +
+        f"      }}\n"
+        f"    }}\n"
+        f"#pragma unroll\n"
+        f"    for (int q = 0; q < {tuning.exec_claim}; ++q) {{\n"
+        f"      const int k = kq[q];\n"
+        f"      const long long g0 = g0q[q];\n"
+        + "".join(f"      const uint32_t rw{i} = rwq{i}[q];\n" for i in range(pmw)) +
+        f"      uint32_t sel = __ballot_sync(FULL, wantq[q] != 0u);\n"
+        f"      while (sel) {{\n"
+        f"        const int l = __ffs(sel) - 1;\n"
+        f"        sel &= sel - 1u;\n"
+        f"        setup_tile(p, t, (unsigned int)(g0 + l), true, false);\n"
+        f"        S b[8];\n"
+        f"        load_basis(p, t, b);\n"
         + dispatch +
+        f"      }}\n"
         f"    }}\n"
         f"  }}\n"
         f"}}\n")

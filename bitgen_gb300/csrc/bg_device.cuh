@@ -152,7 +152,6 @@ struct Tile {
   S em;              /* per word: the bits of positions before the input end */
   bool edge;         /* the tile has words before the input start or reaches its last word */
   uint32_t pcin[NPRE_WORDS]; /* bit k: carry entering pre-pass addition k (warp-uniform)   */
-  uint32_t run[BG_NRUN];     /* prefilter: bit r = term r (or pre-pass marker) may be set    */
 };
 
 /* Advance(x, N): marks move N positions forward; words before the input start read as 0. */
@@ -710,9 +709,37 @@ __device__ __forceinline__ void load_word_bytes(const BgParams &p, const Tile &t
 #pragma unroll
     for (int q = 0; q < 8; ++q) u[q] = 0u;
     if (w >= 0 && w < t.W) {
+      /* the input's last, partial word: its bytes one by one (static indices keep u in
+         registers) */
       const long long rem = t.n - 32 * w;
-      for (long long k = 0; k < rem; ++k)
-        u[k >> 2] |= (uint32_t)__ldg(src + 32 * w + k) << (8 * (k & 3));
+#pragma unroll
+      for (int k = 0; k < 32; ++k)
+        if (k < rem) u[k >> 2] |= (uint32_t)__ldg(src + 32 * w + k) << (8 * (k & 3));
+    }
+  }
+}
+
+/* load_word_bytes for the tile `delta` words after t in the same input (the classify pass's
+ * prefetch of its next tile: a chunk inside one input walks consecutive tiles). */
+__device__ __forceinline__ void load_word_bytes_ahead(const BgParams &p, const Tile &t,
+                                                      long long delta, int j, uint32_t u[8]) {
+  const uint8_t *src = p.in_bytes + p.in_off[t.input];
+  const long long w = t.base + delta + t.lane * WPT + j;
+  if (w >= 0 && 32 * w + 32 <= t.n) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(src + 32 * w);
+    const uint4 a = __ldg(q), c = __ldg(q + 1);
+    u[0] = a.x; u[1] = a.y; u[2] = a.z; u[3] = a.w;
+    u[4] = c.x; u[5] = c.y; u[6] = c.z; u[7] = c.w;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) u[q] = 0u;
+    if (w >= 0 && w < t.W) {
+      /* the input's last, partial word: its bytes one by one (static indices keep u in
+         registers) */
+      const long long rem = t.n - 32 * w;
+#pragma unroll
+      for (int k = 0; k < 32; ++k)
+        if (k < rem) u[k >> 2] |= (uint32_t)__ldg(src + 32 * w + k) << (8 * (k & 3));
     }
   }
 }
@@ -971,9 +998,11 @@ __device__ __forceinline__ void resolve_hits(const BgParams &p, ClsCtx &c, int l
  * scanned the same way (the padding can only add hits).  The basis planes of the bytes, where
  * a caller needs them, come from basis_of. */
 __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t raw[WPT][8],
-                                          ClsCtx &c, int l) {
+                                          ClsCtx &c, int l, bool have_bytes = false) {
   uint32_t *run = c.runs_s + l;
-  if (p.input_kind == BG_INPUT_BASIS) {
+  if (have_bytes) {
+    /* raw already holds the tile's bytes (prefetched by the caller) */
+  } else if (p.input_kind == BG_INPUT_BASIS) {
     S b[8];
     load_basis(p, t, b);
 #pragma unroll
