@@ -414,9 +414,88 @@ def dna_leg(dev, n_bytes, steps, check_bytes):
             "streams": streams_equal(got_out, cpu_streams, (check_bytes + 31) // 32)}
         del cpu_streams
         res["cpu_baseline"] = cb
+    res["reference_gpu"] = reference_gpu_baseline(prog, ps.groups(4), data, dev)
     prog.close()
     del out, data
     return res
+
+
+def popcounts(words):
+    """Set bits per row of a device uint32 tensor [..., R, W] summed over the leading axes."""
+    import torch
+    x = words.reshape(-1, words.shape[-2], words.shape[-1]).view(torch.int32).to(torch.int64) \
+        & 0xFFFFFFFF
+    x = x - ((x >> 1) & 0x55555555)
+    x = (x & 0x33333333) + ((x >> 2) & 0x33333333)
+    x = (x + (x >> 4)) & 0x0F0F0F0F
+    x = (x * 0x01010101 & 0xFFFFFFFF) >> 24
+    return x.sum(dim=(0, 2)).tolist()
+
+
+def reference_gpu_baseline(prog, groups, data, dev, target_s=0.25, guard_s=5.0):
+    """The reference's own generated kernel (BitGen's KernelGenerated for these groups, made by
+    oracle/ref_gpu.py with --pass-cc-advanced=0 --pass-short-circuit=0 --pass-graph-break=-1)
+    timed on this GPU beside the engine, as a baseline.  One block scans one group over one
+    whole input (grid = (groups, inputs), gen_cuda.py:409-411), so two forms are timed: one
+    input (the runner's multi_input=1) and the input cut into 4 x SMs / groups inputs, the most
+    blocks its grid can take.  Each form is calibrated on 1 MiB, then timed on a sample sized
+    for about `target_s` per launch; a form whose calibration launch takes over `guard_s` is
+    not timed further.  The streams of the one-input form and the counts of both are compared
+    with this engine's on the same bytes."""
+    import torch
+    from oracle import ref_gpu
+    from bitgen_gb300.backend import byte_stream_transpose
+    from bitgen_gb300.engine import bytes_input, pack_bytes
+
+    if not ref_gpu.available(ref_gpu.DNA):
+        return {"unavailable": "generated kernel absent (oracle/ref_gpu.py makes it where the "
+                               "reference tree is)"}
+    k = ref_gpu.RefKernel(ref_gpu.DNA, groups)
+    s = torch.cuda.current_stream(dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    rec = {"kernel": "BitGen KernelGenerated (bitgen/codegen/gen_cuda.py) from this project's "
+                     "Pablo, --pass-cc-advanced=0 --pass-short-circuit=0 --pass-graph-break=-1",
+           "block": k.block}
+
+    def run(n_bytes, inputs, reps):
+        words = n_bytes // 32 // inputs
+        flat, basis = k.basis_buffer(inputs, words, dev)
+        byte_stream_transpose(data[:inputs * words * 32].view(1, inputs, words * 32), basis)
+        res = torch.zeros((inputs, k.groups, words), dtype=torch.uint32, device=dev)
+        k.launch(flat, inputs, words, res, s)                       # the checked result
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            k.launch(flat, inputs, words, res, s)
+        e1.record(s)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps, res, words
+
+    for form, inputs in (("one_input", 1), ("filled", max(1, 4 * sms // k.groups))):
+        unit = 32 * inputs
+        t0 = time.perf_counter()
+        ms1, _, _ = run(-(-(1 << 20) // unit) * unit, inputs, 1)
+        if time.perf_counter() - t0 > guard_s:
+            rec[form] = {"skipped": f"1 MiB calibration launch took over {guard_s} s"}
+            continue
+        n = int(min(data.numel(), (1 << 20) * target_s * 1e3 / max(ms1, 1e-3))) // unit * unit
+        ms, res, words = run(n, inputs, 3)
+        got = popcounts(res)
+        sub = data[:inputs * words * 32]
+        if inputs == 1:
+            r = prog.scan(bytes_input(sub.contiguous()))
+            want = r.counts[:, 0].tolist()
+            eq = {"streams_equal": bool(torch.equal(res[0], r.streams[:, :words]))}
+        else:
+            r = prog.scan(pack_bytes(list(sub.view(inputs, words * 32)), device=dev))
+            want = r.counts.sum(dim=1).tolist()
+            eq = {}
+        rec[form] = {"grid": [k.groups, inputs], "bytes": inputs * words * 32, "ms": round(ms, 3),
+                     "GBps": round(inputs * words * 32 / ms / 1e6, 3),
+                     "counts_equal": [int(x) for x in got] == [int(x) for x in want], **eq}
+        del res, r
+    return rec
 
 
 def served_leg(dev, n_req, probe_req=3000, plain_req=1000, arena_bytes=1 << 30):
