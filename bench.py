@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-modes", action="store_true", help="skip the batched / transpose / DNA / served legs")
     ap.add_argument("--served-requests", type=int, default=20000)
     ap.add_argument("--dna-bytes", type=int, default=1 << 30, help="DNA text of the dna leg")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip the reference's generated kernel in the dna leg (profiling runs)")
     ap.add_argument("--dna-only", action="store_true",
                     help="run only the dna leg and print its JSON (profiling the DNA kernel)")
     return ap.parse_args()
@@ -363,7 +365,7 @@ def transpose_leg(dev, n_bytes=1 << 30, reps=20, check_bytes=1 << 20, cpu_bytes=
                                                        f"bitstream.py:228-258, {cpu_s:.2f} s"}}
 
 
-def dna_leg(dev, n_bytes, steps, check_bytes):
+def dna_leg(dev, n_bytes, steps, check_bytes, ref_gpu=True):
     """64 IUPAC motifs (6-20 bases, every fourth split by a gap .{a,b}, 3 <= a <= 5, b <= a + 4) in 4 groups over DNA text
     (i.i.d. A/C/G/T, GC 42%, N runs, 80-column lines, 2^16 planted motif instances); per-group
     streams and counts, the program's default tuning (on a 4-letter text the trigram filter
@@ -414,7 +416,8 @@ def dna_leg(dev, n_bytes, steps, check_bytes):
             "streams": streams_equal(got_out, cpu_streams, (check_bytes + 31) // 32)}
         del cpu_streams
         res["cpu_baseline"] = cb
-    res["reference_gpu"] = reference_gpu_baseline(prog, ps.groups(4), data, dev)
+    if ref_gpu:
+        res["reference_gpu"] = reference_gpu_baseline(prog, ps.groups(4), data, dev)
     prog.close()
     del out, data
     return res
@@ -606,7 +609,8 @@ def main():
 
     if args.dna_only:
         print(json.dumps(dna_leg(torch.device("cuda", 0), args.dna_bytes, max(1, args.steps),
-                                 None if args.no_cpu else args.cpu_sample)), flush=True)
+                                 None if args.no_cpu else args.cpu_sample,
+                                 ref_gpu=not args.no_ref_gpu)), flush=True)
         return
 
     from bitgen_gb300.compiler import Tuning

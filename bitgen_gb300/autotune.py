@@ -25,7 +25,8 @@ SPACE = [
     Tuning(part_cap=1),
     Tuning(part_cap=4, exec_groups=8),
     Tuning(merge_outputs=False, part_cap=32),              # parts of whole outputs
-    Tuning(single_wpt=4, single_min_blocks=2),             # unselective sets: 4 words per lane
+    Tuning(single_wpt=2, single_min_blocks=1, chain_batch=8),  # unselective sets: 2 words
+                                                           # per lane, 255 registers
     Tuning(wpt=1, min_blocks=4, prefilter=False),          # single-kernel form forced
 ]
 
@@ -74,7 +75,9 @@ def autotune(groups: Sequence[Group], sample: Inputs, space: Optional[List[Tunin
         except (OSError, ValueError):
             cache = {}
         if key in cache:
-            return Tuning(**cache[key]["tuning"]), cache[key]["report"]
+            fields = {k: tuple(v) if isinstance(v, list) else v     # JSON keeps tuples as lists
+                      for k, v in cache[key]["tuning"].items()}
+            return Tuning(**fields), cache[key]["report"]
     report = []
     best, best_ms = None, float("inf")
     for t in space:

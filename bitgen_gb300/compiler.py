@@ -28,6 +28,7 @@ Pipeline
 from __future__ import annotations
 
 import hashlib
+import sys
 from dataclasses import dataclass, field, replace
 from typing import Dict, List, Optional, Sequence, Tuple
 
@@ -306,6 +307,242 @@ class Dag:
                 self._cc.append(False)
 
 
+def push_advances(dag: Dag, outs: Sequence[int]) -> List[int]:
+    """Rewrite the outputs so that Advances sit on character classes.
+
+    A shift distributes over AND, OR and XOR exactly (zeros shift in at the input start either
+    way), and consecutive shifts add up, so ``Advance(Advance(m, 1) & C, 1) & D`` becomes
+    ``Advance(m, 2) & Advance(C, 1) & D``.  A concatenation of classes then costs one AND per
+    position on class streams shifted once per (class, distance), shared by every pattern
+    that reads the class at that distance, instead of a shift of the running marker per
+    position.  The rewrite goes through a node only where it has one user (or at distance 0),
+    so no work is duplicated: a shared node is computed once and its result shifted, as
+    before.  Other operations (NOT, SEL, the additions, look-aheads) are rebuilt over their
+    rewritten operands."""
+    dag.analyse()
+    cc = list(dag._cc)
+    uses: Dict[int, int] = {}
+    live, stack = set(), list(outs)
+    while stack:
+        v = stack.pop()
+        if v in live:
+            continue
+        live.add(v)
+        stack.extend(dag.nodes[v].args)
+    for v in live:
+        for a in dag.nodes[v].args:
+            uses[a] = uses.get(a, 0) + 1
+    for o in outs:
+        uses[o] = uses.get(o, 0) + 1
+    memo: Dict[Tuple[int, int], int] = {}
+
+    def push(v: int, s: int) -> int:
+        key = (v, s)
+        hit = memo.get(key)
+        if hit is not None:
+            return hit
+        n = dag.nodes[v]
+        through = s == 0 or uses.get(v, 0) <= 1
+        if cc[v]:
+            r = dag.make("advance", (v,), s)
+        elif n.op == "advance" and through:
+            r = push(n.args[0], s + n.shift)
+        elif n.op in ("and", "or", "xor") and through:
+            r = dag.make(n.op, (push(n.args[0], s), push(n.args[1], s)))
+        elif s == 0:
+            r = dag.make(n.op, tuple(push(a, 0) for a in n.args), n.shift)
+        else:
+            u = push(v, 0)
+            if dag.nodes[u].op == "advance":    # shifts add up
+                r = dag.make("advance", dag.nodes[u].args, dag.nodes[u].shift + s)
+            else:
+                r = dag.make("advance", (u,), s)
+        memo[key] = r
+        return r
+
+    limit = sys.getrecursionlimit()
+    sys.setrecursionlimit(max(limit, 20 * len(dag.nodes) + 1000))
+    try:
+        out = [push(o, 0) for o in outs]
+    finally:
+        sys.setrecursionlimit(limit)
+    dag.analyse()
+    return out
+
+
+def _cluster_chains(members: List[int], leaves: Dict[int, List[Tuple[int, int]]],
+                    batch: int) -> List[List[int]]:
+    """Split chains into batches of at most `batch` that share shifted classes: each batch
+    starts from the remaining chain with the most leaves and greedily takes the chain whose
+    leaves are most often already in the batch (ties: fewer new leaves, then lower id), so
+    that a batch computes fewer distinct shifted classes.  Beyond 512 chains the chains keep
+    their order (the greedy search is quadratic)."""
+    if len(members) <= batch or len(members) > 512:
+        return [members[i:i + batch] for i in range(0, len(members), batch)]
+    sets = {r: set(leaves[r]) for r in members}
+    left = sorted(members)
+    out = []
+    while left:
+        seed = max(left, key=lambda r: (len(sets[r]), -r))
+        grp, have = [seed], set(sets[seed])
+        left.remove(seed)
+        while left and len(grp) < batch:
+            best = max(left, key=lambda r: (len(sets[r] & have), -len(sets[r] - have), -r))
+            grp.append(best)
+            have |= sets[best]
+            left.remove(best)
+        out.append(sorted(grp))
+    return out
+
+
+def interleave_chains(dag: Dag, outs: Sequence[int], batch: int) -> Tuple[List[int], Dict[int, int]]:
+    """Re-associate the AND chains of a pushed program distance-major.
+
+    After ``push_advances`` a pattern is an AND of shifted classes ``Advance(C, d)`` (and of
+    a few shared markers).  Computed pattern by pattern, a shifted class that several patterns
+    read must either be recomputed or held in a register from its first to its last use.  Here
+    the chains (maximal trees of single-use ANDs) are rebuilt together, `batch` chains at a
+    time: for each distance d, largest first, every class shifted by d is computed once and
+    ANDed into each chain of the batch that reads it; the chain's other operands (shared
+    markers, ORs, additions) are ANDed in last.  A chain that reads another chain's result is
+    built in a later wave than that chain.  AND is associative and commutative, so the values
+    are unchanged.  Returns the new outputs and, for each AND node built here, its batch
+    number (the code generator shares a shifted class within a batch)."""
+    dag.analyse()
+    cc = dag._cc
+    live, stack = set(), list(outs)
+    while stack:
+        v = stack.pop()
+        if v in live:
+            continue
+        live.add(v)
+        stack.extend(dag.nodes[v].args)
+    users: Dict[int, List[int]] = {}
+    for v in live:
+        for a in dag.nodes[v].args:
+            users.setdefault(a, []).append(v)
+
+    def is_and(v):
+        return dag.nodes[v].op == "and" and not cc[v]
+
+    def leaf(v):
+        """(class, distance) of a shifted class, else None."""
+        n = dag.nodes[v]
+        if cc[v]:
+            return (v, 0)
+        if n.op == "advance" and cc[n.args[0]]:
+            return (n.args[0], n.shift)
+        return None
+
+    out_set = set(outs)
+
+    def inner(v):   # an AND folded into its single user's chain
+        return (is_and(v) and v not in out_set and len(users.get(v, ())) == 1
+                and is_and(users[v][0]))
+
+    roots = [v for v in sorted(live) if is_and(v) and not inner(v)]
+    flat: Dict[int, Tuple[List[Tuple[int, int]], List[int]]] = {}
+    for r in roots:
+        leaves, others, st = [], [], list(dag.nodes[r].args)
+        while st:
+            a = st.pop()
+            if inner(a):
+                st.extend(dag.nodes[a].args)
+            elif leaf(a) is not None:
+                leaves.append(leaf(a))
+            else:
+                others.append(a)
+        flat[r] = (leaves, others)
+    root_set = set(roots)
+    need_memo: Dict[int, int] = {}
+    wave: Dict[int, int] = {}
+
+    def need(x):
+        if x in need_memo:
+            return need_memo[x]
+        if leaf(x) is not None:
+            r = 0
+        elif x in root_set:
+            r = wave_of(x) + 1
+        else:
+            r = max([need(a) for a in dag.nodes[x].args] + [0])
+        need_memo[x] = r
+        return r
+
+    def wave_of(r):
+        if r not in wave:
+            wave[r] = max([need(o) for o in flat[r][1]] + [0])
+        return wave[r]
+
+    built: Dict[int, int] = {}
+    memo: Dict[int, int] = {}
+
+    def rebuild(v):
+        if v in built:
+            return built[v]
+        if leaf(v) is not None:
+            return v
+        if v in memo:
+            return memo[v]
+        n = dag.nodes[v]
+        assert v not in root_set, "chain used before its wave"
+        r = dag.make(n.op, tuple(rebuild(a) for a in n.args), n.shift)
+        memo[v] = r
+        return r
+
+    def fresh_and(a, b):
+        """A new AND node (no hash-consing: the pushed chains' own nodes hold the same
+        operands, and the code generator emits nodes in creation order)."""
+        if dag.zero in (a, b):
+            return dag.zero
+        if a == dag.ones:
+            return b
+        if b == dag.ones:
+            return a
+        return dag._new(Node(0, "and", (a, b)))
+
+    epochs: Dict[int, int] = {}
+    limit = sys.getrecursionlimit()
+    sys.setrecursionlimit(max(limit, 20 * len(dag.nodes) + 1000))
+    try:
+        for r in roots:
+            wave_of(r)
+        k = 0
+        for w in sorted(set(wave.values())):
+            members = [r for r in roots if wave[r] == w]
+            for grp in _cluster_chains(members, {r: flat[r][0] for r in members}, max(1, batch)):
+                acc: Dict[int, Optional[int]] = {r: None for r in grp}
+                dists = sorted({d for r in grp for _, d in flat[r][0]}, reverse=True)
+                by_d = {r: {} for r in grp}
+                for r in grp:
+                    for c, d in flat[r][0]:
+                        by_d[r].setdefault(d, []).append(c)
+                for d in dists:
+                    for r in grp:
+                        for c in sorted(by_d[r].get(d, [])):
+                            lf = dag.make("advance", (c,), d)
+                            if acc[r] is None:
+                                acc[r] = lf
+                            else:
+                                acc[r] = fresh_and(acc[r], lf)
+                                epochs.setdefault(acc[r], k)
+                for r in grp:
+                    for o in flat[r][1]:
+                        ro = rebuild(o)
+                        if acc[r] is None:
+                            acc[r] = ro
+                        else:
+                            acc[r] = fresh_and(acc[r], ro)
+                            epochs.setdefault(acc[r], k)
+                    built[r] = acc[r]
+                k += 1
+        new = [rebuild(o) for o in outs]
+    finally:
+        sys.setrecursionlimit(limit)
+    dag.analyse()
+    return new, epochs
+
+
 # ----------------------------------------------------------------------------------------
 # 3/4. Kernel generation
 # ----------------------------------------------------------------------------------------
@@ -340,15 +577,21 @@ class Tuning:
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
     exec_claim: int = 2      # split form: work items an execute warp claims at once
     inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
-    single_wpt: int = 2      # words per lane (and blocks per SM below) when the compiler falls
-    single_min_blocks: int = 3   # back to the single-kernel form because the filters are
-                                 # unselective (0: keep wpt / min_blocks)
+    single_wpt: int = 1      # words per lane (and blocks per SM below) when the compiler falls
+    single_min_blocks: int = 2   # back to the single-kernel form because the filters are
+                                 # unselective (0: keep wpt / min_blocks); 2 blocks of 256
+                                 # give the distance-major chains 128 registers a thread
     basis_filter: bool = True    # split form: rebuild the bytes of basis-plane inputs and run
                                  # the q-gram filter on them (else every term runs there)
     filter_config: Optional[Tuple[int, int]] = None  # prefilter (q-gram length, stride); None:
                                                      # the cheapest by the filter's cost model
     bulk_zero: bool = True   # split form: classify zeroes the outputs with bulk copies from
                              # shared memory (else with vector stores of its lanes)
+    push_advances: bool = True   # single-kernel form: Advances pushed through single-use
+                                 # AND/OR/XOR down to the character classes, each class shifted
+                                 # once per distance; a word read from another lane is shared
+    chain_batch: int = 8         # with push_advances: AND chains re-associated distance-major,
+                                 # this many at a time (0: each chain computed on its own)
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
@@ -356,7 +599,8 @@ class Tuning:
                 self.lookback_width, self.lookback_spin, self.carry_prepass, self.prefilter,
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
-                self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim)
+                self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim,
+                self.push_advances, self.chain_batch)
 
 
 @dataclass
@@ -397,6 +641,10 @@ class _Gen:
         self.pre: Dict[int, int] = {}   # pre-pass additions -> their index (= add index)
         self.uses: Dict[int, int] = {}
         self.tmp = 0
+        self.share_reads = False
+        self.inline: Dict[str, List[str]] = {}   # pseudo-values: per-word expressions
+        self.epochs: Dict[int, int] = {}   # AND node -> batch of chains (interleave_chains)
+        self.epoch = -1                    # batch of the node being computed
 
     # analysis ---------------------------------------------------------------------------
     def byteset(self, v: int) -> int:
@@ -530,7 +778,30 @@ class _Gen:
     def w(self, ref: str, j: int) -> str:
         if ref in ("0u", "0xffffffffu"):
             return ref
+        e = self.inline.get(ref)
+        if e is not None:
+            return e[j]
         return f"{ref}_{j}"
+
+    def operand(self, v: int) -> str:
+        """Operand `v` of a bitwise operation on markers.  With shared reads on, a character
+        class is read through its masked words (the reads its shifts use): the mask clears
+        only positions before the input start, which no output keeps and every shift and
+        addition clears again, so one copy of the class stays live instead of two."""
+        n = self.d.nodes[v]
+        if not (self.share_reads and self.d.is_cc(v) and n.op not in ("zero", "ones")):
+            return self.mat(v)
+        c = self.mat(v)
+        name = f"@cls{self.tmp}"
+        self.tmp += 1
+        self.inline[name] = [self.shared(self.word_back(c, j)) for j in range(self.t.wpt)]
+        return name
+
+    def leaf(self, v: int) -> bool:
+        """A shifted character class, recomputed at each use from the shared reads of its
+        class (one funnel shift a word) instead of held in registers across the part."""
+        n = self.d.nodes[v]
+        return self.share_reads and n.op == "advance" and self.d.is_cc(n.args[0])
 
     def word_back(self, ref: str, J: int) -> str:
         """Word (lane*WPT + J) of `ref` as seen from this lane (J < 0 reads earlier lanes);
@@ -581,15 +852,30 @@ class _Gen:
                     e = f"__funnelshift_l({nxt}, {cur}, {r})"
             elif op == "advance":
                 q, r = divmod(n.shift, 32)
-                cur = self.word_back(a[0], j - q)
+                cur = self.shared(self.word_back(a[0], j - q))
                 if r == 0:
                     e = cur
                 else:
-                    prev = self.word_back(a[0], j - q - 1)
+                    prev = self.shared(self.word_back(a[0], j - q - 1))
                     e = f"__funnelshift_r({cur}, {prev}, {r})"
             else:
                 raise AssertionError(op)
             self.emit(f"{pre}{name}_{j} = {e};")
+
+    def shared(self, expr: str) -> str:
+        """With shared reads on, a temporary holding `expr` (a masked word or a word read from
+        another lane), declared once per scope, so that every shift of a class reuses it."""
+        if not self.share_reads or expr in ("0u", "0xffffffffu"):
+            return expr
+        key = ("read", expr)
+        for sc in reversed(self.scopes):
+            if key in sc:
+                return sc[key]
+        name = f"sr{self.tmp}"
+        self.tmp += 1
+        self.emit(f"const uint32_t {name} = {expr};")
+        self.scopes[-1][key] = name
+        return name
 
     def declare_zero(self, name: str):
         self.emit("uint32_t " + ", ".join(f"{name}_{j} = 0u" for j in range(self.t.wpt)) + ";")
@@ -613,6 +899,33 @@ class _Gen:
             return "0u"
         if n.op == "ones":
             return "0xffffffffu"
+        if self.leaf(v):
+            key = ("leaf", v, self.epoch)
+            if self.epoch >= 0:
+                for sc in reversed(self.scopes):
+                    if key in sc:
+                        return sc[key]
+            c = self.mat(n.args[0])
+            q, r = divmod(n.shift, 32)
+            exprs = []
+            for j in range(self.t.wpt):
+                cur = self.shared(self.word_back(c, j - q))
+                if r == 0:
+                    exprs.append(cur)
+                else:
+                    prev = self.shared(self.word_back(c, j - q - 1))
+                    exprs.append(f"shr_funnel<{r}>({cur}, {prev})")
+            if self.epoch >= 0:     # one temporary per batch, read by its chains
+                name = f"lf{self.tmp}"
+                self.tmp += 1
+                for j, e in enumerate(exprs):
+                    self.emit(f"const uint32_t {name}_{j} = {e};")
+                self.scopes[-1][key] = name
+                return name
+            name = f"@leaf{self.tmp}"
+            self.tmp += 1
+            self.inline[name] = exprs
+            return name
         name = f"v{v}"
         if self.d.is_cc(v):
             a = [self.mat(x) for x in n.args]
@@ -750,7 +1063,7 @@ class _Gen:
         out, stack = set(), [v]
         while stack:
             x = stack.pop()
-            if x in out or self.d.is_cc(x):
+            if x in out or self.d.is_cc(x) or self.leaf(x):
                 continue
             out.add(x)
             stack.extend(self.d.nodes[x].args)
@@ -791,6 +1104,15 @@ class _Gen:
         term_outs: Dict[int, List[int]] = {}
         for v, o in terms:
             term_outs.setdefault(v, []).append(o)
+        # outputs with several terms here OR them in registers and reach the shared-memory
+        # accumulator once, at the end of the part (a term costs one OR instead of a vote,
+        # a load and a store)
+        n_terms: Dict[int, int] = {}
+        for _, o in terms:
+            n_terms[o] = n_terms.get(o, 0) + 1
+        reg_out = sorted(o for o, c in n_terms.items() if c > 1)
+        for o in reg_out:
+            self.declare_zero(f"oa{o}")
         # heavy nodes of this part, in topological (id) order
         heavy = sorted(set().union(*[self.heavy_ancestors(v) for v in term_outs]))
         hs = set(heavy)
@@ -902,6 +1224,7 @@ class _Gen:
             n = d.nodes[v]
             name = f"v{v}"
             declare = decl[v] == home[v]
+            self.epoch = self.epochs.get(v, -1)
             if n.op in ADD_OPS:
                 if v not in begun:
                     add_begin(v)
@@ -913,13 +1236,18 @@ class _Gen:
                     pre = "const uint32_t " if declare else ""
                     self.emit(f"{pre}{name}_{j} = {name}_s.w[{j}];")
             else:
-                a = [self.mat(x) for x in n.args]
+                a = [self.operand(x) if n.op in ("and", "or", "xor") else self.mat(x)
+                     for x in n.args]
                 self.emit_op(name, n, a, declare=declare)
             self.scopes[-1][v] = name
             if declare is False:
                 self.scopes[0][v] = name  # visible everywhere below its declaration
             for o in term_outs.get(v, []):
-                self.emit(f"acc_or(acc, {o}, {self.pack(name)});")
+                if o in reg_out:
+                    for j in range(self.t.wpt):
+                        self.emit(f"oa{o}_{j} |= {name}_{j};")
+                else:
+                    self.emit(f"acc_or(acc, {o}, {self.pack(name)});")
 
         def emit_top():
             for v in lifted_at.get(TOP, []):
@@ -1002,7 +1330,13 @@ class _Gen:
                 r = self.mat(v)
                 if r != "0u":
                     for o in os_:
-                        self.emit(f"acc_or(acc, {o}, {self.pack(r)});")
+                        if o in reg_out:
+                            for j in range(self.t.wpt):
+                                self.emit(f"oa{o}_{j} |= {self.w(r, j)};")
+                        else:
+                            self.emit(f"acc_or(acc, {o}, {self.pack(r)});")
+        for o in reg_out:
+            self.emit(f"acc_or(acc, {o}, {self.pack(f'oa{o}')});")
         return "\n".join(self.lines)
 
 def _basis_params(wpt: int) -> str:
@@ -1145,18 +1479,32 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
             # (programs whose terms have no filter at all keep the requested shape)
             # (the terms run on every tile and mostly stay non-zero for several steps, so
             # zero-block skipping costs more branches than it saves: off by default)
-            if filt.enabled and tuning.single_wpt and tuning.single_wpt != tuning.wpt:
+            if filt.enabled and tuning.single_wpt and (tuning.single_wpt != tuning.wpt or
+                                                        tuning.single_min_blocks != tuning.min_blocks):
                 return generate_kernel(groups, replace(
                     tuning, prefilter=False, wpt=tuning.single_wpt,
                     min_blocks=tuning.single_min_blocks,
                     skip_interval=0 if tuning.skip_interval < 0 else tuning.skip_interval),
                     per_regex, name)
+            if filt.enabled and tuning.skip_interval < 0:
+                tuning = replace(tuning, skip_interval=0)
+                gen.t = tuning
             filt = None
     if tuning.skip_interval < 0:
         tuning = replace(tuning, skip_interval=0 if filt is not None else 1)
         gen.t = tuning
     if filt is not None:
         return _generate_filtered(gen, tuning, terms, names, filt, name)
+    if tuning.push_advances:
+        outs = push_advances(dag, outs)
+        epochs: Dict[int, int] = {}
+        if tuning.chain_batch > 0:
+            outs, epochs = interleave_chains(dag, outs, tuning.chain_batch)
+        gen = _Gen(dag, tuning)
+        gen.analyse(outs)
+        gen.share_reads = True
+        gen.epochs = epochs
+        terms = [(leaf, o) for o, v in enumerate(outs) for leaf in gen.or_leaves(v)]
     budget = SMEM_BUDGET
     per_warp = max(1, n_out) * wpt * 32 * 4
     if per_warp > budget:

@@ -75,6 +75,16 @@ struct S {
   uint32_t w[WPT];
 };
 
+// Low word of (hi:lo) >> R, as __funnelshift_r(lo, hi, R).  Written as a volatile instruction
+// so that a shifted character class is recomputed where it is used (one instruction) rather
+// than merged with its other uses and held in a register across the whole part.
+template <int R>
+__device__ __forceinline__ uint32_t shr_funnel(uint32_t lo, uint32_t hi) {
+  uint32_t d;
+  asm volatile("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(lo), "r"(hi), "n"(R));
+  return d;
+}
+
 __device__ __forceinline__ S zero() {
   S r;
 #pragma unroll
