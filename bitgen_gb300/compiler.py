@@ -508,34 +508,35 @@ def interleave_chains(dag: Dag, outs: Sequence[int], batch: int) -> Tuple[List[i
         for r in roots:
             wave_of(r)
         k = 0
-        for w in sorted(set(wave.values())):
-            members = [r for r in roots if wave[r] == w]
-            for grp in _cluster_chains(members, {r: flat[r][0] for r in members}, max(1, batch)):
-                acc: Dict[int, Optional[int]] = {r: None for r in grp}
-                dists = sorted({d for r in grp for _, d in flat[r][0]}, reverse=True)
-                by_d = {r: {} for r in grp}
+        steps = [g for w in sorted(set(wave.values()))
+                 for g in _cluster_chains([r for r in roots if wave[r] == w],
+                                          {r: flat[r][0] for r in roots}, max(1, batch))]
+        for grp in steps:
+            acc: Dict[int, Optional[int]] = {r: None for r in grp}
+            dists = sorted({d for r in grp for _, d in flat[r][0]}, reverse=True)
+            by_d = {r: {} for r in grp}
+            for r in grp:
+                for c, d in flat[r][0]:
+                    by_d[r].setdefault(d, []).append(c)
+            for d in dists:
                 for r in grp:
-                    for c, d in flat[r][0]:
-                        by_d[r].setdefault(d, []).append(c)
-                for d in dists:
-                    for r in grp:
-                        for c in sorted(by_d[r].get(d, [])):
-                            lf = dag.make("advance", (c,), d)
-                            if acc[r] is None:
-                                acc[r] = lf
-                            else:
-                                acc[r] = fresh_and(acc[r], lf)
-                                epochs.setdefault(acc[r], k)
-                for r in grp:
-                    for o in flat[r][1]:
-                        ro = rebuild(o)
+                    for c in sorted(by_d[r].get(d, [])):
+                        lf = dag.make("advance", (c,), d)
                         if acc[r] is None:
-                            acc[r] = ro
+                            acc[r] = lf
                         else:
-                            acc[r] = fresh_and(acc[r], ro)
+                            acc[r] = fresh_and(acc[r], lf)
                             epochs.setdefault(acc[r], k)
-                    built[r] = acc[r]
-                k += 1
+            for r in grp:
+                for o in flat[r][1]:
+                    ro = rebuild(o)
+                    if acc[r] is None:
+                        acc[r] = ro
+                    else:
+                        acc[r] = fresh_and(acc[r], ro)
+                        epochs.setdefault(acc[r], k)
+                built[r] = acc[r]
+            k += 1
         new = [rebuild(o) for o in outs]
     finally:
         sys.setrecursionlimit(limit)
@@ -1083,7 +1084,7 @@ class _Gen:
                       f"pg[{k >> 5}] |= G << {k & 31}; pp[{k >> 5}] |= P << {k & 31}; }}")
         return "\n".join(self.lines)
 
-    def part(self, terms: Sequence[Tuple[int, int]]) -> str:
+    def part(self, terms: Sequence[Tuple[int, int]], outer_regs: bool = False) -> str:
         """Body of one part function: every (node, output) term OR-ed into the warp's
         shared-memory accumulator of its output.
 
@@ -1095,7 +1096,10 @@ class _Gen:
         checkpoint in cz(v) other than itself (its home); a value used outside its home is
         declared zero in the enclosing region both share.  Within a region the unguarded work
         is emitted first and child guard blocks are opened as late as dependencies allow, so
-        the dense part of all terms forms one basic block."""
+        the dense part of all terms forms one basic block.
+
+        With `outer_regs` every term ORs into register accumulators `oa<o>_<j>` that the
+        caller declares and stores (the split form's parts)."""
         d = self.d
         k = max(1, self.t.skip_interval) if self.t.skip_interval > 0 else 0
         self.lines = []
@@ -1110,9 +1114,10 @@ class _Gen:
         n_terms: Dict[int, int] = {}
         for _, o in terms:
             n_terms[o] = n_terms.get(o, 0) + 1
-        reg_out = sorted(o for o, c in n_terms.items() if c > 1)
-        for o in reg_out:
-            self.declare_zero(f"oa{o}")
+        reg_out = sorted(o for o, c in n_terms.items() if c > 1 or outer_regs)
+        if not outer_regs:
+            for o in reg_out:
+                self.declare_zero(f"oa{o}")
         # heavy nodes of this part, in topological (id) order
         heavy = sorted(set().union(*[self.heavy_ancestors(v) for v in term_outs]))
         hs = set(heavy)
@@ -1335,8 +1340,9 @@ class _Gen:
                                 self.emit(f"oa{o}_{j} |= {self.w(r, j)};")
                         else:
                             self.emit(f"acc_or(acc, {o}, {self.pack(r)});")
-        for o in reg_out:
-            self.emit(f"acc_or(acc, {o}, {self.pack(f'oa{o}')});")
+        if not outer_regs:
+            for o in reg_out:
+                self.emit(f"acc_or(acc, {o}, {self.pack(f'oa{o}')});")
         return "\n".join(self.lines)
 
 def _basis_params(wpt: int) -> str:
@@ -1725,16 +1731,19 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         words = sorted(masks)
         for r in rs:
             li = outs_k.index(terms[r][1])
-            code = gen.part([(terms[r][0], li)])
+            code = gen.part([(terms[r][0], li)], outer_regs=True)
             body = "\n".join("  " + ln for ln in code.split("\n"))
             blocks.append(f"  if ((r{words.index(r >> 5)} >> {r & 31}) & 1u) {{\n{body}\n  }}")
         part_masks.append(masks)
         fn = "merge_store" if merge else "store"
-        stores = "\n".join(f"  {fn}(p, t, {o}, acc_get(acc, t, {li}));" for li, o in enumerate(outs_k))
+        # the terms OR into register accumulators, one per output of the part
+        regs = "\n".join(f"  uint32_t " + ", ".join(f"oa{li}_{j} = 0u" for j in range(wpt)) + ";"
+                         for li in range(len(outs_k)))
+        stores = "\n".join(f"  {fn}(p, t, {o}, {gen.pack(f'oa{li}')});" for li, o in enumerate(outs_k))
         funcs.append(f"{{PART}}"
                      f'{{QUAL}} void bg_part_{ci}({sig}) {{\n'
                      f"  constexpr bool E = true;\n"
-                     f"  acc_clear_n(acc, t, {len(outs_k)});\n" + "\n".join(blocks) + "\n" + stores + "\n}\n")
+                     f"{regs}\n" + "\n".join(blocks) + "\n" + stores + "\n}\n")
     # up to inline_parts parts are inlined into the execute kernel (one translation unit, no call
     # per tile: the call would save the item loop's registers and pass the tile by memory);
     # more parts are separate translation units compiled in parallel and called through a table
