@@ -576,12 +576,14 @@ class Tuning:
                                    # over the bytes the filters name); >= 1: always
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
-    exec_claim: int = 2      # split form: work items an execute warp claims at once
+    exec_claim: int = 1      # split form: work items an execute warp claims at once
     inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
     single_wpt: int = 1      # words per lane (and blocks per SM below) when the compiler falls
     single_min_blocks: int = 2   # back to the single-kernel form because the filters are
                                  # unselective (0: keep wpt / min_blocks); 2 blocks of 256
                                  # give the distance-major chains 128 registers a thread
+    single_edge: bool = True     # that form also gets unmasked part code for tiles that touch
+                                 # no input end (edge_variants)
     basis_filter: bool = True    # split form: rebuild the bytes of basis-plane inputs and run
                                  # the q-gram filter on them (else every term runs there)
     filter_config: Optional[Tuple[int, int]] = None  # prefilter (q-gram length, stride); None:
@@ -601,7 +603,7 @@ class Tuning:
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
                 self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim,
-                self.push_advances, self.chain_batch)
+                self.push_advances, self.chain_batch, self.single_edge)
 
 
 @dataclass
@@ -1486,10 +1488,11 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
             # (the terms run on every tile and mostly stay non-zero for several steps, so
             # zero-block skipping costs more branches than it saves: off by default)
             if filt.enabled and tuning.single_wpt and (tuning.single_wpt != tuning.wpt or
-                                                        tuning.single_min_blocks != tuning.min_blocks):
+                                                        tuning.single_min_blocks != tuning.min_blocks or
+                                                        tuning.single_edge != tuning.edge_variants):
                 return generate_kernel(groups, replace(
                     tuning, prefilter=False, wpt=tuning.single_wpt,
-                    min_blocks=tuning.single_min_blocks,
+                    min_blocks=tuning.single_min_blocks, edge_variants=tuning.single_edge,
                     skip_interval=0 if tuning.skip_interval < 0 else tuning.skip_interval),
                     per_regex, name)
             if filt.enabled and tuning.skip_interval < 0:
