@@ -1,22 +1,26 @@
 """Benchmark: input GB/s of the fused bitstream scan on the 256-regex throughput workload.
 
-Workload (one step = one scan of the whole input): 256 seeded synthetic regexes (8-40 chars,
-30% with an unbounded repetition), 16 groups of 16, over 1 MiB of printable ASCII with ~1
-planted match per 4 KiB, tiled to 256 MiB.  Each step writes the 16 per-group match streams
-(the reference's result shape) and the per-group match counts.  The input (256 MiB) is larger
-than L2 (129 MB), so no flush is needed between steps.  The CPU evaluator scans the same
-256 MiB once (a few seconds on the host's cores); its counts must equal the GPU's.
+Workload (one step = one scan of the whole input): 256 seeded synthetic regexes of the
+benchmark grammar (4-12-byte literals mixed with [a-z0-9] classes, {2,5} repeats, a .* gap, a
+2-way alternation), 16 groups of 16, over 1 MiB of printable ASCII with planted matches, tiled
+to 256 MiB.  Each step writes the 16 per-group match streams (the reference's result shape) and
+the per-group match counts.  The input (256 MiB) is larger than L2 (129 MB), so no flush is
+needed between steps.  The CPU evaluator scans the same 256 MiB once; the streams and counts of
+the timed launches must equal its own.
 
-Further legs on the same line: ``batched`` (4096 small inputs, one graph launch vs one launch
-per input), ``dna`` (64 IUPAC motifs over 1 GiB of DNA text, its own CPU check) and ``served``
-(Poisson request arrivals over three resident pattern sets, p50/p99 latency).
+Further legs on the same line: ``positions_only`` and ``basis_hook`` (the same scan with
+positions instead of streams, and through the reference's run_fn(basis) hook), ``batched``
+(4096 small inputs, one graph launch vs one launch per input, with an autotune report),
+``transpose``, ``dna`` (64 IUPAC motifs over 1 GiB of DNA text, its own CPU check, and the
+reference's generated kernel timed beside it) and ``served`` (Poisson request arrivals over
+three resident pattern sets, p50/p99 latency).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 ``--impl reference`` times the CPU evaluator (``oracle/bg_cpu.c``, all host threads) on the same
-workload, one scan of the 256 MiB input per step: the reference's own GPU path cannot execute these programs (its
-parser rejects MatchStar, ``bitgen/bitparser/bitstream_parser.py:202-211``) and its CPU
-comparison point, icgrep, is not part of the reference tree.
+workload, one scan of the 256 MiB input per step: the reference's CPU comparison point, icgrep,
+is not part of the reference tree, and its GPU path cannot run these programs (its parser
+rejects MatchStar; the while-loop form needs whole-stream loop tests its kernel does per tile).
 """
 
 from __future__ import annotations
