@@ -1396,6 +1396,8 @@ PRE_CHUNK_OPEN = _CHUNK_HEAD + _TILE_LOOP
 CLS_CHUNK_OPEN = (                   # classify: PRE_CHUNK_OPEN plus the chunk's output zeroing
     _CHUNK_HEAD +
     "   const int zin = chunk_input(p, g0, g1);\n"
+    "   /* a chunk inside one input: its first tile and length, for every tile's setup */\n"
+    "   const long long zfirst = zin >= 0 ? p.tile_prefix[zin] : 0, zn = zin >= 0 ? p.in_len[zin] : 0;\n"
     "   if (zin >= 0) { @ZERO@ }\n"
     "   cx.row = row;\n"
     "   bool pf = false;\n"
@@ -2025,7 +2027,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         + CLS_CHUNK_OPEN.replace("@ZERO@", (f"zero_chunk_bulk(p, zin, g0, g1, {len(names)}, t.lane, zsm, {zero_bytes}u);"
                                              if tuning.bulk_zero else
                                              f"zero_chunk(p, zin, g0, g1, {len(names)}, t.lane);") if merge else "") +
-        f"    setup_tile(p, t, (unsigned int)g, false, true);\n"
+        f"    if (zin >= 0) setup_tile_in(p, t, (unsigned int)g, zin, zfirst, zn);\n"
+        f"    else setup_tile(p, t, (unsigned int)g, false, true);\n"
         f"    uint32_t raw[BG_WPT][8];\n"
         f"    const bool have = pf;\n"
         f"    if (have) {{\n"

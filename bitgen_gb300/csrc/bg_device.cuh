@@ -152,6 +152,7 @@ __device__ __forceinline__ uint32_t word_back(const S &x, int J) {
 struct Tile {
   long long gtile;   /* global tile id                                   */
   long long first;   /* global id of the first tile of this input        */
+  long long last;    /* global id of the first tile of the next input    */
   long long base;    /* input word index of lane 0 word 0 (may be < 0)   */
   long long n;       /* characters in the input                          */
   long long W;       /* words in the input                               */
@@ -627,6 +628,7 @@ __device__ __forceinline__ AddState add_known(const BgParams &p, const Tile &t, 
 __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
   t.lane = threadIdx.x & 31;
   t.input = 0;
+  t.first = t.last = 0;   /* no input held yet */
   t.epoch = *(volatile const unsigned long long *)(p.state + 2);
 }
 
@@ -653,22 +655,20 @@ __device__ __forceinline__ void load_pre_carries(const BgParams &p, Tile &t) {
 __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g,
                                            bool carries = true, bool debug_wait = true) {
   /* find i: prefix[i] <= g < prefix[i+1]; a warp's tiles mostly stay in the input of its
-   * previous tile, so that one is tried first */
-  int lo = t.input;
-  if (!(lo >= 0 && lo < p.n_inputs && p.tile_prefix[lo] <= (long long)g &&
-        (long long)g < p.tile_prefix[lo + 1])) {
-    lo = 0;
-    int hi = p.n_inputs;
+   * previous tile, whose bounds and length the tile holds (no loads then) */
+  if (!((long long)g >= t.first && (long long)g < t.last)) {
+    int lo = 0, hi = p.n_inputs;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
       if (p.tile_prefix[mid] <= (long long)g) lo = mid; else hi = mid;
     }
+    t.input = lo;
+    t.first = p.tile_prefix[lo];
+    t.last = p.tile_prefix[lo + 1];
+    t.n = p.in_len[lo];
+    t.W = (t.n + 31) >> 5;
   }
-  t.input = lo;
   t.gtile = g;
-  t.first = p.tile_prefix[lo];
-  t.n = p.in_len[lo];
-  t.W = (t.n + 31) >> 5;
   t.base = ((long long)g - t.first) * SW - (long long)HL * WPT;
 #pragma unroll
   for (int j = 0; j < WPT; ++j) {
@@ -680,6 +680,30 @@ __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned 
   t.edge = t.base < 0 || t.base + 32 * WPT >= t.W;
   if (NPRE > 0 && carries) load_pre_carries(p, t);
   if (debug_wait && (long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
+    (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
+                      p.spin_limit, p.state, t.lane);
+}
+
+/* setup_tile for tile g of a known input (first tile `first`, n bytes), from values the caller
+ * holds: no table lookups (the classify pass walks a chunk of one input). */
+__device__ __forceinline__ void setup_tile_in(const BgParams &p, Tile &t, unsigned int g,
+                                              int input, long long first, long long n) {
+  t.input = input;
+  t.gtile = g;
+  t.first = first;
+  t.last = first;     /* the next setup_tile looks its input up */
+  t.n = n;
+  t.W = (n + 31) >> 5;
+  t.base = ((long long)g - first) * SW - (long long)HL * WPT;
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    const long long w = t.base + t.lane * WPT + j;
+    t.vm.w[j] = (w >= 0) ? FULL : 0u;
+    const long long rem = n - 32 * w;
+    t.em.w[j] = rem >= 32 ? FULL : (rem <= 0 ? 0u : (FULL << (32 - rem)));
+  }
+  t.edge = t.base < 0 || t.base + 32 * WPT >= t.W;
+  if ((long long)g == p.debug_wait_tile) /* wait-limit test: nobody writes this record */
     (void)wait_record(reinterpret_cast<const unsigned long long *>(p.state + 4), t.epoch,
                       p.spin_limit, p.state, t.lane);
 }
