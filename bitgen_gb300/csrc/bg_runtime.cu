@@ -115,13 +115,26 @@ __device__ __forceinline__ void carry_scan_block(int k, uint32_t *pre_bits, int6
     }
     in0 = a;
   }
+  /* rows are taken RB at a time, their bitmap words loaded together (the loads of a thread's
+   * rows do not wait for one another; only the carry chains through them) */
+  constexpr int RB = 8;
   uint32_t c0 = 0u, c1 = 1u;
   int in = in0;
-  for (int64_t r = r0; r < r1; ++r) {
-    const uint32_t kill = row_kill(r, tile_prefix, n_inputs, in);
-    const uint32_t A = (Gw[r] | Pw[r]) & ~kill, B = Gw[r] & ~kill;
-    c0 = (uint32_t)((((unsigned long long)A + B + c0) >> 32) & 1ull);
-    c1 = (uint32_t)((((unsigned long long)A + B + c1) >> 32) & 1ull);
+  for (int64_t rb = r0; rb < r1; rb += RB) {
+    uint32_t g[RB], q[RB];
+#pragma unroll
+    for (int i = 0; i < RB; ++i) {
+      g[i] = rb + i < r1 ? Gw[rb + i] : 0u;
+      q[i] = rb + i < r1 ? Pw[rb + i] : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < RB; ++i) {
+      if (rb + i >= r1) break;
+      const uint32_t kill = row_kill(rb + i, tile_prefix, n_inputs, in);
+      const uint32_t A = (g[i] | q[i]) & ~kill, B = g[i] & ~kill;
+      c0 = (uint32_t)((((unsigned long long)A + B + c0) >> 32) & 1ull);
+      c1 = (uint32_t)((((unsigned long long)A + B + c1) >> 32) & 1ull);
+    }
   }
   /* (G, P) of this thread's run: carry-out = G | (P & carry-in) */
   uint32_t iG = c0, iP = c1 & ~c0 & 1u;
@@ -160,12 +173,22 @@ __device__ __forceinline__ void carry_scan_block(int k, uint32_t *pre_bits, int6
   uint32_t c = eG;
   if (warp > 0) c = eG | (eP & wg[warp - 1]);
   in = in0;
-  for (int64_t r = r0; r < r1; ++r) {
-    const uint32_t kill = row_kill(r, tile_prefix, n_inputs, in);
-    const uint32_t A = (Gw[r] | Pw[r]) & ~kill, B = Gw[r] & ~kill;
-    const unsigned long long sum = (unsigned long long)A + B + c;
-    Cw[r] = (uint32_t)sum ^ A ^ B;
-    c = (uint32_t)((sum >> 32) & 1ull);
+  for (int64_t rb = r0; rb < r1; rb += RB) {
+    uint32_t g[RB], q[RB];
+#pragma unroll
+    for (int i = 0; i < RB; ++i) {
+      g[i] = rb + i < r1 ? Gw[rb + i] : 0u;
+      q[i] = rb + i < r1 ? Pw[rb + i] : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < RB; ++i) {
+      if (rb + i >= r1) break;
+      const uint32_t kill = row_kill(rb + i, tile_prefix, n_inputs, in);
+      const uint32_t A = (g[i] | q[i]) & ~kill, B = g[i] & ~kill;
+      const unsigned long long sum = (unsigned long long)A + B + c;
+      Cw[rb + i] = (uint32_t)sum ^ A ^ B;
+      c = (uint32_t)((sum >> 32) & 1ull);
+    }
   }
 }
 
@@ -185,10 +208,12 @@ __global__ void __launch_bounds__(1024) bg_carry_scan_kernel(uint32_t *pre_bits,
  * a ballot to keep them in order), and the warps' counts are scanned across the block.  The
  * execute pass orders the parts one after the other (part-major, so that the whole GPU runs one
  * part at a time) and claims a part's rows in increasing order. */
+constexpr int64_t LIST_KEEP = 1024; /* steps whose ballots a block keeps in shared memory */
 __device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
                                                 const uint32_t *pmask, int pmw, uint32_t *work,
                                                 int n_parts, int64_t rows) {
   __shared__ uint32_t wsum[32];
+  __shared__ uint32_t bal[LIST_KEEP];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
   uint32_t *out = work + BG_WORK_HEAD + n_parts + (int64_t)p * rows;
@@ -197,18 +222,47 @@ __device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
   const int64_t per = (steps + nwarps - 1) / nwarps;
   const int64_t s0 = (int64_t)warp * per < steps ? (int64_t)warp * per : steps;
   const int64_t s1 = s0 + per < steps ? s0 + per : steps;
-  auto present = [&](int64_t step) -> uint32_t {
+  /* the part's (word, mask) pairs, in registers for up to PM pairs */
+  constexpr int PM = 4;
+  uint32_t pw_[PM], pm_[PM];
+#pragma unroll
+  for (int e = 0; e < PM; ++e) {
+    pw_[e] = e < pmw ? pm[2 * e] : 0u;
+    pm_[e] = e < pmw ? pm[2 * e + 1] : 0u;
+  }
+  auto present_any = [&](int64_t step) -> uint32_t {
     const int64_t r = step * 32 + lane;
     uint32_t any = 0u;
-    if (r < rows)
-      for (int e = 0; e < pmw; ++e) {
-        const uint32_t m = pm[2 * e + 1];
-        if (m) any |= rowrun[(int64_t)pm[2 * e] * rows + r] & m;
+    if (step < s1 && r < rows) {
+      if (pmw <= PM) {
+#pragma unroll
+        for (int e = 0; e < PM; ++e)
+          if (pm_[e]) any |= rowrun[(int64_t)pw_[e] * rows + r] & pm_[e];
+      } else {
+        for (int e = 0; e < pmw; ++e) {
+          const uint32_t m = pm[2 * e + 1];
+          if (m) any |= rowrun[(int64_t)pm[2 * e] * rows + r] & m;
+        }
       }
-    return __ballot_sync(0xffffffffu, any != 0u);
+    }
+    return any;
   };
+  /* first walk: SB steps at a time, their loads issued together; the ballots are kept */
+  constexpr int SB = 8;
+  const bool keep = steps <= LIST_KEEP;
   uint32_t cnt = 0;
-  for (int64_t st = s0; st < s1; ++st) cnt += __popc(present(st));
+  for (int64_t sb = s0; sb < s1; sb += SB) {
+    uint32_t any[SB];
+#pragma unroll
+    for (int i = 0; i < SB; ++i) any[i] = present_any(sb + i);
+#pragma unroll
+    for (int i = 0; i < SB; ++i) {
+      if (sb + i >= s1) break;
+      const uint32_t b = __ballot_sync(0xffffffffu, any[i] != 0u);
+      cnt += __popc(b);
+      if (keep && lane == 0) bal[sb + i] = b;
+    }
+  }
   if (lane == 0) wsum[warp] = cnt;
   __syncthreads();
   uint32_t pos = 0, total = 0;
@@ -217,7 +271,7 @@ __device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
     total += wsum[w];
   }
   for (int64_t st = s0; st < s1; ++st) {
-    const uint32_t b = present(st);
+    const uint32_t b = keep ? bal[st] : __ballot_sync(0xffffffffu, present_any(st) != 0u);
     if ((b >> lane) & 1u) out[pos + __popc(b & ((1u << lane) - 1u))] = (uint32_t)(st * 32 + lane);
     pos += __popc(b);
   }
@@ -225,7 +279,7 @@ __device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
 }
 
 /* work_list_block for launches of at most WARP_LIST_ROWS rows: one warp lists part p, walking
- * the rows 32 at a time (no block-wide scan), so one block serves 32 parts. */
+ * the rows 32 at a time (no block-wide scan), so one block serves a part per warp. */
 constexpr int64_t WARP_LIST_ROWS = 256;
 __device__ __forceinline__ void work_list_warp(int p, const uint32_t *rowrun, const uint32_t *pmask,
                                                int pmw, uint32_t *work, int n_parts, int64_t rows) {
@@ -252,7 +306,7 @@ __device__ __forceinline__ void work_list_warp(int p, const uint32_t *rowrun, co
 /* The split form's row-level work between classify and execute in one launch: blocks
  * [0, n_pre) scan the pre-pass carries (one addition each), the other blocks list the parts'
  * rows: one part per block, or, for launches of few rows, one part per warp. */
-__global__ void __launch_bounds__(1024) bg_rows_kernel(uint32_t *pre_bits, int64_t n_tiles,
+__global__ void __launch_bounds__(512, 2) bg_rows_kernel(uint32_t *pre_bits, int64_t n_tiles,
                                                        const int64_t *tile_prefix, int n_inputs,
                                                        int n_pre, const uint32_t *rowrun,
                                                        const uint32_t *pmask, int pmw,
@@ -261,7 +315,7 @@ __global__ void __launch_bounds__(1024) bg_rows_kernel(uint32_t *pre_bits, int64
   if ((int)blockIdx.x < n_pre) {
     carry_scan_block(blockIdx.x, pre_bits, n_tiles, tile_prefix, n_inputs);
   } else if (rows <= WARP_LIST_ROWS) {
-    const int p = ((int)blockIdx.x - n_pre) * 32 + (int)(threadIdx.x >> 5);
+    const int p = ((int)blockIdx.x - n_pre) * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
     if (p < n_parts) work_list_warp(p, rowrun, pmask, pmw, work, n_parts, rows);
   } else {
     work_list_block(blockIdx.x - n_pre, rowrun, pmask, pmw, work, n_parts, rows);
@@ -940,8 +994,9 @@ static int launch_passes(const bg_program *prog, BgParams &prm, int grid, cudaSt
     cfg.attrs = &pdl;
     cfg.numAttrs = 1;
     const int n_parts = std::max(1, prog->desc.n_parts);
-    cfg.gridDim = dim3(prog->desc.n_pre + (rows <= WARP_LIST_ROWS ? (n_parts + 31) / 32 : n_parts));
-    cfg.blockDim = dim3(1024);
+    /* 512 threads, two blocks per SM: one wave for up to 2 x SMs parts and additions */
+    cfg.gridDim = dim3(prog->desc.n_pre + (rows <= WARP_LIST_ROWS ? (n_parts + 15) / 16 : n_parts));
+    cfg.blockDim = dim3(512);
     BG_CUDA(cudaLaunchKernelEx(&cfg, bg_rows_kernel, prm.pre_bits, prm.n_tiles,
                                (const int64_t *)prm.tile_prefix, (int)prm.n_inputs,
                                (int)prog->desc.n_pre,
