@@ -2117,7 +2117,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"    const unsigned int gb = bg_pref[bg_gpos[grp]], ge = bg_pref[bg_gpos[grp + 1]];\n"
         f"    unsigned int it0 = 0u;\n"
         f"    if (t.lane == 0)\n"
-        f"      it0 = gb < ge && !((*(volatile unsigned int *)&bg_spent >> grp) & 1u) ? gb + atomicAdd(p.work + grp, {tuning.exec_claim}u) : ge;\n"
+        f"      it0 = gb < ge && !((*(volatile unsigned int *)&bg_spent >> grp) & 1u) ? gb + atomicAdd(p.work + grp * BG_CLAIM_STRIDE, {tuning.exec_claim}u) : ge;\n"
         f"    it0 = __shfl_sync(FULL, it0, 0);\n"
         f"    if (it0 >= ge) {{\n"
         f"      if (t.lane == 0) atomicOr(&bg_spent, 1u << grp);\n"

@@ -57,7 +57,8 @@ typedef struct BgParams {
   uint32_t *pre_bits;        /* pre-pass bitmaps, 3 * ceil(n_tiles / 32) words per addition */
   uint32_t *work;            /* split form, R = ceil(n_tiles / 32) rows of 32 tiles, H =
                                 BG_WORK_HEAD: [0, H) the execute pass's claim counters (one
-                                per group of SMs); [H + p] = number of rows part p runs on; at
+                                per group of SMs, BG_CLAIM_STRIDE words apart);
+                                [H + p] = number of rows part p runs on; at
                                 H + n_parts + p * R those rows (ascending); at
                                 H + n_parts * (1 + R) the OR of each row's run masks, [n_run][R] */
   int32_t n_inputs;
@@ -66,7 +67,10 @@ typedef struct BgParams {
                                 1..32, a power of two (the runtime's choice per launch)       */
 } BgParams;
 
-/* Words before the part counts in BgParams.work: the execute pass's claim counters. */
-#define BG_WORK_HEAD 16
+/* Words before the part counts in BgParams.work: the execute pass's claim counters, one per
+ * group of SMs (at most 16), each in its own 128-byte line so that the groups' atomic claims
+ * do not queue on one line. */
+#define BG_CLAIM_STRIDE 32
+#define BG_WORK_HEAD (16 * BG_CLAIM_STRIDE)
 
 #endif

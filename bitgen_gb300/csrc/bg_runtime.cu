@@ -217,7 +217,8 @@ __device__ __forceinline__ void work_list_block(int p, const uint32_t *rowrun,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
   uint32_t *out = work + BG_WORK_HEAD + n_parts + (int64_t)p * rows;
-  if (p == 0 && threadIdx.x < BG_WORK_HEAD) work[threadIdx.x] = 0u;
+  if (p == 0)
+    for (int i = threadIdx.x; i < BG_WORK_HEAD; i += blockDim.x) work[i] = 0u;
   const int64_t steps = (rows + 31) / 32;
   const int64_t per = (steps + nwarps - 1) / nwarps;
   const int64_t s0 = (int64_t)warp * per < steps ? (int64_t)warp * per : steps;
@@ -286,7 +287,8 @@ __device__ __forceinline__ void work_list_warp(int p, const uint32_t *rowrun, co
   const int lane = threadIdx.x & 31;
   const uint32_t *pm = pmask + (int64_t)p * pmw * 2;
   uint32_t *out = work + BG_WORK_HEAD + n_parts + (int64_t)p * rows;
-  if (p == 0 && lane < BG_WORK_HEAD) work[lane] = 0u;
+  if (p == 0)
+    for (int i = lane; i < BG_WORK_HEAD; i += 32) work[i] = 0u;
   uint32_t pos = 0;
   for (int64_t st = 0; st * 32 < rows; ++st) {
     const int64_t r = st * 32 + lane;

@@ -186,7 +186,7 @@ int bg_plan_destroy(bg_plan *plan);
  *
  * Limit: for T tiles of (32 - halo_lanes - tail_lanes) * wpt words and R = ceil(T / 32), the
  * scratch must hold max(1, additions) * T + ceil(3 * n_pre * R / 2) + ceil(n_run * T / 2) +
- * ceil(w / 2) 64-bit words out of BG_NOALLOC_RECORDS, where w = n_parts * (R + 1) + 16 +
+ * ceil(w / 2) 64-bit words out of BG_NOALLOC_RECORDS, where w = n_parts * (R + 1) + 512 +
  * n_run * R for the split form (n_run > 0) and 0 otherwise.  Larger inputs are rejected with BG_ERR_CAPACITY before
  * anything is enqueued, and bg_last_error() gives the sizes and the largest input that fits.
  * The first call on each device looks up the array's device address once

@@ -102,7 +102,7 @@ def test_limit_is_exact_and_enforced(program, cuda):
 
     def words(tiles):   # the scratch rule stated in include/bitgen_gb300.h
         rows = -(-tiles // 32)
-        w = s.n_parts * (rows + 1) + 16 + s.n_run * rows if s.n_run else 0
+        w = s.n_parts * (rows + 1) + 512 + s.n_run * rows if s.n_run else 0
         return (max(1, s.n_adds) * tiles + (3 * s.n_pre * rows + 1) // 2
                 + (s.n_run * tiles + 1) // 2 + (w + 1) // 2)
     lo, hi = 1, RECORDS
@@ -136,7 +136,7 @@ def _max_bytes(prog: Program) -> int:
 
     def words(tiles):   # the scratch rule stated in include/bitgen_gb300.h
         rows = -(-tiles // 32)
-        w = s.n_parts * (rows + 1) + 16 + s.n_run * rows if s.n_run else 0
+        w = s.n_parts * (rows + 1) + 512 + s.n_run * rows if s.n_run else 0
         return (max(1, s.n_adds) * tiles + (3 * s.n_pre * rows + 1) // 2
                 + (s.n_run * tiles + 1) // 2 + (w + 1) // 2)
     lo, hi = 1, RECORDS
