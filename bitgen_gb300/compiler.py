@@ -1372,6 +1372,7 @@ def build_dag(groups: Sequence[Group], per_regex: bool = False) -> Tuple[Dag, Li
 
 
 SMEM_BUDGET = 48 * 1024
+WCOUNT_MAX = 64    # split-form programs with at most this many outputs keep match counts per warp
 # Passes that visit every tile once without waiting take chunks of 32 consecutive tiles per warp,
 # so that each pre-pass addition's aggregate bits of a chunk fill one word (pre_collect/flush).
 _CHUNK_HEAD = (
@@ -1554,11 +1555,17 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
     else:
         calls = "\n".join(f"    bg_part_{ci}_1(p, t, acc, {ba});" for ci in range(len(clusters)))
     comments = "\n".join(f"/* output {o}: {nm.replace('*/', '* /')} */" for o, nm in enumerate(names))
+    # (the single-kernel form adds each tile's counts directly: a count cache measured slower
+    # there, its registers being taken by the terms)
+    wcount = 0
+    counts_begin = (f"  __shared__ unsigned long long bg_cnt_s[{warps} * {max(1, wcount)}];\n"
+                    f"  if (BG_WCOUNT > 0) count_cache_begin(t, bg_cnt_s + (threadIdx.x >> 5) * BG_WCOUNT);\n")
     kernel_free = (
         f"  __shared__ uint32_t bg_acc[{warps} * BG_NOUT * BG_WPT * 32];\n"
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
+        + counts_begin +
         f"  while (next_tile(p, t)) {{\n"
         f"    acc_clear(acc, t);\n"
         f"    S b[8];\n"
@@ -1566,6 +1573,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"{calls}\n"
         f"    acc_store(p, t, acc);\n"
         f"  }}\n"
+        f"  flush_counts(p, t);\n"
         f"}}\n")
     lock_calls = "\n".join(f"    if (has) bg_part_{ci}_1(p, t, acc, {ba});\n    __syncthreads();"
                             for ci in range(len(clusters)))
@@ -1575,6 +1583,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * (BG_NOUT * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
+        + counts_begin +
         f"  for (;;) {{\n"
         f"    const unsigned int g0 = claim_block(p, &bg_claim);\n"
         f"    if ((long long)g0 >= p.n_tiles) break;\n"
@@ -1585,6 +1594,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"{lock_calls}\n"
         f"    if (has) acc_store(p, t, acc);\n"
         f"  }}\n"
+        f"  flush_counts(p, t);\n"
         f"}}\n")
     # registers a thread may use so that min_blocks blocks fit: each of the SM's four
     # sub-partitions holds 16K registers for its share of the resident warps
@@ -1615,6 +1625,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"#define BG_HL {gen.hl}\n"
         f"#define BG_TL {gen.tl}\n"
         f"#define BG_NOUT {n_out}\n"
+        f"#define BG_WCOUNT {wcount}\n"
         f"#define BG_LOOKBACK_INLINE {int(tuning.inline_lookback)}\n"
         f"#define BG_LBK {tuning.lookback_width}\n"
         f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
@@ -2060,6 +2071,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_HL {gen.hl}\n"
         f"#define BG_TL {gen.tl}\n"
         f"#define BG_NOUT {len(names)}\n"
+        f"#define BG_WCOUNT {len(names) if len(names) <= WCOUNT_MAX else 0}\n"
         f"#define BG_LOOKBACK_INLINE {int(tuning.inline_lookback)}\n"
         f"#define BG_LBK {tuning.lookback_width}\n"
         f"#define BG_LB_SPIN {tuning.lookback_spin}\n"
@@ -2086,6 +2098,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *acc = bg_acc + (threadIdx.x >> 5) * ({nacc} * BG_WPT * 32);\n"
         f"  Tile t;\n"
         f"  init(p, t);\n"
+        f"  __shared__ unsigned long long bg_cnt_s[{warps} * BG_WCOUNT + 1];\n"
+        f"  if (BG_WCOUNT > 0) count_cache_begin(t, bg_cnt_s + (threadIdx.x >> 5) * BG_WCOUNT);\n"
         f"  __shared__ unsigned int bg_pref[{len(parts) + 1}];\n"
         f"  __shared__ unsigned int bg_spent;  /* bit g: the block saw group g's items run out */\n"
         f"  if (threadIdx.x == 0) bg_spent = 0u;\n"
@@ -2163,6 +2177,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"      }}\n"
         f"    }}\n"
         f"  }}\n"
+        f"  flush_counts(p, t);\n"
         f"}}\n")
     return KernelSpec(source=src, name=name, n_outputs=len(names), n_adds=len(gen.adds),
                       halo_lanes=gen.hl, wpt=wpt, block=tuning.block, max_depth_bits=gen.max_dbits,

@@ -162,6 +162,8 @@ struct Tile {
   S vm;              /* per word: all ones if the word index is >= 0     */
   S em;              /* per word: the bits of positions before the input end */
   bool edge;         /* the tile has words before the input start or reaches its last word */
+  unsigned long long *cnt_s; /* the warp's match counts of `input` per output, in shared memory
+                                (added to counts when the input changes and at the end), or NULL */
   uint32_t pcin[NPRE_WORDS]; /* bit k: carry entering pre-pass addition k (warp-uniform)   */
 };
 
@@ -629,6 +631,7 @@ __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
   t.lane = threadIdx.x & 31;
   t.input = 0;
   t.first = t.last = 0;   /* no input held yet */
+  t.cnt_s = nullptr;
   t.epoch = *(volatile const unsigned long long *)(p.state + 2);
 }
 
@@ -652,11 +655,36 @@ __device__ __forceinline__ void load_pre_carries(const BgParams &p, Tile &t) {
 /* Fill `t` for global tile g.  `carries`: read the pre-pass carries (false in the passes that
  * run before the carry scan); `debug_wait`: take part in the wait-limit test (exactly one pass
  * over every tile does). */
+#ifndef BG_WCOUNT
+#define BG_WCOUNT 0
+#endif
+/* Match counts kept per warp (BG_WCOUNT outputs): counts[o][input] gets one atomic add per
+ * output and input a warp worked on, instead of one per tile and output (the counts of all
+ * outputs share a few cache lines, whose atomics would queue). */
+__device__ __forceinline__ void count_cache_begin(Tile &t, unsigned long long *slots) {
+  t.cnt_s = slots;
+  for (int o = t.lane; o < BG_WCOUNT; o += 32) slots[o] = 0ull;
+  __syncwarp();
+}
+__device__ __forceinline__ void flush_counts(const BgParams &p, const Tile &t) {
+  if (BG_WCOUNT == 0 || t.cnt_s == nullptr) return;
+  __syncwarp();
+  for (int o = t.lane; o < BG_WCOUNT; o += 32) {
+    const unsigned long long c = t.cnt_s[o];
+    if (c) {
+      if (p.counts) atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, c);
+      t.cnt_s[o] = 0ull;
+    }
+  }
+  __syncwarp();
+}
+
 __device__ __forceinline__ void setup_tile(const BgParams &p, Tile &t, unsigned int g,
                                            bool carries = true, bool debug_wait = true) {
   /* find i: prefix[i] <= g < prefix[i+1]; a warp's tiles mostly stay in the input of its
    * previous tile, whose bounds and length the tile holds (no loads then) */
   if (!((long long)g >= t.first && (long long)g < t.last)) {
+    flush_counts(p, t);   /* the counts gathered for the previous input */
     int lo = 0, hi = p.n_inputs;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -841,8 +869,10 @@ static __device__ __forceinline__ void store_new_bits(const BgParams &p, const T
   if (p.counts) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(FULL, cnt, d);
-    if (t.lane == 0 && cnt)
-      atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, (unsigned long long)cnt);
+    if (t.lane == 0 && cnt) {
+      if (BG_WCOUNT > 0 && t.cnt_s != nullptr && o < BG_WCOUNT) t.cnt_s[o] += cnt;
+      else atomicAdd(p.counts + (long long)o * p.n_inputs + t.input, (unsigned long long)cnt);
+    }
   }
 }
 
