@@ -593,6 +593,7 @@ class Tuning:
     push_advances: bool = True   # single-kernel form: Advances pushed through single-use
                                  # AND/OR/XOR down to the character classes, each class shifted
                                  # once per distance; a word read from another lane is shared
+    claim_tiles: int = 4         # single-kernel form: consecutive tiles a warp claims at once
     chain_batch: int = 8         # with push_advances: AND chains re-associated distance-major,
                                  # this many at a time (0: each chain computed on its own)
 
@@ -603,7 +604,7 @@ class Tuning:
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
                 self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim,
-                self.push_advances, self.chain_batch, self.single_edge)
+                self.push_advances, self.chain_batch, self.single_edge, self.claim_tiles)
 
 
 @dataclass
@@ -1626,6 +1627,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         f"#define BG_TL {gen.tl}\n"
         f"#define BG_NOUT {n_out}\n"
         f"#define BG_WCOUNT {wcount}\n"
+        f"#define BG_CLAIM_TILES {max(1, tuning.claim_tiles)}\n"
         f"#define BG_LOOKBACK_INLINE {int(tuning.inline_lookback)}\n"
         f"#define BG_LBK {tuning.lookback_width}\n"
         f"#define BG_LB_SPIN {tuning.lookback_spin}\n"

@@ -162,6 +162,8 @@ struct Tile {
   S vm;              /* per word: all ones if the word index is >= 0     */
   S em;              /* per word: the bits of positions before the input end */
   bool edge;         /* the tile has words before the input start or reaches its last word */
+  unsigned int claim_g;      /* next_tile: the last tile handed out of the current claim  */
+  int claim_left;            /* next_tile: tiles of the current claim not yet handed out  */
   unsigned long long *cnt_s; /* the warp's match counts of `input` per output, in shared memory
                                 (added to counts when the input changes and at the end), or NULL */
   uint32_t pcin[NPRE_WORDS]; /* bit k: carry entering pre-pass addition k (warp-uniform)   */
@@ -632,6 +634,8 @@ __device__ __forceinline__ void init(const BgParams &p, Tile &t) {
   t.input = 0;
   t.first = t.last = 0;   /* no input held yet */
   t.cnt_s = nullptr;
+  t.claim_g = 0u;
+  t.claim_left = 0;
   t.epoch = *(volatile const unsigned long long *)(p.state + 2);
 }
 
@@ -738,10 +742,22 @@ __device__ __forceinline__ void setup_tile_in(const BgParams &p, Tile &t, unsign
 
 /* Claim the next tile (tiles are handed out in increasing order, which is what makes the
  * look-back deadlock free: a tile only waits for tiles claimed before it). */
+#ifndef BG_CLAIM_TILES
+#define BG_CLAIM_TILES 1
+#endif
 __device__ __forceinline__ bool next_tile(const BgParams &p, Tile &t) {
+  /* BG_CLAIM_TILES consecutive tiles per claim (fewer atomics on the one counter); the warp
+   * runs them in order, so every tile still waits only for tiles claimed before it */
   unsigned int g = 0;
-  if (t.lane == 0) g = atomicAdd(p.state, 1u);
-  g = __shfl_sync(FULL, g, 0);
+  if (BG_CLAIM_TILES > 1 && t.claim_left > 0) {
+    g = ++t.claim_g;
+    --t.claim_left;
+  } else {
+    if (t.lane == 0) g = atomicAdd(p.state, (unsigned int)BG_CLAIM_TILES);
+    g = __shfl_sync(FULL, g, 0);
+    t.claim_g = g;
+    t.claim_left = BG_CLAIM_TILES - 1;
+  }
   if ((long long)g >= p.n_tiles) return false;
   setup_tile(p, t, g);
   return true;
