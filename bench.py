@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--dna-bytes", type=int, default=1 << 30, help="DNA text of the dna leg")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip the reference's generated kernel in the dna leg (profiling runs)")
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the served leg and print its JSON")
     ap.add_argument("--dna-only", action="store_true",
                     help="run only the dna leg and print its JSON (profiling the DNA kernel)")
     return ap.parse_args()
@@ -614,6 +616,10 @@ def main():
     import numpy as np
     import torch
     import torch.distributed as dist
+
+    if args.served_only:
+        print(json.dumps(served_leg(torch.device("cuda", 0), args.served_requests)), flush=True)
+        return
 
     if args.dna_only:
         print(json.dumps(dna_leg(torch.device("cuda", 0), args.dna_bytes, max(1, args.steps),
