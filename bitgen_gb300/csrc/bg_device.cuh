@@ -1093,14 +1093,16 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t r
       untranspose32(o, raw[j]);
     }
     if (!BG_BASIS_FILTER) {
-      if (t.lane < BG_NRUN) run[32 * t.lane] = FULL;
+      for (int w = t.lane; w < BG_NRUN; w += 32) run[32 * w] = FULL;
       return;
     }
   } else {
 #pragma unroll
     for (int j = 0; j < WPT; ++j) load_word_bytes(p, t, j, raw[j]);
   }
-  if (t.lane < BG_NRUN) run[32 * t.lane] = c.always[t.lane];
+  /* every run word of the tile starts from the terms that always run (a lane per word, more
+     than 32 words in turns) */
+  for (int w = t.lane; w < BG_NRUN; w += 32) run[32 * w] = c.always[w];
   uint32_t prev = __shfl_up_sync(FULL, raw[WPT - 1][7], 1);
   if (t.lane == 0) prev = 0u;
   constexpr uint32_t KEEP = NPROBE == 32 ? FULL : ~((1u << (32 - NPROBE)) - 1u);
@@ -1122,7 +1124,7 @@ __device__ __forceinline__ void load_scan(const BgParams &p, Tile &t, uint32_t r
     if (n > BG_HIT_CAP) {
       /* more hits than the chunk's record buffer holds (text dense in filter keys): every
        * term runs on this tile, which is exact, and its hits need no lookup */
-      if (t.lane < BG_NRUN) run[32 * t.lane] = FULL;
+      for (int w = t.lane; w < BG_NRUN; w += 32) run[32 * w] = FULL;
       return;
     }
 #pragma unroll

@@ -195,11 +195,6 @@ class Server:
         plan = slot.plans[pset]
         plan.set_layout(Inputs(slot.dev_in, N.BG_INPUT_BYTES, offs, lens), out_offs, total, sp)
         out_ptr = slot.dev_out.data_ptr() if slot.dev_out is not None else 0
-        if slot.dev_out is not None:
-            # the batch's output rows start from zeros: scans of large pattern sets (1024
-            # regexes) over outputs that hold an earlier batch's bits measured many times slower
-            with torch.cuda.stream(s):
-                slot.dev_out.view(-1)[:prog.n_outputs * total].zero_()
         plan.launch(slot.dev_in.data_ptr(), out_ptr, slot.dev_counts.data_ptr(), sp)
         with torch.cuda.stream(s):
             n = len(batch)
@@ -301,11 +296,6 @@ def serve_plain(programs: Dict[str, Program], requests: Sequence[Request], devic
     dev_in = torch.empty(biggest + ALIGN, dtype=torch.uint8, device=device)
     host_in = torch.empty(biggest + ALIGN, dtype=torch.uint8).pin_memory()
     max_out = max(p.n_outputs for p in programs.values())
-    # output rows for programs that merge outputs across parts, zeroed before each launch as
-    # the reference runner's reset_tensor does (bitgen/from_icgrep.py:546-552)
-    merges = any(p.merges for p in programs.values())
-    dev_out = (torch.empty(max_out * (-(-biggest // 32) + 4), dtype=torch.uint32, device=device)
-               if merges else None)
     dev_counts = torch.empty(max_out, dtype=torch.int64, device=device)
     host_counts = torch.empty(max_out, dtype=torch.int64).pin_memory()
     plans = {name: Plan.reserve(p, N.BG_INPUT_BYTES, 1, biggest // (32 * p.spec.tile_words) + 2)
@@ -330,12 +320,7 @@ def serve_plain(programs: Dict[str, Program], requests: Sequence[Request], devic
             dev_in[:r.data.size].copy_(src, non_blocking=True)
         offs, words, total = out_layout([r.data.size])
         plans[r.pset].set_layout(Inputs(dev_in, N.BG_INPUT_BYTES, [0], [int(r.data.size)]), offs, total, sp)
-        out_ptr = 0
-        if dev_out is not None and prog.merges:
-            with torch.cuda.stream(stream):
-                dev_out[:prog.n_outputs * total].zero_()
-            out_ptr = dev_out.data_ptr()
-        plans[r.pset].launch(dev_in.data_ptr(), out_ptr, dev_counts.data_ptr(), sp)
+        plans[r.pset].launch(dev_in.data_ptr(), 0, dev_counts.data_ptr(), sp)
         with torch.cuda.stream(stream):
             host_counts[:prog.n_outputs].copy_(dev_counts[:prog.n_outputs], non_blocking=True)
         plans[r.pset].sync(sp)

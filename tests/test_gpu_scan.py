@@ -377,3 +377,25 @@ def test_text_dense_in_filter_keys(cuda, every):
     for k, w in enumerate(want):
         assert first_diff(res.stream(k, 0).cpu().numpy(), w[:W]) is None, k
     assert res.counts[:, 0].tolist() == counts
+
+
+@pytest.mark.parametrize("every", [4096, 64])
+def test_more_than_1024_terms(cuda, every):
+    """1024 regexes (more than 1024 terms, so more than 32 run-mask words per tile): every run
+    word starts from the terms that always run and, past the record buffer, every word runs
+    everything.  The scan is repeated over the same output and counts buffers, which must not
+    change its result.  Streams equal the C oracle's."""
+    from oracle import cpu
+    ps = workloads.throughput_patterns(seed=83, n=1024)
+    groups = [compile_group(g) for g in ps.groups(16)]
+    text = workloads.plant(workloads.printable_text(300_000, 63), ps.witnesses, every, 64)
+    prog = Program(groups)
+    assert prog.spec.n_parts > 0 and prog.spec.n_run > 32
+    inp = pack_bytes([text])
+    want, counts = cpu.run_groups(groups, text)
+    W = (text.size + 31) // 32
+    for _ in range(2):
+        res = prog.scan(inp)
+        for k, w in enumerate(want):
+            assert first_diff(res.stream(k, 0).cpu().numpy(), w[:W]) is None, k
+        assert res.counts[:, 0].tolist() == counts
