@@ -106,3 +106,22 @@ def test_pushed_dag_shifts_classes_not_markers():
     off = generate_kernel(groups, Tuning(push_advances=False))
     assert off.source.count("__funnelshift_r") > spec.source.count("__funnelshift_r") or \
         off.source.count("__shfl_up_sync") > spec.source.count("__shfl_up_sync")
+
+
+def test_cluster_chains_batches_share_classes():
+    """Batches are at most `batch` chains, cover every chain once, and a batch formed around
+    shared shifted classes needs fewer distinct classes than chains taken in id order."""
+    from bitgen_gb300.compiler import _cluster_chains
+    leaves = {
+        1: [(10, 0), (11, 1)], 2: [(20, 0), (21, 1)], 3: [(10, 0), (11, 1), (12, 2)],
+        4: [(20, 0), (21, 1), (22, 2)], 5: [(10, 0)], 6: [(20, 0)],
+    }
+    members = sorted(leaves)
+    groups = _cluster_chains(members, leaves, 3)
+    assert sorted(x for g in groups for x in g) == members
+    assert all(len(g) <= 3 for g in groups)
+    distinct = sum(len({lf for r in g for lf in leaves[r]}) for g in groups)
+    in_order = sum(len({lf for r in members[i:i + 3] for lf in leaves[r]}) for i in range(0, 6, 3))
+    assert distinct < in_order
+    # few chains: one batch, in order
+    assert _cluster_chains([3, 1], leaves, 8) == [[3, 1]]
