@@ -378,7 +378,7 @@ def transpose_leg(dev, n_bytes=1 << 30, reps=20, check_bytes=1 << 20, cpu_bytes=
 def dna_leg(dev, n_bytes, steps, check_bytes, ref_gpu=True):
     """64 IUPAC motifs (6-20 bases, every fourth split by a gap .{a,b}, 3 <= a <= 5, b <= a + 4) in 4 groups over DNA text
     (i.i.d. A/C/G/T, GC 42%, N runs, 80-column lines, 2^16 planted motif instances); per-group
-    streams and counts, the program's default tuning (on a 4-letter text the trigram filter
+    streams and counts, the program's default tuning (on a 4-letter text the q-gram filter
     passes nearly every tile, so the compiler picks the single-kernel form)."""
     import torch
     from bitgen_gb300 import workloads

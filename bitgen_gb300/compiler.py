@@ -554,7 +554,7 @@ class Tuning:
     block: int = 256        # threads per CTA
     skip_interval: int = -1  # check for an all-zero marker every k AND steps (0 = never; -1:
                              # never in the split form, whose tiles mostly hold the marker's
-                             # trigram, nor when unselective filters choose the single-kernel
+                             # q-gram, nor when unselective filters choose the single-kernel
                              # form; every AND when the single-kernel form is forced)
     part_cap: int = 0       # most OR-ed terms one part function computes (0: 2 in the split
                             # form, 64 in the single-kernel form)
@@ -566,7 +566,7 @@ class Tuning:
     lookback_width: int = 1  # predecessor records each lane examines per look-back step
     lookback_spin: int = 0   # look-back polls before sleeping
     carry_prepass: bool = True  # carries of wide-class additions from a pre-pass, not look-back
-    prefilter: bool = True   # run a term only in tiles holding one of its trigrams
+    prefilter: bool = True   # run a term only in tiles holding one of its q-grams
     bloom_bits: int = 20     # prefilter: log2 of the Bloom bitmap's size (shared memory)
     cls_block: int = 1024    # split form: threads per classify block (one block per SM holds
                              # the Bloom bitmap, the exact keys and the warps' run masks)
@@ -1660,7 +1660,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     """The split, prefiltered form of the program: two kernels.
 
     ``<name>_cls`` (classify) visits every tile once, with nothing to wait for: it scans the
-    tile's trigrams (bg_device.cuh load_scan), publishes the carry pre-pass aggregates, adds the
+    tile's q-grams (bg_device.cuh load_scan), publishes the carry pre-pass aggregates, adds the
     terms whose look-back additions could take or owe a carry (class all ones at the carry lane
     or at the successor's) and those whose filter holds only through a pre-pass carry, and
     writes the tile's run mask (one bit per term) to ``p.runs``.

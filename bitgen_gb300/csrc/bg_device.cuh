@@ -53,7 +53,7 @@
 #define BG_NPRE 0 /* additions whose carries are computed by the pre-pass (numbered first) */
 #endif
 #ifndef BG_NRUN
-#define BG_NRUN 1 /* words of the per-tile run mask (trigram prefilter) */
+#define BG_NRUN 1 /* words of the per-tile run mask (q-gram prefilter) */
 #endif
 #ifndef BG_BLOOM_BITS
 #define BG_BLOOM_BITS 16 /* log2 of the prefilter's Bloom bitmap size */
