@@ -16,7 +16,9 @@ have the same set of match ends as their greedy forms and are compiled alike.
 
 Supported syntax: literals and escapes (``\\xHH``, ``\\n \\r \\t \\f \\v \\e \\a``, escaped
 punctuation), classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S``, ``.``,
-groups ``(...)`` / ``(?:...)``, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
+groups ``(...)`` / ``(?:...)``, the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
+and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing
+group or ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
 and ``$`` where nothing can follow it (end of the regex or of a final alternative): a match ending
 at p counts only if byte p+1 is LF or p is the last position, i.e.
 ``L & ~Lookahead(~LF, 1)``.
@@ -90,10 +92,21 @@ _CLASS_ESC = {"d": DIGIT, "D": ALL_BYTES - DIGIT, "w": WORD, "W": ALL_BYTES - WO
               "s": SPACE, "S": ALL_BYTES - SPACE}
 
 
+def _fold(bs) -> frozenset:
+    """The byte set with both cases of every ASCII letter in it."""
+    out = set(bs)
+    for b in bs:
+        if 0x41 <= b <= 0x5A or 0x61 <= b <= 0x7A:
+            out.add(b ^ 0x20)
+    return frozenset(out)
+
+
 class _Parser:
     def __init__(self, s: str):
         self.s = s
         self.i = 0
+        self.icase = False    # (?i): ASCII letters match either case
+        self.dotall = False   # (?s): '.' matches LF too
 
     def peek(self):
         return self.s[self.i] if self.i < len(self.s) else None
@@ -161,33 +174,68 @@ class _Parser:
             return False
         return re.fullmatch(r"\d+(,\d*)?|,\d+", self.s[self.i + 1:j]) is not None
 
+    def _flags(self):
+        """Parse the letters of a `(?flags` group up to ':' or ')'; returns (icase, dotall, end)
+        with the flags as they hold inside and `end` the closing character."""
+        icase, dotall, on = self.icase, self.dotall, True
+        while True:
+            c = self.peek()
+            if c is None:
+                raise UnsupportedRegex("unterminated group flags")
+            self.take()
+            if c in ":)":
+                return icase, dotall, c
+            if c == "-":
+                on = False
+            elif c == "i":
+                icase = on
+            elif c == "s":
+                dotall = on
+            elif c == "m":
+                pass    # ^ and $ already hold at every line (grep line semantics)
+            else:
+                raise UnsupportedRegex(f"group flag {c!r} is not supported")
+
     def atom(self):
         c = self.take()
         if c == "(":
+            saved = (self.icase, self.dotall)
             if self.s.startswith("?:", self.i):
                 self.i += 2
+            elif self.peek() == "?" and self.i + 1 < len(self.s) and self.s[self.i + 1] in "imsx-":
+                self.take()
+                icase, dotall, end = self._flags()
+                if end == ")":
+                    # (?flags): the flags hold to the end of the enclosing group
+                    self.icase, self.dotall = icase, dotall
+                    return Seq(())
+                self.icase, self.dotall = icase, dotall
             elif self.peek() == "?":
-                raise UnsupportedRegex("group modifiers other than (?: are not supported")
+                raise UnsupportedRegex("group modifiers other than (?: and flags are not supported")
             node = self.alt()
             if self.peek() != ")":
                 raise UnsupportedRegex("missing )")
             self.take()
+            self.icase, self.dotall = saved
             return node
         if c == "[":
             return CC(self.cls())
         if c == ".":
-            return CC(DOT)
+            return CC(ALL_BYTES if self.dotall else DOT)
         if c == "^":
             return Start()
         if c == "$":
             return End()
         if c == "\\":
             e = self.escape()
-            return CC(e) if isinstance(e, frozenset) else CC(frozenset([e]))
+            return CC(e) if isinstance(e, frozenset) else CC(self._lit(e))
         if c in "*+?":
             raise UnsupportedRegex(f"nothing to repeat at {self.i - 1}")
         b = c.encode("latin1")
-        return CC(frozenset([b[0]]))
+        return CC(self._lit(b[0]))
+
+    def _lit(self, b: int) -> frozenset:
+        return _fold([b]) if self.icase else frozenset([b])
 
     def escape(self):
         c = self.take()
@@ -237,7 +285,7 @@ class _Parser:
                 items |= set(range(lo, hi + 1))
             else:
                 items.add(lo)
-        s = frozenset(items)
+        s = _fold(items) if self.icase else frozenset(items)
         if neg:
             s = ALL_BYTES - s - {LF}
         return s

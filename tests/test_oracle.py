@@ -114,6 +114,28 @@ def test_emitter_matches_nfa_and_python_re(matchstar_form):
             assert run_group(g, data) == match_ends(r, data) == want_re, (r, data)
 
 
+FLAG_REGEXES = [r"(?i)abc", r"(?i)a[b-d]+e", r"x(?i:yz)w", r"(?i)x(?-i:y)z", r"(?s)a.b",
+                r"(?i)[^a]b", r"a(?s:.)c", r"(?i)\x41b", r"(?im)^ab", r"(?i:a|B)c"]
+
+
+@pytest.mark.parametrize("matchstar_form", [True, False])
+def test_emitter_flags_match_nfa_and_python_re(matchstar_form):
+    """Inline flags: i (ASCII case-insensitive), s (dot matches LF), m (no effect), global
+    and scoped, against Python's re on mixed-case text with line feeds."""
+    rnd = random.Random(11)
+    for r in FLAG_REGEXES:
+        g = parse_pablo(compile_regex(r, matchstar=matchstar_form).to_pablo())
+        pr = re.compile(r.replace("[^", "[^\\n").encode(), re.M)
+        for _ in range(6):
+            n = rnd.randint(0, 90)
+            data = bytes(rnd.choice(b"aAbBcCdDeExXyYzZwW\n0") for _ in range(n))
+            want_re = 0
+            for e in range(n):
+                if any(pr.fullmatch(data, s, e + 1) for s in range(e + 1)):
+                    want_re |= 1 << e
+            assert run_group(g, data) == match_ends(r, data) == want_re, (r, data)
+
+
 def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
     """The genomic motif grammar (IUPAC classes, gapped `.{lo,hi}` motifs) over DNA text with N
     runs, line feeds and planted motifs: emitter + big-int oracle == NFA == C evaluator."""
@@ -132,7 +154,7 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$b", "(?=x)", r"\bword", "a++"):
+    for r in ("a$b", "(?=x)", r"\bword", "a++", "(?x)a b", "(?i"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
 
