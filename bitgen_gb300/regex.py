@@ -16,6 +16,7 @@ have the same set of match ends as their greedy forms and are compiled alike.
 
 Supported syntax: literals and escapes (``\\xHH``, ``\\n \\r \\t \\f \\v \\e \\a``, escaped
 punctuation), classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S``, ``.``,
+word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class),
 groups ``(...)`` / ``(?:...)``, the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
 and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing
 group or ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
@@ -79,6 +80,13 @@ class Start:
 @dataclass(frozen=True)
 class End:
     pass
+
+
+@dataclass(frozen=True)
+class WordB:
+    """``\\b`` (or ``\\B`` with neg): a word/non-word transition between two bytes (the input's
+    ends count as non-word)."""
+    neg: bool = False
 
 
 ALL_BYTES = frozenset(range(256))
@@ -227,6 +235,8 @@ class _Parser:
         if c == "$":
             return End()
         if c == "\\":
+            if self.peek() in ("b", "B"):
+                return WordB(neg=self.take() == "B")
             e = self.escape()
             return CC(e) if isinstance(e, frozenset) else CC(self._lit(e))
         if c in "*+?":
@@ -237,8 +247,10 @@ class _Parser:
     def _lit(self, b: int) -> frozenset:
         return _fold([b]) if self.icase else frozenset([b])
 
-    def escape(self):
+    def escape(self, in_class: bool = False):
         c = self.take()
+        if c == "b" and in_class:
+            return 0x08   # backspace inside a class, as in PCRE
         if c == "x":
             h = self.s[self.i:self.i + 2]
             if len(h) != 2:
@@ -270,7 +282,7 @@ class _Parser:
             first = False
             self.take()
             if c == "\\":
-                lo = self.escape()
+                lo = self.escape(in_class=True)
             else:
                 lo = c.encode("latin1")[0]
             if isinstance(lo, frozenset):
@@ -279,7 +291,7 @@ class _Parser:
             if self.peek() == "-" and self.i + 1 < len(self.s) and self.s[self.i + 1] != "]":
                 self.take()
                 h = self.take()
-                hi = self.escape() if h == "\\" else h.encode("latin1")[0]
+                hi = self.escape(in_class=True) if h == "\\" else h.encode("latin1")[0]
                 if isinstance(hi, frozenset) or hi < lo:
                     raise UnsupportedRegex("bad class range")
                 items |= set(range(lo, hi + 1))
@@ -448,6 +460,26 @@ class _Compiler:
             self.b.top = saved
         return self._eol
 
+    def word_boundary(self, neg: bool):
+        """(after, before): bit p of `after` = a word/non-word transition between bytes p and
+        p + 1, i.e. W ^ Lookahead(W, 1); bit q of `before` = one between bytes q - 1 and q,
+        i.e. Advance(W, 1) ^ W (W = the word class; positions outside the input are non-word).
+        With `neg`, the complements (\\B)."""
+        key = "_wb_neg" if neg else "_wb"
+        hit = getattr(self, key, None)
+        if hit is None:
+            w = self.b.cc(WORD)
+            saved, self.b.top = self.b.top, True
+            la = self.b.emit("lookahead", (w,), shift=1)
+            after = self.b.emit("xor", tuple(sorted((w, la))))
+            before = self.b.emit("xor", tuple(sorted((self.b.ADV(w, 1), w))))
+            if neg:
+                after, before = self.b.NOT(after), self.b.NOT(before)
+            self.b.top = saved
+            hit = (after, before)
+            setattr(self, key, hit)
+        return hit
+
     def sol(self):
         if self._sol is None:
             lf = self.b.cc(frozenset([LF]))
@@ -480,6 +512,9 @@ class _Compiler:
             return (L, P)
         if isinstance(node, Start):
             return ("0", b.AND(self.P(st), self.sol()))
+        if isinstance(node, WordB):
+            after, before = self.word_boundary(node.neg)
+            return (b.AND(st[0], after), b.AND(self.P(st), before))
         if isinstance(node, Rep):
             return self.rep(node, st)
         raise UnsupportedRegex(str(node))

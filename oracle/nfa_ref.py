@@ -12,7 +12,7 @@ regexes' streams (``bitgen/bitstream.py:60-61``).
 
 from __future__ import annotations
 
-from bitgen_gb300.regex import CC, Alt, End, Rep, Seq, Start, parse_regex
+from bitgen_gb300.regex import CC, WORD, Alt, End, Rep, Seq, Start, WordB, parse_regex
 
 LF = 0x0A
 
@@ -43,6 +43,11 @@ class _NFA:
             return a, e
         if isinstance(node, Start):
             a = self.new("sol")
+            e = self.new("eps")
+            self.out[a].append(e)
+            return a, e
+        if isinstance(node, WordB):
+            a = self.new("nwb" if node.neg else "wb")
             e = self.new("eps")
             self.out[a].append(e)
             return a, e
@@ -96,7 +101,7 @@ def match_ends(regex: str, data: bytes) -> int:
     acc = nfa.new("acc")
     nfa.out[end].append(acc)
 
-    def closure(states, sol, eol=False):
+    def closure(states, sol, eol=False, wb=False):
         seen = set()
         stack = list(states)
         while stack:
@@ -111,14 +116,19 @@ def match_ends(regex: str, data: bytes) -> int:
                 stack.extend(nfa.out[s])
             elif k == "eol" and eol:
                 stack.extend(nfa.out[s])
+            elif (k == "wb" and wb) or (k == "nwb" and not wb):
+                stack.extend(nfa.out[s])
         return seen
+
+    def word(q):   # positions outside the input are non-word
+        return 0 <= q < n and data[q] in WORD
 
     result = 0
     cur = set()
     n = len(data)
     for p in range(n):
         sol = p == 0 or data[p - 1] == LF
-        active = closure(cur | {start}, sol)
+        active = closure(cur | {start}, sol, wb=word(p - 1) != word(p))
         byte = data[p]
         nxt = set()
         for s in active:
@@ -126,7 +136,7 @@ def match_ends(regex: str, data: bytes) -> int:
                 nxt.update(nfa.out[s])
         sol_next = byte == LF
         eol_next = p + 1 == n or data[p + 1] == LF
-        cur = closure(nxt, sol_next, eol_next)
+        cur = closure(nxt, sol_next, eol_next, wb=word(p) != word(p + 1))
         if acc in cur:
             result |= 1 << p
     return result

@@ -399,3 +399,26 @@ def test_more_than_1024_terms(cuda, every):
         for k, w in enumerate(want):
             assert first_diff(res.stream(k, 0).cpu().numpy(), w[:W]) is None, k
         assert res.counts[:, 0].tolist() == counts
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_word_boundaries_and_case_flags(cuda, single):
+    """Word boundaries (\\b, \\B: a look-ahead and a shift of the word class) and inline
+    case-insensitive groups, in the split and the single-kernel form: streams and counts equal
+    the C oracle's over text with planted witnesses, per regex and per group."""
+    from oracle import cpu
+    regexes = [r"\bhello\w+world\b", r"(?i)\bselect\s+\*\s+from\b", r"\Bing\b", r"\bzq\d{2,5}\b",
+               r"(?i)passwd", r"x(?i:ab)y\B", r"\b[a-c]{3}\b", r"(?i)\bget /[a-z]+\.php"]
+    wit = [b" helloXworld ", b" SeLeCt * FROM ", b"ringing ", b" zq123 ", b"PassWD", b"xABya",
+           b" abc ", b" gEt /index.php"]
+    groups = [compile_group(regexes[i::3]) for i in range(3)]
+    text = workloads.plant(workloads.printable_text(250_000, 71), wit, 500, 72)
+    prog = Program(groups, tuning=Tuning(prefilter=False) if single else Tuning(), per_regex=True)
+    assert (prog.spec.n_parts == 0) == single
+    res = prog.scan(pack_bytes([text]))
+    want, counts = cpu.run_groups(groups, text, per_regex=True)
+    W = (text.size + 31) // 32
+    for k, w in enumerate(want):
+        assert first_diff(res.stream(k, 0).cpu().numpy(), w[:W]) is None, k
+    assert res.counts[:, 0].tolist() == counts
+    assert min(counts) > 0

@@ -90,16 +90,32 @@ def _probe_hits(f, text):
     return key, pre3, probed, hit
 
 
+class _FlagPatterns:
+    """Word boundaries and case-insensitive groups (PCRE-style rule fragments), with witnesses."""
+    regexes = [r"\bhello\w+world\b", r"(?i)\bselect\s+\*\s+from\b", r"\Bing\b",
+               r"\bzq\d{2,5}\b", r"(?i)passwd", r"x(?i:ab)y\B", r"\b[a-c]{3}\b",
+               r"(?i)\bget /[a-z]+\.php"]
+    witnesses = [b" helloXworld ", b" SeLeCt * FROM ", b"ringing ", b" zq123 ", b"PassWD",
+                 b"xABya", b" abc ", b" gEt /index.php"]
+
+    def groups(self, n):
+        return [self.regexes[i::n] for i in range(n)]
+
+
 @pytest.mark.parametrize("wpt,kind,config", [(1, "throughput", None), (2, "throughput", (4, 2)),
                                              (1, "throughput", (4, 1)), (2, "throughput", (3, 1)),
-                                             (2, "dna", None)])
+                                             (2, "dna", None), (1, "flags", None)])
 def test_prefilter_is_sound(wpt, kind, config):
     """Also on IUPAC motifs over DNA text (the filter the split form would use there if forced;
-    the compiler picks the single-kernel form for it)."""
+    the compiler picks the single-kernel form for it), and on word boundaries and
+    case-insensitive groups."""
     n = 300_000
     if kind == "dna":
         ps = workloads.dna_motifs(24, seed=5)
         text = workloads.plant(workloads.dna_text(n, seed=43), ps.witnesses, 700, 42)
+    elif kind == "flags":
+        ps = _FlagPatterns()
+        text = workloads.plant(workloads.printable_text(n, 44), ps.witnesses, 300, 45)
     else:
         ps = workloads.throughput_patterns(seed=3, n=64)
         text = workloads.plant(workloads.printable_text(n, 41), ps.witnesses, 700, 42)
