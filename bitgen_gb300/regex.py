@@ -16,7 +16,8 @@ have the same set of match ends as their greedy forms and are compiled alike.
 
 Supported syntax: literals and escapes (``\\xHH``, ``\\n \\r \\t \\f \\v \\e \\a``, escaped
 punctuation), classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S``, ``.``,
-word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class),
+word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``\\A`` and, where
+nothing can follow them, ``\\z`` / ``\\Z``, ``\\x{HH}``,
 groups ``(...)`` / ``(?:...)``, the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
 and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing
 group or ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
@@ -80,6 +81,17 @@ class Start:
 @dataclass(frozen=True)
 class End:
     pass
+
+
+@dataclass(frozen=True)
+class TextStart:
+    """``\\A``: the start of the input only."""
+
+
+@dataclass(frozen=True)
+class TextEnd:
+    """``\\z`` (the end of the input), or ``\\Z`` with final_lf (also before a final LF)."""
+    final_lf: bool = False
 
 
 @dataclass(frozen=True)
@@ -237,6 +249,11 @@ class _Parser:
         if c == "\\":
             if self.peek() in ("b", "B"):
                 return WordB(neg=self.take() == "B")
+            if self.peek() == "A":
+                self.take()
+                return TextStart()
+            if self.peek() in ("z", "Z"):
+                return TextEnd(final_lf=self.take() == "Z")
             e = self.escape()
             return CC(e) if isinstance(e, frozenset) else CC(self._lit(e))
         if c in "*+?":
@@ -252,6 +269,13 @@ class _Parser:
         if c == "b" and in_class:
             return 0x08   # backspace inside a class, as in PCRE
         if c == "x":
+            if self.peek() == "{":      # \x{H..}: one byte value
+                j = self.s.find("}", self.i)
+                h = self.s[self.i + 1:j] if j > 0 else ""
+                if not h or not re.fullmatch(r"[0-9A-Fa-f]{1,2}", h):
+                    raise UnsupportedRegex("bad \\x{} escape (one byte only)")
+                self.i = j + 1
+                return int(h, 16)
             h = self.s[self.i:self.i + 2]
             if len(h) != 2:
                 raise UnsupportedRegex("bad \\x escape")
@@ -480,6 +504,30 @@ class _Compiler:
             setattr(self, key, hit)
         return hit
 
+    def text_start(self):
+        """Position 0 only: ~Advance(1, 1)."""
+        if getattr(self, "_sot", None) is None:
+            saved, self.b.top = self.b.top, True
+            self._sot = self.b.NOT(self.b.ADV("1", 1))
+            self.b.top = saved
+        return self._sot
+
+    def text_end(self, final_lf: bool):
+        """The last position, ~Lookahead(1, 1); with final_lf also the position before a final
+        LF: last | Lookahead(LF & last, 1)."""
+        key = "_eotz" if final_lf else "_eot"
+        hit = getattr(self, key, None)
+        if hit is None:
+            saved, self.b.top = self.b.top, True
+            last = self.b.NOT(self.b.emit("lookahead", ("1",), shift=1))
+            hit = last
+            if final_lf:
+                lf = self.b.cc(frozenset([LF]))
+                hit = self.b.OR(last, self.b.emit("lookahead", (self.b.AND(lf, last),), shift=1))
+            self.b.top = saved
+            setattr(self, key, hit)
+        return hit
+
     def sol(self):
         if self._sol is None:
             lf = self.b.cc(frozenset([LF]))
@@ -494,6 +542,12 @@ class _Compiler:
             if not at_end:
                 raise UnsupportedRegex("$ is only supported where nothing can follow it")
             return (b.AND(st[0], self.eol()), "0")
+        if isinstance(node, TextEnd):
+            if not at_end:
+                raise UnsupportedRegex("\\z / \\Z are only supported where nothing can follow them")
+            return (b.AND(st[0], self.text_end(node.final_lf)), "0")
+        if isinstance(node, TextStart):
+            return ("0", b.AND(self.P(st), self.text_start()))
         if isinstance(node, CC):
             c = b.cc(node.bytes_)
             L = b.AND(self.P(st), c)

@@ -4,7 +4,8 @@ It shares nothing with the bitstream compiler except the regex parser: the parse
 turned into an epsilon-NFA and simulated position by position, injecting the start state at
 every position (matches may start anywhere).  Bit ``p`` of the result is set iff some non-empty
 match ends with the byte at ``p``.  ``^`` holds at position 0 and after an LF; ``$`` holds before
-an LF and at the end of the input.  This is the
+an LF and at the end of the input; ``\\A`` at position 0, ``\\z`` at the end of the input and
+``\\Z`` there or before a final LF.  This is the
 match-end convention stated in ``bitgen_gb300.regex`` for BitGen's count check against icgrep
 (``bitgen/from_icgrep.py:59-121``): the count of a group is the popcount of the OR of its
 regexes' streams (``bitgen/bitstream.py:60-61``).
@@ -12,14 +13,15 @@ regexes' streams (``bitgen/bitstream.py:60-61``).
 
 from __future__ import annotations
 
-from bitgen_gb300.regex import CC, WORD, Alt, End, Rep, Seq, Start, WordB, parse_regex
+from bitgen_gb300.regex import (CC, WORD, Alt, End, Rep, Seq, Start, TextEnd, TextStart, WordB,
+                                parse_regex)
 
 LF = 0x0A
 
 
 class _NFA:
     def __init__(self):
-        self.kind = []   # 'eps' | 'cc' | 'sol' | 'acc'
+        self.kind = []   # 'eps' | 'cc' | 'acc' | an assertion: sol eol wb nwb sot eot eotz
         self.arg = []    # byte set for 'cc'
         self.out = []    # list of successor ids
 
@@ -36,18 +38,13 @@ class _NFA:
             e = self.new("eps")
             self.out[a].append(e)
             return a, e
-        if isinstance(node, End):
-            a = self.new("eol")
-            e = self.new("eps")
-            self.out[a].append(e)
-            return a, e
-        if isinstance(node, Start):
-            a = self.new("sol")
-            e = self.new("eps")
-            self.out[a].append(e)
-            return a, e
+        assertion = {End: "eol", Start: "sol", TextStart: "sot"}.get(type(node))
         if isinstance(node, WordB):
-            a = self.new("nwb" if node.neg else "wb")
+            assertion = "nwb" if node.neg else "wb"
+        if isinstance(node, TextEnd):
+            assertion = "eotz" if node.final_lf else "eot"
+        if assertion is not None:     # a zero-width state passed when its condition holds
+            a = self.new(assertion)
             e = self.new("eps")
             self.out[a].append(e)
             return a, e
@@ -101,7 +98,20 @@ def match_ends(regex: str, data: bytes) -> int:
     acc = nfa.new("acc")
     nfa.out[end].append(acc)
 
-    def closure(states, sol, eol=False, wb=False):
+    def closure(states, gap):
+        """Epsilon closure at the gap before byte ``gap`` (0 .. n)."""
+        holds = {"eps"}
+        if gap == 0 or data[gap - 1] == LF:
+            holds.add("sol")
+        if gap == n or data[gap] == LF:
+            holds.add("eol")
+        holds.add("wb" if word(gap - 1) != word(gap) else "nwb")
+        if gap == 0:
+            holds.add("sot")
+        if gap == n or (gap == n - 1 and data[gap] == LF):
+            holds.add("eotz")
+            if gap == n:
+                holds.add("eot")
         seen = set()
         stack = list(states)
         while stack:
@@ -109,14 +119,7 @@ def match_ends(regex: str, data: bytes) -> int:
             if s in seen:
                 continue
             seen.add(s)
-            k = nfa.kind[s]
-            if k == "eps":
-                stack.extend(nfa.out[s])
-            elif k == "sol" and sol:
-                stack.extend(nfa.out[s])
-            elif k == "eol" and eol:
-                stack.extend(nfa.out[s])
-            elif (k == "wb" and wb) or (k == "nwb" and not wb):
+            if nfa.kind[s] in holds:
                 stack.extend(nfa.out[s])
         return seen
 
@@ -127,16 +130,13 @@ def match_ends(regex: str, data: bytes) -> int:
     cur = set()
     n = len(data)
     for p in range(n):
-        sol = p == 0 or data[p - 1] == LF
-        active = closure(cur | {start}, sol, wb=word(p - 1) != word(p))
+        active = closure(cur | {start}, p)
         byte = data[p]
         nxt = set()
         for s in active:
             if nfa.kind[s] == "cc" and byte in nfa.arg[s]:
                 nxt.update(nfa.out[s])
-        sol_next = byte == LF
-        eol_next = p + 1 == n or data[p + 1] == LF
-        cur = closure(nxt, sol_next, eol_next, wb=word(p) != word(p + 1))
+        cur = closure(nxt, p + 1)
         if acc in cur:
             result |= 1 << p
     return result

@@ -422,3 +422,28 @@ def test_word_boundaries_and_case_flags(cuda, single):
         assert first_diff(res.stream(k, 0).cpu().numpy(), w[:W]) is None, k
     assert res.counts[:, 0].tolist() == counts
     assert min(counts) > 0
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_input_anchors_on_ragged_inputs(cuda, single):
+    r"""\A, \z, \Z (an Advance and a Lookahead of the all-ones stream, i.e. the input's own first
+    and last positions) on one launch over many inputs of ragged lengths, some ending in LF:
+    every input's streams and counts equal the C oracle's, split and single-kernel form."""
+    regexes = [r"\A\w+", r"(?i)\Ahttp", r"\d\z", r"[a-z]\Z", r"(a|\A)b", r"\x{41}\x{42}\b",
+               r"\A\n", r"z\Z"]
+    groups = [compile_group(regexes[i::2]) for i in range(2)]
+    prog = Program(groups, tuning=Tuning(prefilter=False) if single else Tuning(wpt=1),
+                   per_regex=True)
+    assert (prog.spec.n_parts == 0) == single
+    tile_chars = prog.spec.tile_words * 32
+    lens = list(range(0, 40)) + [tile_chars + d for d in (-33, -1, 0, 1, 32)] + [3 * tile_chars + 7]
+    rnd = np.random.default_rng(5)
+    items = []
+    for k, n in enumerate(lens):
+        t = bytearray(rand_text(n, 300 + k, b"abzAB09 \nhtTP").tobytes())
+        if n > 4 and k % 3 == 0:
+            t[:4] = b"HtTp"
+        if n and rnd.random() < 0.4:
+            t[-1] = 0x0A
+        items.append(np.frombuffer(bytes(t), np.uint8))
+    check(prog, groups, items, per_regex=True)

@@ -117,14 +117,15 @@ def test_emitter_matches_nfa_and_python_re(matchstar_form):
 FLAG_REGEXES = [r"(?i)abc", r"(?i)a[b-d]+e", r"x(?i:yz)w", r"(?i)x(?-i:y)z", r"(?s)a.b",
                 r"(?i)[^a]b", r"a(?s:.)c", r"(?i)\x41b", r"(?im)^ab", r"(?i:a|B)c",
                 r"\bab", r"ab\b", r"\bx\w*\b", r"a\Bb", r"\B0", r"(a|\b)b", r"[\b-c]x",
-                r"\b(?i:yz)\b"]
+                r"\b(?i:yz)\b", r"\Aab", r"\A\w+", r"(?i)\Axy|z\z", r"b\z", r"\w\Z", r"(a|\A)b",
+                r"\x{41}b", r"(?i)[\x{61}-c]\Z"]
 
 
 @pytest.mark.parametrize("matchstar_form", [True, False])
 def test_emitter_flags_match_nfa_and_python_re(matchstar_form):
     """Inline flags: i (ASCII case-insensitive), s (dot matches LF), m (no effect), global
-    and scoped, and word boundaries \\b \\B, against Python's re on mixed-case text with line
-    feeds, spaces and a backspace."""
+    and scoped, word boundaries \\b \\B, input anchors \\A \\z \\Z and \\x{HH}, against the
+    regex module on mixed-case text with line feeds, spaces and a backspace."""
     rx = pytest.importorskip("regex")
     rnd = random.Random(11)
     for r in FLAG_REGEXES:
@@ -133,13 +134,17 @@ def test_emitter_flags_match_nfa_and_python_re(matchstar_form):
         # so that an assertion at its end still sees the byte after it (these patterns match
         # no empty string)
         flags = ""
-        body = r.replace("[^", "[^\\n")
+        body = r.replace("[^", "[^\\n").replace(r"\A", r"(?<![\s\S])").replace(
+            r"\z", r"(?![\s\S])").replace(r"\Z", r"(?=\n?(?![\s\S]))")
+        body = re.sub(r"\\x\{(\w+)\}", lambda m: "\\x%02x" % int(m.group(1), 16), body)
         if body.startswith("(?") and body[2:body.index(")")].isalpha():
             flags, body = body[:body.index(")") + 1], body[body.index(")") + 1:]
         pr = rx.compile((flags + "(?<=" + body + ")").encode(), rx.M)
         for _ in range(6):
             n = rnd.randint(0, 90)
             data = bytes(rnd.choice(b"aAbBcCdDeExXyYzZwW\n0 _\x08") for _ in range(n))
+            if rnd.random() < 0.3:
+                data += b"\n"
             want_re = 0
             for e in range(n):
                 if pr.match(data, e + 1):
@@ -165,7 +170,7 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$b", "(?=x)", r"\Aword", "a++", "(?x)a b", "(?i"):
+    for r in ("a$b", "(?=x)", r"a\zb", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
 
