@@ -432,8 +432,8 @@ def test_input_anchors_on_ragged_inputs(cuda, single):
     regexes = [r"\A\w+", r"(?i)\Ahttp", r"\d\z", r"[a-z]\Z", r"(a|\A)b", r"\x{41}\x{42}\b",
                r"\A\n", r"z\Z"]
     groups = [compile_group(regexes[i::2]) for i in range(2)]
-    prog = Program(groups, tuning=Tuning(prefilter=False) if single else Tuning(wpt=1),
-                   per_regex=True)
+    prog = Program(groups, tuning=Tuning(prefilter=False) if single else
+                   Tuning(wpt=1, prefilter_limit=1.0), per_regex=True)
     assert (prog.spec.n_parts == 0) == single
     tile_chars = prog.spec.tile_words * 32
     lens = list(range(0, 40)) + [tile_chars + d for d in (-33, -1, 0, 1, 32)] + [3 * tile_chars + 7]
