@@ -1968,7 +1968,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     zero_bytes = 4096                  # zeros in shared memory, the bulk zeroing's source
 
     def cls_words(bits, block):     # up to the warps' hit records (16-byte aligned)
-        w = ((1 << bits) // 32 + len(keys) + len(info_tab) + 256 + len(rec_tab)
+        w = ((1 << bits) // 32 + len(keys) + len(info_tab) + 256
              + (block // 32) * nw * 32 + -(-nw // 4) * 4)
         return -(-w // 4) * 4
 
@@ -2007,16 +2007,15 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  uint32_t *bg_exkeys_s = bg_dyn_s + {len(bloom)};            /* {len(keys)} words */\n"
         f"  uint32_t *bg_exinfo_s = bg_exkeys_s + {len(keys)};         /* {len(info_tab)} words */\n"
         f"  uint32_t *bg_obl_s = bg_exinfo_s + {len(info_tab)};        /* 256 words */\n"
-        f"  uint32_t *bg_exrecs_s = bg_obl_s + 256;                     /* {len(rec_tab)} words */\n"
-        f"  uint32_t *bg_runs_s = bg_exrecs_s + {len(rec_tab)};        /* {cls_warps * nw * 32} words */\n"
+        f"  uint32_t *bg_runs_s = bg_obl_s + 256;                     /* {cls_warps * nw * 32} words */\n"
         f"  uint32_t *bg_always_s = bg_runs_s + {cls_warps * nw * 32};  /* {nw} words */\n"
-        f"  /* the tables, 16 bytes per load with several loads in flight (sizes are multiples of 4 words) */\n"
+        f"  /* the tables, 16 bytes per load with several loads in flight (sizes are multiples of 4 words);\n"
+        f"     the exact table's records, read only for a q-gram found in it, stay in global memory */\n"
         f"#pragma unroll 4\n"
         f"  for (int i = threadIdx.x; i < {len(bloom) // 4}; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_bloom_s)[i] = reinterpret_cast<const uint4 *>(bg_bloom_g)[i];\n"
         f"  for (int i = threadIdx.x; i < {len(info_tab) // 4}; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_exinfo_s)[i] = reinterpret_cast<const uint4 *>(bg_exinfo)[i];\n"
-        f"  for (int i = threadIdx.x; i < {len(rec_tab)}; i += blockDim.x) bg_exrecs_s[i] = bg_exrecs[i];\n"
         f"  for (int i = threadIdx.x; i < 64; i += blockDim.x)\n"
         f"    reinterpret_cast<uint4 *>(bg_obl_s)[i] = reinterpret_cast<const uint4 *>(bg_obl)[i];\n"
         f"  for (int i = threadIdx.x; i < {nw}; i += blockDim.x) bg_always_s[i] = bg_always[i];\n"
@@ -2025,7 +2024,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"  __syncthreads();\n"
         f"  uint32_t *runs_s = bg_runs_s + (threadIdx.x >> 5) * {nw * 32};\n"
         f"  ClsCtx cx;\n"
-        f"  cx.bloom = bg_bloom_s; cx.keys = bg_exkeys_s; cx.info = bg_exinfo_s; cx.recs = bg_exrecs_s;\n"
+        f"  cx.bloom = bg_bloom_s; cx.keys = bg_exkeys_s; cx.info = bg_exinfo_s; cx.recs = bg_exrecs;\n"
         f"  cx.always = bg_always_s; cx.log2 = BG_EXLOG2; cx.runs_s = runs_s; cx.n_hits = 0; cx.row = 0;\n"
         f"  cx.hits_s = reinterpret_cast<uint2 *>(bg_dyn_s + {cls_words(bloom_bits, cls_block)}) + (threadIdx.x >> 5) * BG_HIT_CAP;\n"
         f"  /* {zero_bytes} bytes of zeros, read by the bulk copies that zero the outputs (16-byte aligned) */\n"
@@ -2083,6 +2082,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
         f"#define BG_QGRAM {filt.q}\n"
         f"#define BG_HIT_CAP {hit_cap}\n"
         f"#define BG_STRIDE {filt.stride}\n"
+        f"#define BG_WILD {int(bool(filt.wild_old)) | 2 * int(bool(filt.wild_new))}\n"
         f"#define BG_PREFILTER 1\n"
         f"#define BG_BASIS_FILTER {int(tuning.basis_filter)}\n"
         f'#include "bg_device.cuh"\n'

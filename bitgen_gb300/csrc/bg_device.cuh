@@ -925,6 +925,9 @@ static __device__ __noinline__ void store(const BgParams &p, const Tile &t, int 
 #ifndef BG_STRIDE
 #define BG_STRIDE 1
 #endif
+#ifndef BG_WILD
+#define BG_WILD 0 /* bit 0 / 1: the exact table holds 4-grams with a free oldest / newest byte */
+#endif
 constexpr int QG = BG_QGRAM, QS = BG_STRIDE;
 constexpr int NPROBE = 32 / QS;              /* probes per 32-byte lane word */
 static_assert((QG == 3 || QG == 4) && (QS == 1 || QS == 2), "q-gram configuration");
@@ -1064,6 +1067,11 @@ __device__ __forceinline__ void resolve_hits(const BgParams &p, ClsCtx &c, int l
       const uint32_t pre3 = QG == 4 ? (v[4] | v[5] << 8 | v[6] << 16)
                                     : (v[3] | v[4] << 8 | v[5] << 16);
       qgram_exact(key, pre3, c.keys, c.info, c.recs, c.log2, c.runs_s + l);
+      /* q-grams registered with a free oldest / newest byte are stored with that byte zeroed */
+      if (BG_WILD & 1) qgram_exact(key & ~0xffu, pre3, c.keys, c.info, c.recs, c.log2, c.runs_s + l);
+      if (BG_WILD & 2)
+        qgram_exact(key & (QG == 4 ? 0x00ffffffu : 0x0000ffffu), pre3, c.keys, c.info, c.recs,
+                    c.log2, c.runs_s + l);
     }
   }
   __syncwarp();

@@ -34,6 +34,13 @@ Extensions.  Where the bounds also fix single bytes 1, 2 and 3 positions before 
 table holds, under the q-gram, an extension record (those bytes and the term's bit), and the
 kernel sets the bit only when the bytes before the q-gram match.
 
+Wildcards.  A 4-gram may leave its oldest or its newest byte unconstrained (a literal of four
+bytes probed at stride 2 has, in one phase, only three known bytes in the probed gram).  Its
+Bloom bits are set for all 256 values of that byte; the exact table holds it once, with the
+byte zeroed, and a Bloom hit is looked up as itself and with that byte zeroed.  Sharing the
+table with exact keys can only add bits (a masked lookup that finds an exact key whose byte is
+zero), never lose one.
+
 The kernel probes the q-grams in a Bloom bitmap (2^20 bits by default, in shared memory) and
 resolves the rare hits in an exact open-addressed table that maps a q-gram to the records of
 the filters containing it.  Both tables are generated here and compiled into the kernel.
@@ -46,6 +53,7 @@ from dataclasses import dataclass, field
 from typing import Dict, FrozenSet, List, Optional, Sequence, Tuple
 
 ALL = (1 << 256) - 1
+WILD_OLD, WILD_NEW = 1, 2   # a 4-gram whose oldest / newest byte is unconstrained
 MAX_KEYS = 4096         # most q-grams one filter may register
 MAX_EXT = 3             # bytes before a q-gram an extension record may fix
 DEPTH = 12              # positions before a set bit the bounds are followed for
@@ -54,8 +62,10 @@ HASH_BLOOM = 0x9E3779B1
 HASH_EXACT = 0x85EBCA6B
 CONFIGS = ((4, 2), (4, 1), (3, 1))   # (q, stride), cheapest probes first
 # estimated warp instructions per tile, for choosing the configuration: a probe per lane, a
-# Bloom hit (the slow path: bytes to shared memory, lookup), a term run by the execute pass
-COST_PROBE, COST_HIT, COST_RUN = 5.0, 150.0, 600.0
+# Bloom hit (recorded, then looked up with up to 31 others of its chunk at once), a term run
+# by the execute pass.  On the 256-regex workload stride 2 (1.6 hits per tile) measured 3%
+# faster over the whole scan than stride 1 (0.5 hits per tile)
+COST_PROBE, COST_HIT, COST_RUN = 5.0, 40.0, 600.0
 
 
 def bloom_hash(key: int, bits: int = BLOOM_BITS, q: int = 3) -> int:
@@ -121,6 +131,7 @@ class Window:
     ext: Tuple[Tuple[int, ...], ...]
 
     def keys(self) -> int:
+        """Bloom keys (a wildcard byte counts 256)."""
         return sum(math.prod(_n(x) for x in g) for g in self.grams)
 
     def chance(self, alpha: int) -> float:
@@ -146,12 +157,14 @@ def windows(gen, PB, q: int, stride: int) -> Dict[int, List[Window]]:
         ws = []
         for o in range(0, len(b) - W + 1):
             seg = b[o:o + W]
-            if any(x == ALL or x == 0 for x in seg):
+            if any(x == 0 for x in seg):
                 continue
             grams, exts = [], []
             for j in range(stride):
                 # the q-gram ending at distance o + j covers distances o + j .. o + j + q - 1
                 g = tuple(b[o + j + q - 1 - i] for i in range(q))      # oldest first
+                if wildcard(g) < 0:
+                    break
                 e = []
                 for k in range(o + j + q, min(len(b), o + j + q + MAX_EXT)):
                     if _n(b[k]) != 1:
@@ -159,6 +172,8 @@ def windows(gen, PB, q: int, stride: int) -> Dict[int, List[Window]]:
                     e.append(b[k].bit_length() - 1)
                 grams.append(g)
                 exts.append(tuple(e))
+            if len(grams) < stride:
+                continue
             w = Window(tuple(grams), tuple(exts))
             if w.keys() <= MAX_KEYS:
                 ws.append(w)
@@ -203,6 +218,24 @@ def qgram_set(sets: Tuple[int, ...]) -> List[int]:
     return keys
 
 
+def wildcard(g: Tuple[int, ...]) -> int:
+    """0 for a gram of constrained bytes; WILD_OLD / WILD_NEW when only its oldest / newest
+    byte is unconstrained (4-grams only); -1 for any other gram with an unconstrained byte."""
+    free = [i for i, x in enumerate(g) if x == ALL]
+    if not free:
+        return 0
+    if len(g) == 4 and free == [0]:
+        return WILD_OLD
+    if len(g) == 4 and free == [len(g) - 1]:
+        return WILD_NEW
+    return -1
+
+
+def table_keys(g: Tuple[int, ...]) -> List[int]:
+    """Exact-table keys of a gram: a wildcard byte is stored as zero."""
+    return qgram_set(tuple(1 if x == ALL else x for x in g))
+
+
 @dataclass
 class TermFilter:
     """Per-program prefilter: bit r (r < n_terms) = term r may be non-zero, bit n_terms + k =
@@ -222,6 +255,8 @@ class TermFilter:
     stride: int = 1
     alphabet: int = 0                                     # estimated text alphabet (bit set)
     windows: List[Optional[Window]] = field(default_factory=list)
+    wild_old: FrozenSet[int] = frozenset()   # table keys of grams with a free oldest byte
+    wild_new: FrozenSet[int] = frozenset()   # ... with a free newest byte
     cost: float = 0.0                                     # estimated instructions per tile
     hits: float = 0.0                                     # estimated slow-path hits per tile
 
@@ -253,16 +288,31 @@ class TermFilter:
     def mask_key(self, key: int) -> int:
         return key & ((1 << (8 * self.q)) - 1)
 
+    def lookup_keys(self, key: int) -> List[int]:
+        """The table keys a probe of q-gram `key` looks up: itself, and with its oldest /
+        newest byte zeroed when the table holds wildcard grams of that kind."""
+        key = self.mask_key(key)
+        ks = [key]
+        if self.wild_old:
+            ks.append(key & ~0xFF)
+        if self.wild_new:
+            ks.append(key & ((1 << (8 * (self.q - 1))) - 1))
+        return ks
+
     def match(self, key: int, pre3: int) -> int:
         """Bits set by q-gram `key` when the three bytes before it, packed like the records
         (the nearest in bits 0-7), are `pre3`."""
-        key = self.mask_key(key)
-        m = self.table.get(key, 0)
-        for b, n, bit in self.ext.get(key, ()):
-            mask = (1 << (8 * n)) - 1
-            if (pre3 ^ b) & mask == 0:
-                m |= 1 << bit
+        m = 0
+        for k in self.lookup_keys(key):
+            m |= self.table.get(k, 0)
+            for b, n, bit in self.ext.get(k, ()):
+                mask = (1 << (8 * n)) - 1
+                if (pre3 ^ b) & mask == 0:
+                    m |= 1 << bit
         return m
+
+    def bloom_keys(self) -> int:
+        return len(self.table) + 255 * (len(self.wild_old) + len(self.wild_new))
 
     def always_mask(self) -> int:
         m = 0
@@ -277,9 +327,16 @@ class TermFilter:
     def bloom(self, bits: int = BLOOM_BITS) -> List[int]:
         assert 10 <= bits <= 24
         words = [0] * ((1 << bits) // 32)
+        top = 8 * (self.q - 1)
         for key in self.table:
-            h = bloom_hash(key, bits, self.q)
-            words[h >> 5] |= 1 << (h & 31)
+            variants = [key]
+            if key in self.wild_old:
+                variants += [(key & ~0xFF) | b for b in range(256)]
+            if key in self.wild_new:
+                variants += [(key & ~(0xFF << top)) | (b << top) for b in range(256)]
+            for k in variants:
+                h = bloom_hash(k, bits, self.q)
+                words[h >> 5] |= 1 << (h & 31)
         return words
 
     def records(self, key: int) -> List[Tuple[int, int, int]]:
@@ -296,7 +353,7 @@ class TermFilter:
         sets (see `records`).  All of it fits the kernel's shared memory."""
         n = len(self.table)
         log2 = 4
-        while (1 << log2) < 2 * max(1, n):
+        while (1 << log2) < (3 * max(1, n) + 1) // 2:     # at most two thirds full
             log2 += 1
         slots = 1 << log2
         keys = [0] * slots
@@ -376,12 +433,16 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], key_limit: int = 1 << 1
                        windows=tw + pw)
         table: Dict[int, int] = {}
         ext: Dict[int, List[Tuple[int, int, int]]] = {}
+        wild = {WILD_OLD: set(), WILD_NEW: set()}
         for bit, w in enumerate(tw + pw):
             if w is None:
                 continue
             for g, e in zip(w.grams, w.ext):
                 packed = sum(b << (8 * i) for i, b in enumerate(e))
-                for key in qgram_set(g):
+                kind = wildcard(g)
+                for key in table_keys(g):
+                    if kind:
+                        wild[kind].add(key)
                     if e:
                         table.setdefault(key, 0)
                         ext.setdefault(key, []).append((packed, len(e), bit))
@@ -390,12 +451,15 @@ def build(gen, terms: Sequence[int], pre: Sequence[int], key_limit: int = 1 << 1
         if len(table) > key_limit or any(
                 bin(table.get(k, 0)).count("1") + len(ext.get(k, [])) > 255 for k in table):
             table, ext = {}, {}
+        if not table:
+            wild = {WILD_OLD: set(), WILD_NEW: set()}
         f.table, f.ext = table, ext
+        f.wild_old, f.wild_new = frozenset(wild[WILD_OLD]), frozenset(wild[WILD_NEW])
         if not f.enabled:
             continue
         # per tile of `positions` bytes (a warp of 32 lanes): probes per lane, slow-path hits
         # (Bloom false hits and chance q-grams), terms run
-        hits = positions / stride * (len(table) / (1 << bloom_bits)
+        hits = positions / stride * (f.bloom_keys() / (1 << bloom_bits)
                                      + sum(w.chance(alpha) for w in tw + pw if w is not None))
         cost = (positions / 32 / stride * COST_PROBE + hits * COST_HIT
                 + f.expected_per_tile(positions) * COST_RUN)

@@ -62,6 +62,20 @@ def test_generated_kernels_compile_for_sm103a(native, wpt, basis_filter):
     assert rc == N.BG_OK, buf.value.decode()
 
 
+def test_wildcard_filter_kernels_compile_for_sm103a(native):
+    """A stride-2 filter with wildcard 4-grams (their exact records read from global memory)."""
+    ps = workloads.throughput_patterns(seed=3, n=256)
+    groups = [compile_group(g) for g in ps.groups(16)]
+    spec = generate_kernel(groups, Tuning(filter_config=(4, 2)))
+    assert spec.n_parts > 0 and "#define BG_STRIDE 2" in spec.source
+    assert "#define BG_WILD 0" not in spec.source
+    assert "bg_cls_cfg[2] = {1024u" in spec.source      # the tables still fit a full block
+    buf = C.create_string_buffer(1 << 16)
+    src = spec.source.encode()
+    rc = native.bg_nvrtc_check(src, len(src), b"bg_scan", buf, len(buf))
+    assert rc == N.BG_OK, buf.value.decode()
+
+
 def test_runner_configuration_flags():
     """init_kernel reads flags from an object with get_config (the reference's config module
     returns None for an unset key; this one raises KeyError) or from a plain dict."""

@@ -29,9 +29,9 @@ def _setup(patterns, n_groups, per_regex=True, wpt=2, config=None):
     return groups, gen, terms, f
 
 
-def _lookup(f, key, pre3, log2, keys, info, recs):
-    """The kernel's exact lookup (bg_device.cuh qgram_exact), over the generated tables."""
-    key = f.mask_key(key)
+def _lookup1(key, pre3, log2, keys, info, recs):
+    """The kernel's exact lookup of one key (bg_device.cuh qgram_exact), over the generated
+    tables."""
     s = prefilter.exact_hash(key, log2)
     for _ in range(len(keys)):
         if info[s] == 0:
@@ -47,6 +47,22 @@ def _lookup(f, key, pre3, log2, keys, info, recs):
             return m
         s = (s + 1) & (len(keys) - 1)
     return 0
+
+
+def _lookup(f, key, pre3, *tabs):
+    """A Bloom hit's lookups (resolve_hits): the q-gram itself, and with its oldest / newest
+    byte zeroed when the table holds wildcard q-grams of that kind."""
+    key = f.mask_key(key)
+    m = _lookup1(key, pre3, *tabs)
+    if f.wild_old:
+        m |= _lookup1(key & ~0xFF, pre3, *tabs)
+    if f.wild_new:
+        m |= _lookup1(key & ((1 << (8 * (f.q - 1))) - 1), pre3, *tabs)
+    return m
+
+
+def _found(f, key):
+    return any(k in f.table for k in f.lookup_keys(key))
 
 
 @pytest.mark.parametrize("config", prefilter.CONFIGS)
@@ -84,7 +100,13 @@ def _probe_hits(f, text):
     probed = (np.arange(n) % f.stride) == f.stride - 1
     probed[:f.q - 1] = False
     hit = np.zeros(n, dtype=object)
-    cand = probed & np.isin(key, np.array(sorted(f.table), dtype=np.int64))
+    ks = np.array(sorted(f.table), dtype=np.int64)
+    cand = np.isin(key, ks)
+    if f.wild_old:
+        cand |= np.isin(key & ~0xFF, ks)
+    if f.wild_new:
+        cand |= np.isin(key & ((1 << (8 * (f.q - 1))) - 1), ks)
+    cand &= probed
     for p in np.nonzero(cand)[0]:
         hit[p] = f.match(int(key[p]), int(pre3[p]))
     return key, pre3, probed, hit
@@ -142,7 +164,7 @@ def test_prefilter_is_sound(wpt, kind, config):
         for p in range(lo_b + q - 1, hi_b):
             if not probed[p]:
                 continue
-            if p < lo_b + q + 2 and f.mask_key(int(key[p])) in f.table:
+            if p < lo_b + q + 2 and _found(f, int(key[p])):
                 # bytes before the warp's first byte read as zero in the kernel
                 keep = (1 << (8 * max(0, p - q + 1 - lo_b))) - 1
                 cand |= f.match(int(key[p]), int(pre3[p]) & keep)
@@ -221,3 +243,30 @@ def test_split_form_part_outputs():
     assert sorted({o for outs in spec.part_outputs for o in outs}) == list(range(spec.n_outputs))
     assert all(0 < len(outs) <= 2 for outs in spec.part_outputs)
     assert generate_kernel(gs, Tuning(prefilter_limit=0.0)).part_outputs == []
+
+
+def test_wildcard_grams_cover_four_byte_literals_at_stride_two():
+    """At stride 2 a four-byte literal has, in one phase, only three known bytes in the probed
+    4-gram: such grams are registered with a free oldest or newest byte, so that no term of the
+    256-regex workload is left without a filter; the Bloom bitmap holds all 256 variants of
+    each, and the lookups of every variant find the gram's records."""
+    _, _, terms, f = _setup(workloads.throughput_patterns(seed=3, n=256), 16, per_regex=False,
+                            wpt=1, config=(4, 2))
+    assert f.always_mask() == 0 and (f.wild_old or f.wild_new)
+    bloom = f.bloom()
+    tabs = f.exact()
+    top = 8 * (f.q - 1)
+    for key in sorted(f.wild_old | f.wild_new)[:6]:
+        want = f.table[key]
+        for b in (0, 1, 0x41, 0xFF):
+            for v, ok in (((key & ~0xFF) | b, key in f.wild_old),
+                          ((key & ~(0xFF << top)) | (b << top), key in f.wild_new)):
+                if not ok:
+                    continue
+                h = prefilter.bloom_hash(v, q=f.q)
+                assert (bloom[h >> 5] >> (h & 31)) & 1
+                assert _lookup(f, v, 0, *tabs) & want == want == f.match(v, 0) & want
+    assert prefilter.wildcard((prefilter.ALL, 1, 2, 4)) == prefilter.WILD_OLD
+    assert prefilter.wildcard((1, 2, 4, prefilter.ALL)) == prefilter.WILD_NEW
+    assert prefilter.wildcard((1, prefilter.ALL, 2, 4)) < 0
+    assert prefilter.wildcard((prefilter.ALL, 2, 4)) < 0    # trigrams keep every byte
