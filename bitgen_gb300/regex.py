@@ -14,11 +14,13 @@ follow grep with LF-only line breaks (``-disable-Unicode-linebreak``): ``.`` and
 do not match LF, ``^`` matches at position 0 and after every LF.  ``*?`` / ``+?`` / ``??`` (lazy)
 have the same set of match ends as their greedy forms and are compiled alike.
 
-Supported syntax: literals and escapes (``\\xHH``, ``\\n \\r \\t \\f \\v \\e \\a``, escaped
-punctuation), classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S``, ``.``,
+Supported syntax: literals and escapes (``\\xHH``, ``\\x{HH}``, ``\\n \\r \\t \\f \\v \\e \\a``,
+octal ``\\0oo`` / ``\\o{ooo}``, control ``\\cX``, escaped punctuation, ``\\Q...\\E`` quoting),
+classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S \\h \\H``, ``.``, ``\\N``,
 word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``\\A`` and, where
 nothing can follow them, ``\\z`` / ``\\Z``, ``\\x{HH}``,
-groups ``(...)`` / ``(?:...)``, the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
+groups ``(...)`` / ``(?:...)`` / named (``(?P<n>...)``, ``(?<n>...)``, ``(?'n'...)``), comments
+``(?#...)``, the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
 and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing
 group or ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
 and ``$`` where nothing can follow it (end of the regex or of a final alternative): a match ending
@@ -107,9 +109,10 @@ WORD = frozenset(list(range(0x30, 0x3A)) + list(range(0x41, 0x5B)) + list(range(
 SPACE = frozenset([0x20, 0x09, 0x0A, 0x0B, 0x0C, 0x0D])
 DOT = ALL_BYTES - {LF}
 
-_SIMPLE_ESC = {"n": 0x0A, "r": 0x0D, "t": 0x09, "f": 0x0C, "v": 0x0B, "e": 0x1B, "a": 0x07, "0": 0x00}
+_SIMPLE_ESC = {"n": 0x0A, "r": 0x0D, "t": 0x09, "f": 0x0C, "v": 0x0B, "e": 0x1B, "a": 0x07}
+HSPACE = frozenset([0x09, 0x20, 0xA0])      # PCRE's \h on bytes
 _CLASS_ESC = {"d": DIGIT, "D": ALL_BYTES - DIGIT, "w": WORD, "W": ALL_BYTES - WORD,
-              "s": SPACE, "S": ALL_BYTES - SPACE}
+              "s": SPACE, "S": ALL_BYTES - SPACE, "h": HSPACE, "H": ALL_BYTES - HSPACE}
 
 
 def _fold(bs) -> frozenset:
@@ -121,9 +124,31 @@ def _fold(bs) -> frozenset:
     return frozenset(out)
 
 
+def _unquote(s: str) -> str:
+    """The regex with every ``\\Q...\\E`` span (to ``\\E`` or the end) replaced by its characters
+    escaped one by one, so that a quantifier after it applies to the last one, as in PCRE."""
+    out, i = [], 0
+    while i < len(s):
+        if s[i] == "\\" and s.startswith("Q", i + 1):
+            j = s.find("\\E", i + 2)
+            end = len(s) if j < 0 else j
+            for ch in s[i + 2:end]:
+                if ord(ch) > 0xFF:
+                    raise UnsupportedRegex("characters above 0xFF are not supported")
+                out.append(ch if ch.isalnum() and ord(ch) < 0x80 else "\\x%02x" % ord(ch))
+            i = end if j < 0 else j + 2
+        elif s[i] == "\\":
+            out.append(s[i:i + 2])
+            i += 2
+        else:
+            out.append(s[i])
+            i += 1
+    return "".join(out)
+
+
 class _Parser:
     def __init__(self, s: str):
-        self.s = s
+        self.s = _unquote(s)
         self.i = 0
         self.icase = False    # (?i): ASCII letters match either case
         self.dotall = False   # (?s): '.' matches LF too
@@ -230,8 +255,18 @@ class _Parser:
                     self.icase, self.dotall = icase, dotall
                     return Seq(())
                 self.icase, self.dotall = icase, dotall
+            elif self.s.startswith("?#", self.i):     # (?#comment)
+                j = self.s.find(")", self.i)
+                if j < 0:
+                    raise UnsupportedRegex("unterminated comment")
+                self.i = j + 1
+                return Seq(())
+            elif re.match(r"\?(P?<|')[A-Za-z_]\w*[>']", self.s[self.i:]):
+                # named group (?P<name>...), (?<name>...), (?'name'...): a plain group
+                self.i = self.s.index(">" if self.s[self.i + 1] in "P<" else "'", self.i + 3) + 1
             elif self.peek() == "?":
-                raise UnsupportedRegex("group modifiers other than (?: and flags are not supported")
+                raise UnsupportedRegex("group modifiers other than (?:, names, comments and flags "
+                                       "are not supported")
             node = self.alt()
             if self.peek() != ")":
                 raise UnsupportedRegex("missing )")
@@ -254,6 +289,9 @@ class _Parser:
                 return TextStart()
             if self.peek() in ("z", "Z"):
                 return TextEnd(final_lf=self.take() == "Z")
+            if self.peek() == "N":          # any byte but LF
+                self.take()
+                return CC(DOT)
             e = self.escape()
             return CC(e) if isinstance(e, frozenset) else CC(self._lit(e))
         if c in "*+?":
@@ -283,6 +321,22 @@ class _Parser:
             return int(h, 16)
         if c in _SIMPLE_ESC:
             return _SIMPLE_ESC[c]
+        if c == "0":                    # \0, \0o, \0oo: octal
+            m = re.match(r"[0-7]{0,2}", self.s[self.i:])
+            self.i += m.end()
+            return int("0" + m.group(0), 8)
+        if c == "o" and self.peek() == "{":
+            j = self.s.find("}", self.i)
+            o = self.s[self.i + 1:j] if j > 0 else ""
+            if not re.fullmatch(r"[0-7]{1,3}", o) or int(o, 8) > 255:
+                raise UnsupportedRegex("bad \\o{} escape (one byte only)")
+            self.i = j + 1
+            return int(o, 8)
+        if c == "c":                    # \cX: control character X ^ 0x40 (X upper-cased)
+            x = self.take()
+            if x is None or not (0x20 <= ord(x) < 0x7F):
+                raise UnsupportedRegex("bad \\c escape")
+            return ord(x.upper()) ^ 0x40
         if c in _CLASS_ESC:
             return _CLASS_ESC[c]
         if c.isalnum():

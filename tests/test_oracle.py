@@ -152,6 +152,35 @@ def test_emitter_flags_match_nfa_and_python_re(matchstar_form):
             assert run_group(g, data) == match_ends(r, data) == want_re, (r, data)
 
 
+# PCRE syntax the emitter accepts, each with an equivalent the regex module reads
+PCRE_EQUIV = [(r"(?P<n>ab)+c", r"(?:ab)+c"), (r"(?<n>x|y)z", r"(?:x|y)z"), (r"(?'n'q)r", r"qr"),
+              (r"a(?#note)b", r"ab"), (r"\Qa.b\E+", r"a\.b+"), (r"x\Q(*)\E", r"x\(\*\)"),
+              (r"(?i)\Qab\E", r"(?i)ab"), (r"\012a", r"\na"), (r"\0", r"\x00"),
+              (r"\o{101}b", r"Ab"), (r"\cAx|\cz", r"\x01x|\x1a"), (r"[\cA-\cC]x", r"[\x01-\x03]x"),
+              (r"\h+x", r"[ \t\xa0]+x"), (r"[\h\d]y", r"[ \t\xa0\d]y"), (r"a\H", r"a[^ \t\xa0]"),
+              (r"a\N", r"a[^\n]"), (r"b\N+c", r"b[^\n]+c")]
+
+
+@pytest.mark.parametrize("matchstar_form", [True, False])
+def test_emitter_pcre_syntax_matches_equivalents(matchstar_form):
+    """Named groups, comments, \\Q...\\E, octal and control escapes, \\h \\H \\N: the emitter's
+    streams equal the NFA's and the regex module's for an equivalent pattern."""
+    rx = pytest.importorskip("regex")
+    rnd = random.Random(12)
+    alphabet = b"abcqrxyzAB.()*\n\t \x00\x01\x02\x03\x1a\xa0"
+    for ours, theirs in PCRE_EQUIV:
+        g = parse_pablo(compile_regex(ours, matchstar=matchstar_form).to_pablo())
+        pr = rx.compile(("(?<=" + theirs + ")").encode("latin1"), rx.M)
+        for _ in range(6):
+            n = rnd.randint(0, 80)
+            data = bytes(rnd.choice(alphabet) for _ in range(n))
+            want = 0
+            for e in range(n):
+                if pr.match(data, e + 1):
+                    want |= 1 << e
+            assert run_group(g, data) == match_ends(ours, data) == want, (ours, data)
+
+
 def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
     """The genomic motif grammar (IUPAC classes, gapped `.{lo,hi}` motifs) over DNA text with N
     runs, line feeds and planted motifs: emitter + big-int oracle == NFA == C evaluator."""
@@ -170,7 +199,8 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$b", "(?=x)", r"a\zb", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}"):
+    for r in ("a$b", "(?=x)", r"a\zb", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}", r"\101",
+              r"(?<=a)b", r"\o{400}", r"[\N]", "\\Q\u0100\\E", r"(?#open"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
 
