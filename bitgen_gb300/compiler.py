@@ -577,6 +577,8 @@ class Tuning:
     merge_outputs: bool = True   # split form: parts of part_cap terms, outputs merged by atomicOr
     exec_groups: int = 16    # split form: SM groups of the execute pass (each starts on its own parts)
     exec_claim: int = 1      # split form: work items an execute warp claims at once
+    exec_min_blocks: int = 4     # split form: min_blocks of the execute kernel (its loads wait on
+                                 # HBM, so more warps beat more registers; 0: min_blocks)
     inline_parts: int = 160  # split form: inline the parts into the execute kernel up to this many
     single_wpt: int = 1      # words per lane (and blocks per SM below) when the compiler falls
     single_min_blocks: int = 2   # back to the single-kernel form because the filters are
@@ -604,6 +606,7 @@ class Tuning:
                 self.merge_outputs, self.bloom_bits, self.prefilter_limit, self.exec_groups,
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
                 self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim,
+                self.exec_min_blocks,
                 self.push_advances, self.chain_batch, self.single_edge, self.claim_tiles)
 
 
@@ -1507,6 +1510,9 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         tuning = replace(tuning, skip_interval=0 if filt is not None else 1)
         gen.t = tuning
     if filt is not None:
+        if tuning.exec_min_blocks:
+            tuning = replace(tuning, min_blocks=tuning.exec_min_blocks)
+            gen.t = tuning
         return _generate_filtered(gen, tuning, terms, names, filt, name)
     if tuning.push_advances:
         outs = push_advances(dag, outs)
