@@ -1832,7 +1832,10 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     full256 = (1 << 256) - 1
 
     def excluded(cnode):
-        """The bytes outside class `cnode` when there are one to three of them, else None."""
+        """The bytes outside class `cnode` when there are one to three of them, else None (also
+        when the addition runs over a stream that is not a class, e.g. shifted classes)."""
+        if not d.is_cc(cnode):
+            return None
         comp = ~gen.byteset(cnode) & full256
         xs = [b for b in range(256) if (comp >> b) & 1]
         return xs if 1 <= len(xs) <= 3 else None
@@ -1905,7 +1908,8 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     obl_tab = [0] * 256
     if 0 < len(obl_classes) <= 32:
         for i, c in enumerate(obl_classes):
-            bs = gen.byteset(c)
+            # a stream that is not a class bounds nothing about the lane's own bytes
+            bs = gen.byteset(c) if d.is_cc(c) else full256
             for b in range(256):
                 if (bs >> b) & 1:
                     obl_tab[b] |= 1 << i
@@ -1923,7 +1927,7 @@ def _generate_filtered(gen: "_Gen", tuning: Tuning, terms: List[Tuple[int, int]]
     # when one class contains all the others, a lane that is not all ones in it is not all ones
     # in any: test that class at the carry lanes first and skip the rest (the common case)
     guard = None
-    if len({c for c, _, _ in live_needs}) > 1:
+    if len({c for c, _, _ in live_needs}) > 1 and all(d.is_cc(c) for c, _, _ in live_needs):
         sup = max((c for c, _, _ in live_needs), key=lambda c: (bin(gen.byteset(c)).count("1"), c))
         if all(gen.byteset(c) & ~gen.byteset(sup) == 0 for c, _, _ in live_needs):
             lanes = 0

@@ -651,6 +651,11 @@ class _Compiler:
             else:
                 ms = self._star_loop_cc(P, c)
             return (b.OR(st[0], b.AND(ms, c)), ms)
+        U = _fixed_sets(item) if self.use_matchstar else None
+        if U is not None and len(U) == 1:
+            return self.star(CC(U[0]), st)
+        if U is not None and not _self_overlapping(U):
+            return self._star_fixed(item, len(U), st)
         # general star: while loop over the frontier of post-positions
         test = b.fresh("test")
         accum = b.fresh("accum")
@@ -671,6 +676,23 @@ class _Compiler:
         b.scopes[-1][0].append(While(test, body))
         return (b.OR(st[0], accL), accum)
 
+    def _star_fixed(self, item, n, st):
+        """``item*`` for an item of fixed length n whose matches cannot overlap (two can start
+        less than n apart nowhere), without a loop.  E = the end positions of the item's matches,
+        H = E | Advance(E, 1) | ... | Advance(E, n - 1) (the bytes they cover).  A chain of
+        matches starting at a next-position p ends at q = p + n - 1, q + n, ...: since matches
+        cannot overlap, the run of H from q holds exactly that chain, so its ends are
+        MatchStar(Advance(P, n - 1) & E, H) & E, and the next-positions follow them."""
+        b = self.b
+        saved, b.top = b.top, True      # E and H depend on the bytes only
+        E = self.run(item, ("0", "1"))[0]
+        H = E
+        for d in range(1, n):
+            H = b.OR(H, b.ADV(E, d))
+        b.top = saved
+        ends = b.AND(b.MATCHSTAR(b.AND(b.ADV(self.P(st), n - 1), E), H), E)
+        return (b.OR(st[0], ends), b.OR(self.P(st), b.ADV(ends, 1)))
+
     def _star_loop_cc(self, P, c):
         """icgrep's -disable-matchstar form of MatchStar(P, c)."""
         b = self.b
@@ -689,6 +711,37 @@ class _Compiler:
         b.scopes.pop()
         b.scopes[-1][0].append(While(test, body))
         return accum
+
+
+def _fixed_sets(node) -> Optional[List[frozenset]]:
+    """Per offset, the bytes a match of `node` can hold there, if every match of it has the same
+    length and it holds no zero-width assertion; else None."""
+    if isinstance(node, CC):
+        return [node.bytes_]
+    if isinstance(node, Seq):
+        out: List[frozenset] = []
+        for it in node.items:
+            u = _fixed_sets(it)
+            if u is None:
+                return None
+            out += u
+        return out
+    if isinstance(node, Alt):
+        us = [_fixed_sets(it) for it in node.items]
+        if not us or any(u is None for u in us) or len({len(u) for u in us}) != 1:
+            return None
+        return [frozenset().union(*col) for col in zip(*us)]
+    if isinstance(node, Rep) and node.hi == node.lo:
+        u = _fixed_sets(node.item)
+        return None if u is None else u * node.lo
+    return None
+
+
+def _self_overlapping(U: List[frozenset]) -> bool:
+    """Whether two matches of a fixed-length item with per-offset byte sets U could start d < n
+    positions apart (for every offset they share, the two sets meet)."""
+    n = len(U)
+    return n == 0 or any(all(U[j + d] & U[j] for j in range(n - d)) for d in range(1, n))
 
 
 def compile_group(regexes: List[str], matchstar: bool = True) -> Group:

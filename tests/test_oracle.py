@@ -181,6 +181,35 @@ def test_emitter_pcre_syntax_matches_equivalents(matchstar_form):
             assert run_group(g, data) == match_ends(ours, data) == want, (ours, data)
 
 
+# (regex, loop-free): stars over fixed-length items whose matches cannot overlap compile without
+# a while loop; the others keep icgrep's loop form
+GROUP_STARS = [("q(rs)*t", True), ("(ab)+c", True), ("x(abc)*y", True), ("(a[0-9]){2,}z", True),
+               ("(ab|cd)*e", True), ("(?i)(ab)*c", True), ("z(ab)*", True), ("(a(bc){2})*x", True),
+               ("(a\\d)*", True), ("(aa)*b", False), ("((ab){2})*c", False), ("(a.)*b", False),
+               ("(abc|b)*d", False)]
+
+
+@pytest.mark.parametrize("regex,loop_free", GROUP_STARS)
+def test_group_stars_match_the_loop_form_and_nfa(regex, loop_free):
+    """The loop-free star (MatchStar over the bytes the item's matches cover) equals the NFA,
+    icgrep's while-loop form and the C evaluator, on text biased toward long chains."""
+    g = compile_regex(regex)
+    assert fusable(g) == loop_free
+    loop = compile_regex(regex, matchstar=False)
+    assert any(isinstance(st, While) for st in loop.stmts)
+    rnd = random.Random(hash(regex) & 0xFFFF)
+    chars = sorted(set(re.sub(r"[^a-z0-9]", "", regex.replace("\\d", "7")).encode()))
+    for k in range(30):
+        n = rnd.choice([0, 1, 5, 40, 200])
+        alphabet = bytes(chars) + (b"AB\n." if k % 3 == 0 else b"")
+        data = bytes(rnd.choice(alphabet) for _ in range(n))
+        want = match_ends(regex, data)
+        assert run_group(g, data) == want == run_group(loop, data), (regex, data)
+        if n:
+            st, cnt = cpu.run_groups([g], np.frombuffer(data, np.uint8))
+            assert int(cnt[0]) == bin(want).count("1")
+
+
 def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
     """The genomic motif grammar (IUPAC classes, gapped `.{lo,hi}` motifs) over DNA text with N
     runs, line feeds and planted motifs: emitter + big-int oracle == NFA == C evaluator."""
