@@ -39,6 +39,10 @@ CHAIN_OPS = ("and", "advance")
 ADD_OPS = ("matchstar", "scanthru")
 
 
+class _OrderError(Exception):
+    """A part's zero-skip regions would read a node before the code computing it has run."""
+
+
 class NotFusable(ValueError):
     pass
 
@@ -652,6 +656,7 @@ class _Gen:
         self.inline: Dict[str, List[str]] = {}   # pseudo-values: per-word expressions
         self.epochs: Dict[int, int] = {}   # AND node -> batch of chains (interleave_chains)
         self.epoch = -1                    # batch of the node being computed
+        self._order = None                 # (a part's heavy nodes, those computed so far)
 
     # analysis ---------------------------------------------------------------------------
     def byteset(self, v: int) -> int:
@@ -896,6 +901,11 @@ class _Gen:
 
     # materialisation --------------------------------------------------------------------
     def mat(self, v: int) -> str:
+        order = self._order
+        if order is not None and v in order[2] and v not in order[1]:
+            # declared for a later guarded block and still its zero there: not readable yet
+            # (anything else not computed yet is recomputed here from its operands)
+            raise _OrderError(v)
         hit = self.lookup(v)
         if hit is not None:
             return hit
@@ -1091,6 +1101,17 @@ class _Gen:
         return "\n".join(self.lines)
 
     def part(self, terms: Sequence[Tuple[int, int]], outer_regs: bool = False) -> str:
+        """`_part` with zero-block skipping, or, where its guard regions would order a read of
+        a node before its computation (a block opened early that uses a node declared for a
+        later block), without it: one region, every node in topological order."""
+        try:
+            return self._part(terms, outer_regs, skip=True)
+        except _OrderError:
+            return self._part(terms, outer_regs, skip=False)
+        finally:
+            self._order = None
+
+    def _part(self, terms: Sequence[Tuple[int, int]], outer_regs: bool, skip: bool) -> str:
         """Body of one part function: every (node, output) term OR-ed into the warp's
         shared-memory accumulator of its output.
 
@@ -1107,7 +1128,7 @@ class _Gen:
         With `outer_regs` every term ORs into register accumulators `oa<o>_<j>` that the
         caller declares and stores (the split form's parts)."""
         d = self.d
-        k = max(1, self.t.skip_interval) if self.t.skip_interval > 0 else 0
+        k = max(1, self.t.skip_interval) if self.t.skip_interval > 0 and skip else 0
         self.lines = []
         self.indent = 2
         self.scopes = [{}]
@@ -1127,6 +1148,9 @@ class _Gen:
         # heavy nodes of this part, in topological (id) order
         heavy = sorted(set().union(*[self.heavy_ancestors(v) for v in term_outs]))
         hs = set(heavy)
+        computed: set = set()
+        lifted: set = set()
+        self._order = (hs, computed, lifted)   # see mat()
         andd: Dict[int, int] = {}
         cz: Dict[int, frozenset] = {}
         ckpt = set()
@@ -1251,6 +1275,7 @@ class _Gen:
                      for x in n.args]
                 self.emit_op(name, n, a, declare=declare)
             self.scopes[-1][v] = name
+            computed.add(v)
             if declare is False:
                 self.scopes[0][v] = name  # visible everywhere below its declaration
             for o in term_outs.get(v, []):
@@ -1264,6 +1289,7 @@ class _Gen:
             for v in lifted_at.get(TOP, []):
                 self.emit("uint32_t " + ", ".join(f"v{v}_{j} = 0u" for j in range(self.t.wpt)) + ";")
                 self.scopes[-1][v] = f"v{v}"
+                lifted.add(v)
             kids = children.get(TOP, [])
             done_children = set()
             for phase in (1, 2):
@@ -1305,6 +1331,7 @@ class _Gen:
             for v in lifted_at.get(R, []):
                 self.emit("uint32_t " + ", ".join(f"v{v}_{j} = 0u" for j in range(self.t.wpt)) + ";")
                 self.scopes[-1][v] = f"v{v}"
+                lifted.add(v)
             kids = set(children.get(R, []))
             ready: List[int] = []          # computed checkpoints whose block is not emitted yet
             done_children = set()
