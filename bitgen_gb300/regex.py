@@ -97,6 +97,14 @@ class TextEnd:
 
 
 @dataclass(frozen=True)
+class Look:
+    """A lookaround: ``(?=X)`` / ``(?!X)`` (ahead) or ``(?<=X)`` / ``(?<!X)`` (behind, neg)."""
+    item: object
+    behind: bool = False
+    neg: bool = False
+
+
+@dataclass(frozen=True)
 class WordB:
     """``\\b`` (or ``\\B`` with neg): a word/non-word transition between two bytes (the input's
     ends count as non-word)."""
@@ -255,6 +263,16 @@ class _Parser:
                     self.icase, self.dotall = icase, dotall
                     return Seq(())
                 self.icase, self.dotall = icase, dotall
+            elif self.s.startswith(("?=", "?!", "?<=", "?<!"), self.i):
+                behind = self.s[self.i + 1] == "<"
+                neg = self.s[self.i + (2 if behind else 1)] == "!"
+                self.i += 3 if behind else 2
+                node = self.alt()
+                if self.peek() != ")":
+                    raise UnsupportedRegex("missing )")
+                self.take()
+                self.icase, self.dotall = saved
+                return Look(node, behind, neg)
             elif self.s.startswith("?#", self.i):     # (?#comment)
                 j = self.s.find(")", self.i)
                 if j < 0:
@@ -538,6 +556,37 @@ class _Compiler:
             self.b.top = saved
         return self._eol
 
+    def lookaround(self, node: "Look"):
+        """(after, before) of a lookaround, like word_boundary's.  Behind: E = the ends of X's
+        matches (starting anywhere), so X ends just before the next position q iff
+        Advance(E, 1) holds at q, and just before position p + 1 iff E holds at p.  Ahead, for
+        X of fixed length m: X starts at q iff Lookahead(E, m - 1) holds at q (G), and at
+        p + 1 iff Lookahead(G, 1) holds at p.  Negation complements after the shift, so that the
+        positions past the input's end count as no match.  X must be bounded (no ``*``, ``+``
+        or open ``{m,}``) and, ahead, of fixed length."""
+        b = self.b
+        if not _bounded(node.item):
+            raise UnsupportedRegex("lookaround content must be bounded")
+        saved, b.top = b.top, True     # depends on the bytes only
+        try:
+            if node.behind:
+                if _matches_empty(node.item):
+                    raise UnsupportedRegex("lookbehind content that matches the empty string")
+                E = self.run(node.item, ("0", "1"), at_end=True)[0]
+                after, before = E, b.ADV(E, 1)
+            else:
+                U = _fixed_sets(node.item, assertions=True)
+                if U is None or not U:
+                    raise UnsupportedRegex("lookahead content must have a fixed, non-zero length")
+                E = self.run(node.item, ("0", "1"), at_end=True)[0]
+                G = b.emit("lookahead", (E,), shift=len(U) - 1) if len(U) > 1 else E
+                after, before = b.emit("lookahead", (G,), shift=1), G
+            if node.neg:
+                after, before = b.NOT(after), b.NOT(before)
+        finally:
+            b.top = saved
+        return after, before
+
     def word_boundary(self, neg: bool):
         """(after, before): bit p of `after` = a word/non-word transition between bytes p and
         p + 1, i.e. W ^ Lookahead(W, 1); bit q of `before` = one between bytes q - 1 and q,
@@ -622,6 +671,9 @@ class _Compiler:
             return ("0", b.AND(self.P(st), self.sol()))
         if isinstance(node, WordB):
             after, before = self.word_boundary(node.neg)
+            return (b.AND(st[0], after), b.AND(self.P(st), before))
+        if isinstance(node, Look):
+            after, before = self.lookaround(node)
             return (b.AND(st[0], after), b.AND(self.P(st), before))
         if isinstance(node, Rep):
             return self.rep(node, st)
@@ -713,28 +765,55 @@ class _Compiler:
         return accum
 
 
-def _fixed_sets(node) -> Optional[List[frozenset]]:
+def _fixed_sets(node, assertions: bool = False) -> Optional[List[frozenset]]:
     """Per offset, the bytes a match of `node` can hold there, if every match of it has the same
-    length and it holds no zero-width assertion; else None."""
+    length and (unless `assertions`, which then count as length 0) it holds no zero-width
+    assertion; else None."""
     if isinstance(node, CC):
         return [node.bytes_]
     if isinstance(node, Seq):
         out: List[frozenset] = []
         for it in node.items:
-            u = _fixed_sets(it)
+            u = _fixed_sets(it, assertions)
             if u is None:
                 return None
             out += u
         return out
     if isinstance(node, Alt):
-        us = [_fixed_sets(it) for it in node.items]
+        us = [_fixed_sets(it, assertions) for it in node.items]
         if not us or any(u is None for u in us) or len({len(u) for u in us}) != 1:
             return None
         return [frozenset().union(*col) for col in zip(*us)]
     if isinstance(node, Rep) and node.hi == node.lo:
-        u = _fixed_sets(node.item)
+        u = _fixed_sets(node.item, assertions)
         return None if u is None else u * node.lo
+    if assertions and isinstance(node, (Start, End, WordB, TextStart, TextEnd, Look)):
+        return []
     return None
+
+
+def _bounded(node) -> bool:
+    """No unbounded repetition inside."""
+    if isinstance(node, Rep):
+        return node.hi is not None and _bounded(node.item)
+    if isinstance(node, (Seq, Alt)):
+        return all(_bounded(it) for it in node.items)
+    if isinstance(node, Look):
+        return _bounded(node.item)
+    return True
+
+
+def _matches_empty(node) -> bool:
+    """Whether the node can match the empty string (assertions count as empty)."""
+    if isinstance(node, CC):
+        return False
+    if isinstance(node, Seq):
+        return all(_matches_empty(it) for it in node.items)
+    if isinstance(node, Alt):
+        return any(_matches_empty(it) for it in node.items)
+    if isinstance(node, Rep):
+        return node.lo == 0 or _matches_empty(node.item)
+    return True
 
 
 def _self_overlapping(U: List[frozenset]) -> bool:

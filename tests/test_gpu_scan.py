@@ -466,3 +466,31 @@ def test_group_stars_without_loops(cuda, single):
     items = [text, np.frombuffer(b"q" + b"rs" * 5000 + b"t", np.uint8),
              np.frombuffer(b"ab" * 4000, np.uint8), np.zeros(0, np.uint8)]
     check(prog, groups, items, per_regex=True)
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_lookarounds_on_ragged_inputs(cuda, single):
+    """Lookahead (a Lookahead of the content's match ends) and lookbehind (an Advance of them),
+    positive and negative, over many inputs of ragged lengths with planted witnesses: streams
+    and counts equal the C oracle's per regex, split and single-kernel form."""
+    regexes = [r"abcd(?=x)", r"qrst(?!u)", r"(?<=ab)cdqx", r"(?<!a)bcdq",
+               r"(?<![0-9])12[0-9]{2}(?![0-9])", r"(?<=ab|c)dqrs", r"qrr(?=r)r+",
+               r"(?<=[0-9])xabc(?=[0-9])"]
+    wit = [b"abcdx", b"abcdy", b"qrstu", b"qrstv", b"abcdqx", b"zbcdq", b"abcdq", b"1234",
+           b"012345", b"abdqrs", b"cdqrs", b"qrrrr", b"1xabc2", b"xabc2"]
+    groups = [compile_group(regexes[i::2]) for i in range(2)]
+    prog = Program(groups, tuning=Tuning(prefilter=False) if single else
+                   Tuning(wpt=1, prefilter_limit=1.0), per_regex=True)
+    assert (prog.spec.n_parts == 0) == single
+    tile_chars = prog.spec.tile_words * 32
+    lens = list(range(0, 40)) + [tile_chars + d for d in (-33, -1, 0, 1, 32)] + [5 * tile_chars + 3]
+    rnd = np.random.default_rng(9)
+    items = []
+    for k, n in enumerate(lens):
+        t = bytearray(rand_text(n, 700 + k, b"abcdqrx0129 \n").tobytes())
+        for _ in range(n // 40):
+            w = wit[rnd.integers(len(wit))]
+            at = int(rnd.integers(0, max(1, n - len(w))))
+            t[at:at + len(w)] = w[:n - at]
+        items.append(np.frombuffer(bytes(t), np.uint8))
+    check(prog, groups, items, per_regex=True)

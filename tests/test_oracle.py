@@ -181,6 +181,34 @@ def test_emitter_pcre_syntax_matches_equivalents(matchstar_form):
             assert run_group(g, data) == match_ends(ours, data) == want, (ours, data)
 
 
+LOOK_REGEXES = [r"a(?=b)", r"a(?!b)", r"(?<=a)b", r"(?<!a)b", r"x(?=y[a-c])", r"(?<=ab|c)d",
+                r"(?<![0-9])[0-9]{2}(?![0-9])", r"q(?=r)r+", r"(?i)(?<=x)y", r"(?<=a.)b",
+                r"(?<=[0-9])x(?=[0-9])", r"b(?!c)(?!a)", r"(?<=^a)b", r"a(?=b$)", r"(?<!\w)ab"]
+
+
+@pytest.mark.parametrize("matchstar_form", [True, False])
+def test_lookarounds_match_nfa_and_regex_module(matchstar_form):
+    """Lookahead (fixed length) and lookbehind (bounded), positive and negative, at the start,
+    middle and end of patterns: the emitter's streams equal the NFA's and the regex module's."""
+    rx = pytest.importorskip("regex")
+    rnd = random.Random(13)
+    for r in LOOK_REGEXES:
+        g = parse_pablo(compile_regex(r, matchstar=matchstar_form).to_pablo())
+        pr = rx.compile(("(?<=" + r.replace("(?i)", "") + ")").encode(),
+                        rx.M | (rx.I if "(?i)" in r else 0))
+        for _ in range(8):
+            n = rnd.randint(0, 70)
+            data = bytes(rnd.choice(b"abcdqrxyXY0129 \n") for _ in range(n))
+            want = 0
+            for e in range(n):
+                if pr.match(data, e + 1):
+                    want |= 1 << e
+            assert run_group(g, data) == match_ends(r, data) == want, (r, data)
+    for r in (r"a(?=b*)", r"(?<=a*)b", r"(?<=a?)b", r"x(?=a|bc)"):
+        with pytest.raises(UnsupportedRegex):
+            compile_regex(r)
+
+
 # (regex, loop-free): stars over fixed-length items whose matches cannot overlap compile without
 # a while loop; the others keep icgrep's loop form
 GROUP_STARS = [("q(rs)*t", True), ("(ab)+c", True), ("x(abc)*y", True), ("(a[0-9]){2,}z", True),
@@ -228,8 +256,8 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$b", "(?=x)", r"a\zb", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}", r"\101",
-              r"(?<=a)b", r"\o{400}", r"[\N]", "\\Q\u0100\\E", r"(?#open"):
+    for r in ("a$b", "(?=x*)", r"a\zb", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}", r"\101",
+              r"(?<=a+)b", r"\o{400}", r"[\N]", "\\Q\u0100\\E", r"(?#open"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
 
