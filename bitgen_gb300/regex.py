@@ -20,7 +20,8 @@ classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S \\h \\H
 word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``\\A`` and, where
 nothing can follow them, ``\\z`` / ``\\Z``, ``\\x{HH}``,
 groups ``(...)`` / ``(?:...)`` / named (``(?P<n>...)``, ``(?<n>...)``, ``(?'n'...)``), comments
-``(?#...)``, the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
+``(?#...)``, lookahead ``(?=X)`` / ``(?!X)`` (X of fixed length) and lookbehind ``(?<=X)`` /
+``(?<!X)`` (X bounded, not matching the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
 and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing
 group or ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
 and ``$`` where nothing can follow it (end of the regex or of a final alternative): a match ending
