@@ -17,16 +17,15 @@ have the same set of match ends as their greedy forms and are compiled alike.
 Supported syntax: literals and escapes (``\\xHH``, ``\\x{HH}``, ``\\n \\r \\t \\f \\v \\e \\a``,
 octal ``\\0oo`` / ``\\o{ooo}``, control ``\\cX``, escaped punctuation, ``\\Q...\\E`` quoting),
 classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S \\h \\H``, ``.``, ``\\N``,
-word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``\\A`` and, where
-nothing can follow them, ``\\z`` / ``\\Z``, ``\\x{HH}``,
-groups ``(...)`` / ``(?:...)`` / named (``(?P<n>...)``, ``(?<n>...)``, ``(?'n'...)``), comments
-``(?#...)``, lookahead ``(?=X)`` / ``(?!X)`` (X of fixed length) and lookbehind ``(?<=X)`` /
-``(?<!X)`` (X bounded, not matching the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF)
-and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing
-group or ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or lazy), ``^``,
-and ``$`` where nothing can follow it (end of the regex or of a final alternative): a match ending
-at p counts only if byte p+1 is LF or p is the last position, i.e.
-``L & ~Lookahead(~LF, 1)``.
+word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``^``, ``$``, ``\\A``,
+``\\z``, ``\\Z``, ``\\K`` (no effect on match ends), groups ``(...)`` / ``(?:...)`` / named
+(``(?P<n>...)``, ``(?<n>...)``, ``(?'n'...)``), comments ``(?#...)``, lookahead ``(?=X)`` /
+``(?!X)`` (X of fixed length) and lookbehind ``(?<=X)`` / ``(?<!X)`` (X bounded, not matching
+the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF) and ``m``
+(no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing group or
+``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or
+lazy).  Zero-width assertions filter both markers (below): ``$`` keeps the last bytes followed by
+an LF or the end, ``L & ~Lookahead(~LF, 1)``, and the next positions that hold an LF.
 
 Compilation keeps two markers per regex state: ``L`` (positions of the last byte consumed) and
 ``P`` (positions where the next byte is to be matched, i.e. ``Advance(L, 1)`` plus any
@@ -192,8 +191,11 @@ class _Parser:
         return Seq(tuple(items))
 
     def quant(self, a):
+        zero_width = isinstance(a, (Start, End, WordB, TextStart, TextEnd, Look))
         while True:
             c = self.peek()
+            if zero_width and c is not None and (c in "*+?" or (c == "{" and self._is_counted())):
+                raise UnsupportedRegex("a quantifier on an assertion")
             if c == "*":
                 self.take(); a = Rep(a, 0, None)
             elif c == "+":
@@ -308,6 +310,9 @@ class _Parser:
                 return TextStart()
             if self.peek() in ("z", "Z"):
                 return TextEnd(final_lf=self.take() == "Z")
+            if self.peek() == "K":          # \K: resets the reported start, so match ends stay
+                self.take()
+                return Seq(())
             if self.peek() == "N":          # any byte but LF
                 self.take()
                 return CC(DOT)
@@ -643,13 +648,12 @@ class _Compiler:
     def run(self, node, st, at_end=False):
         b = self.b
         if isinstance(node, End):
-            if not at_end:
-                raise UnsupportedRegex("$ is only supported where nothing can follow it")
-            return (b.AND(st[0], self.eol()), "0")
+            # after a last byte p: p + 1 is LF or the end; at a next position q: q is an LF
+            return (b.AND(st[0], self.eol()), b.AND(self.P(st), self.b.cc(frozenset([LF]))))
         if isinstance(node, TextEnd):
-            if not at_end:
-                raise UnsupportedRegex("\\z / \\Z are only supported where nothing can follow them")
-            return (b.AND(st[0], self.text_end(node.final_lf)), "0")
+            # at a next position q < n only \Z can hold: q is the last byte and an LF
+            before = b.AND(b.cc(frozenset([LF])), self.text_end(False)) if node.final_lf else "0"
+            return (b.AND(st[0], self.text_end(node.final_lf)), b.AND(self.P(st), before))
         if isinstance(node, TextStart):
             return ("0", b.AND(self.P(st), self.text_start()))
         if isinstance(node, CC):

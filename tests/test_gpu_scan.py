@@ -427,10 +427,11 @@ def test_word_boundaries_and_case_flags(cuda, single):
 @pytest.mark.parametrize("single", [False, True])
 def test_input_anchors_on_ragged_inputs(cuda, single):
     r"""\A, \z, \Z (an Advance and a Lookahead of the all-ones stream, i.e. the input's own first
-    and last positions) on one launch over many inputs of ragged lengths, some ending in LF:
-    every input's streams and counts equal the C oracle's, split and single-kernel form."""
+    and last positions), also with pattern after $ and \Z, on one launch over many inputs of
+    ragged lengths, some ending in LF: every input's streams and counts equal the C oracle's,
+    split and single-kernel form."""
     regexes = [r"\A\w+", r"(?i)\Ahttp", r"\d\z", r"[a-z]\Z", r"(a|\A)b", r"\x{41}\x{42}\b",
-               r"\A\n", r"z\Z"]
+               r"\A\n", r"z\Z", r"b$\na", r"[ab]\Z\n"]
     groups = [compile_group(regexes[i::2]) for i in range(2)]
     prog = Program(groups, tuning=Tuning(prefilter=False) if single else
                    Tuning(wpt=1, prefilter_limit=1.0), per_regex=True)

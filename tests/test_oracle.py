@@ -209,6 +209,32 @@ def test_lookarounds_match_nfa_and_regex_module(matchstar_form):
             compile_regex(r)
 
 
+MID_ASSERTIONS = [r"a$\nb", r"a$", r"ab$|c", r"a\z", r"a$\n^b", r"a\Z\n", r"(?:a$\n)+b",
+                  r"a$b", r"a\zb", r"[ab]$[\na]", r"a\Z"]
+
+
+@pytest.mark.parametrize("matchstar_form", [True, False])
+def test_end_assertions_inside_patterns(matchstar_form):
+    """$, \\z and \\Z followed by more pattern (filtering the next positions as well as the last
+    bytes) equal the NFA and the regex module; \\K leaves match ends unchanged."""
+    rx = pytest.importorskip("regex")
+    rnd = random.Random(14)
+    for r in MID_ASSERTIONS:
+        g = parse_pablo(compile_regex(r, matchstar=matchstar_form).to_pablo())
+        body = r.replace(r"\z", r"(?![\s\S])").replace(r"\Z", r"(?=\n?(?![\s\S]))")
+        pr = rx.compile(("(?<=" + body + ")").encode(), rx.M)
+        for _ in range(10):
+            n = rnd.randint(0, 40)
+            data = bytes(rnd.choice(b"abab\n\nc") for _ in range(n))
+            want = 0
+            for e in range(n):
+                if pr.match(data, e + 1):
+                    want |= 1 << e
+            assert run_group(g, data) == match_ends(r, data) == want, (r, data)
+    data = b"xaby xay abyab"
+    assert run_group(compile_regex(r"a\Kb"), data) == run_group(compile_regex("ab"), data) != 0
+
+
 # (regex, loop-free): stars over fixed-length items whose matches cannot overlap compile without
 # a while loop; the others keep icgrep's loop form
 GROUP_STARS = [("q(rs)*t", True), ("(ab)+c", True), ("x(abc)*y", True), ("(a[0-9]){2,}z", True),
@@ -256,7 +282,7 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$b", "(?=x*)", r"a\zb", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}", r"\101",
+    for r in ("a$+", "(?=x*)", r"a\b*", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}", r"\101",
               r"(?<=a+)b", r"\o{400}", r"[\N]", "\\Q\u0100\\E", r"(?#open"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
