@@ -713,6 +713,9 @@ class _Compiler:
             return self.star(CC(U[0]), st)
         if U is not None and not _self_overlapping(U):
             return self._star_fixed(item, len(U), st)
+        branches = _branches(item) if self.use_matchstar and U is None else None
+        if branches and not _branches_overlap(branches):
+            return self._star_disjoint(branches, st)
         # general star: while loop over the frontier of post-positions
         test = b.fresh("test")
         accum = b.fresh("accum")
@@ -749,6 +752,27 @@ class _Compiler:
         b.top = saved
         ends = b.AND(b.MATCHSTAR(b.AND(b.ADV(self.P(st), n - 1), E), H), E)
         return (b.OR(st[0], ends), b.OR(self.P(st), b.ADV(ends, 1)))
+
+    def _star_disjoint(self, branches, st):
+        """``item*`` for an item that is a union of fixed-length branches of different lengths,
+        no two of whose matches can overlap, without a loop.  Per branch b of length m: E_b =
+        its match ends, S_b = Lookahead(E_b, m - 1) its starts, and it covers S_b | Advance(S_b,
+        1) | ... | Advance(S_b, m - 1).  Matches that cannot overlap make every run of covered
+        bytes one chain of touching matches, so from a start x the chain's bytes are
+        R = MatchStar(P & S, covered), its ends R & E and its next positions R & Advance(E, 1)."""
+        b = self.b
+        saved, b.top = b.top, True      # the branches' streams depend on the bytes only
+        S, E, H = "0", "0", "0"
+        for U in branches:
+            m = len(U)
+            Eb = self.run(Seq(tuple(CC(u) for u in U)), ("0", "1"))[0]
+            Sb = b.emit("lookahead", (Eb,), shift=m - 1) if m > 1 else Eb
+            E, S, H = b.OR(E, Eb), b.OR(S, Sb), b.OR(H, Sb)
+            for d in range(1, m):
+                H = b.OR(H, b.ADV(Sb, d))
+        b.top = saved
+        R = b.MATCHSTAR(b.AND(self.P(st), S), H)
+        return (b.OR(st[0], b.AND(R, E)), b.OR(self.P(st), b.AND(R, b.ADV(E, 1))))
 
     def _star_loop_cc(self, P, c):
         """icgrep's -disable-matchstar form of MatchStar(P, c)."""
@@ -795,6 +819,66 @@ def _fixed_sets(node, assertions: bool = False) -> Optional[List[frozenset]]:
     if assertions and isinstance(node, (Start, End, WordB, TextStart, TextEnd, Look)):
         return []
     return None
+
+
+def _branches(node, cap: int = 16, max_len: int = 24) -> Optional[List[Tuple[frozenset, ...]]]:
+    """The item as a list of distinct fixed-length branches (per-offset byte sets), if it is a
+    finite union of at most `cap` of them, none empty or longer than `max_len`; else None."""
+    def expand(n):
+        if isinstance(n, CC):
+            return [(n.bytes_,)]
+        if isinstance(n, Seq):
+            out = [()]
+            for it in n.items:
+                sub = expand(it)
+                if sub is None:
+                    return None
+                out = [a + c for a in out for c in sub]
+                if len(out) > cap:
+                    return None
+            return out
+        if isinstance(n, Alt):
+            out = []
+            for it in n.items:
+                sub = expand(it)
+                if sub is None:
+                    return None
+                out += sub
+            return out if len(out) <= cap else None
+        if isinstance(n, Rep) and n.hi is not None:
+            sub = expand(n.item)
+            if sub is None:
+                return None
+            out, power = [], [()]
+            for k in range(n.hi + 1):
+                if k >= n.lo:
+                    out += power
+                power = [a + c for a in power for c in sub]
+                if len(out) + len(power) > cap:
+                    return None
+            return out
+        return None
+    bs = expand(node)
+    if bs is None:
+        return None
+    bs = sorted(set(bs), key=lambda u: (len(u), [sorted(x) for x in u]))
+    if not bs or any(len(u) == 0 or len(u) > max_len for u in bs):
+        return None
+    return bs
+
+
+def _branches_overlap(bs) -> bool:
+    """Whether two matches of these branches could overlap: branch j starting d >= 0 bytes
+    after branch i's start, inside it, with every shared offset's byte sets meeting (the same
+    branch at d = 0 is the same match)."""
+    for i, U in enumerate(bs):
+        for j, V in enumerate(bs):
+            for d in range(len(U)):
+                if i == j and d == 0:
+                    continue
+                if all(U[t] & V[t - d] for t in range(d, min(len(U), d + len(V)))):
+                    return True
+    return False
 
 
 def _bounded(node) -> bool:

@@ -452,17 +452,19 @@ def test_input_anchors_on_ragged_inputs(cuda, single):
 
 @pytest.mark.parametrize("single", [False, True])
 def test_group_stars_without_loops(cuda, single):
-    """Stars over fixed-length groups compile to MatchStar over the bytes their matches cover
-    (no while loop), so they run fused; chains thousands of bytes long cross many tiles.
+    """Stars over fixed-length groups, or unions of fixed-length branches, compile to MatchStar
+    over the bytes their matches cover (no while loop), so they run fused; chains thousands of
+    bytes long cross many tiles.
     Streams and counts equal the C oracle's per regex, split and single-kernel form."""
     regexes = ["q(rs)*t", "(ab)+c", "x(abc)*y", "(a[0-9]){2,}z", "(ab|cd)*e", "k(xy)*",
-               "(?i)(gh)+i", "m(n(op){2})*w"]
+               "(?i)(gh)+i", "m(n(op){2})*w", "u(vw|xyz)*u", "(jk|lmn|o)+p"]
     groups = [compile_group(regexes[i::2]) for i in range(2)]
     prog = Program(groups, tuning=Tuning(prefilter=False) if single else
                    Tuning(wpt=1, prefilter_limit=1.0), per_regex=True)
     assert (prog.spec.n_parts == 0) == single
     wit = [b"q" + b"rs" * 3000 + b"t", b"ab" * 700 + b"c", b"xabcabcy", b"a1a2a3z",
-           b"abcdcdabe" * 3, b"kxyxyxy" * 500, b"GhgHghi", b"mnopopnopopw", b"rsrst", b"qt"]
+           b"abcdcdabe" * 3, b"kxyxyxy" * 500, b"GhgHghi", b"mnopopnopopw", b"rsrst", b"qt",
+           b"u" + b"vwxyz" * 900 + b"u", b"jkolmnojkp", b"lmnoooop"]
     text = workloads.plant(workloads.printable_text(200_000, 81), wit, 60, 82)
     items = [text, np.frombuffer(b"q" + b"rs" * 5000 + b"t", np.uint8),
              np.frombuffer(b"ab" * 4000, np.uint8), np.zeros(0, np.uint8)]

@@ -235,12 +235,14 @@ def test_end_assertions_inside_patterns(matchstar_form):
     assert run_group(compile_regex(r"a\Kb"), data) == run_group(compile_regex("ab"), data) != 0
 
 
-# (regex, loop-free): stars over fixed-length items whose matches cannot overlap compile without
-# a while loop; the others keep icgrep's loop form
+# (regex, loop-free): stars over fixed-length items, or over unions of fixed-length branches,
+# whose matches cannot overlap compile without a while loop; the others keep icgrep's loop form
 GROUP_STARS = [("q(rs)*t", True), ("(ab)+c", True), ("x(abc)*y", True), ("(a[0-9]){2,}z", True),
                ("(ab|cd)*e", True), ("(?i)(ab)*c", True), ("z(ab)*", True), ("(a(bc){2})*x", True),
                ("(a\\d)*", True), ("(aa)*b", False), ("((ab){2})*c", False), ("(a.)*b", False),
-               ("(abc|b)*d", False)]
+               ("(ab|cde)*f", True), ("x(ab|cde)+y", True), ("(q|rst)*u", True), ("(a|bc)*d", True),
+               ("z(ab|cde|fghi)*", True), ("(abc|d)+", True), ("(ab|abc)*d", False),
+               ("(ab|b)*c", False), ("(x[0-9]{1,3})*y", False), ("(ab|ba)*c", False)]
 
 
 @pytest.mark.parametrize("regex,loop_free", GROUP_STARS)
