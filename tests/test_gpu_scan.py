@@ -497,3 +497,20 @@ def test_lookarounds_on_ragged_inputs(cuda, single):
             t[at:at + len(w)] = w[:n - at]
         items.append(np.frombuffer(bytes(t), np.uint8))
     check(prog, groups, items, per_regex=True)
+
+
+@pytest.mark.parametrize("single", [False, True])
+def test_wide_class_repeats(cuda, single):
+    """Class repeats with bounds of 16 and more, built by doubling (Advances of up to half the
+    bound), over text with runs around the bounds: streams and counts equal the C oracle's per
+    regex, split and single-kernel form."""
+    regexes = ["abcd.{0,40}wxyz", "kq[a-z]{10,40}yy", "zq[0-9]{16}", "mnop[ab]{20,}st"]
+    wit = [b"abcd" + b"." * k + b"wxyz" for k in (0, 39, 40, 41)] + \
+          [b"kq" + b"r" * k + b"yy" for k in (9, 10, 40, 41)] + \
+          [b"zq" + b"7" * k for k in (15, 16, 17)] + [b"mnop" + b"ab" * k + b"st" for k in (9, 10, 30)]
+    groups = [compile_group(regexes[i::2]) for i in range(2)]
+    prog = Program(groups, tuning=Tuning(prefilter=False) if single else
+                   Tuning(wpt=1, prefilter_limit=1.0), per_regex=True)
+    assert (prog.spec.n_parts == 0) == single
+    text = workloads.plant(workloads.printable_text(100_000, 91), wit, 40, 92)
+    check(prog, groups, [text, np.frombuffer(b"".join(wit), np.uint8)], per_regex=True)

@@ -235,6 +235,33 @@ def test_end_assertions_inside_patterns(matchstar_form):
     assert run_group(compile_regex(r"a\Kb"), data) == run_group(compile_regex("ab"), data) != 0
 
 
+WIDE_REPEATS = ["a.{0,20}b", "x[a-z]{10,40}y", "q[0-9]{16}", "(?s)a.{17,30}", "z[ab]{0,16}",
+                "c.{20,}d", "[ab]{16,}", "k[ab]{3,18}", "^.{16}$", "(?i)q{16,17}"]
+
+
+def test_wide_class_repeats_match_nfa_and_regex_module():
+    """Class repeats with a bound of 16 or more are built by doubling (O(log) steps): equal to
+    the NFA and the regex module, at every count around the bounds and on random text."""
+    rx = pytest.importorskip("regex")
+    rnd = random.Random(15)
+    for r in WIDE_REPEATS:
+        g = compile_regex(r)
+        assert len(g.stmts) < 80
+        pr = rx.compile(("(?<=" + r.replace("(?i)", "").replace("(?s)", "") + ")").encode(),
+                        rx.M | (rx.I if "(?i)" in r else 0) | (rx.S if "(?s)" in r else 0))
+        texts = [bytes(rnd.choice(b"aabbbaq1xyzcdk\n") for _ in range(rnd.choice([0, 30, 90])))
+                 for _ in range(12)]
+        for k in range(0, 45):     # one run of k bytes between the literals
+            for fill in (b"b", b"5", b"Q"):
+                texts.append(r.encode()[:1].lstrip(b"^([(?") + fill * k + b"dby")
+        for data in texts:
+            want = 0
+            for e in range(len(data)):
+                if pr.match(data, e + 1):
+                    want |= 1 << e
+            assert run_group(g, data) == match_ends(r, data) == want, (r, data)
+
+
 # (regex, loop-free): stars over fixed-length items, or over unions of fixed-length branches,
 # whose matches cannot overlap compile without a while loop; the others keep icgrep's loop form
 GROUP_STARS = [("q(rs)*t", True), ("(ab)+c", True), ("x(abc)*y", True), ("(a[0-9]){2,}z", True),
