@@ -690,8 +690,10 @@ class _Compiler:
 
     def rep(self, node, st):
         b = self.b
-        if isinstance(node.item, CC) and (node.lo >= WIDE_REPEAT or (node.hi or 0) >= WIDE_REPEAT):
-            return self._rep_class(node, st)
+        if node.lo >= WIDE_REPEAT or (node.hi or 0) >= WIDE_REPEAT:
+            U = _fixed_sets(node.item)
+            if U:
+                return self._rep_fixed(node, st, len(U))
         for _ in range(node.lo):
             st = self.run(node.item, st)
         if node.hi is not None:
@@ -700,35 +702,37 @@ class _Compiler:
             return st
         return self.star(node.item, st)
 
-    def _rep_class(self, node, st):
-        """``c{lo,hi}`` (hi None: ``c{lo,}``) for a class c with a wide count, in O(log) steps
-        instead of one per count: B_k = c on the k bytes ending at q (B_{i+j} = B_i &
-        Advance(B_j, i)); the last bytes of runs of k in [lo, hi] from a next position are
-        V = Advance(P, lo - 1) & B_lo, widened while fewer than hi by V |= Advance(V, s) & B_s
-        with s at most the count covered so far plus one (so no count is skipped)."""
+    def _rep_fixed(self, node, st, m):
+        """``X{lo,hi}`` (hi None: ``X{lo,}``) for an item X of fixed length m and a wide count,
+        in O(log) steps instead of one per count: B_k = k matches of X back to back ending at
+        q (B_1 = X's match ends, B_{i+j} = B_i & Advance(B_j, i m)); the last bytes of k in
+        [lo, hi] matches from a next position are V = Advance(P, lo m - 1) & B_lo, widened while
+        fewer than hi by V |= Advance(V, s m) & B_s with s at most the count covered so far plus
+        one (so no count is skipped)."""
         b = self.b
-        c = b.cc(node.item.bytes_)
-        memo = {1: c}
+        saved, b.top = b.top, True      # X's match ends depend on the bytes only
+        memo = {1: self.run(node.item, ("0", "1"))[0]}
+        b.top = saved
 
         def B(k):
             if k not in memo:
                 i = k // 2
-                memo[k] = b.AND(B(i), b.ADV(B(k - i), i))
+                memo[k] = b.AND(B(i), b.ADV(B(k - i), i * m))
             return memo[k]
 
-        def widen(V, d):       # V holds the runs of k bytes: those of k .. k + d
+        def widen(V, d):       # V holds the runs of k matches: those of k .. k + d
             done = 0
             while done < d:
                 step = min(done + 1, d - done)
-                V = b.OR(V, b.AND(b.ADV(V, step), B(step)))
+                V = b.OR(V, b.AND(b.ADV(V, step * m), B(step)))
                 done += step
             return V
 
         P = self.P(st)
         if node.lo == 0:        # then hi >= WIDE_REPEAT
-            V = widen(b.AND(P, c), node.hi - 1)
+            V = widen(b.AND(b.ADV(P, m - 1), B(1)), node.hi - 1)
             return (b.OR(st[0], V), b.OR(P, b.ADV(V, 1)))
-        V = b.AND(b.ADV(P, node.lo - 1), B(node.lo))
+        V = b.AND(b.ADV(P, node.lo * m - 1), B(node.lo))
         if node.hi is None:
             return self.star(node.item, (V, None))
         return (widen(V, node.hi - node.lo), None)
@@ -829,7 +833,7 @@ class _Compiler:
         return accum
 
 
-WIDE_REPEAT = 16   # class repeats with a bound from here on are built in O(log) steps
+WIDE_REPEAT = 16   # repeats of fixed-length items with a bound from here on: O(log) steps
 
 
 def _fixed_sets(node, assertions: bool = False) -> Optional[List[frozenset]]:

@@ -501,13 +501,15 @@ def test_lookarounds_on_ragged_inputs(cuda, single):
 
 @pytest.mark.parametrize("single", [False, True])
 def test_wide_class_repeats(cuda, single):
-    """Class repeats with bounds of 16 and more, built by doubling (Advances of up to half the
-    bound), over text with runs around the bounds: streams and counts equal the C oracle's per
-    regex, split and single-kernel form."""
-    regexes = ["abcd.{0,40}wxyz", "kq[a-z]{10,40}yy", "zq[0-9]{16}", "mnop[ab]{20,}st"]
+    """Repeats of classes and of fixed-length groups with bounds of 16 and more, built by
+    doubling (Advances of up to half the bound), over text with runs around the bounds: streams
+    and counts equal the C oracle's per regex, split and single-kernel form."""
+    regexes = ["abcd.{0,40}wxyz", "kq[a-z]{10,40}yy", "zq[0-9]{16}", "mnop[ab]{20,}st",
+               "gh(ij){2,20}kl", "uv(wx|yz){16,}"]
     wit = [b"abcd" + b"." * k + b"wxyz" for k in (0, 39, 40, 41)] + \
           [b"kq" + b"r" * k + b"yy" for k in (9, 10, 40, 41)] + \
-          [b"zq" + b"7" * k for k in (15, 16, 17)] + [b"mnop" + b"ab" * k + b"st" for k in (9, 10, 30)]
+          [b"zq" + b"7" * k for k in (15, 16, 17)] + [b"mnop" + b"ab" * k + b"st" for k in (9, 10, 30)] + \
+          [b"gh" + b"ij" * k + b"kl" for k in (1, 2, 20, 21)] + [b"uv" + b"wxyz" * k for k in (7, 8, 9, 40)]
     groups = [compile_group(regexes[i::2]) for i in range(2)]
     prog = Program(groups, tuning=Tuning(prefilter=False) if single else
                    Tuning(wpt=1, prefilter_limit=1.0), per_regex=True)

@@ -236,12 +236,14 @@ def test_end_assertions_inside_patterns(matchstar_form):
 
 
 WIDE_REPEATS = ["a.{0,20}b", "x[a-z]{10,40}y", "q[0-9]{16}", "(?s)a.{17,30}", "z[ab]{0,16}",
-                "c.{20,}d", "[ab]{16,}", "k[ab]{3,18}", "^.{16}$", "(?i)q{16,17}"]
+                "c.{20,}d", "[ab]{16,}", "k[ab]{3,18}", "^.{16}$", "(?i)q{16,17}", "(ab){16}",
+                "x(ab){2,20}y", "(abc){0,17}d", "(ab|cd){16,}e", "(aa){16,18}", "z(a[bc]){0,30}"]
 
 
 def test_wide_class_repeats_match_nfa_and_regex_module():
-    """Class repeats with a bound of 16 or more are built by doubling (O(log) steps): equal to
-    the NFA and the regex module, at every count around the bounds and on random text."""
+    """Repeats of classes and fixed-length groups with a bound of 16 or more are built by
+    doubling (O(log) steps): equal to the NFA and the regex module, at every count around the
+    bounds and on random text."""
     rx = pytest.importorskip("regex")
     rnd = random.Random(15)
     for r in WIDE_REPEATS:
@@ -251,9 +253,9 @@ def test_wide_class_repeats_match_nfa_and_regex_module():
                         rx.M | (rx.I if "(?i)" in r else 0) | (rx.S if "(?s)" in r else 0))
         texts = [bytes(rnd.choice(b"aabbbaq1xyzcdk\n") for _ in range(rnd.choice([0, 30, 90])))
                  for _ in range(12)]
-        for k in range(0, 45):     # one run of k bytes between the literals
-            for fill in (b"b", b"5", b"Q"):
-                texts.append(r.encode()[:1].lstrip(b"^([(?") + fill * k + b"dby")
+        for k in range(0, 45):     # one run of k bytes (or pairs) between the literals
+            for fill in (b"b", b"5", b"Q", b"ab", b"ac", b"cd", b"abc"):
+                texts.append(r.encode()[:1].lstrip(b"^([(?") + fill * k + b"dbye")
         for data in texts:
             want = 0
             for e in range(len(data)):
