@@ -112,6 +112,19 @@ def _probe_hits(f, text):
     return key, pre3, probed, hit
 
 
+class _EmitterPatterns:
+    """Lookarounds, loop-free group stars, wide repeats and end assertions inside patterns."""
+    regexes = [r"abcd(?=x)", r"qrst(?!u)", r"(?<=ab)cdqx", r"xyzq(ab|cde)*f", r"mnop(rs)+t",
+               r"hijk.{0,40}lmno", r"wxyz[0-9]{16}", r"klmn$\nopq", r"(?<![0-9])1234(?![0-9])",
+               r"efgh(ij){2,20}kl"]
+    witnesses = [b"abcdx", b"qrstv", b"abcdqx", b"xyzqabcdecdef", b"mnoprsrsrst",
+                 b"hijk" + b"." * 30 + b"lmno", b"wxyz" + b"5" * 16, b"klmn\nopq", b" 1234 ",
+                 b"efgh" + b"ij" * 5 + b"kl"]
+
+    def groups(self, n):
+        return [self.regexes[i::n] for i in range(n)]
+
+
 class _FlagPatterns:
     """Word boundaries and case-insensitive groups (PCRE-style rule fragments), with witnesses."""
     regexes = [r"\bhello\w+world\b", r"(?i)\bselect\s+\*\s+from\b", r"\Bing\b",
@@ -126,11 +139,12 @@ class _FlagPatterns:
 
 @pytest.mark.parametrize("wpt,kind,config", [(1, "throughput", None), (2, "throughput", (4, 2)),
                                              (1, "throughput", (4, 1)), (2, "throughput", (3, 1)),
-                                             (2, "dna", None), (1, "flags", None)])
+                                             (2, "dna", None), (1, "flags", None),
+                                             (1, "emitter", None), (2, "emitter", (4, 2))])
 def test_prefilter_is_sound(wpt, kind, config):
     """Also on IUPAC motifs over DNA text (the filter the split form would use there if forced;
-    the compiler picks the single-kernel form for it), and on word boundaries and
-    case-insensitive groups."""
+    the compiler picks the single-kernel form for it), on word boundaries and case-insensitive
+    groups, and on lookarounds, loop-free group stars and wide repeats."""
     n = 300_000
     if kind == "dna":
         ps = workloads.dna_motifs(24, seed=5)
@@ -138,6 +152,9 @@ def test_prefilter_is_sound(wpt, kind, config):
     elif kind == "flags":
         ps = _FlagPatterns()
         text = workloads.plant(workloads.printable_text(n, 44), ps.witnesses, 300, 45)
+    elif kind == "emitter":
+        ps = _EmitterPatterns()
+        text = workloads.plant(workloads.printable_text(n, 46), ps.witnesses, 300, 47)
     else:
         ps = workloads.throughput_patterns(seed=3, n=64)
         text = workloads.plant(workloads.printable_text(n, 41), ps.witnesses, 700, 42)

@@ -125,3 +125,30 @@ def test_cluster_chains_batches_share_classes():
     assert distinct < in_order
     # few chains: one batch, in order
     assert _cluster_chains([3, 1], leaves, 8) == [[3, 1]]
+
+
+def test_guard_regions_never_read_a_later_block(monkeypatch):
+    """A part whose zero-skip regions would open a guard block that reads a node declared for
+    a later block (still zero there) is generated as one unguarded region; the programs of the
+    benchmark workloads keep their guards."""
+    import bitgen_gb300.compiler as C
+    used = []
+    orig = C._Gen._part
+
+    def spy(self, terms, outer_regs, skip):
+        r = orig(self, terms, outer_regs, skip)
+        used.append(skip)
+        return r
+
+    monkeypatch.setattr(C._Gen, "_part", spy)
+    regexes = ["q(rs)*t", "(ab)+c", "x(abc)*y", "(a[0-9]){2,}z", "(ab|cd)*e", "k(xy)*",
+               "(?i)(gh)+i", "m(n(op){2})*w"]
+    stars = [compile_group(regexes[i::2]) for i in range(2)]
+    generate_kernel(stars, Tuning(prefilter=False), per_regex=True)
+    assert used == [False]
+    used.clear()
+    small, _ = workloads.small_workload()
+    thr = workloads.throughput_patterns(seed=3, n=64)
+    for gs in ([compile_group(g) for g in small.groups(4)], [compile_group(g) for g in thr.groups(4)]):
+        generate_kernel(gs, Tuning(prefilter=False))
+    assert used and all(used)
