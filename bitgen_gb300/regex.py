@@ -578,13 +578,13 @@ class _Compiler:
             if node.behind:
                 if _matches_empty(node.item):
                     raise UnsupportedRegex("lookbehind content that matches the empty string")
-                E = self.run(node.item, ("0", "1"), at_end=True)[0]
+                E = self.run(node.item, ("0", "1"))[0]
                 after, before = E, b.ADV(E, 1)
             else:
                 U = _fixed_sets(node.item, assertions=True)
                 if U is None or not U:
                     raise UnsupportedRegex("lookahead content must have a fixed, non-zero length")
-                E = self.run(node.item, ("0", "1"), at_end=True)[0]
+                E = self.run(node.item, ("0", "1"))[0]
                 G = b.emit("lookahead", (E,), shift=len(U) - 1) if len(U) > 1 else E
                 after, before = b.emit("lookahead", (G,), shift=1), G
             if node.neg:
@@ -645,7 +645,7 @@ class _Compiler:
             self.b.top = saved
         return self._sol
 
-    def run(self, node, st, at_end=False):
+    def run(self, node, st):
         b = self.b
         if isinstance(node, End):
             # after a last byte p: p + 1 is LF or the end; at a next position q: q is an LF
@@ -661,11 +661,11 @@ class _Compiler:
             L = b.AND(self.P(st), c)
             return (L, None)
         if isinstance(node, Seq):
-            for i, it in enumerate(node.items):
-                st = self.run(it, st, at_end and i == len(node.items) - 1)
+            for it in node.items:
+                st = self.run(it, st)
             return st
         if isinstance(node, Alt):
-            outs = [self.run(it, st, at_end) for it in node.items]
+            outs = [self.run(it, st) for it in node.items]
             L = "0"
             P = "0"
             for o in outs:
@@ -966,7 +966,7 @@ def compile_group(regexes: List[str], matchstar: bool = True) -> Group:
     for r in regexes:
         ast = parse_regex(r)
         comp = _Compiler(b, matchstar)
-        L, _ = comp.run(ast, ("0", "1"), at_end=True)
+        L, _ = comp.run(ast, ("0", "1"))
         results.append(L)
     acc = "0"
     for L in results:
