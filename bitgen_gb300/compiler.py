@@ -399,7 +399,32 @@ def _cluster_chains(members: List[int], leaves: Dict[int, List[Tuple[int, int]]]
     return out
 
 
-def interleave_chains(dag: Dag, outs: Sequence[int], batch: int) -> Tuple[List[int], Dict[int, int]]:
+def _shared_pairs(leaf_sets: Dict[int, List[Tuple[int, int]]]) -> Dict[int, List[Tuple]]:
+    """Per chain of a batch, the pairs of its shifted classes that it ANDs through a node shared
+    with other chains of the batch: greedily the pair most chains hold, while two or more do,
+    each class of a chain in one pair at most."""
+    free = {r: set(ls) for r, ls in leaf_sets.items()}
+    out: Dict[int, List[Tuple]] = {r: [] for r in leaf_sets}
+    while True:
+        count: Dict[Tuple, int] = {}
+        for r, ls in free.items():
+            srt = sorted(ls)
+            for i in range(len(srt)):
+                for j in range(i + 1, len(srt)):
+                    count[(srt[i], srt[j])] = count.get((srt[i], srt[j]), 0) + 1
+        best = max(count.items(), key=lambda kv: (kv[1], kv[0]), default=None)
+        if best is None or best[1] < 2:
+            return out
+        pair = best[0]
+        for r, ls in free.items():
+            if pair[0] in ls and pair[1] in ls:
+                ls.discard(pair[0])
+                ls.discard(pair[1])
+                out[r].append(pair)
+
+
+def interleave_chains(dag: Dag, outs: Sequence[int], batch: int,
+                      pairs: bool = False) -> Tuple[List[int], Dict[int, int]]:
     """Re-associate the AND chains of a pushed program distance-major.
 
     After ``push_advances`` a pattern is an AND of shifted classes ``Advance(C, d)`` (and of
@@ -411,7 +436,9 @@ def interleave_chains(dag: Dag, outs: Sequence[int], batch: int) -> Tuple[List[i
     markers, ORs, additions) are ANDed in last.  A chain that reads another chain's result is
     built in a later wave than that chain.  AND is associative and commutative, so the values
     are unchanged.  Returns the new outputs and, for each AND node built here, its batch
-    number (the code generator shares a shifted class within a batch)."""
+    number (the code generator shares a shifted class within a batch).  With `pairs`, two
+    shifted classes that several chains of a batch read are ANDed once into a node those chains
+    share (`_shared_pairs`), at the distance of the later of the two."""
     dag.analyse()
     cc = dag._cc
     live, stack = set(), list(outs)
@@ -522,10 +549,36 @@ def interleave_chains(dag: Dag, outs: Sequence[int], batch: int) -> Tuple[List[i
             for r in grp:
                 for c, d in flat[r][0]:
                     by_d[r].setdefault(d, []).append(c)
+            # shared pairs: a chain ANDs a pair's node in place of its two classes, at the pair's
+            # later distance (the smaller d; ties: the larger class)
+            paired: Dict[int, Dict[Tuple[int, int], Optional[Tuple]]] = {r: {} for r in grp}
+            if pairs:
+                for r, prs in _shared_pairs({r: flat[r][0] for r in grp}).items():
+                    for a_, b_ in prs:
+                        late = min(a_, b_, key=lambda x: (x[1], -x[0]))
+                        paired[r][a_] = (a_, b_) if a_ == late else None
+                        paired[r][b_] = (a_, b_) if b_ == late else None
+            pair_node: Dict[Tuple, int] = {}
+
+            def operand_at(r, c, d):
+                lf = (c, d)
+                if lf not in paired[r]:
+                    return dag.make("advance", (c,), d)
+                pr = paired[r][lf]
+                if pr is None:          # the pair is ANDed at its other class's distance
+                    return None
+                if pr not in pair_node:
+                    pa, pb = (dag.make("advance", (x[0],), x[1]) for x in pr)
+                    pair_node[pr] = fresh_and(pa, pb)
+                    epochs.setdefault(pair_node[pr], k)
+                return pair_node[pr]
+
             for d in dists:
                 for r in grp:
                     for c in sorted(by_d[r].get(d, [])):
-                        lf = dag.make("advance", (c,), d)
+                        lf = operand_at(r, c, d)
+                        if lf is None:
+                            continue
                         if acc[r] is None:
                             acc[r] = lf
                         else:
@@ -602,6 +655,9 @@ class Tuning:
     claim_tiles: int = 4         # single-kernel form: consecutive tiles a warp claims at once
     chain_batch: int = 8         # with push_advances: AND chains re-associated distance-major,
                                  # this many at a time (0: each chain computed on its own)
+    pair_share: bool = True      # with chain_batch: pairs of shifted classes that several chains
+                                 # of a batch read are ANDed once (interleave_chains(pairs=));
+                                 # 64 DNA motifs: 2% faster
 
     def key(self):
         return (self.wpt, self.block, self.skip_interval, self.part_cap, self.window,
@@ -611,7 +667,8 @@ class Tuning:
                 self.cls_block, self.single_wpt, self.single_min_blocks, self.inline_parts,
                 self.basis_filter, self.filter_config, self.bulk_zero, self.exec_claim,
                 self.exec_min_blocks,
-                self.push_advances, self.chain_batch, self.single_edge, self.claim_tiles)
+                self.push_advances, self.chain_batch, self.single_edge, self.claim_tiles,
+                self.pair_share)
 
 
 @dataclass
@@ -1545,7 +1602,7 @@ def generate_kernel(groups: Sequence[Group], tuning: Optional[Tuning] = None,
         outs = push_advances(dag, outs)
         epochs: Dict[int, int] = {}
         if tuning.chain_batch > 0:
-            outs, epochs = interleave_chains(dag, outs, tuning.chain_batch)
+            outs, epochs = interleave_chains(dag, outs, tuning.chain_batch, tuning.pair_share)
         gen = _Gen(dag, tuning)
         gen.analyse(outs)
         gen.share_reads = True

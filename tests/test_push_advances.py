@@ -70,9 +70,10 @@ def test_pushed_outputs_equal(label, groups, text, per_regex):
     assert _eval(dag, new, text) == want
     assert any(want)
     for batch in (1, 5, 64):
-        inter, epochs = interleave_chains(dag, new, batch)
-        assert _eval(dag, inter, text) == want, batch
-        assert all(dag.nodes[v].op == "and" for v in epochs)
+        for pairs in (False, True):
+            inter, epochs = interleave_chains(dag, new, batch, pairs)
+            assert _eval(dag, inter, text) == want, (batch, pairs)
+            assert all(dag.nodes[v].op == "and" for v in epochs)
 
 
 def test_pushed_dag_shifts_classes_not_markers():
