@@ -295,6 +295,64 @@ def test_group_stars_match_the_loop_form_and_nfa(regex, loop_free):
             assert int(cnt[0]) == bin(want).count("1")
 
 
+_FUZZ_ATOMS = ["a", "b", "c", "ab", ".", "[ab]", "[^a]", "\\d", "\\w", "\\s", "x", "[a-c]", "\\n"]
+
+
+def _fuzz_regex(rnd, depth):
+    """A random regex over the constructs the emitter accepts (seeded)."""
+    k = rnd.random()
+    if depth <= 0 or k < 0.35:
+        return rnd.choice(_FUZZ_ATOMS)
+    if k < 0.55:
+        return _fuzz_regex(rnd, depth - 1) + _fuzz_regex(rnd, depth - 1)
+    if k < 0.65:
+        return "(?:" + _fuzz_regex(rnd, depth - 1) + "|" + _fuzz_regex(rnd, depth - 1) + ")"
+    if k < 0.80:
+        q = rnd.choice(["*", "+", "?", "{2}", "{1,3}", "{0,2}", "{2,}", "{16,18}", "{0,17}"])
+        return "(?:" + _fuzz_regex(rnd, depth - 1) + ")" + q
+    if k < 0.85:
+        return rnd.choice(["^", "$", "\\b", "\\B"]) + _fuzz_regex(rnd, depth - 1)
+    if k < 0.90:
+        return _fuzz_regex(rnd, depth - 1) + rnd.choice(["(?=a)", "(?!b)", "(?=ab)", "(?=[ab]c)"])
+    if k < 0.95:
+        return rnd.choice(["(?<=a)", "(?<!b)", "(?<=ab|c)", "(?<![0-9])"]) + _fuzz_regex(rnd, depth - 1)
+    return "(?i:" + _fuzz_regex(rnd, depth - 1) + ")"
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_random_regexes_match_nfa_and_regex_module(seed):
+    """Differential test on seeded random regexes mixing every construct (groups, alternation,
+    all quantifiers including wide ones, anchors, word boundaries, lookarounds, case groups):
+    the emitter's streams (MatchStar and while-loop forms), the NFA, the C evaluator and the
+    regex module agree.  Patterns that can match the empty string are skipped (the convention
+    counts non-empty matches only)."""
+    rx = pytest.importorskip("regex")
+    from bitgen_gb300.regex import _matches_empty, parse_regex
+    rnd = random.Random(seed)
+    tested = 0
+    while tested < 150:
+        r = _fuzz_regex(rnd, 4)
+        try:
+            if _matches_empty(parse_regex(r)):
+                continue
+            g = compile_regex(r)
+            loop = compile_regex(r, matchstar=False)
+        except UnsupportedRegex:
+            continue
+        pr = rx.compile(("(?<=" + r.replace("[^", "[^\n") + ")").encode(), rx.M)
+        tested += 1
+        for _ in range(3):
+            n = rnd.randint(1, 50)
+            data = bytes(rnd.choice(b"aabbcx0 \nAB") for _ in range(n))
+            want = 0
+            for e in range(n):
+                if pr.match(data, e + 1):
+                    want |= 1 << e
+            assert run_group(g, data) == run_group(loop, data) == match_ends(r, data) == want, (r, data)
+            st, cnt = cpu.run_groups([g], np.frombuffer(data, np.uint8))
+            assert int(cnt[0]) == bin(want).count("1"), (r, data)
+
+
 def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
     """The genomic motif grammar (IUPAC classes, gapped `.{lo,hi}` motifs) over DNA text with N
     runs, line feeds and planted motifs: emitter + big-int oracle == NFA == C evaluator."""
