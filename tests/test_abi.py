@@ -171,3 +171,38 @@ def test_c_host_builds_and_calls_the_abi(native, tmp_path):
                    check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0 and out.stdout.strip() == "ok", (out.returncode, out.stdout, out.stderr)
+
+
+def test_random_regex_programs_compile_in_both_forms(native):
+    """Seeded random regex groups (every emitter construct) generate kernels that NVRTC
+    compiles for sm_103a, in the split form and the single-kernel form with and without
+    zero-block skipping."""
+    import random
+    from bitgen_gb300.compiler import NotFusable
+    from bitgen_gb300.regex import UnsupportedRegex, _matches_empty, parse_regex
+    from tests.test_oracle import _fuzz_regex
+    rnd = random.Random(21)
+    compiled = 0
+    for _ in range(4):
+        rs = []
+        while len(rs) < 6:
+            r = "qz" + _fuzz_regex(rnd, 3) + "k"
+            try:
+                if not _matches_empty(parse_regex(r)):
+                    compile_group([r])
+                    rs.append(r)
+            except UnsupportedRegex:
+                pass
+        groups = [compile_group(rs[i::2]) for i in range(2)]
+        for t in (Tuning(prefilter=False), Tuning(wpt=1, prefilter_limit=1.0),
+                  Tuning(prefilter=False, wpt=2, skip_interval=1)):
+            try:
+                spec = generate_kernel(groups, t, per_regex=True)
+            except NotFusable:
+                continue        # programs that keep a while loop run on the whole-stream executor
+            buf = C.create_string_buffer(1 << 16)
+            src = spec.source.encode()
+            rc = native.bg_nvrtc_check(src, len(src), b"bg_scan", buf, len(buf))
+            assert rc == N.BG_OK, (rs, buf.value.decode()[:2000])
+            compiled += 1
+    assert compiled >= 6
