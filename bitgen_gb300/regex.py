@@ -21,8 +21,8 @@ word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``^``
 ``\\z``, ``\\Z``, ``\\K`` (no effect on match ends), groups ``(...)`` / ``(?:...)`` / named
 (``(?P<n>...)``, ``(?<n>...)``, ``(?'n'...)``), comments ``(?#...)``, lookahead ``(?=X)`` /
 ``(?!X)`` (X of fixed length) and lookbehind ``(?<=X)`` / ``(?<!X)`` (X bounded, not matching
-the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF) and ``m``
-(no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing group or
+the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF), ``x`` (white space and
+``#`` comments outside classes ignored) and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing group or
 ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or
 lazy).  Zero-width assertions filter both markers (below): ``$`` keeps the last bytes followed by
 an LF or the end, ``L & ~Lookahead(~LF, 1)``, and the next positions that hold an LF.
@@ -160,6 +160,7 @@ class _Parser:
         self.i = 0
         self.icase = False    # (?i): ASCII letters match either case
         self.dotall = False   # (?s): '.' matches LF too
+        self.extended = False  # (?x): white space and #-comments outside classes are ignored
 
     def peek(self):
         return self.s[self.i] if self.i < len(self.s) else None
@@ -175,8 +176,21 @@ class _Parser:
             raise UnsupportedRegex(f"unexpected {self.s[self.i]!r} at {self.i} in {self.s!r}")
         return node
 
+    def _skip_x(self):
+        """In (?x) mode, step over white space and comments (to the end of the line)."""
+        while self.extended and self.i < len(self.s):
+            c = self.s[self.i]
+            if c in " \t\n\r\f\v":
+                self.i += 1
+            elif c == "#":
+                j = self.s.find("\n", self.i)
+                self.i = len(self.s) if j < 0 else j + 1
+            else:
+                return
+
     def alt(self):
         items = [self.seq()]
+        self._skip_x()
         while self.peek() == "|":
             self.take()
             items.append(self.seq())
@@ -184,15 +198,18 @@ class _Parser:
 
     def seq(self):
         items = []
+        self._skip_x()
         while self.peek() is not None and self.peek() not in "|)":
             a = self.atom()
             a = self.quant(a)
             items.append(a)
+            self._skip_x()
         return Seq(tuple(items))
 
     def quant(self, a):
         zero_width = isinstance(a, (Start, End, WordB, TextStart, TextEnd, Look))
         while True:
+            self._skip_x()
             c = self.peek()
             if zero_width and c is not None and (c in "*+?" or (c == "{" and self._is_counted())):
                 raise UnsupportedRegex("a quantifier on an assertion")
@@ -231,22 +248,24 @@ class _Parser:
         return re.fullmatch(r"\d+(,\d*)?|,\d+", self.s[self.i + 1:j]) is not None
 
     def _flags(self):
-        """Parse the letters of a `(?flags` group up to ':' or ')'; returns (icase, dotall, end)
-        with the flags as they hold inside and `end` the closing character."""
-        icase, dotall, on = self.icase, self.dotall, True
+        """Parse the letters of a `(?flags` group up to ':' or ')'; returns (icase, dotall,
+        extended, end) with the flags as they hold inside and `end` the closing character."""
+        icase, dotall, extended, on = self.icase, self.dotall, self.extended, True
         while True:
             c = self.peek()
             if c is None:
                 raise UnsupportedRegex("unterminated group flags")
             self.take()
             if c in ":)":
-                return icase, dotall, c
+                return icase, dotall, extended, c
             if c == "-":
                 on = False
             elif c == "i":
                 icase = on
             elif c == "s":
                 dotall = on
+            elif c == "x":
+                extended = on
             elif c == "m":
                 pass    # ^ and $ already hold at every line (grep line semantics)
             else:
@@ -255,17 +274,17 @@ class _Parser:
     def atom(self):
         c = self.take()
         if c == "(":
-            saved = (self.icase, self.dotall)
+            saved = (self.icase, self.dotall, self.extended)
             if self.s.startswith("?:", self.i):
                 self.i += 2
             elif self.peek() == "?" and self.i + 1 < len(self.s) and self.s[self.i + 1] in "imsx-":
                 self.take()
-                icase, dotall, end = self._flags()
+                icase, dotall, extended, end = self._flags()
                 if end == ")":
                     # (?flags): the flags hold to the end of the enclosing group
-                    self.icase, self.dotall = icase, dotall
+                    self.icase, self.dotall, self.extended = icase, dotall, extended
                     return Seq(())
-                self.icase, self.dotall = icase, dotall
+                self.icase, self.dotall, self.extended = icase, dotall, extended
             elif self.s.startswith(("?=", "?!", "?<=", "?<!"), self.i):
                 behind = self.s[self.i + 1] == "<"
                 neg = self.s[self.i + (2 if behind else 1)] == "!"
@@ -274,7 +293,7 @@ class _Parser:
                 if self.peek() != ")":
                     raise UnsupportedRegex("missing )")
                 self.take()
-                self.icase, self.dotall = saved
+                self.icase, self.dotall, self.extended = saved
                 return Look(node, behind, neg)
             elif self.s.startswith("?#", self.i):     # (?#comment)
                 j = self.s.find(")", self.i)
@@ -292,7 +311,7 @@ class _Parser:
             if self.peek() != ")":
                 raise UnsupportedRegex("missing )")
             self.take()
-            self.icase, self.dotall = saved
+            self.icase, self.dotall, self.extended = saved
             return node
         if c == "[":
             return CC(self.cls())

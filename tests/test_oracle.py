@@ -117,7 +117,8 @@ def test_emitter_matches_nfa_and_python_re(matchstar_form):
 FLAG_REGEXES = [r"(?i)abc", r"(?i)a[b-d]+e", r"x(?i:yz)w", r"(?i)x(?-i:y)z", r"(?s)a.b",
                 r"(?i)[^a]b", r"a(?s:.)c", r"(?i)\x41b", r"(?im)^ab", r"(?i:a|B)c",
                 r"\bab", r"ab\b", r"\bx\w*\b", r"a\Bb", r"\B0", r"(a|\b)b", r"[\b-c]x",
-                r"\b(?i:yz)\b", r"\Aab", r"\A\w+", r"(?i)\Axy|z\z", r"b\z", r"\w\Z", r"(a|\A)b",
+                r"\b(?i:yz)\b", "(?x) a b | c d", "(?x)[ ]x # a comment\n y", r"a(?x: b c )d",
+                r"(?ix) A \  B", r"\Aab", r"\A\w+", r"(?i)\Axy|z\z", r"b\z", r"\w\Z", r"(a|\A)b",
                 r"\x{41}b", r"(?i)[\x{61}-c]\Z"]
 
 
@@ -371,7 +372,7 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$+", "(?=x*)", r"a\b*", r"a\Z+", "a++", "(?x)a b", "(?i", r"\x{100}", r"\101",
+    for r in ("a$+", "(?=x*)", r"a\b*", r"a\Z+", "a++", "(?>ab)", "(?i", r"\x{100}", r"\101",
               r"(?<=a+)b", r"\o{400}", r"[\N]", "\\Q\u0100\\E", r"(?#open"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
