@@ -18,7 +18,7 @@ Supported syntax: literals and escapes (``\\xHH``, ``\\x{HH}``, ``\\n \\r \\t \\
 octal ``\\0oo`` / ``\\o{ooo}``, control ``\\cX``, escaped punctuation, ``\\Q...\\E`` quoting),
 classes ``[...]`` / ``[^...]`` with ranges and ``\\d \\D \\w \\W \\s \\S \\h \\H``, ``.``, ``\\N``,
 word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``^``, ``$``, ``\\A``,
-``\\z``, ``\\Z``, ``\\K`` (no effect on match ends), groups ``(...)`` / ``(?:...)`` / named
+``\\z``, ``\\Z``, ``\\K`` (no effect on match ends), ``\\R`` (a line break, CR LF as one), groups ``(...)`` / ``(?:...)`` / named
 (``(?P<n>...)``, ``(?<n>...)``, ``(?'n'...)``), comments ``(?#...)``, lookahead ``(?=X)`` /
 ``(?!X)`` (X of fixed length) and lookbehind ``(?<=X)`` / ``(?<!X)`` (X bounded, not matching
 the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF), ``x`` (white space and
@@ -329,6 +329,11 @@ class _Parser:
                 return TextStart()
             if self.peek() in ("z", "Z"):
                 return TextEnd(final_lf=self.take() == "Z")
+            if self.peek() == "R":          # \R: CR LF, or one of LF VT FF CR NEL alone (it never
+                self.take()                 # gives back the LF of a CR LF): (?>\r\n|[...])
+                crlf = Seq((CC(frozenset([0x0D])), CC(frozenset([LF]))))
+                return Alt((crlf, Seq((Look(crlf, behind=False, neg=True),
+                                       CC(frozenset([LF, 0x0B, 0x0C, 0x0D, 0x85]))))))
             if self.peek() == "K":          # \K: resets the reported start, so match ends stay
                 self.take()
                 return Seq(())

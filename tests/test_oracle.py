@@ -159,16 +159,20 @@ PCRE_EQUIV = [(r"(?P<n>ab)+c", r"(?:ab)+c"), (r"(?<n>x|y)z", r"(?:x|y)z"), (r"(?
               (r"(?i)\Qab\E", r"(?i)ab"), (r"\012a", r"\na"), (r"\0", r"\x00"),
               (r"\o{101}b", r"Ab"), (r"\cAx|\cz", r"\x01x|\x1a"), (r"[\cA-\cC]x", r"[\x01-\x03]x"),
               (r"\h+x", r"[ \t\xa0]+x"), (r"[\h\d]y", r"[ \t\xa0\d]y"), (r"a\H", r"a[^ \t\xa0]"),
-              (r"a\N", r"a[^\n]"), (r"b\N+c", r"b[^\n]+c")]
+              (r"a\N", r"a[^\n]"), (r"b\N+c", r"b[^\n]+c"),
+              (r"a\R", r"a(?:\r\n|(?!\r\n)[\n\x0b\x0c\r\x85])"),
+              (r"a\R\n", r"a(?:\r\n|(?!\r\n)[\n\x0b\x0c\r\x85])\n"),
+              (r"\R+b", r"(?:\r\n|(?!\r\n)[\n\x0b\x0c\r\x85])+b")]
 
 
 @pytest.mark.parametrize("matchstar_form", [True, False])
 def test_emitter_pcre_syntax_matches_equivalents(matchstar_form):
-    """Named groups, comments, \\Q...\\E, octal and control escapes, \\h \\H \\N: the emitter's
-    streams equal the NFA's and the regex module's for an equivalent pattern."""
+    """Named groups, comments, \\Q...\\E, octal and control escapes, \\h \\H \\N, \\R (CR LF as one
+    break, never given back): the emitter's streams equal the NFA's and the regex module's for
+    an equivalent pattern."""
     rx = pytest.importorskip("regex")
     rnd = random.Random(12)
-    alphabet = b"abcqrxyzAB.()*\n\t \x00\x01\x02\x03\x1a\xa0"
+    alphabet = b"abcqrxyzAB.()*\n\t \x00\x01\x02\x03\x1a\xa0\r\r\x85"
     for ours, theirs in PCRE_EQUIV:
         g = parse_pablo(compile_regex(ours, matchstar=matchstar_form).to_pablo())
         pr = rx.compile(("(?<=" + theirs + ")").encode("latin1"), rx.M)
