@@ -24,7 +24,8 @@ word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``^``
 the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF), ``x`` (white space and
 ``#`` comments outside classes ignored) and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing group or
 ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or
-lazy).  Zero-width assertions filter both markers (below): ``$`` keeps the last bytes followed by
+lazy) and, over one class, possessive (``c*+ c++ c?+``, also as an atomic group ``(?>c*)``).
+Zero-width assertions filter both markers (below): ``$`` keeps the last bytes followed by
 an LF or the end, ``L & ~Lookahead(~LF, 1)``, and the next positions that hold an LF.
 
 Compilation keeps two markers per regex state: ``L`` (positions of the last byte consumed) and
@@ -239,7 +240,8 @@ class _Parser:
             if self.peek() == "?":
                 self.take()
             elif self.peek() == "+":
-                raise UnsupportedRegex("possessive quantifiers are not supported")
+                self.take()
+                a = _possessive(a)
 
     def _is_counted(self):
         j = self.s.find("}", self.i)
@@ -295,6 +297,20 @@ class _Parser:
                 self.take()
                 self.icase, self.dotall, self.extended = saved
                 return Look(node, behind, neg)
+            elif self.s.startswith("?>", self.i):     # atomic group: a possessive class repeat
+                self.i += 2
+                node = self.alt()
+                if self.peek() != ")":
+                    raise UnsupportedRegex("missing )")
+                self.take()
+                self.icase, self.dotall, self.extended = saved
+                while isinstance(node, Seq) and len(node.items) == 1:
+                    node = node.items[0]
+                if isinstance(node, CC):
+                    return node
+                if isinstance(node, Rep) and isinstance(node.item, CC):
+                    return _possessive(node)
+                raise UnsupportedRegex("atomic groups other than over one class (repeated or not)")
             elif self.s.startswith("?#", self.i):     # (?#comment)
                 j = self.s.find(")", self.i)
                 if j < 0:
@@ -945,6 +961,18 @@ def _branches_overlap(bs) -> bool:
                 if all(U[t] & V[t - d] for t in range(d, min(len(U), d + len(V)))):
                     return True
     return False
+
+
+def _possessive(node):
+    """A possessive repeat of a class, as a repeat and a negative lookahead that forces it to
+    take the whole run: ``c*+`` = ``c*(?!c)``, ``c++`` = ``c+(?!c)``, ``c?+`` = ``c|(?!c)``."""
+    if not (isinstance(node, Rep) and isinstance(node.item, CC)) or \
+            (node.lo, node.hi) not in ((0, None), (1, None), (0, 1)):
+        raise UnsupportedRegex("possessive repeats other than c*+, c++ and c?+ of one class")
+    not_c = Look(node.item, behind=False, neg=True)
+    if node.hi == 1:
+        return Alt((node.item, not_c))
+    return Seq((node, not_c))
 
 
 def _bounded(node) -> bool:

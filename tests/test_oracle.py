@@ -269,6 +269,33 @@ def test_wide_class_repeats_match_nfa_and_regex_module():
             assert run_group(g, data) == match_ends(r, data) == want, (r, data)
 
 
+def _forward_ends(rx, r, data):
+    """Ends e of non-empty matches [s, e] of `r`, by forward matching forced to stop at e + 1
+    (a look-behind wrapper would run possessive repeats backwards)."""
+    out = 0
+    for e in range(len(data)):
+        pe = rx.compile(("(?:" + r + ")(?<=\\A[\\s\\S]{%d})" % (e + 1)).encode(), rx.M)
+        if any(pe.match(data, s) for s in range(e + 1)):
+            out |= 1 << e
+    return out
+
+
+def test_possessive_and_atomic_class_repeats():
+    """c*+, c++, c?+ and (?>c*) etc. take the whole run (a repeat and a negative lookahead of
+    the class): equal to the NFA and to the regex module's forward matching."""
+    rx = pytest.importorskip("regex")
+    rnd = random.Random(16)
+    for r in ["a*+a", "xa++b", "a?+a", "x(?>a*)b", "x(?>[ab]+)b", "[ab]*+c", r"\d++\d",
+              "q(?>a)b", "a++", "(?i)x?+X"]:
+        g = parse_pablo(compile_regex(r).to_pablo())
+        for _ in range(25):
+            data = bytes(rnd.choice(b"aabbxXqc019\n") for _ in range(rnd.randint(0, 20)))
+            assert run_group(g, data) == match_ends(r, data) == _forward_ends(rx, r, data), (r, data)
+    for r in ("a{2,3}+", "(?>ab|a)c", "(ab)++"):
+        with pytest.raises(UnsupportedRegex):
+            compile_regex(r)
+
+
 # (regex, loop-free): stars over fixed-length items, or over unions of fixed-length branches,
 # whose matches cannot overlap compile without a while loop; the others keep icgrep's loop form
 GROUP_STARS = [("q(rs)*t", True), ("(ab)+c", True), ("x(abc)*y", True), ("(a[0-9]){2,}z", True),
@@ -376,7 +403,7 @@ def test_emitter_on_dna_motifs_matches_nfa_and_c_oracle():
 
 
 def test_emitter_rejects_unsupported():
-    for r in ("a$+", "(?=x*)", r"a\b*", r"a\Z+", "a++", "(?>ab)", "(?i", r"\x{100}", r"\101",
+    for r in ("a$+", "(?=x*)", r"a\b*", r"a\Z+", "(ab)++", "(?>ab|c)", "(?i", r"\x{100}", r"\101",
               r"(?<=a+)b", r"\o{400}", r"[\N]", "\\Q\u0100\\E", r"(?#open"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
