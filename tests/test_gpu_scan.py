@@ -516,3 +516,35 @@ def test_wide_class_repeats(cuda, single):
     assert (prog.spec.n_parts == 0) == single
     text = workloads.plant(workloads.printable_text(100_000, 91), wit, 40, 92)
     check(prog, groups, [text, np.frombuffer(b"".join(wit), np.uint8)], per_regex=True)
+
+
+@pytest.mark.skipif(not os.environ.get("BG_FUZZ_GPU"), reason="set BG_FUZZ_GPU=<programs> to run")
+@pytest.mark.parametrize("single", [False, True])
+def test_random_regex_programs_match_c_oracle(cuda, single):
+    """Seeded random regex groups over every emitter construct (as in the CPU differential
+    test), each program in both kernel forms over text biased to the regexes' bytes: streams
+    and counts equal the C oracle's per regex.  Programs that keep a while loop are skipped."""
+    import random
+    from bitgen_gb300.compiler import NotFusable
+    from bitgen_gb300.regex import UnsupportedRegex, _matches_empty, parse_regex
+    from tests.test_oracle import _fuzz_regex
+    rnd = random.Random(33)
+    for _ in range(int(os.environ["BG_FUZZ_GPU"])):
+        rs = []
+        while len(rs) < 8:
+            r = "qz" + _fuzz_regex(rnd, 3) + "k"
+            try:
+                if not _matches_empty(parse_regex(r)):
+                    compile_group([r])
+                    rs.append(r)
+            except UnsupportedRegex:
+                pass
+        groups = [compile_group(rs[i::2]) for i in range(2)]
+        try:
+            prog = Program(groups, tuning=Tuning(prefilter=False) if single else
+                           Tuning(wpt=1, prefilter_limit=1.0), per_regex=True, executor="fused")
+        except NotFusable:
+            continue
+        items = [rand_text(n, rnd.randrange(1 << 30), b"qzkabcx0 \nAB") for n in (0, 5, 3000, 70000)]
+        check(prog, groups, items, per_regex=True)
+        prog.close()
