@@ -24,7 +24,8 @@ word boundaries ``\\b`` / ``\\B`` (``\\b`` is a backspace inside a class), ``^``
 the empty string), the flags ``i`` (ASCII case-insensitive), ``s`` (``.`` matches LF), ``x`` (white space and
 ``#`` comments outside classes ignored) and ``m`` (no effect: lines are always honoured) as ``(?flags)`` up to the end of the enclosing group or
 ``(?flags:...)``, with ``-`` to turn them off, alternation, ``* + ? {m} {m,} {m,n}`` (greedy or
-lazy) and, over one class, possessive (``c*+ c++ c?+``, also as an atomic group ``(?>c*)``).
+lazy) and, over one class, possessive (``c*+ c++ c?+ c{m,n}+``, also as an atomic group
+``(?>c*)``).
 Zero-width assertions filter both markers (below): ``$`` keeps the last bytes followed by
 an LF or the end, ``L & ~Lookahead(~LF, 1)``, and the next positions that hold an LF.
 
@@ -964,15 +965,18 @@ def _branches_overlap(bs) -> bool:
 
 
 def _possessive(node):
-    """A possessive repeat of a class, as a repeat and a negative lookahead that forces it to
-    take the whole run: ``c*+`` = ``c*(?!c)``, ``c++`` = ``c+(?!c)``, ``c?+`` = ``c|(?!c)``."""
-    if not (isinstance(node, Rep) and isinstance(node.item, CC)) or \
-            (node.lo, node.hi) not in ((0, None), (1, None), (0, 1)):
-        raise UnsupportedRegex("possessive repeats other than c*+, c++ and c?+ of one class")
+    """A possessive repeat of a class, as repeats and a negative lookahead that force it to
+    take as much of the run as it may: ``c{m,}+`` = ``c{m,}(?!c)``, and ``c{m,n}+`` =
+    ``c{n}|c{m,n-1}(?!c)`` (all n bytes when the run has them, else the whole run)."""
+    if not (isinstance(node, Rep) and isinstance(node.item, CC)):
+        raise UnsupportedRegex("possessive repeats of anything but one class")
     not_c = Look(node.item, behind=False, neg=True)
-    if node.hi == 1:
-        return Alt((node.item, not_c))
-    return Seq((node, not_c))
+    if node.hi is None:
+        return Seq((node, not_c))
+    full = Rep(node.item, node.hi, node.hi)
+    if node.hi == node.lo:
+        return full
+    return Alt((full, Seq((Rep(node.item, node.lo, node.hi - 1), not_c))))
 
 
 def _bounded(node) -> bool:

@@ -281,17 +281,19 @@ def _forward_ends(rx, r, data):
 
 
 def test_possessive_and_atomic_class_repeats():
-    """c*+, c++, c?+ and (?>c*) etc. take the whole run (a repeat and a negative lookahead of
-    the class): equal to the NFA and to the regex module's forward matching."""
+    """c*+, c++, c?+, c{m,n}+ and (?>c*) etc. take as much of the run as they may (repeats and
+    a negative lookahead of the class): equal to the NFA and to the regex module's forward
+    matching."""
     rx = pytest.importorskip("regex")
     rnd = random.Random(16)
     for r in ["a*+a", "xa++b", "a?+a", "x(?>a*)b", "x(?>[ab]+)b", "[ab]*+c", r"\d++\d",
-              "q(?>a)b", "a++", "(?i)x?+X"]:
+              "q(?>a)b", "a++", "(?i)x?+X", "a{1,3}+a", "xa{2,3}+", "a{2}+b", "x(?>a{0,2})a",
+              "a{2,}+b"]:
         g = parse_pablo(compile_regex(r).to_pablo())
         for _ in range(25):
             data = bytes(rnd.choice(b"aabbxXqc019\n") for _ in range(rnd.randint(0, 20)))
             assert run_group(g, data) == match_ends(r, data) == _forward_ends(rx, r, data), (r, data)
-    for r in ("a{2,3}+", "(?>ab|a)c", "(ab)++"):
+    for r in ("(?>ab|a)c", "(ab)++", "(a|b)*+"):
         with pytest.raises(UnsupportedRegex):
             compile_regex(r)
 
